@@ -1,0 +1,212 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the harness built by ``oracle/ref/build_ref.sh`` (the unmodified
+reference C++ sources of mathiasgartner/TDVMC linked with
+``oracle/ref/harness.cpp``) on seeded inputs and stores inputs and reference
+outputs as ``.npz`` files.  Needs the reference checkout (default
+``/root/reference``); the fixtures are committed so the tests never need it.
+
+    python tests/golden/make_golden.py [/path/to/reference]
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def fmt(a):
+    return " ".join("%.17g" % v for v in np.asarray(a, dtype=np.float64).reshape(-1))
+
+
+def run(ref_root, script):
+    cfg = os.path.join(ref_root, "config") + "/"
+    out = subprocess.run([HARNESS, cfg], input=script, capture_output=True, text=True, check=True).stdout
+    rows = {}
+    for line in out.splitlines():
+        parts = line.split()
+        if not parts or parts[0] not in ("EVAL", "MOVE", "SOLVE", "BLOCK", "NIC", "NODES", "WEIGHTS"):
+            continue
+        rows.setdefault(parts[0], []).append(np.array([float(x) for x in parts[1:]]))
+    return rows
+
+
+def system_cmd(dim, n, p, L, user_knots, sysp, time):
+    uk = [] if user_knots is None else list(user_knots)
+    return "SYSTEM %d %d %d %.17g %d %s %d %s %.17g\n" % (dim, n, p, L, len(uk), fmt(uk), len(sysp), fmt(sysp), time)
+
+
+def lattice(n, dim, L, rng, jitter=0.1):
+    """Simple-cubic start with jitter as InitCoordinateConfiguration (TDVMC.cpp:713-760)."""
+    m = int(round(n ** (1.0 / dim)))
+    l = L / m
+    idx = np.stack(np.meshgrid(*[np.arange(m)] * dim, indexing="ij"), -1).reshape(-1, dim)[:n]
+    return idx * l + (rng.uniform(size=(n, dim)) - 0.5) * l * jitter
+
+
+def nic_cases(ref_root):
+    """Parse the 48 known-answer displacement tests of src/test/Tests.h:76-156."""
+    text = open(os.path.join(ref_root, "src", "test", "Tests.h")).read()
+    body = text[text.index("void TestVectorDisplacements()"):]
+    cases = []
+    L = dim = None
+    for line in body.splitlines():
+        m = re.search(r"LBOX = (\d+);", line)
+        if m:
+            L = float(m.group(1))
+        m = re.search(r"DIM = (\d+);", line)
+        if m:
+            dim = int(m.group(1))
+        m = re.search(r"^\s*TestVectorDisplacement\((.*)\);", line)
+        if m:
+            args = [eval(a.strip(), {"sqrt": np.sqrt}) for a in m.group(1).split(",")]
+            cases.append((L, dim, args))
+    return cases
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not os.path.exists(HARNESS):
+        subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root])
+
+    # ---- NIC known answers (the reference's own unit test vectors) ----
+    cases = nic_cases(ref_root)
+    script = ""
+    ins, exp = [], []
+    for L, dim, args in cases:
+        k = 3 if dim == 3 else 1
+        ri, rj = args[:k], args[k:2 * k]
+        script += "NIC %d %.17g 1 %s %s\n" % (k, L, fmt(ri), fmt(rj))
+        pad = lambda v: list(v) + [0.0] * (3 - len(v))
+        ins.append([L, k] + pad(ri) + pad(rj))
+        exp.append([args[2 * k]] + pad(args[2 * k + 1:]))
+    rows = run(ref_root, script)["NIC"]
+    refout = np.array([list(r) + [0.0] * (4 - len(r)) for r in rows])
+    np.savez(os.path.join(HERE, "nic_kat.npz"), inputs=np.array(ins), expected=np.array(exp), reference=refout)
+    print("nic cases", len(cases))
+
+    # ---- systems for fixed-configuration evaluation ----
+    systems = []
+    # 1D, N=20, L=20, P=10 uniform, square well (BosonsBulk.cpp:268-271)
+    systems.append(dict(name="d1_n20_p10", dim=1, n=20, p=10, L=20.0, knots=None, sysp=[0.5, 2.0], time=0.0,
+                        ncfg=24, seed=11))
+    # same with the quench rule active (BosonsBulk.cpp:239-242)
+    systems.append(dict(name="d1_n20_p10_quench", dim=1, n=20, p=10, L=20.0, knots=None,
+                        sysp=[0.5, 2.0, 0.5, 0.8, 4.0], time=1.0, ncfg=8, seed=12))
+    # 2D, N=64, density 0.3, 20 non-uniform knots through SetNodes (BosonsBulk.cpp:35-44)
+    L2 = float(np.sqrt(64 / 0.3))
+    g = np.linspace(0.0, 1.0, 20)
+    knots2 = np.concatenate([[0.0], 0.7 + (L2 / 2 - 0.7) * (g[1:] - g[1]) ** 1.3 / (1 - g[1]) ** 1.3])
+    systems.append(dict(name="d2_n64_k20", dim=2, n=64, p=20, L=L2, knots=knots2, sysp=[1.0, 0.5], time=0.0,
+                        ncfg=16, seed=13))
+    # 3D, N=64, L=4 (the fixture box of src/VMCSampler.h:18)
+    systems.append(dict(name="d3_n64_p10", dim=3, n=64, p=10, L=4.0, knots=None, sysp=[0.6, 1.0], time=0.0,
+                        ncfg=16, seed=14))
+    # 3D, N=343, density 0.365, 30 parameters (the benchmark system)
+    L3 = float((343 / 0.365) ** (1.0 / 3.0))
+    systems.append(dict(name="d3_n343_p30", dim=3, n=343, p=30, L=L3, knots=None, sysp=[0.9, 1.0], time=0.0,
+                        ncfg=4, seed=15))
+
+    for sysd in systems:
+        rng = np.random.default_rng(sysd["seed"])
+        dim, n, p, L = sysd["dim"], sysd["n"], sysd["p"], sysd["L"]
+        uR = rng.normal(0.0, 0.3, size=p)
+        uI = rng.normal(0.0, 0.1, size=p)
+        phiR, phiI = 0.1, -0.2
+        cfgs = []
+        for c in range(sysd["ncfg"]):
+            if dim == 1:
+                R = rng.uniform(-L / 2, L / 2, size=(n, dim))
+            else:
+                R = lattice(n, dim, L, rng, jitter=0.5) - L / 2
+            cfgs.append(R)
+        cfgs = np.array(cfgs)
+        script = system_cmd(dim, n, p, L, sysd["knots"], sysd["sysp"], sysd["time"])
+        script += "PARAMS %s %s %.17g %.17g\n" % (fmt(uR), fmt(uI), phiR, phiI)
+        script += "WEIGHTS\n"
+        script += "EVAL %d\n" % len(cfgs)
+        for R in cfgs:
+            script += fmt(R) + "\n"
+        # single-particle moves on the first configurations
+        moves = []
+        nmove = 16
+        for c in range(nmove):
+            R = cfgs[c % len(cfgs)]
+            part = int(rng.integers(n))
+            newpos = R[part] + rng.normal(0.0, 0.4, size=dim)
+            moves.append((R, part, newpos))
+        script += "MOVE %d\n" % nmove
+        for R, part, newpos in moves:
+            script += "%s %d %s\n" % (fmt(R), part, fmt(newpos))
+        rows = run(ref_root, script)
+        ev = np.array(rows["EVAL"])
+        mv = np.array(rows["MOVE"])
+        np.savez(os.path.join(HERE, "eval_%s.npz" % sysd["name"]),
+                 dim=dim, n=n, p=p, L=L, knots=np.zeros(0) if sysd["knots"] is None else sysd["knots"],
+                 sysp=np.array(sysd["sysp"]), time=sysd["time"], uR=uR, uI=uI, phiR=phiR, phiI=phiI,
+                 cfgs=cfgs, ref_nodes=rows["NODES"][0][1:], ref_weights=rows["WEIGHTS"][0][1:],
+                 ref_lnpsi=ev[:, 0], ref_wf=ev[:, 1], ref_O=ev[:, 2:2 + p], ref_ER=ev[:, 2 + p],
+                 ref_EI=ev[:, 3 + p], ref_other=ev[:, 4 + p:13 + p], ref_lj=ev[:, 13 + p],
+                 move_cfg=np.array([m[0] for m in moves]), move_part=np.array([m[1] for m in moves]),
+                 move_new=np.array([m[2] for m in moves]), ref_move=mv)
+        print("eval", sysd["name"], ev.shape, mv.shape)
+
+    # ---- TDVP linear solve (SolveForParametersDot, TDVMC.cpp:1713-1828) ----
+    solve_rows = []
+    for p, seed in ((10, 21), (30, 22)):
+        rng = np.random.default_rng(seed)
+        nsamp = 4 * p
+        O = rng.normal(size=(nsamp, p)) @ rng.normal(size=(p, p)) * 0.3 + rng.normal(size=p) * 2.0
+        ER = rng.normal(size=nsamp) * 0.5 - 3.0 + O[:, 0] * 0.1
+        EI = rng.normal(size=nsamp) * 0.2 + O[:, 1] * 0.05
+        mom = dict(O=O.mean(0), ER=ER.mean(), EI=EI.mean(), OO=O.T @ O / nsamp,
+                   OER=(O * ER[:, None]).mean(0), OEI=(O * EI[:, None]).mean(0))
+        script = system_cmd(3, 8, p, 4.0, None, [0.5, 1.0], 0.0)
+        combos = [(imag, pre, solver) for imag in (0, 1) for pre in (0, 1) for solver in (0, 1)]
+        for imag, pre, solver in combos:
+            script += "SOLVE %d %d %d %s %.17g %.17g %s %s %s\n" % (imag, pre, solver, fmt(mom["O"]), mom["ER"],
+                                                                 mom["EI"], fmt(mom["OO"]), fmt(mom["OER"]),
+                                                                 fmt(mom["OEI"]))
+        rows = run(ref_root, script)["SOLVE"]
+        for (imag, pre, solver), r in zip(combos, rows):
+            solve_rows.append(dict(p=p, imag=imag, pre=pre, solver=solver, mom=mom, out=r))
+    np.savez(os.path.join(HERE, "solve.npz"),
+             p=np.array([r["p"] for r in solve_rows]), imag=np.array([r["imag"] for r in solve_rows]),
+             pre=np.array([r["pre"] for r in solve_rows]), solver=np.array([r["solver"] for r in solve_rows]),
+             **{"O_%d" % i: r["mom"]["O"] for i, r in enumerate(solve_rows)},
+             **{"ER_%d" % i: r["mom"]["ER"] for i, r in enumerate(solve_rows)},
+             **{"EI_%d" % i: r["mom"]["EI"] for i, r in enumerate(solve_rows)},
+             **{"OO_%d" % i: r["mom"]["OO"] for i, r in enumerate(solve_rows)},
+             **{"OER_%d" % i: r["mom"]["OER"] for i, r in enumerate(solve_rows)},
+             **{"OEI_%d" % i: r["mom"]["OEI"] for i, r in enumerate(solve_rows)},
+             **{"out_%d" % i: r["out"] for i, r in enumerate(solve_rows)})
+    print("solve cases", len(solve_rows))
+
+    # ---- sampled averages from the reference's own Metropolis chain ----
+    # 3D, N=27, L=3.6, square well; block averages give the 3-sigma band.
+    dim, n, p, L = 3, 27, 10, 3.6
+    rng = np.random.default_rng(31)
+    r_greville = np.linspace(0.0, L / 2, p)
+    uR = -0.5 * (0.6 / np.maximum(r_greville, 0.25)) ** 5  # McMillan-like ramp
+    uR -= uR[-1]
+    uI = 0.05 * rng.normal(size=p)
+    R0 = lattice(n, dim, L, rng, jitter=0.1) - L / 2
+    nblock, nsamp, ntherm, step = 40, 400, n, 0.35
+    script = system_cmd(dim, n, p, L, None, [0.6, 1.0], 0.0)
+    script += "PARAMS %s %s 0 0\n" % (fmt(uR), fmt(uI))
+    script += "SAMPLE 12345 %.17g %d %d %d %d %s\n" % (step, 50 * n, nsamp, ntherm, nblock, fmt(R0))
+    blocks = np.array(run(ref_root, script)["BLOCK"])
+    np.savez(os.path.join(HERE, "sample_d3_n27.npz"), dim=dim, n=n, p=p, L=L, sysp=np.array([0.6, 1.0]),
+             uR=uR, uI=uI, R0=R0, nblock=nblock, nsamp=nsamp, ntherm=ntherm, step=step, blocks=blocks)
+    print("sample blocks", blocks.shape)
+
+
+if __name__ == "__main__":
+    main()

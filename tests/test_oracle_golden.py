@@ -1,0 +1,158 @@
+"""Pin the FP64 oracle against outputs of the reference itself.
+
+The fixtures in tests/golden/ were produced by the unmodified reference
+sources (oracle/ref/build_ref.sh + oracle/ref/harness.cpp, driven by
+tests/golden/make_golden.py).
+
+Tolerances: the reference evaluates its B-splines from closed-form monomial
+weights in absolute r (SplineFactory.cpp:54-101).  Those weights carry
+rounding errors of order 1e-9 in the spline values themselves, which
+test_reference_weights_roundoff demonstrates through the partition of
+unity; the oracle evaluates the same polynomials in local coordinates
+(exact to ~1e-15).  Agreement with the reference is therefore asserted at
+the level of the reference's own roundoff (RTOL_REF below), and every
+quantity that does not involve the weights (minimum image, knots, solve) is
+asserted at 1e-12 or tighter.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+RTOL_REF = 5e-9
+
+
+def relmax(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def load_system(z):
+    kn = z["knots"] if z["knots"].size else None
+    return orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), user_knots=kn,
+                            pot_kind=orc.POT_SQUARE, pot=z["sysp"], time=float(z["time"]))
+
+
+EVAL_FILES = sorted(glob.glob(os.path.join(GOLD, "eval_*.npz")))
+
+
+def test_nic_known_answers():
+    """The 48 minimum-image checks of src/test/Tests.h:76-156 (tolerance 1e-9 as there)."""
+    z = np.load(os.path.join(GOLD, "nic_kat.npz"))
+    assert len(z["inputs"]) == 48
+    for inp, exp, ref in zip(z["inputs"], z["expected"], z["reference"]):
+        L, dim = inp[0], int(inp[1])
+        ri, rj = inp[2:2 + dim], inp[5:5 + dim]
+        r, d = orc.nic_disp(ri, rj, L)
+        assert abs(r - exp[0]) < 1e-9
+        assert np.all(np.abs(d - exp[1:1 + dim]) < 1e-9)
+        # and bit-for-bit the reference's own output on the same input
+        assert r == ref[0]
+        assert np.array_equal(d, ref[1:1 + dim])
+
+
+@pytest.mark.parametrize("path", EVAL_FILES, ids=[os.path.basename(p)[5:-4] for p in EVAL_FILES])
+def test_knots_and_weights(path):
+    z = np.load(path)
+    s = load_system(z)
+    assert np.array_equal(s.knots(), z["ref_nodes"])
+    W = s.abs_weights().reshape(-1, 4)
+    RW = z["ref_weights"].reshape(-1, 4)
+    scale = np.abs(RW).max(1, keepdims=True)
+    assert (np.abs(W - RW) / scale).max() < 1e-12
+
+
+@pytest.mark.parametrize("path", EVAL_FILES, ids=[os.path.basename(p)[5:-4] for p in EVAL_FILES])
+def test_reference_weights_roundoff(path):
+    """Partition of unity: the oracle's local pieces are exact to 1e-14; the
+    reference's closed-form weights are not, which bounds parity with it."""
+    z = np.load(path)
+    s = load_system(z)
+    kn = s.knots()
+    loc = s.local_weights()
+    W = z["ref_weights"].reshape(-1, 4, 4).astype(np.longdouble)
+    rng = np.random.default_rng(1)
+    worst_o, worst_r = 0.0, 0.0
+    for r in rng.uniform(1e-6, s.rmax, 2000):
+        b = np.searchsorted(kn, r, side="left") - 1
+        t = (r - kn[b]) / (kn[b + 1] - kn[b])
+        so = sum(np.polyval(loc[b, q][::-1], t) for q in range(4))
+        rl = np.longdouble(r)
+        sr = sum(W[b - q, q, 0] + W[b - q, q, 1] * rl + W[b - q, q, 2] * rl ** 2 + W[b - q, q, 3] * rl ** 3
+                 for q in range(4))
+        worst_o = max(worst_o, abs(so - 1.0))
+        worst_r = max(worst_r, abs(float(sr) - 1.0))
+    assert worst_o < 1e-14
+    assert worst_r < RTOL_REF
+
+
+@pytest.mark.parametrize("path", EVAL_FILES, ids=[os.path.basename(p)[5:-4] for p in EVAL_FILES])
+def test_eval_matches_reference(path):
+    """ln psi, O_k, E_loc and the kinetic partial sums on fixed configurations
+    (BosonsBulk.cpp:179-218, 220-336, 349-458, 522-545)."""
+    z = np.load(path)
+    s = load_system(z)
+    p = int(z["p"])
+    for c, R in enumerate(z["cfgs"]):
+        r = s.eval(z["uR"], z["uI"], R)
+        assert relmax(r["lnpsi"], z["ref_lnpsi"][c]) < RTOL_REF
+        assert relmax(r["O"], z["ref_O"][c]) < RTOL_REF
+        scaleE = max(abs(z["ref_other"][c][0]), abs(z["ref_other"][c][1]), 1.0)
+        assert abs(r["eloc"][0] - z["ref_ER"][c]) < RTOL_REF * scaleE
+        assert abs(r["eloc"][1] - z["ref_EI"][c]) < RTOL_REF * scaleE
+        # other: kineticR, V_int (reference slots 0,1) and the partial sums (slots 4..8)
+        assert abs(r["other"][0] - z["ref_other"][c][0]) < RTOL_REF * scaleE
+        assert r["other"][1] == z["ref_other"][c][1]
+        assert relmax(r["other"][2:7], z["ref_other"][c][4:9]) < RTOL_REF
+        # exponent slot and wf slot of the reference's other-values
+        assert relmax(r["lnpsi"], z["ref_other"][c][3]) < RTOL_REF
+        assert relmax(np.exp(r["lnpsi"] + float(z["phiR"])), z["ref_wf"][c]) < RTOL_REF * max(1.0, abs(r["lnpsi"]))
+        assert r["O"].shape == (p,)
+
+
+@pytest.mark.parametrize("path", EVAL_FILES, ids=[os.path.basename(p)[5:-4] for p in EVAL_FILES])
+def test_lj_pair_sum_matches_reference(path):
+    """Lennard-Jones pair sum (Potentials/LJ.cpp:16-22) over pairs inside the cut-off."""
+    z = np.load(path)
+    kn = z["knots"] if z["knots"].size else None
+    s = orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), user_knots=kn,
+                         pot_kind=orc.POT_LJ, pot=(1.0, 1.0), time=0.0)
+    for c, R in enumerate(z["cfgs"]):
+        r = s.eval(z["uR"], z["uI"], R)
+        assert relmax(r["other"][1], z["ref_lj"][c]) < 1e-12
+
+
+@pytest.mark.parametrize("path", EVAL_FILES, ids=[os.path.basename(p)[5:-4] for p in EVAL_FILES])
+def test_move_matches_reference(path):
+    """Exponent change of a single-particle move (BosonsBulk.cpp:553-657)."""
+    z = np.load(path)
+    s = load_system(z)
+    for R, part, new, ref in zip(z["move_cfg"], z["move_part"], z["move_new"], z["ref_move"]):
+        d = s.move_delta(z["uR"], R, int(part), new)
+        scale = max(abs(ref[0]), abs(ref[1]), 1.0)
+        assert abs(d - (ref[1] - ref[0])) < RTOL_REF * scale
+        assert np.isclose(np.exp(2.0 * d), ref[2], rtol=1e-6)
+
+
+def test_solve_matches_reference():
+    """SolveForParametersDot, Cholesky and QR variants, real and imaginary time,
+    with and without preconditioning (TDVMC.cpp:1713-1828)."""
+    z = np.load(os.path.join(GOLD, "solve.npz"))
+    for i in range(len(z["p"])):
+        p = int(z["p"][i])
+        uR, uI, pR, pI, bad = orc.solve(z["O_%d" % i], z["ER_%d" % i], z["EI_%d" % i], z["OO_%d" % i],
+                                        z["OER_%d" % i], z["OEI_%d" % i], imag=int(z["imag"][i]),
+                                        precond=int(z["pre"][i]), solver=int(z["solver"][i]))
+        out = z["out_%d" % i]
+        tol = 1e-12 if int(z["solver"][i]) == 0 else 1e-9
+        assert relmax(uR, out[:p]) < tol
+        assert relmax(uI, out[p:2 * p]) < tol
+        assert abs(pR - out[2 * p]) < tol * max(1.0, abs(out[2 * p]))
+        assert abs(pI - out[2 * p + 1]) < tol * max(1.0, abs(out[2 * p + 1]))
+        assert bad == bool(out[2 * p + 2])
