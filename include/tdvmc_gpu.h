@@ -1,0 +1,196 @@
+/*
+ * tdvmc_gpu.h -- C ABI of the GB300 (sm_103a) TDVP hot path.
+ *
+ * Drop-in for the batched form of the reference's physics plugin and TDVP
+ * driver step (mathiasgartner/TDVMC):
+ *   - PhysicalSystems::IPhysicalSystem (src/PhysicalSystems/IPhysicalSystem.h:16-123)
+ *     as implemented by PhysicalSystems::BosonsBulk
+ *     (src/PhysicalSystems/BosonsBulk.cpp), evaluated for all walkers at once;
+ *   - the sampling loop DoMetropolisStep / UpdateExpectationValues
+ *     (src/TDVMC.cpp:858-924, 1038-1150);
+ *   - the rank reduction ParallelUpdateExpectationValues (src/TDVMC.cpp:1152-1220,
+ *     src/MPIMethods.h:191-206), here one on-device reduction;
+ *   - SolveForParametersDot and the RK4 integrator (src/TDVMC.cpp:1506-1828,
+ *     1969-2035).
+ *
+ * Conventions: every entry point returns an int status (TDVMC_OK = 0, >0 an
+ * error code, see tdvmc_status_string); no C++ exception crosses the ABI.
+ * Array arguments are HOST pointers with the layouts documented per call;
+ * they are copied to/from device memory on the context's CUDA stream and the
+ * call returns after the copy-out completes.  A context is bound to the
+ * current CUDA device at creation, owns one stream, and is not thread-safe.
+ *
+ * Walker layout: walker-major structure of arrays, x[w][d][i] for walker w,
+ * Cartesian component d < dim and particle i < n (doubles on the host; the
+ * device keeps them in the context precision).
+ */
+#ifndef TDVMC_GPU_H
+#define TDVMC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDVMC_OK 0
+#define TDVMC_ERR_ARG 1        /* invalid argument or size */
+#define TDVMC_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define TDVMC_ERR_NOMEM 3      /* device allocation failed */
+#define TDVMC_ERR_STATE 4      /* call order (e.g. no walkers set) */
+#define TDVMC_ERR_NOT_PD 5     /* Cholesky met a non-positive pivot (reference: doNotAcceptStep) */
+#define TDVMC_ERR_NONFINITE 6  /* a non-finite parameter or energy was produced */
+
+/* arithmetic of the walker / pair kernels */
+#define TDVMC_PREC_FP64 0  /* plain FP64 everywhere */
+#define TDVMC_PREC_MIXED 1 /* FP32 pairs and walkers, 3xTF32 tensor-core S, FP64 centring/solve/RK4 */
+
+/* pair potentials; parameters [a, b, t_quench, a', b'] as BosonsBulk.cpp:237-242 */
+#define TDVMC_POT_NONE 0
+#define TDVMC_POT_SQUARE 1 /* b if r < a           (BosonsBulk.cpp:268-271) */
+#define TDVMC_POT_GAUSS 2  /* b exp(-(r/a)^2 / 2)  (BosonsBulk.cpp:263-265)  */
+#define TDVMC_POT_LJ 3     /* 4 b ((a/r)^12 - (a/r)^6) (Potentials/LJ.cpp:16-22) */
+
+typedef struct tdvmc_ctx tdvmc_ctx;
+
+/* System description: the reference's globals N, DIM, N_PARAM, LBOX
+ * (src/TDVMC.cpp:84-89), SYSTEM_PARAMS, NURBS_GRID (TDVMC.cpp:128-131) and
+ * the compile-time HBAR2_2M (src/Constants.h:12), plus the walker count. */
+typedef struct tdvmc_system_desc {
+	int32_t dim;               /* 1, 2 or 3 */
+	int32_t n;                 /* particles per walker, 2..1024 */
+	int32_t p;                 /* variational parameters (N_PARAM), 4..128 */
+	int32_t n_user_knots;      /* 0: uniform knots on [0, L/2] (BosonsBulk.cpp:61-67) */
+	const double* user_knots;  /* n_user_knots values (SetNodes, BosonsBulk.cpp:35-44); must equal p */
+	double box_length;         /* LBOX */
+	int32_t pot_kind;          /* TDVMC_POT_* */
+	int32_t n_pot;             /* number of entries used in pot[] (2 or 5) */
+	double pot[5];
+	double hbar2_2m;           /* HBAR2_2M; 1.0 in the reference */
+	int32_t precision;         /* TDVMC_PREC_* */
+	int64_t n_walkers;         /* independent Markov chains, >= 1 */
+} tdvmc_system_desc;
+
+/* Walker-mean statistics of the last evaluation, FP64.  The moments are the
+ * reference's accumulators (TDVMC.cpp:147-153) after ReduceToAverage, with S
+ * and the force already centred (S_kl = <O_k O_l> - <O_k><O_l>). */
+typedef struct tdvmc_stats {
+	int64_t n_walkers;
+	double energy_re, energy_im;   /* <E^R>, <E^I> */
+	double other[9];               /* otherExpectationValues (BosonsBulk.cpp:449-457) */
+	double accept_rate;            /* accepted / proposed moves of the last sampling pass */
+	int32_t status;                /* TDVMC_OK or TDVMC_ERR_NOT_PD / NONFINITE of the last solve */
+	int32_t reserved;
+} tdvmc_stats;
+
+/* Options of one TDVP step. */
+typedef struct tdvmc_step_opts {
+	double dt;                 /* TIMESTEP */
+	int32_t imaginary_time;    /* IMAGINARY_TIME: 0 real, 1 imaginary */
+	int32_t ode_solver;        /* ODE_SOLVER_TYPE: 0 Euler, 2 RK4 */
+	int32_t lin_solver;        /* LINEAR_EQUATION_SOLVER_TYPE: 0 Cholesky (+1e-3 I) */
+	int32_t precondition;      /* USE_PRECONDITIONING */
+	int32_t normalize_wf;      /* USE_NORMALIZE_WF: phiR <- -ln psi of walker 0 */
+	int32_t moves_per_stage;   /* single-particle moves per walker per sampling pass (MC_NTHERMSTEPS) */
+	double mc_step;            /* MC_STEP: Gaussian displacement width */
+	uint64_t seed;             /* Philox key */
+	int32_t use_adjoint;       /* also compute <dE_loc/d alpha> each stage */
+	int32_t reserved;
+} tdvmc_step_opts;
+
+const char* tdvmc_status_string(int status);
+
+/* Create / destroy.  Replaces IPhysicalSystem construction + InitSystem
+ * (BosonsBulk.cpp:8-156) for n_walkers walkers.  Fails with TDVMC_ERR_ARG
+ * on the parameter-count mismatch that makes the reference exit
+ * (BosonsBulk.cpp:85-91). */
+int tdvmc_create(const tdvmc_system_desc* desc, tdvmc_ctx** out);
+int tdvmc_destroy(tdvmc_ctx* ctx);
+/* the context's CUDA stream (cudaStream_t), for callers that time or order work */
+int tdvmc_get_stream(tdvmc_ctx* ctx, void** stream);
+
+/* IPhysicalSystem::SetTime (IPhysicalSystem.h:70): selects the quench branch
+ * of the pair potential (BosonsBulk.cpp:239-242). */
+int tdvmc_set_time(tdvmc_ctx* ctx, double time);
+
+/* Parameters uR[p], uI[p], phiR, phiI (BroadcastNewParameters, TDVMC.cpp:506-512). */
+int tdvmc_set_params(tdvmc_ctx* ctx, const double* uR, const double* uI, double phiR, double phiI);
+int tdvmc_get_params(tdvmc_ctx* ctx, double* uR, double* uI, double* phiR, double* phiI);
+
+/* Walker coordinates, layout x[w][d][i] (nw = n_walkers). */
+int tdvmc_set_walkers(tdvmc_ctx* ctx, const double* x, int64_t nw);
+int tdvmc_get_walkers(tdvmc_ctx* ctx, double* x, int64_t nw);
+
+/* `moves` single-particle Metropolis moves per walker (DoMetropolisStep,
+ * TDVMC.cpp:858-916) with the current parameters.  Random numbers: Philox
+ * with key `seed` and counter {move, walker, pass, call}.  *accepted (may be
+ * NULL) receives the total number of accepted moves. */
+int tdvmc_sample(tdvmc_ctx* ctx, int32_t moves, double mc_step, uint64_t seed, uint32_t pass, int64_t* accepted);
+
+/* Forward evaluation at the current walkers (CalculateWavefunction +
+ * CalculateExpectationValues, BosonsBulk.cpp:179-545).  Outputs (any may be
+ * NULL): lnpsi[nw]; O[nw*p] walker-major; eloc[nw*2] = (E^R, E^I);
+ * other7[nw*7] = {kineticR, V_int, sumR1, sumI1, sumR2, sumI2, sumR1I1}. */
+int tdvmc_eval_local(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, double* other7);
+
+/* Backward: the same forward pass plus one reverse sweep over the pairs,
+ * giving dE[nw*p*2] = (Re, Im) of dE_loc/d uR_k (holomorphic: d/d uI_k is
+ * i times it).  Minimum-image distances are recomputed, no pair table is
+ * stored.  No counterpart exists in the reference (its force is the SR
+ * covariance only, TDVMC.cpp:1527-1528). */
+int tdvmc_eval_local_adjoint(tdvmc_ctx* ctx, double* dE);
+
+/* Walker-mean reduction of the last evaluation (ParallelUpdateExpectationValues,
+ * TDVMC.cpp:1152-1220).  Optional outputs: O_mean[p], S[p*p] (centred),
+ * cov_OER[p], cov_OEI[p], dE_mean[2p] (zeros unless the last evaluation was
+ * the adjoint one). */
+int tdvmc_reduce_stats(tdvmc_ctx* ctx, tdvmc_stats* stats, double* O_mean, double* S, double* cov_OER,
+                       double* cov_OEI, double* dE_mean);
+
+/* SolveForParametersDot (TDVMC.cpp:1713-1828) on the last reduction.
+ * Returns TDVMC_ERR_NOT_PD (with the outputs filled as the reference would)
+ * when the Cholesky met a non-positive pivot. */
+int tdvmc_tdvp_rhs(tdvmc_ctx* ctx, int32_t imaginary_time, int32_t precondition, int32_t lin_solver,
+                   double* uDotR, double* uDotI, double* phiDotR, double* phiDotI);
+
+/* One TDVP time step (CalculateNextParameters with ODE_SOLVER_TYPE 0 or 2,
+ * TDVMC.cpp:1834-1858, 1969-2035, including the stage-1 sampling of the main
+ * loop, TDVMC.cpp:3656): each stage is one CUDA-graph launch of
+ * sample -> evaluate (+adjoint) -> reduce -> solve.  Parameters are updated
+ * on the device; `stats` (may be NULL) receives the statistics of the first
+ * stage, which the reference records per step (TDVMC.cpp:3748-3755).  The
+ * Philox pass counter advances by one per stage. */
+int tdvmc_step(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, tdvmc_stats* stats);
+
+/* `nsteps` steps back to back without host synchronisation (benchmarking
+ * and long runs); statistics of the last step's first stage in *stats. */
+int tdvmc_run_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, int32_t nsteps, tdvmc_stats* stats);
+
+/* Run `nsteps` steps as tdvmc_run_steps and return the device time between
+ * two CUDA events recorded on the context stream around them (*ms).  For
+ * benchmarking; no reference counterpart (the reference times whole steps
+ * on the host, TDVMC.cpp:3400-3423). */
+int tdvmc_time_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, int32_t nsteps, float* ms);
+
+/* Run ONE stage of a step eagerly (no graph) with a CUDA event pair around
+ * every kernel; ms[i] receives the duration of kernel i and names[i] (may be
+ * NULL) a static name.  *count receives the number of kernels (<= 16).
+ * The stage advances the state like a graph launch would. */
+int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, float* ms, const char** names, int32_t* count);
+
+/* Choose the group width (lanes per walker) and walkers per block of the
+ * sampling and evaluation kernels by timing the candidates on the current
+ * walkers.  Results are kept in the context. */
+int tdvmc_autotune(tdvmc_ctx* ctx, int32_t moves, double mc_step);
+/* Report the chosen tiles: lanes per walker and walkers per block of the
+ * sampler and the evaluation kernels. */
+int tdvmc_get_tiles(tdvmc_ctx* ctx, int32_t* sample_lanes, int32_t* sample_walkers_per_block,
+                    int32_t* eval_lanes, int32_t* eval_walkers_per_block);
+
+/* Number of kernel launches issued by this context since creation. */
+int64_t tdvmc_launch_count(tdvmc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -76,6 +76,8 @@ def lib():
         L.orc_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_double, C.c_double,
                                 _dp, _dp, _dp, _dp, _dp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_solve.restype = C.c_int
+        L.orc_solve_centred.argtypes = L.orc_solve.argtypes
+        L.orc_solve_centred.restype = C.c_int
         _lib = L
     return _lib
 
@@ -196,6 +198,20 @@ def solve(O, ER, EI, OO, OER, OEI, imag=0, precond=0, solver=0):
     return uR, uI, pR.value, pI.value, bool(bad)
 
 
+def solve_centred(O, ER, EI, S, covOER, covOEI, imag=0, precond=0, solver=0):
+    """The solve from centred moments (S, cov(O,E^R), cov(O,E^I))."""
+    P = len(O)
+    uR = np.zeros(P)
+    uI = np.zeros(P)
+    pR = C.c_double(0.0)
+    pI = C.c_double(0.0)
+    bad = lib().orc_solve_centred(P, int(imag), int(precond), int(solver), np.ascontiguousarray(O, dtype=np.float64),
+                                  float(ER), float(EI), np.ascontiguousarray(S, dtype=np.float64).reshape(-1),
+                                  np.ascontiguousarray(covOER, dtype=np.float64),
+                                  np.ascontiguousarray(covOEI, dtype=np.float64), uR, uI, C.byref(pR), C.byref(pI))
+    return uR, uI, pR.value, pI.value, bool(bad)
+
+
 def moments(O, eloc):
     """Raw sample moments as accumulated in UpdateExpectationValues (TDVMC.cpp:1103-1108)."""
     O = np.asarray(O, dtype=np.float64)
@@ -204,6 +220,18 @@ def moments(O, eloc):
     n = O.shape[0]
     return dict(O=O.mean(0), ER=ER.mean(), EI=EI.mean(), OO=O.T @ O / n,
                 OER=(O * ER[:, None]).mean(0), OEI=(O * EI[:, None]).mean(0))
+
+
+def centred(O, eloc):
+    """Two-pass centred moments: <O>, <E^R>, <E^I>, S, cov(O,E^R), cov(O,E^I)."""
+    O = np.asarray(O, dtype=np.float64)
+    E = np.asarray(eloc, dtype=np.float64)
+    n = O.shape[0]
+    Om = O.mean(0)
+    Em = E.mean(0)
+    Oc = O - Om
+    Ec = E - Em
+    return dict(O=Om, ER=Em[0], EI=Em[1], S=Oc.T @ Oc / n, cOER=Oc.T @ Ec[:, 0] / n, cOEI=Oc.T @ Ec[:, 1] / n)
 
 
 def rk4_combine(u, k, dt):

@@ -579,8 +579,9 @@ static int64_t sample_walker(const orc_sys* s, const double* uR, double* R, int 
 		double nn;
 		double enew = move_exponent(s, uR, &st, R, p, R + p * D, xnew, Snew, &nn);
 		double delta = enew - st.exponent;
-		/* TDVMC.cpp:886-915: exp(2 delta) >= U accepts; non-finite rejects */
-		if (isfinite(delta) && 2.0 * delta >= log(U))
+		/* TDVMC.cpp:886-915: exp(2 delta) >= U accepts; a non-finite quotient,
+		 * including exp overflow beyond log(DBL_MAX), rejects */
+		if (isfinite(delta) && 2.0 * delta >= log(U) && 2.0 * delta < 709.782712893384)
 		{
 			for (int a = 0; a < D; a++) R[p * D + a] = xnew[a];
 			memcpy(st.S, Snew, (size_t)ns * sizeof(double));
@@ -770,6 +771,9 @@ static void lu_solve(int P, const double* A, const double* b, double* x)
 	free(m);
 }
 
+static int solve_core(int P, int imag, int precond, int solver, const double* O, double ER, double* m, double* fr,
+                      double* fi, double* uDotR, double* uDotI, double* phiDotR, double* phiDotI);
+
 int orc_solve(int P, int imag, int precond, int solver, const double* O, double ER, double EI,
               const double* OO, const double* OER, const double* OEI,
               double* uDotR, double* uDotI, double* phiDotR, double* phiDotI)
@@ -777,8 +781,6 @@ int orc_solve(int P, int imag, int precond, int solver, const double* O, double 
 	double* m = (double*)malloc((size_t)P * P * sizeof(double));
 	double* fr = (double*)malloc((size_t)P * sizeof(double));
 	double* fi = (double*)malloc((size_t)P * sizeof(double));
-	double* sc = (double*)malloc((size_t)P * sizeof(double));
-	int bad = 0;
 	for (int i = 0; i < P; i++)
 	{
 		if (imag == 0)
@@ -797,6 +799,46 @@ int orc_solve(int P, int imag, int precond, int solver, const double* O, double 
 			m[j * P + i] = m[i * P + j];
 		}
 	}
+	int bad = solve_core(P, imag, precond, solver, O, ER, m, fr, fi, uDotR, uDotI, phiDotR, phiDotI);
+	free(m);
+	free(fr);
+	free(fi);
+	return bad;
+}
+
+int orc_solve_centred(int P, int imag, int precond, int solver, const double* O, double ER, double EI,
+                      const double* S, const double* covOER, const double* covOEI,
+                      double* uDotR, double* uDotI, double* phiDotR, double* phiDotI)
+{
+	double* m = (double*)malloc((size_t)P * P * sizeof(double));
+	double* fr = (double*)malloc((size_t)P * sizeof(double));
+	double* fi = (double*)malloc((size_t)P * sizeof(double));
+	for (int i = 0; i < P; i++)
+	{
+		if (imag == 0)
+		{
+			fr[i] = covOEI[i];
+			fi[i] = -covOER[i];
+		}
+		else
+		{
+			fr[i] = -covOER[i];
+			fi[i] = -(covOEI[i] + O[i] * EI);
+		}
+		for (int j = 0; j < P; j++) m[i * P + j] = S[i * P + j];
+	}
+	int bad = solve_core(P, imag, precond, solver, O, ER, m, fr, fi, uDotR, uDotI, phiDotR, phiDotI);
+	free(m);
+	free(fr);
+	free(fi);
+	return bad;
+}
+
+static int solve_core(int P, int imag, int precond, int solver, const double* O, double ER, double* m, double* fr,
+                      double* fi, double* uDotR, double* uDotI, double* phiDotR, double* phiDotI)
+{
+	double* sc = (double*)malloc((size_t)P * sizeof(double));
+	int bad = 0;
 	if (precond)
 	{
 		for (int i = 0; i < P; i++) sc[i] = sqrt(m[i * P + i]);
@@ -852,9 +894,6 @@ int orc_solve(int P, int imag, int precond, int solver, const double* O, double 
 			uDotR[i] /= sc[i];
 			uDotI[i] /= sc[i];
 		}
-	free(m);
-	free(fr);
-	free(fi);
 	free(sc);
 	return bad;
 }

@@ -86,12 +86,19 @@ int64_t orc_stage_threads(const orc_sys* s, const double* uR, const double* uI, 
 
 /* TDVP linear solve from raw sample moments, as SolveForParametersDot
  * (TDVMC.cpp:1506-1537, 1560-1622, 1658-1682, 1684-1711, 1713-1828).
- * solver 0: Cholesky (+1e-3 I); solver 1: pivoted Householder QR with the
- * mean of the solution subtracted.  Returns 1 when the Cholesky met a
+ * solver 0: Cholesky (+1e-3 I); solver 1: the reference solves with Eigen's
+ * FullPivHouseholderQR and subtracts the mean of the solution; here a dense
+ * elimination with partial pivoting gives the same unique solution of the
+ * nonsingular system, then the mean is subtracted.  Returns 1 when the Cholesky met a
  * non-positive pivot (the reference's doNotAcceptStep), else 0. */
 int orc_solve(int p, int imag, int precond, int solver, const double* O, double ER, double EI,
               const double* OO, const double* OER, const double* OEI,
               double* uDotR, double* uDotI, double* phiDotR, double* phiDotI);
+
+/* The same solve from centred moments: S (p*p), cov(O, E^R), cov(O, E^I). */
+int orc_solve_centred(int p, int imag, int precond, int solver, const double* O, double ER, double EI,
+                      const double* S, const double* covOER, const double* covOEI,
+                      double* uDotR, double* uDotI, double* phiDotR, double* phiDotI);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,174 @@
+// Device building blocks shared by the TDVP kernels: system constants,
+// minimum image, knot-interval location, Philox random numbers and
+// compensated sums.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tdvmc {
+
+constexpr int kMaxBins = 128;   // knot intervals on [0, r_max] (p - 1 for uniform knots)
+constexpr int kMaxSplines = 130;
+constexpr int kMaxP = 128;
+constexpr int kMaxLut = 1024;   // non-uniform knots: interval lookup cells
+constexpr double kLogDblMax = 709.782712893384;  // log(DBL_MAX): exp(2 delta) overflows beyond
+
+// Static description of a system, passed by value to every kernel.
+struct SysConst {
+	int n;        // particles per walker
+	int dim;      // 1..3 (coordinates beyond dim are zero)
+	int p;        // parameters
+	int ns;       // splines = p + 2
+	int nbin;     // knot intervals on [0, r_max]
+	int uniform;  // 1: equal interval widths
+	int ncell;    // non-uniform: lookup cells
+	int pot_kind;
+	double L, Lr;
+	double rmax;
+	double hinv;      // uniform: 1 / interval width
+	double cell_inv;  // non-uniform: 1 / lookup cell width
+	double hbar2_2m;
+};
+
+// Values that change between stages or steps live in device memory so a
+// captured CUDA graph stays valid: stage parameters, derived spline
+// coefficients, potential branch and the Philox pass counter.
+struct DynState {
+	double pa, pb;      // active potential parameters (after the quench rule)
+	uint32_t pass;      // Philox pass counter of the next sampling pass
+	uint32_t stage;     // RK stage being computed
+	int32_t status;     // OR of TDVMC_ERR_* flags of the solves since last read
+	int32_t pad;
+};
+
+// Minimum image of one Cartesian difference with the reference's rounding:
+// k = (int)(x / L + (x >= 0 ? 0.5 : -0.5)) (Utils.cpp:266-281).  The 1e-10
+// nudge at exactly +-L/2 of the reference is not applied (it changes r by
+// 1e-10 on a set of measure zero).
+__device__ __forceinline__ float nic(float d, float L, float Lr) {
+	float k = truncf(fmaf(d, Lr, copysignf(0.5f, d)));
+	return fmaf(-k, L, d);
+}
+__device__ __forceinline__ double nic(double d, double L, double Lr) {
+	double k = trunc(fma(d, Lr, copysign(0.5, d)));
+	return fma(-k, L, d);
+}
+
+__device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_(double x) { return rsqrt(x); }
+
+// Interval lookup over [0, r_max]: returns j (interval index; knot k_{j+3})
+// and the local coordinate t in [0, 1].  kb[j] = left knot, hv[j] = 1/width,
+// lut[c] = first candidate interval of lookup cell c (non-uniform grids).
+template <typename T>
+__device__ __forceinline__ int locate(const SysConst& s, T r, const T* kb, const T* hv, const int* lut, T& t) {
+	if (s.uniform) {
+		T x = r * (T)s.hinv;
+		int j = (int)x;
+		j = j < s.nbin - 1 ? j : s.nbin - 1;
+		t = x - (T)j;
+		return j;
+	}
+	int c = (int)(r * (T)s.cell_inv);
+	c = c < s.ncell - 1 ? c : s.ncell - 1;
+	int j = lut[c];
+	if (j + 1 < s.nbin && r >= kb[j + 1]) j++;
+	if (j + 1 < s.nbin && r >= kb[j + 1]) j++;
+	t = (r - kb[j]) * hv[j];
+	return j;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
+#pragma unroll
+	for (int r = 0; r < 10; r++) {
+		uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+		uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+		c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+		k.x += 0x9E3779B9u;
+		k.y += 0xBB67AE85u;
+	}
+	return c;
+}
+
+// uniform (0,1) from 32 random bits
+__device__ __forceinline__ double u01d(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+__device__ __forceinline__ float u01f(uint32_t x) { return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f); }
+
+// Random numbers of one Metropolis move: particle, acceptance uniform and
+// three standard normals (Box-Muller); the same assignment of Philox words
+// as the oracle.
+template <typename T> struct MoveRand {
+	int part;
+	T u, z0, z1, z2;
+};
+
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double& c, double& s) {
+	double rho = sqrt(-2.0 * log(u01d(a)));
+	double sn, cs;
+	sincospi(2.0 * u01d(b), &sn, &cs);
+	c = rho * cs;
+	s = rho * sn;
+}
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& c, float& s) {
+	float rho = sqrtf(-2.0f * logf(u01f(a)));
+	float sn, cs;
+	sincospif(2.0f * u01f(b), &sn, &cs);
+	c = rho * cs;
+	s = rho * sn;
+}
+__device__ __forceinline__ double uacc(uint32_t x, double) { return u01d(x); }
+__device__ __forceinline__ float uacc(uint32_t x, float) { return u01f(x); }
+
+template <typename T>
+__device__ __forceinline__ MoveRand<T> move_rand(uint32_t move, uint32_t walker, uint32_t pass, uint2 key, int n, int dim) {
+	MoveRand<T> m;
+	uint4 a = philox(make_uint4(move, walker, pass, 0u), key);
+	m.part = (int)__umulhi(a.x, (uint32_t)n);
+	m.u = uacc(a.y, T(0));
+	T c, s;
+	box_muller(a.z, a.w, c, s);
+	m.z0 = c;
+	m.z1 = dim > 1 ? s : T(0);
+	m.z2 = T(0);
+	if (dim > 2) {
+		uint4 b = philox(make_uint4(move, walker, pass, 1u), key);
+		T c2, s2;
+		box_muller(b.x, b.y, c2, s2);
+		m.z2 = c2;
+	}
+	return m;
+}
+
+// Kahan-compensated running sum.
+template <typename T> struct KSum {
+	T s, c;
+	__device__ __forceinline__ KSum() : s(0), c(0) {}
+	__device__ __forceinline__ void add(T x) {
+		T y = x - c;
+		T t = s + y;
+		c = (t - s) - y;
+		s = t;
+	}
+	__device__ __forceinline__ T value() const { return s - c; }
+};
+
+// pair potential (a, b from the quench rule): BosonsBulk.cpp:263-271, LJ.cpp:16-22
+template <typename T>
+__device__ __forceinline__ T pair_pot(int kind, T r, T rinv, T a, T b) {
+	if (kind == 1) return r < a ? b : T(0);
+	if (kind == 2) {
+		T x = r / a;
+		return b * exp(-(x * x) * T(0.5));
+	}
+	if (kind == 3) {
+		T s2 = a * rinv;
+		s2 = s2 * s2;
+		T s6 = s2 * s2 * s2;
+		return T(4) * b * s6 * (s6 - T(1));
+	}
+	return T(0);
+}
+
+}  // namespace tdvmc

@@ -1,0 +1,32 @@
+// Kernel dispatch tables; the template instantiations live in the
+// inst_*.cu translation units so the library builds in parallel.
+#pragma once
+
+#include "common.cuh"
+#include "k_sample.cuh"
+
+namespace tdvmc {
+
+template <typename T>
+using SampleFn = void (*)(SysConst, const Q4<T>*, const T*, const T*, const T*, const int*, T*, int64_t, int, T, uint2,
+                          const uint32_t*, int*);
+template <typename T>
+using ElocFn = void (*)(SysConst, const DynState*, const Q4<T>*, const T*, const T*, const int*, const T*,
+                        const double*, const double*, const T*, int64_t, T*, T*, T*, T*, T*);
+
+// register slots per lane available for `lanes` lanes per walker
+int sample_slots_for(int n, int lanes);
+
+SampleFn<float> pick_sample_f32(int lanes, int slots);
+SampleFn<double> pick_sample_f64(int lanes, int slots);
+ElocFn<float> pick_eloc_f32(int lanes, bool adj);
+ElocFn<double> pick_eloc_f64(int lanes, bool adj);
+
+template <typename T> SampleFn<T> pick_sample(int lanes, int slots);
+template <> inline SampleFn<float> pick_sample<float>(int g, int s) { return pick_sample_f32(g, s); }
+template <> inline SampleFn<double> pick_sample<double>(int g, int s) { return pick_sample_f64(g, s); }
+template <typename T> ElocFn<T> pick_eloc(int lanes, bool adj);
+template <> inline ElocFn<float> pick_eloc<float>(int g, bool a) { return pick_eloc_f32(g, a); }
+template <> inline ElocFn<double> pick_eloc<double>(int g, bool a) { return pick_eloc_f64(g, a); }
+
+}  // namespace tdvmc

@@ -1,0 +1,18 @@
+#include "dispatch.cuh"
+#define TDVMC_T float
+#define TDVMC_FN pick_sample_f32
+#include "inst_sample.inc"
+namespace tdvmc {
+int sample_slots_for(int n, int G) {
+	static const int l32[] = {1, 2, 4, 8, 11, 16, 32};
+	static const int l16[] = {1, 2, 4, 8};
+	static const int l8[] = {1, 2, 4};
+	const int need = (n + G - 1) / G;
+	const int* l = G == 32 ? l32 : (G == 16 ? l16 : l8);
+	const int m = G == 32 ? 7 : (G == 16 ? 4 : 3);
+	if (G != 32 && G != 16 && G != 8) return -1;
+	for (int i = 0; i < m; i++)
+		if (l[i] >= need) return l[i];
+	return -1;
+}
+}  // namespace tdvmc

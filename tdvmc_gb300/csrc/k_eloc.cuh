@@ -1,0 +1,361 @@
+// Per-walker local quantities of the pair-spline Jastrow wave function:
+// ln psi, O_k = d ln psi / d uR_k (BC-folded spline sums), the complex local
+// energy with its kinetic partial sums, and optionally the adjoint
+// dE_loc / d alpha_k.  Follows BosonsBulk::CalculateLocalOperators,
+// CalculateOtherLocalOperators and CalculateExpectationValues
+// (BosonsBulk.cpp:179-218, 220-336, 349-458, 522-545).
+//
+// One group of G lanes owns one walker.  Forward sweep: lane l owns row
+// particle n = s*G + l of slot s and loops over all partners i (the partner
+// coordinate is a shared-memory broadcast), accumulating the complex
+// gradient G_n and Laplacian of ln psi in registers with compensated block
+// sums.  Pair statistics that are linear in the spline basis (O_k, and for
+// the adjoint the alpha-independent Laplacian of O_k) are accumulated as
+// per-interval moments sum t^c (and sum t^c / r) in lane-private shared
+// histograms; partners below the slot base are counted once per unordered
+// pair with warp-uniform control flow (the diagonal block is the only mixed
+// region).  Reverse sweep (adjoint): one pass over unordered pairs that
+// recomputes minimum-image distances and accumulates sum t^c g with
+// g = (G_n - G_i) . rhat_ni; no pair table is stored.  Moments are turned
+// into spline values with the local piece polynomials and folded to the p
+// parameters at the end.
+#pragma once
+
+#include "common.cuh"
+#include "k_sample.cuh"
+
+namespace tdvmc {
+
+constexpr int kFwdMoments = 4;     // sum t^c, c = 0..3
+constexpr int kFwdMomentsAdj = 7;  // + sum t^c / r, c = 0..2
+constexpr int kRevMoments = 6;     // complex sum g t^c, c = 0..2
+
+// Shared memory layout:
+//   CTA:   coefC[2*nbin] (uR, uI cubics) | kb[nbin] | hv[nbin] | lut[ncell]
+//   group: xs[n] | Gs[n*6] (adjoint) | hist[nbin*NM*G] | red[nbin*NMtot] | spl[ns*4] | misc[16]
+template <typename T>
+__host__ __device__ inline size_t eloc_cta_bytes(int nbin, int ncell) {
+	size_t b = 2 * (size_t)nbin * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+	return (b + 31) & ~(size_t)31;
+}
+template <typename T>
+__host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G, bool adj) {
+	int nm = adj ? kFwdMomentsAdj : kFwdMoments;
+	int nmh = nm > kRevMoments ? nm : kRevMoments;
+	size_t b = (size_t)n * sizeof(Q4<T>);
+	if (adj) b += (size_t)n * 6 * sizeof(T);
+	b += (size_t)nbin * nmh * G * sizeof(T);
+	b += (size_t)nbin * (nm + (adj ? kRevMoments : 0)) * sizeof(T);
+	b += (size_t)ns * 4 * sizeof(T) + 16 * sizeof(T);
+	return (b + 31) & ~(size_t)31;
+}
+
+template <typename T, int G>
+__device__ __forceinline__ T group_sum(T v, unsigned gmask) {
+#pragma unroll
+	for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o, G);
+	return v;
+}
+
+// Pair kernel of the forward sweep for partners [i0, i1).
+// ON: 0 = no pair statistics, 1 = all lanes count the pair, 2 = count iff i < nrow.
+template <typename T, int G, int ON, bool ADJ>
+__device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
+                                           const Q4<T>* xs, const Q4<T>* coefC, const T* kb, const T* hv,
+                                           const int* lut, T* hist, int lane, T pa, T pb,
+                                           KSum<T>* acc /* gRx gRy gRz gIx gIy gIz lR lI */, KSum<T>& vsum, int& nout) {
+	constexpr int NM = ADJ ? kFwdMomentsAdj : kFwdMoments;
+	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax, dm1 = (T)(sc.dim - 1);
+	for (int c0 = i0; c0 < i1; c0 += 32) {
+		const int c1 = (c0 + 32 < i1) ? c0 + 32 : i1;
+		T a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+		T vb = T(0);
+		for (int i = c0; i < c1; i++) {
+			const Q4<T> xi = xs[i];
+			const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
+			const T r2 = dx * dx + dy * dy + dz * dz;
+			const T rinv = rsqrt_(r2);
+			const T r = r2 * rinv;
+			const bool notself = (i != nrow);
+			const bool in = rowok && notself && (r <= rmax);
+			T t;
+			const int j = locate<T>(sc, r, kb, hv, lut, t);
+			const Q4<T> cR = coefC[2 * j];
+			const Q4<T> cI = coefC[2 * j + 1];
+			const T hj = sc.uniform ? (T)sc.hinv : hv[j];
+			const T d1R = (cR.y + t * (T(2) * cR.z + T(3) * t * cR.w)) * hj;
+			const T d1I = (cI.y + t * (T(2) * cI.z + T(3) * t * cI.w)) * hj;
+			const T d2R = (T(2) * cR.z + T(6) * t * cR.w) * (hj * hj);
+			const T d2I = (T(2) * cI.z + T(6) * t * cI.w) * (hj * hj);
+			const T gR = in ? d1R * rinv : T(0);
+			const T gI = in ? d1I * rinv : T(0);
+			a[0] += gR * dx;
+			a[1] += gR * dy;
+			a[2] += gR * dz;
+			a[3] += gI * dx;
+			a[4] += gI * dy;
+			a[5] += gI * dz;
+			a[6] += in ? d2R + dm1 * gR : T(0);
+			a[7] += in ? d2I + dm1 * gI : T(0);
+			if (ON != 0) {
+				const bool cnt = (ON == 1) ? true : (i < nrow);
+				const bool on = in && cnt;
+				const T one = on ? T(1) : T(0);
+				const T ts = on ? t : T(0);  // t is NaN for the self pair
+				const T t2 = ts * ts;
+				T* hp = hist + (size_t)j * NM * G + lane;
+				hp[0 * G] += one;
+				hp[1 * G] += ts;
+				hp[2 * G] += t2;
+				hp[3 * G] += t2 * ts;
+				if (ADJ) {
+					const T q = on ? rinv : T(0);
+					hp[4 * G] += q;
+					hp[5 * G] += q * ts;
+					hp[6 * G] += q * t2;
+				}
+				vb += on ? pair_pot<T>(sc.pot_kind, r, rinv, pa, pb) : T(0);
+				nout += (rowok && notself && cnt && !(r <= rmax)) ? 1 : 0;
+			}
+		}
+#pragma unroll
+		for (int k = 0; k < 8; k++) acc[k].add(a[k]);
+		if (ON != 0) vsum.add(vb);
+	}
+}
+
+// Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1).
+template <typename T, int G, bool DIAG>
+__device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
+                                           const T* gn, const Q4<T>* xs, const T* Gs, const T* kb, const T* hv,
+                                           const int* lut, T* hist, int lane) {
+	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax;
+	for (int i = i0; i < i1; i++) {
+		const Q4<T> xi = xs[i];
+		const T* gi = Gs + (size_t)i * 6;
+		const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
+		const T r2 = dx * dx + dy * dy + dz * dz;
+		const T rinv = rsqrt_(r2);
+		const T r = r2 * rinv;
+		const bool on = rowok && (r <= rmax) && (DIAG ? (i < nrow) : true);
+		T t;
+		const int j = locate<T>(sc, r, kb, hv, lut, t);
+		t = on ? t : T(0);  // t is NaN for the self pair
+		const T s = on ? rinv : T(0);
+		const T gR = ((gn[0] - gi[0]) * dx + (gn[1] - gi[1]) * dy + (gn[2] - gi[2]) * dz) * s;
+		const T gI = ((gn[3] - gi[3]) * dx + (gn[4] - gi[4]) * dy + (gn[5] - gi[5]) * dz) * s;
+		T* hp = hist + (size_t)j * kRevMoments * G + lane;
+		hp[0 * G] += gR;
+		hp[1 * G] += gR * t;
+		hp[2 * G] += gR * t * t;
+		hp[3 * G] += gI;
+		hp[4 * G] += gI * t;
+		hp[5 * G] += gI * t * t;
+	}
+}
+
+// Sum lane-private histograms [nbin][nm][G] into red[nbin*nm] and clear them.
+template <typename T, int G>
+__device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, int lane, unsigned gmask) {
+	__syncwarp(gmask);
+	for (int e = lane; e < nbin * nm; e += G) {
+		T* hp = hist + (size_t)e * G;
+		T s = T(0);
+#pragma unroll 8
+		for (int l = 0; l < G; l++) s += hp[l];
+		red[e] = s;
+	}
+	__syncwarp(gmask);
+	for (int e = lane; e < nbin * nm * G; e += G) hist[e] = T(0);
+	__syncwarp(gmask);
+}
+
+template <typename T, int G, bool ADJ>
+__global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
+                                              const T* __restrict__ kb_g, const T* __restrict__ hv_g,
+                                              const int* __restrict__ lut_g, const T* __restrict__ loc_g,
+                                              const double* __restrict__ fold_g, const double* __restrict__ params,
+                                              const T* __restrict__ pos, int64_t nw, T* __restrict__ lnpsi_o,
+                                              T* __restrict__ O_o, T* __restrict__ eloc_o, T* __restrict__ other_o,
+                                              T* __restrict__ dE_o) {
+	constexpr int NM = ADJ ? kFwdMomentsAdj : kFwdMoments;
+	constexpr int NMH = NM > kRevMoments ? NM : kRevMoments;
+	extern __shared__ __align__(32) unsigned char smem_raw[];
+	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
+	Q4<T>* coefC = reinterpret_cast<Q4<T>*>(smem_raw);
+	T* kb = reinterpret_cast<T*>(coefC + 2 * nbin);
+	T* hv = kb + nbin;
+	int* lut = reinterpret_cast<int*>(hv + nbin);
+	const size_t cta_b = eloc_cta_bytes<T>(nbin, sc.ncell);
+	const size_t grp_b = eloc_group_bytes<T>(n, nbin, ns, G, ADJ);
+
+	for (int i = threadIdx.x; i < 2 * nbin; i += blockDim.x) coefC[i] = coefC_g[i];
+	for (int i = threadIdx.x; i < nbin; i += blockDim.x) {
+		kb[i] = kb_g[i];
+		hv[i] = hv_g[i];
+	}
+	for (int i = threadIdx.x; i < sc.ncell; i += blockDim.x) lut[i] = lut_g[i];
+
+	const int tid = threadIdx.x;
+	const int lane = tid & (G - 1);
+	const int gib = tid / G;
+	const int gpb = blockDim.x / G;
+	const unsigned wl = tid & 31;
+	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
+	unsigned char* gbase = smem_raw + cta_b + (size_t)gib * grp_b;
+	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
+	T* Gs = reinterpret_cast<T*>(xs + n);
+	T* hist = Gs + (ADJ ? (size_t)n * 6 : 0);
+	T* red = hist + (size_t)nbin * NMH * G;
+	T* redr = red + (size_t)nbin * NM;
+	T* spl = redr + (ADJ ? (size_t)nbin * kRevMoments : 0);  // [ns][4]: S, Lsp, AR, AI
+	T* misc = spl + (size_t)ns * 4;
+
+	for (int e = lane; e < nbin * NMH * G; e += G) hist[e] = T(0);
+	__syncthreads();
+
+	const T pa = (T)dyn->pa, pb = (T)dyn->pb;
+	const int nslot = (n + G - 1) / G;
+
+	for (int64_t w = (int64_t)blockIdx.x * gpb + gib; w < nw; w += (int64_t)gridDim.x * gpb) {
+		const T* pw = pos + (size_t)w * sc.dim * n;
+		for (int i = lane; i < n; i += G) {
+			T x0 = pw[i];
+			T x1 = sc.dim > 1 ? pw[n + i] : T(0);
+			T x2 = sc.dim > 2 ? pw[2 * n + i] : T(0);
+			xs[i] = Q4<T>{x0, x1, x2, T(0)};
+		}
+		__syncwarp(gmask);
+
+		KSum<T> e_r1, e_i1, e_r1i1, e_lR, e_lI, e_v;
+		int nout = 0;
+		for (int s = 0; s < nslot; s++) {
+			const int nrow = s * G + lane;
+			const bool rowok = nrow < n;
+			const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
+			KSum<T> acc[8];
+			const int base = s * G;
+			const int dend = (base + G < n) ? base + G : n;
+			fwd_region<T, G, 1, ADJ>(sc, 0, base, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			fwd_region<T, G, 2, ADJ>(sc, base, dend, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			fwd_region<T, G, 0, ADJ>(sc, dend, n, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			const T gRx = acc[0].value(), gRy = acc[1].value(), gRz = acc[2].value();
+			const T gIx = acc[3].value(), gIy = acc[4].value(), gIz = acc[5].value();
+			if (rowok) {
+				e_r1.add(gRx * gRx + gRy * gRy + gRz * gRz);
+				e_i1.add(gIx * gIx + gIy * gIy + gIz * gIz);
+				e_r1i1.add(T(2) * (gRx * gIx + gRy * gIy + gRz * gIz));
+				e_lR.add(acc[6].value());
+				e_lI.add(acc[7].value());
+				if (ADJ) {
+					T* g = Gs + (size_t)nrow * 6;
+					g[0] = gRx;
+					g[1] = gRy;
+					g[2] = gRz;
+					g[3] = gIx;
+					g[4] = gIy;
+					g[5] = gIz;
+				}
+			}
+		}
+		// group totals (compensated per lane, then a butterfly over lanes)
+		T sR1 = group_sum<T, G>(e_r1.value(), gmask);
+		T sI1 = group_sum<T, G>(e_i1.value(), gmask);
+		T sR1I1 = group_sum<T, G>(e_r1i1.value(), gmask);
+		T sR2 = group_sum<T, G>(e_lR.value(), gmask);
+		T sI2 = group_sum<T, G>(e_lI.value(), gmask);
+		T vint = group_sum<T, G>(e_v.value(), gmask);
+		int nout_all = nout;
+#pragma unroll
+		for (int o = G / 2; o > 0; o >>= 1) nout_all += __shfl_xor_sync(gmask, nout_all, o, G);
+
+		hist_reduce<T, G>(hist, red, nbin, NM, lane, gmask);
+
+		if (ADJ) {
+			for (int s = 0; s < nslot; s++) {
+				const int nrow = s * G + lane;
+				const bool rowok = nrow < n;
+				const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
+				T gn[6] = {0, 0, 0, 0, 0, 0};
+				if (rowok)
+					for (int k = 0; k < 6; k++) gn[k] = Gs[(size_t)nrow * 6 + k];
+				const int base = s * G;
+				const int dend = (base + G < n) ? base + G : n;
+				rev_region<T, G, false>(sc, 0, base, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
+				rev_region<T, G, true>(sc, base, dend, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
+			}
+			hist_reduce<T, G>(hist, redr, nbin, kRevMoments, lane, gmask);
+		}
+
+		// moments -> spline values: spline sp = j + 3 - q on interval j
+		const T dm1 = (T)(sc.dim - 1);
+		for (int sp = lane; sp < ns; sp += G) {
+			T S = T(0), Lsp = T(0), AR = T(0), AI = T(0);
+#pragma unroll
+			for (int q = 0; q < 4; q++) {
+				const int j = sp - 3 + q;
+				if (j < 0 || j >= nbin) continue;
+				const T* l = loc_g + ((size_t)j * 4 + q) * 4;
+				const T l0 = l[0], l1 = l[1], l2 = l[2], l3 = l[3];
+				const T* m = red + (size_t)j * NM;
+				S += l0 * m[0] + l1 * m[1] + l2 * m[2] + l3 * m[3];
+				if (ADJ) {
+					const T hj = sc.uniform ? (T)sc.hinv : hv[j];
+					Lsp += T(2) * (hj * hj * (T(2) * l2 * m[0] + T(6) * l3 * m[1]) +
+					               dm1 * hj * (l1 * m[4] + T(2) * l2 * m[5] + T(3) * l3 * m[6]));
+					const T* g = redr + (size_t)j * kRevMoments;
+					AR += hj * (l1 * g[0] + T(2) * l2 * g[1] + T(3) * l3 * g[2]);
+					AI += hj * (l1 * g[3] + T(2) * l2 * g[4] + T(3) * l3 * g[5]);
+				}
+			}
+			spl[sp * 4 + 0] = S;
+			spl[sp * 4 + 1] = Lsp;
+			spl[sp * 4 + 2] = AR;
+			spl[sp * 4 + 3] = AI;
+		}
+		__syncwarp(gmask);
+		// fold to the p parameters; ln psi in FP64 (BosonsBulk.cpp:522-539)
+		const double c = sc.hbar2_2m;
+		double lnp = 0.0;
+		for (int k = lane; k < P; k += G) {
+			double Ok = 0.0, dR = 0.0, dI = 0.0;
+			for (int sp = 0; sp < ns; sp++) {
+				const double f = fold_g[(size_t)k * ns + sp];
+				if (f == 0.0) continue;
+				Ok += f * (double)spl[sp * 4 + 0];
+				if (ADJ) {
+					dR += f * (2.0 * (double)spl[sp * 4 + 2] + (double)spl[sp * 4 + 1]);
+					dI += f * (2.0 * (double)spl[sp * 4 + 3]);
+				}
+			}
+			O_o[(size_t)w * P + k] = (T)Ok;
+			if (ADJ) {
+				dE_o[((size_t)w * P + k) * 2 + 0] = (T)(-c * dR);
+				dE_o[((size_t)w * P + k) * 2 + 1] = (T)(-c * dI);
+			}
+			lnp += params[k] * Ok;
+		}
+#pragma unroll
+		for (int o = G / 2; o > 0; o >>= 1) lnp += __shfl_xor_sync(gmask, lnp, o, G);
+		if (lane == 0) {
+			lnp += params[P - 1] * (double)nout_all;
+			const double kinR = -((double)sR1 - (double)sI1 + (double)sR2) * c;
+			const double kinI = -((double)sR1I1 + (double)sI2) * c;
+			lnpsi_o[w] = (T)lnp;
+			eloc_o[2 * w + 0] = (T)(kinR + (double)vint);
+			eloc_o[2 * w + 1] = (T)kinI;
+			T* ot = other_o + (size_t)w * 7;
+			ot[0] = (T)kinR;
+			ot[1] = vint;
+			ot[2] = sR1;
+			ot[3] = sI1;
+			ot[4] = sR2;
+			ot[5] = sI2;
+			ot[6] = sR1I1;
+		}
+		__syncwarp(gmask);
+	}
+	(void)misc;
+}
+
+}  // namespace tdvmc

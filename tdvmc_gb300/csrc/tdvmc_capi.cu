@@ -1,0 +1,979 @@
+// C ABI of the GB300 TDVP hot path: context, device tables, kernel dispatch,
+// CUDA-graph capture of the RK stages.  Declarations and the reference
+// interface each entry point replaces: include/tdvmc_gpu.h.
+#include "../../include/tdvmc_gpu.h"
+
+#include "common.cuh"
+#include "dispatch.cuh"
+#include "k_eloc.cuh"
+#include "k_gram_tf32.cuh"
+#include "k_sample.cuh"
+#include "k_solve.cuh"
+#include "k_stats.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+using namespace tdvmc;
+
+namespace {
+
+struct Tiles {
+	int sg = 32;     // sampler lanes per walker
+	int sgpb = 4;    // sampler walkers per block
+	int eg = 32;     // evaluation lanes per walker
+	int egpb = 1;    // evaluation walkers per block
+};
+
+struct GraphKey {
+	double dt, mc_step;
+	int imag, ode, lin, pre, norm, moves, adj;
+	uint64_t seed;
+	bool operator<(const GraphKey& o) const {
+		return std::tie(dt, mc_step, imag, ode, lin, pre, norm, moves, adj, seed) <
+		       std::tie(o.dt, o.mc_step, o.imag, o.ode, o.lin, o.pre, o.norm, o.moves, o.adj, o.seed);
+	}
+};
+
+}  // namespace
+
+struct tdvmc_ctx {
+	SysConst sc{};
+	int prec = TDVMC_PREC_FP64;
+	int64_t nw = 0;
+	int device = 0;
+	int nsm = 0;
+	cudaStream_t st = nullptr;
+	std::vector<double> knots, loc, fold, pot;
+	int npot = 0;
+	double time = 0.0;
+	Tiles tiles;
+	bool have_walkers = false;
+	bool have_eval = false;
+	bool last_adj = false;
+	int last_moves = 0;
+	int64_t launches = 0;
+	// device buffers (T = float or double by precision)
+	void *pos = nullptr, *lnpsi = nullptr, *O = nullptr, *eloc = nullptr, *other7 = nullptr, *dE = nullptr;
+	int* acc = nullptr;
+	double *base = nullptr, *stage = nullptr, *kdot = nullptr, *rhs = nullptr;
+	double *loc_d = nullptr, *fold_d = nullptr;
+	void *coefU = nullptr, *coefC = nullptr, *uout = nullptr, *kb = nullptr, *hv = nullptr, *locT = nullptr;
+	int* lut = nullptr;
+	double *part1 = nullptr, *means1 = nullptr, *means0 = nullptr, *part2 = nullptr, *C2 = nullptr;
+	float* partS = nullptr;
+	double* Sg = nullptr;
+	void* gramws = nullptr;
+	DynState* dyn = nullptr;
+	int nblk1 = 0, nblk2 = 0, chunk2 = 0, nblkS = 0;
+	std::map<GraphKey, cudaGraphExec_t> graphs;
+	std::string err;
+	// eager profiling: events recorded after every kernel when set
+	std::vector<cudaEvent_t>* prof = nullptr;
+	std::vector<const char*>* prof_names = nullptr;
+};
+
+namespace {
+
+#define CK(call)                                                                  \
+	do {                                                                          \
+		cudaError_t e_ = (call);                                                  \
+		if (e_ != cudaSuccess) {                                                  \
+			if (ctx) ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_); \
+			return TDVMC_ERR_CUDA;                                                \
+		}                                                                         \
+	} while (0)
+
+// ---------------------------------------------------------------------------
+// host-side spline tables (same construction as BosonsBulk::InitSystem and
+// SplineFactory::GetWeights3, evaluated in local interval coordinates)
+// ---------------------------------------------------------------------------
+void poly_lin(const double* a, double c0, double c1, double* out) {
+	double o[4] = {0, 0, 0, 0};
+	for (int i = 0; i < 4; i++) {
+		o[i] += a[i] * c0;
+		if (i + 1 < 4) o[i + 1] += a[i] * c1;
+	}
+	for (int i = 0; i < 4; i++) out[i] = o[i];
+}
+
+// polynomial in t of B-spline N_{s,3} on knot interval b
+void piece_local(const std::vector<double>& k, int s, int b, double* out) {
+	double N[4][4][4];
+	std::memset(N, 0, sizeof(N));
+	const double h = k[b + 1] - k[b];
+	for (int i = 0; i < 4; i++)
+		if (s + i == b) N[0][i][0] = 1.0;
+	for (int d = 1; d <= 3; d++)
+		for (int i = 0; i + d <= 3; i++) {
+			const int ii = s + i;
+			double acc[4] = {0, 0, 0, 0}, tmp[4];
+			const double den1 = k[ii + d] - k[ii], den2 = k[ii + d + 1] - k[ii + 1];
+			if (den1 != 0.0) {
+				poly_lin(N[d - 1][i], (k[b] - k[ii]) / den1, h / den1, tmp);
+				for (int c = 0; c < 4; c++) acc[c] += tmp[c];
+			}
+			if (den2 != 0.0) {
+				poly_lin(N[d - 1][i + 1], (k[ii + d + 1] - k[b]) / den2, -h / den2, tmp);
+				for (int c = 0; c < 4; c++) acc[c] += tmp[c];
+			}
+			std::memcpy(N[d][i], acc, sizeof(acc));
+		}
+	std::memcpy(out, N[3][0], 4 * sizeof(double));
+}
+
+size_t tsize(int prec) { return prec == TDVMC_PREC_FP64 ? sizeof(double) : sizeof(float); }
+
+void apply_quench(tdvmc_ctx* c, double& a, double& b) {
+	a = c->npot > 0 ? c->pot[0] : 0.0;
+	b = c->npot > 1 ? c->pot[1] : 0.0;
+	if (c->npot > 4 && c->time >= c->pot[2]) {
+		a = c->pot[3];
+		b = c->pot[4];
+	}
+}
+
+// ---------------------------------------------------------------------------
+// kernel dispatch (instantiations in inst_*.cu)
+// ---------------------------------------------------------------------------
+int slots_for(int n, int G) { return sample_slots_for(n, G); }
+
+void mark(tdvmc_ctx* ctx, const char* name) {
+	if (!ctx->prof) return;
+	cudaEvent_t e;
+	cudaEventCreate(&e);
+	cudaEventRecord(e, ctx->st);
+	ctx->prof->push_back(e);
+	ctx->prof_names->push_back(name);
+}
+
+int grid_for(tdvmc_ctx* ctx, const void* fn, int threads, size_t smem, int64_t work_groups, int gpb) {
+	int per_sm = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+	if (per_sm < 1) per_sm = 1;
+	int64_t need = (work_groups + gpb - 1) / gpb;
+	int64_t g = (int64_t)per_sm * ctx->nsm;
+	return (int)std::max<int64_t>(1, std::min(need, g));
+}
+
+template <typename T>
+int launch_prep(tdvmc_ctx* ctx) {
+	k_prep<T><<<1, 128, 0, ctx->st>>>(ctx->sc.p, ctx->sc.ns, ctx->sc.nbin, ctx->stage, ctx->fold_d, ctx->loc_d,
+	                                  (T*)ctx->coefU, (T*)ctx->coefC, (T*)ctx->uout);
+	ctx->launches++;
+	mark(ctx, "k_prep");
+	CK(cudaGetLastError());
+	return TDVMC_OK;
+}
+
+template <typename T>
+int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed) {
+	const int G = ctx->tiles.sg, gpb = ctx->tiles.sgpb;
+	const int slots = slots_for(ctx->sc.n, G);
+	SampleFn<T> fn = pick_sample<T>(G, slots);
+	if (!fn) return TDVMC_ERR_ARG;
+	const int threads = G * gpb;
+	const size_t smem = sample_smem_bytes<T>(ctx->sc.nbin, ctx->sc.ncell, ctx->sc.n, gpb);
+	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, gpb);
+	uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+	fn<<<grid, threads, smem, ctx->st>>>(ctx->sc, (const Q4<T>*)ctx->coefU, (const T*)ctx->uout, (const T*)ctx->kb,
+	                                     (const T*)ctx->hv, ctx->lut, (T*)ctx->pos, ctx->nw, moves, (T)step, key,
+	                                     &ctx->dyn->pass, ctx->acc);
+	ctx->launches++;
+	mark(ctx, "k_sample");
+	CK(cudaGetLastError());
+	return TDVMC_OK;
+}
+
+template <typename T>
+size_t eloc_smem(tdvmc_ctx* ctx, int G, int gpb, bool adj) {
+	return eloc_cta_bytes<T>(ctx->sc.nbin, ctx->sc.ncell) +
+	       (size_t)gpb * eloc_group_bytes<T>(ctx->sc.n, ctx->sc.nbin, ctx->sc.ns, G, adj);
+}
+
+template <typename T>
+int launch_eloc(tdvmc_ctx* ctx, bool adj) {
+	const int G = ctx->tiles.eg, gpb = ctx->tiles.egpb;
+	ElocFn<T> fn = pick_eloc<T>(G, adj);
+	if (!fn) return TDVMC_ERR_ARG;
+	const int threads = G * gpb;
+	const size_t smem = eloc_smem<T>(ctx, G, gpb, adj);
+	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, gpb);
+	fn<<<grid, threads, smem, ctx->st>>>(ctx->sc, ctx->dyn, (const Q4<T>*)ctx->coefC, (const T*)ctx->kb,
+	                                     (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT, ctx->fold_d, ctx->stage,
+	                                     (const T*)ctx->pos, ctx->nw, (T*)ctx->lnpsi, (T*)ctx->O, (T*)ctx->eloc,
+	                                     (T*)ctx->other7, (T*)ctx->dE);
+	ctx->launches++;
+	mark(ctx, adj ? "k_eloc_adjoint" : "k_eloc");
+	CK(cudaGetLastError());
+	return TDVMC_OK;
+}
+
+template <typename T>
+int launch_reduce(tdvmc_ctx* ctx, bool adj) {
+	const int P = ctx->sc.p;
+	Cols1 c{P};
+	const int K1 = c.count();
+	k_reduce1<T><<<ctx->nblk1, 256, 0, ctx->st>>>(P, ctx->nw, (const T*)ctx->O, (const T*)ctx->eloc,
+	                                               (const T*)ctx->other7, (const T*)ctx->lnpsi, ctx->acc,
+	                                               (const T*)ctx->dE, adj ? 1 : 0, ctx->stage, ctx->part1);
+	mark(ctx, "k_reduce1");
+	k_finalize<<<1, 256, 0, ctx->st>>>(K1, ctx->nblk1, ctx->part1, 1.0 / (double)ctx->nw, ctx->means1);
+	mark(ctx, "k_finalize1");
+	ctx->launches += 2;
+	CK(cudaGetLastError());
+	const bool tc = (ctx->prec == TDVMC_PREC_MIXED) && gram_supported(P);
+	const size_t sm2 = (size_t)ctx->chunk2 * (P + 2) * sizeof(double);
+	CK(cudaFuncSetAttribute((const void*)k_reduce2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+	k_reduce2<T><<<ctx->nblk2, 256, sm2, ctx->st>>>(P, ctx->nw, ctx->chunk2, (const T*)ctx->O, (const T*)ctx->eloc,
+	                                                 ctx->means1, tc ? 0 : 1, ctx->part2);
+	mark(ctx, "k_reduce2");
+	k_finalize<<<1, 256, 0, ctx->st>>>(P * (P + 2), ctx->nblk2, ctx->part2, 1.0 / (double)ctx->nw, ctx->C2);
+	mark(ctx, "k_finalize2");
+	ctx->launches += 2;
+	CK(cudaGetLastError());
+	if (tc) {
+		int rc = launch_gram_tf32(ctx->st, P, ctx->nw, (const float*)ctx->O, ctx->means1, ctx->nblkS, ctx->partS,
+		                          ctx->Sg, ctx->nsm);
+		ctx->launches += 2;
+		mark(ctx, "k_gram_tf32+finalize");
+		if (rc) {
+			ctx->err = "gram launch failed";
+			return TDVMC_ERR_CUDA;
+		}
+		CK(cudaGetLastError());
+	}
+	return TDVMC_OK;
+}
+
+template <typename T>
+int launch_solve(tdvmc_ctx* ctx, int imag, int pre, int lin, int mode, int norm, double dt) {
+	const int P = ctx->sc.p;
+	SolveArgs a;
+	a.p = P;
+	a.imag = imag;
+	a.precond = pre;
+	a.solver = lin;
+	a.mode = mode;
+	a.normalize = norm;
+	a.dt = dt;
+	const bool tc = (ctx->prec == TDVMC_PREC_MIXED) && gram_supported(P);
+	const double* S = tc ? ctx->Sg : ctx->C2;
+	a.ldS = tc ? P : P + 2;
+	a.ldC = P + 2;
+	const size_t smem = (size_t)(P * (P + 2) + 6 * P + 8) * sizeof(double);
+	CK(cudaFuncSetAttribute((const void*)k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	Cols1 c{P};
+	k_solve<T><<<1, 256, smem, ctx->st>>>(a, ctx->dyn, ctx->means1, S, ctx->C2 + P, (const T*)ctx->lnpsi, ctx->base,
+	                                       ctx->stage, ctx->kdot, ctx->rhs, ctx->means0, c.count());
+	ctx->launches++;
+	mark(ctx, "k_solve");
+	CK(cudaGetLastError());
+	return TDVMC_OK;
+}
+
+template <typename T>
+int run_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
+	int rc;
+	if ((rc = launch_prep<T>(ctx))) return rc;
+	if (o->moves_per_stage > 0 && (rc = launch_sample<T>(ctx, o->moves_per_stage, o->mc_step, o->seed))) return rc;
+	if ((rc = launch_eloc<T>(ctx, o->use_adjoint != 0))) return rc;
+	if ((rc = launch_reduce<T>(ctx, o->use_adjoint != 0))) return rc;
+	return launch_solve<T>(ctx, o->imaginary_time, o->precondition, o->lin_solver, o->ode_solver == 0 ? 2 : 1,
+	                       o->normalize_wf, o->dt);
+}
+
+int run_stage_any(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
+	return ctx->prec == TDVMC_PREC_FP64 ? run_stage<double>(ctx, o) : run_stage<float>(ctx, o);
+}
+
+int check_opts(const tdvmc_step_opts* o) {
+	if (!o || !(o->dt == o->dt)) return TDVMC_ERR_ARG;
+	if (o->ode_solver != 0 && o->ode_solver != 2) return TDVMC_ERR_ARG;
+	if (o->lin_solver != 0 && o->lin_solver != 1) return TDVMC_ERR_ARG;
+	if (o->moves_per_stage < 0) return TDVMC_ERR_ARG;
+	return TDVMC_OK;
+}
+
+int get_graph(tdvmc_ctx* ctx, const tdvmc_step_opts* o, cudaGraphExec_t* out) {
+	GraphKey k{o->dt, o->mc_step, o->imaginary_time, o->ode_solver, o->lin_solver, o->precondition,
+	           o->normalize_wf, o->moves_per_stage, o->use_adjoint, o->seed};
+	auto it = ctx->graphs.find(k);
+	if (it != ctx->graphs.end()) {
+		*out = it->second;
+		return TDVMC_OK;
+	}
+	cudaGraph_t g;
+	CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+	const int64_t l0 = ctx->launches;
+	int rc = run_stage_any(ctx, o);
+	cudaError_t e = cudaStreamEndCapture(ctx->st, &g);
+	ctx->launches = l0;  // counted when the graph runs
+	if (rc) return rc;
+	if (e != cudaSuccess) {
+		ctx->err = cudaGetErrorString(e);
+		return TDVMC_ERR_CUDA;
+	}
+	cudaGraphExec_t ex;
+	CK(cudaGraphInstantiate(&ex, g, 0));
+	cudaGraphDestroy(g);
+	ctx->graphs[k] = ex;
+	*out = ex;
+	return TDVMC_OK;
+}
+
+int kernels_per_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
+	int k = 1 + (o->moves_per_stage > 0 ? 1 : 0) + 1 + 4 + 1;
+	if (ctx->prec == TDVMC_PREC_MIXED && gram_supported(ctx->sc.p)) k += 2;
+	return k;
+}
+
+template <typename T>
+int copy_out(tdvmc_ctx* ctx, const void* dsrc, double* host, size_t count) {
+	if (!host) return TDVMC_OK;
+	std::vector<T> tmp(count);
+	CK(cudaMemcpyAsync(tmp.data(), dsrc, count * sizeof(T), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	for (size_t i = 0; i < count; i++) host[i] = (double)tmp[i];
+	return TDVMC_OK;
+}
+
+int copy_out_any(tdvmc_ctx* ctx, const void* d, double* h, size_t n) {
+	return ctx->prec == TDVMC_PREC_FP64 ? copy_out<double>(ctx, d, h, n) : copy_out<float>(ctx, d, h, n);
+}
+
+void fill_stats(tdvmc_ctx* ctx, const std::vector<double>& m, int moves, tdvmc_stats* s) {
+	const int P = ctx->sc.p;
+	Cols1 c{P};
+	s->n_walkers = ctx->nw;
+	s->energy_re = m[c.ER()];
+	s->energy_im = m[c.EI()];
+	const int o = c.other();
+	s->other[0] = m[o + 0];  // kineticR
+	s->other[1] = m[o + 1];  // V_int
+	s->other[2] = m[c.wf()];
+	s->other[3] = m[c.lnpsi()];
+	s->other[4] = m[o + 2];
+	s->other[5] = m[o + 3];
+	s->other[6] = m[o + 4];
+	s->other[7] = m[o + 5];
+	s->other[8] = m[o + 6];
+	s->accept_rate = moves > 0 ? m[c.acc()] / (double)moves : 0.0;
+}
+
+int read_status(tdvmc_ctx* ctx, int32_t* status) {
+	DynState d;
+	CK(cudaMemcpyAsync(&d, ctx->dyn, sizeof(DynState), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	*status = d.status;
+	if (d.status) {
+		int32_t zero = 0;
+		CK(cudaMemcpyAsync(&ctx->dyn->status, &zero, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->st));
+		CK(cudaStreamSynchronize(ctx->st));
+	}
+	return TDVMC_OK;
+}
+
+int status_code(int32_t st) {
+	if (st & kStatusNonFinite) return TDVMC_ERR_NONFINITE;
+	if (st & kStatusNotPD) return TDVMC_ERR_NOT_PD;
+	return TDVMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tdvmc_status_string(int s) {
+	switch (s) {
+	case TDVMC_OK: return "ok";
+	case TDVMC_ERR_ARG: return "invalid argument";
+	case TDVMC_ERR_CUDA: return "CUDA error";
+	case TDVMC_ERR_NOMEM: return "out of device memory";
+	case TDVMC_ERR_STATE: return "invalid call order";
+	case TDVMC_ERR_NOT_PD: return "S matrix not positive definite";
+	case TDVMC_ERR_NONFINITE: return "non-finite parameters";
+	}
+	return "unknown status";
+}
+
+int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
+	tdvmc_ctx* ctx = nullptr;
+	if (!d || !out) return TDVMC_ERR_ARG;
+	*out = nullptr;
+	if (d->dim < 1 || d->dim > 3 || d->n < 2 || d->n > 1024 || d->p < 4 || d->p > kMaxP || d->n_walkers < 1 ||
+	    !(d->box_length > 0) || (d->precision != TDVMC_PREC_FP64 && d->precision != TDVMC_PREC_MIXED) ||
+	    d->n_walkers > 0x7fffffffLL)
+		return TDVMC_ERR_ARG;
+	if (d->n_user_knots > 0 && (d->user_knots == nullptr || d->n_user_knots != d->p)) return TDVMC_ERR_ARG;
+	if (d->n_pot < 0 || d->n_pot > 5) return TDVMC_ERR_ARG;
+	ctx = new tdvmc_ctx();
+	tdvmc_ctx& c = *ctx;
+	c.prec = d->precision;
+	c.nw = d->n_walkers;
+	c.pot.assign(d->pot, d->pot + 5);
+	c.npot = d->n_pot;
+	const int P = d->p;
+	// knots: BosonsBulk.cpp:61-67 (uniform) or SetNodes mirroring (35-44)
+	if (d->n_user_knots > 0) {
+		const int K = d->n_user_knots;
+		for (int i = 0; i < 3; i++) c.knots.push_back(-d->user_knots[3 - i]);
+		for (int i = 0; i < K; i++) c.knots.push_back(d->user_knots[i]);
+		for (int i = 0; i < 3; i++) c.knots.push_back(2.0 * d->user_knots[K - 1] - d->user_knots[K - 2 - i]);
+		for (size_t i = 1; i < c.knots.size(); i++)
+			if (!(c.knots[i] > c.knots[i - 1])) {
+				delete ctx;
+				return TDVMC_ERR_ARG;
+			}
+	} else {
+		const double half = d->box_length / 2.0;
+		for (int i = -3; i < P + 3; i++) c.knots.push_back(((double)i * half) / ((double)P - 1.0));
+	}
+	const int nk = (int)c.knots.size();
+	SysConst& s = c.sc;
+	s.n = d->n;
+	s.dim = d->dim;
+	s.p = P;
+	s.ns = nk - 4;
+	s.nbin = nk - 7;
+	s.rmax = c.knots[nk - 4];
+	s.L = d->box_length;
+	s.Lr = 1.0 / d->box_length;
+	s.hbar2_2m = d->hbar2_2m;
+	s.pot_kind = d->pot_kind;
+	if (s.ns - 2 != P || s.nbin > kMaxBins) {
+		delete ctx;
+		return TDVMC_ERR_ARG;
+	}
+	// local piece polynomials loc[j][q][c]: spline j+3-q on interval j (knot j+3)
+	c.loc.assign((size_t)s.nbin * 16, 0.0);
+	for (int j = 0; j < s.nbin; j++)
+		for (int q = 0; q < 4; q++) piece_local(c.knots, j + 3 - q, j + 3, &c.loc[((size_t)j * 4 + q) * 4]);
+	// boundary-condition fold (uniform factors: SplineFactory.cpp:423-439, 563-579)
+	c.fold.assign((size_t)P * s.ns, 0.0);
+	const double bcs[2][3] = {{0, 1, 0}, {1, 0, 1}};
+	const double bce[2][3] = {{1, 0, 1}, {0, 1, 0}};
+	for (int i = 0; i < 2; i++)
+		for (int j = 0; j < 3; j++) c.fold[(size_t)i * s.ns + j] = bcs[i][j];
+	for (int i = 2, sp = 3; i < P - 2; i++, sp++) c.fold[(size_t)i * s.ns + sp] = 1.0;
+	for (int i = P - 2, idx = 0; i < P; i++, idx++)
+		for (int j = 0; j < 3; j++) c.fold[(size_t)i * s.ns + s.ns - 3 + j] = bce[idx][j];
+	// interval geometry
+	std::vector<double> kb(s.nbin), hv(s.nbin);
+	double hmin = 1e300, hmaxw = 0.0;
+	for (int j = 0; j < s.nbin; j++) {
+		kb[j] = c.knots[j + 3];
+		const double h = c.knots[j + 4] - c.knots[j + 3];
+		hv[j] = 1.0 / h;
+		hmin = std::min(hmin, h);
+		hmaxw = std::max(hmaxw, h);
+	}
+	s.uniform = (hmaxw - hmin) <= 1e-12 * hmaxw ? 1 : 0;
+	s.hinv = hv[0];
+	std::vector<int> lut;
+	if (!s.uniform) {
+		const double span = s.rmax - kb[0];
+		double cell = hmin / 2.0;
+		int ncell = (int)std::ceil(s.rmax / cell) + 1;
+		if (ncell > kMaxLut || kb[0] < 0.0 || span <= 0) {
+			delete ctx;
+			return TDVMC_ERR_ARG;
+		}
+		s.ncell = ncell;
+		s.cell_inv = 1.0 / cell;
+		lut.resize(ncell);
+		for (int ci = 0; ci < ncell; ci++) {
+			const double r = ci * cell;
+			int j = 0;
+			while (j + 1 < s.nbin && kb[j + 1] <= r) j++;
+			lut[ci] = j;
+		}
+	} else {
+		s.ncell = 0;
+		s.cell_inv = 0.0;
+	}
+
+	cudaGetDevice(&c.device);
+	cudaDeviceGetAttribute(&c.nsm, cudaDevAttrMultiProcessorCount, c.device);
+	if (cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) != cudaSuccess) {
+		delete ctx;
+		return TDVMC_ERR_CUDA;
+	}
+	const size_t ts = tsize(c.prec);
+	const int64_t nw = c.nw;
+	const int np = 2 * P + 2;
+	Cols1 cols{P};
+	const int K1 = cols.count();
+	c.nblk1 = (int)std::min<int64_t>(std::max<int64_t>(1, (nw + 63) / 64), 4 * (int64_t)c.nsm);
+	c.chunk2 = (int)std::max<int64_t>(1, std::min<int64_t>(128, (96 * 1024) / ((P + 2) * 8)));
+	c.nblk2 = (int)((nw + c.chunk2 - 1) / c.chunk2);
+	c.nblkS = gram_blocks(nw, c.nsm);
+	bool ok = true;
+	auto A = [&](void** p, size_t bytes) {
+		if (!ok) return;
+		if (cudaMalloc(p, bytes) != cudaSuccess) ok = false;
+	};
+	A(&c.pos, (size_t)nw * d->dim * d->n * ts);
+	A(&c.lnpsi, (size_t)nw * ts);
+	A(&c.O, (size_t)nw * P * ts);
+	A(&c.eloc, (size_t)nw * 2 * ts);
+	A(&c.other7, (size_t)nw * 7 * ts);
+	A(&c.dE, (size_t)nw * 2 * P * ts);
+	A((void**)&c.acc, (size_t)nw * sizeof(int));
+	A((void**)&c.base, np * sizeof(double));
+	A((void**)&c.stage, np * sizeof(double));
+	A((void**)&c.kdot, 4 * np * sizeof(double));
+	A((void**)&c.rhs, np * sizeof(double));
+	A((void**)&c.loc_d, c.loc.size() * sizeof(double));
+	A((void**)&c.fold_d, c.fold.size() * sizeof(double));
+	A(&c.coefU, (size_t)s.nbin * 4 * ts);
+	A(&c.coefC, (size_t)s.nbin * 8 * ts);
+	A(&c.uout, 32);
+	A(&c.kb, (size_t)s.nbin * ts);
+	A(&c.hv, (size_t)s.nbin * ts);
+	A(&c.locT, c.loc.size() * ts);
+	A((void**)&c.lut, (size_t)std::max(1, s.ncell) * sizeof(int));
+	A((void**)&c.part1, (size_t)c.nblk1 * K1 * sizeof(double));
+	A((void**)&c.means1, K1 * sizeof(double));
+	A((void**)&c.means0, K1 * sizeof(double));
+	A((void**)&c.part2, (size_t)c.nblk2 * P * (P + 2) * sizeof(double));
+	A((void**)&c.C2, (size_t)P * (P + 2) * sizeof(double));
+	A((void**)&c.partS, (size_t)c.nblkS * P * P * sizeof(float));
+	A((void**)&c.Sg, (size_t)P * P * sizeof(double));
+	A((void**)&c.dyn, sizeof(DynState));
+	if (!ok) {
+		tdvmc_destroy(ctx);
+		return TDVMC_ERR_NOMEM;
+	}
+	// static tables
+	std::vector<char> kbT(s.nbin * ts), hvT(s.nbin * ts), locT(c.loc.size() * ts);
+	for (int j = 0; j < s.nbin; j++) {
+		if (c.prec == TDVMC_PREC_FP64) {
+			((double*)kbT.data())[j] = kb[j];
+			((double*)hvT.data())[j] = hv[j];
+		} else {
+			((float*)kbT.data())[j] = (float)kb[j];
+			((float*)hvT.data())[j] = (float)hv[j];
+		}
+	}
+	for (size_t i = 0; i < c.loc.size(); i++) {
+		if (c.prec == TDVMC_PREC_FP64) ((double*)locT.data())[i] = c.loc[i];
+		else ((float*)locT.data())[i] = (float)c.loc[i];
+	}
+	DynState dy{};
+	c.time = 0.0;
+	apply_quench(ctx, dy.pa, dy.pb);
+	std::vector<double> zeros((size_t)4 * np, 0.0);
+	bool cp = cudaMemcpy(c.kb, kbT.data(), kbT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.hv, hvT.data(), hvT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.locT, locT.data(), locT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.loc_d, c.loc.data(), c.loc.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.fold_d, c.fold.data(), c.fold.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.dyn, &dy, sizeof(dy), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.base, zeros.data(), np * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.stage, zeros.data(), np * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.kdot, zeros.data(), 4 * np * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemset(c.acc, 0, (size_t)nw * sizeof(int)) == cudaSuccess &&
+	          cudaMemset(c.dE, 0, (size_t)nw * 2 * P * ts) == cudaSuccess;
+	if (cp && s.ncell > 0) cp = cudaMemcpy(c.lut, lut.data(), lut.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
+	if (!cp) {
+		tdvmc_destroy(ctx);
+		return TDVMC_ERR_CUDA;
+	}
+	// default tiles: a full warp per walker from 64 particles up
+	c.tiles.sg = d->n >= 64 ? 32 : (d->n >= 24 ? 16 : 8);
+	if (slots_for(d->n, c.tiles.sg) < 0) c.tiles.sg = 32;
+	if (slots_for(d->n, c.tiles.sg) < 0) {
+		tdvmc_destroy(ctx);
+		return TDVMC_ERR_ARG;
+	}
+	c.tiles.sgpb = 128 / c.tiles.sg;
+	c.tiles.eg = c.tiles.sg;
+	c.tiles.egpb = std::max(1, 32 / c.tiles.eg);
+	*out = ctx;
+	return TDVMC_OK;
+}
+
+int tdvmc_destroy(tdvmc_ctx* ctx) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	if (ctx->st) cudaStreamSynchronize(ctx->st);
+	for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+	void* bufs[] = {ctx->pos, ctx->lnpsi, ctx->O, ctx->eloc, ctx->other7, ctx->dE, ctx->acc, ctx->base, ctx->stage,
+	                ctx->kdot, ctx->rhs, ctx->loc_d, ctx->fold_d, ctx->coefU, ctx->coefC, ctx->uout, ctx->kb, ctx->hv,
+	                ctx->locT, ctx->lut, ctx->part1, ctx->means1, ctx->means0, ctx->part2, ctx->C2, ctx->partS, ctx->Sg,
+	                ctx->dyn, ctx->gramws};
+	for (void* b : bufs)
+		if (b) cudaFree(b);
+	if (ctx->st) cudaStreamDestroy(ctx->st);
+	delete ctx;
+	return TDVMC_OK;
+}
+
+int tdvmc_get_stream(tdvmc_ctx* ctx, void** stream) {
+	if (!ctx || !stream) return TDVMC_ERR_ARG;
+	*stream = (void*)ctx->st;
+	return TDVMC_OK;
+}
+
+int tdvmc_set_time(tdvmc_ctx* ctx, double time) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	ctx->time = time;
+	double ab[2];
+	apply_quench(ctx, ab[0], ab[1]);
+	CK(cudaMemcpyAsync(ctx->dyn, ab, 2 * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	return TDVMC_OK;
+}
+
+int tdvmc_set_params(tdvmc_ctx* ctx, const double* uR, const double* uI, double phiR, double phiI) {
+	if (!ctx || !uR || !uI) return TDVMC_ERR_ARG;
+	const int P = ctx->sc.p;
+	std::vector<double> v(2 * P + 2);
+	std::copy(uR, uR + P, v.begin());
+	std::copy(uI, uI + P, v.begin() + P);
+	v[2 * P] = phiR;
+	v[2 * P + 1] = phiI;
+	CK(cudaMemcpyAsync(ctx->base, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+	CK(cudaMemcpyAsync(ctx->stage, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+	uint32_t zero = 0;
+	CK(cudaMemcpyAsync(&ctx->dyn->stage, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	return TDVMC_OK;
+}
+
+int tdvmc_get_params(tdvmc_ctx* ctx, double* uR, double* uI, double* phiR, double* phiI) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	const int P = ctx->sc.p;
+	std::vector<double> v(2 * P + 2);
+	CK(cudaMemcpyAsync(v.data(), ctx->base, v.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	if (uR) std::copy(v.begin(), v.begin() + P, uR);
+	if (uI) std::copy(v.begin() + P, v.begin() + 2 * P, uI);
+	if (phiR) *phiR = v[2 * P];
+	if (phiI) *phiI = v[2 * P + 1];
+	return TDVMC_OK;
+}
+
+int tdvmc_set_walkers(tdvmc_ctx* ctx, const double* x, int64_t nw) {
+	if (!ctx || !x || nw != ctx->nw) return TDVMC_ERR_ARG;
+	const size_t cnt = (size_t)nw * ctx->sc.dim * ctx->sc.n;
+	if (ctx->prec == TDVMC_PREC_FP64) {
+		CK(cudaMemcpyAsync(ctx->pos, x, cnt * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+		CK(cudaStreamSynchronize(ctx->st));
+	} else {
+		std::vector<float> f(cnt);
+		for (size_t i = 0; i < cnt; i++) f[i] = (float)x[i];
+		CK(cudaMemcpyAsync(ctx->pos, f.data(), cnt * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+		CK(cudaStreamSynchronize(ctx->st));
+	}
+	ctx->have_walkers = true;
+	return TDVMC_OK;
+}
+
+int tdvmc_get_walkers(tdvmc_ctx* ctx, double* x, int64_t nw) {
+	if (!ctx || !x || nw != ctx->nw) return TDVMC_ERR_ARG;
+	return copy_out_any(ctx, ctx->pos, x, (size_t)nw * ctx->sc.dim * ctx->sc.n);
+}
+
+int tdvmc_sample(tdvmc_ctx* ctx, int32_t moves, double mc_step, uint64_t seed, uint32_t pass, int64_t* accepted) {
+	if (!ctx || moves < 0) return TDVMC_ERR_ARG;
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	CK(cudaMemcpyAsync(&ctx->dyn->pass, &pass, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
+	int rc = ctx->prec == TDVMC_PREC_FP64 ? launch_prep<double>(ctx) : launch_prep<float>(ctx);
+	if (rc) return rc;
+	rc = ctx->prec == TDVMC_PREC_FP64 ? launch_sample<double>(ctx, moves, mc_step, seed)
+	                                  : launch_sample<float>(ctx, moves, mc_step, seed);
+	if (rc) return rc;
+	ctx->last_moves = moves;
+	std::vector<int> a((size_t)ctx->nw);
+	CK(cudaMemcpyAsync(a.data(), ctx->acc, a.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	if (accepted) {
+		int64_t t = 0;
+		for (int v : a) t += v;
+		*accepted = t;
+	}
+	return TDVMC_OK;
+}
+
+static int eval_common(tdvmc_ctx* ctx, bool adj) {
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	int rc = ctx->prec == TDVMC_PREC_FP64 ? launch_prep<double>(ctx) : launch_prep<float>(ctx);
+	if (rc) return rc;
+	rc = ctx->prec == TDVMC_PREC_FP64 ? launch_eloc<double>(ctx, adj) : launch_eloc<float>(ctx, adj);
+	if (rc) return rc;
+	ctx->have_eval = true;
+	ctx->last_adj = adj;
+	return TDVMC_OK;
+}
+
+int tdvmc_eval_local(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, double* other7) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	int rc = eval_common(ctx, false);
+	if (rc) return rc;
+	const size_t nw = (size_t)ctx->nw;
+	if ((rc = copy_out_any(ctx, ctx->lnpsi, lnpsi, nw))) return rc;
+	if ((rc = copy_out_any(ctx, ctx->O, O, nw * ctx->sc.p))) return rc;
+	if ((rc = copy_out_any(ctx, ctx->eloc, eloc, nw * 2))) return rc;
+	if ((rc = copy_out_any(ctx, ctx->other7, other7, nw * 7))) return rc;
+	CK(cudaStreamSynchronize(ctx->st));
+	return TDVMC_OK;
+}
+
+int tdvmc_eval_local_adjoint(tdvmc_ctx* ctx, double* dE) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	int rc = eval_common(ctx, true);
+	if (rc) return rc;
+	if ((rc = copy_out_any(ctx, ctx->dE, dE, (size_t)ctx->nw * 2 * ctx->sc.p))) return rc;
+	CK(cudaStreamSynchronize(ctx->st));
+	return TDVMC_OK;
+}
+
+int tdvmc_reduce_stats(tdvmc_ctx* ctx, tdvmc_stats* stats, double* O_mean, double* S, double* cov_OER,
+                       double* cov_OEI, double* dE_mean) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	if (!ctx->have_eval) return TDVMC_ERR_STATE;
+	int rc = ctx->prec == TDVMC_PREC_FP64 ? launch_reduce<double>(ctx, ctx->last_adj)
+	                                      : launch_reduce<float>(ctx, ctx->last_adj);
+	if (rc) return rc;
+	const int P = ctx->sc.p;
+	Cols1 c{P};
+	std::vector<double> m(c.count()), c2((size_t)P * (P + 2)), sg((size_t)P * P);
+	CK(cudaMemcpyAsync(m.data(), ctx->means1, m.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaMemcpyAsync(c2.data(), ctx->C2, c2.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaMemcpyAsync(sg.data(), ctx->Sg, sg.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	const bool tc = (ctx->prec == TDVMC_PREC_MIXED) && gram_supported(P);
+	if (stats) {
+		fill_stats(ctx, m, ctx->last_moves, stats);
+		stats->status = 0;
+	}
+	for (int k = 0; k < P; k++) {
+		if (O_mean) O_mean[k] = m[k];
+		if (cov_OER) cov_OER[k] = c2[(size_t)k * (P + 2) + P];
+		if (cov_OEI) cov_OEI[k] = c2[(size_t)k * (P + 2) + P + 1];
+		if (S)
+			for (int l = 0; l < P; l++) S[(size_t)k * P + l] = tc ? sg[(size_t)k * P + l] : c2[(size_t)k * (P + 2) + l];
+		if (dE_mean) {
+			dE_mean[2 * k] = ctx->last_adj ? m[c.dE() + 2 * k] : 0.0;
+			dE_mean[2 * k + 1] = ctx->last_adj ? m[c.dE() + 2 * k + 1] : 0.0;
+		}
+	}
+	return TDVMC_OK;
+}
+
+int tdvmc_tdvp_rhs(tdvmc_ctx* ctx, int32_t imag, int32_t pre, int32_t lin, double* uDotR, double* uDotI,
+                   double* phiDotR, double* phiDotI) {
+	if (!ctx || (lin != 0 && lin != 1)) return TDVMC_ERR_ARG;
+	if (!ctx->have_eval) return TDVMC_ERR_STATE;
+	int rc = ctx->prec == TDVMC_PREC_FP64 ? launch_solve<double>(ctx, imag, pre, lin, 0, 0, 0.0)
+	                                      : launch_solve<float>(ctx, imag, pre, lin, 0, 0, 0.0);
+	if (rc) return rc;
+	const int P = ctx->sc.p;
+	std::vector<double> v(2 * P + 2);
+	CK(cudaMemcpyAsync(v.data(), ctx->rhs, v.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	if (uDotR) std::copy(v.begin(), v.begin() + P, uDotR);
+	if (uDotI) std::copy(v.begin() + P, v.begin() + 2 * P, uDotI);
+	if (phiDotR) *phiDotR = v[2 * P];
+	if (phiDotI) *phiDotI = v[2 * P + 1];
+	int32_t st = 0;
+	if ((rc = read_status(ctx, &st))) return rc;
+	return status_code(st);
+}
+
+int tdvmc_run_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, tdvmc_stats* stats) {
+	if (!ctx || nsteps < 0) return TDVMC_ERR_ARG;
+	int rc = check_opts(o);
+	if (rc) return rc;
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	cudaGraphExec_t g;
+	if ((rc = get_graph(ctx, o, &g))) return rc;
+	const int nst = o->ode_solver == 0 ? 1 : 4;
+	const int kps = kernels_per_stage(ctx, o);
+	for (int s = 0; s < nsteps; s++)
+		for (int k = 0; k < nst; k++) {
+			CK(cudaGraphLaunch(g, ctx->st));
+			ctx->launches += kps;
+		}
+	ctx->have_eval = true;
+	ctx->last_adj = o->use_adjoint != 0;
+	ctx->last_moves = o->moves_per_stage;
+	int32_t st = 0;
+	if (stats) {
+		const int P = ctx->sc.p;
+		Cols1 c{P};
+		std::vector<double> m(c.count());
+		CK(cudaMemcpyAsync(m.data(), ctx->means0, m.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+		CK(cudaStreamSynchronize(ctx->st));
+		fill_stats(ctx, m, o->moves_per_stage, stats);
+	}
+	if ((rc = read_status(ctx, &st))) return rc;
+	if (stats) stats->status = status_code(st);
+	return status_code(st);
+}
+
+int tdvmc_step(tdvmc_ctx* ctx, const tdvmc_step_opts* o, tdvmc_stats* stats) {
+	return tdvmc_run_steps(ctx, o, 1, stats);
+}
+
+int tdvmc_time_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, float* ms) {
+	if (!ctx || !ms || nsteps < 0) return TDVMC_ERR_ARG;
+	int rc = check_opts(o);
+	if (rc) return rc;
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	cudaGraphExec_t g;
+	if ((rc = get_graph(ctx, o, &g))) return rc;
+	cudaEvent_t e0, e1;
+	CK(cudaEventCreate(&e0));
+	CK(cudaEventCreate(&e1));
+	const int nst = o->ode_solver == 0 ? 1 : 4;
+	const int kps = kernels_per_stage(ctx, o);
+	CK(cudaStreamSynchronize(ctx->st));
+	CK(cudaEventRecord(e0, ctx->st));
+	for (int s = 0; s < nsteps; s++)
+		for (int k = 0; k < nst; k++) {
+			CK(cudaGraphLaunch(g, ctx->st));
+			ctx->launches += kps;
+		}
+	CK(cudaEventRecord(e1, ctx->st));
+	CK(cudaEventSynchronize(e1));
+	CK(cudaEventElapsedTime(ms, e0, e1));
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	ctx->have_eval = true;
+	ctx->last_adj = o->use_adjoint != 0;
+	ctx->last_moves = o->moves_per_stage;
+	return TDVMC_OK;
+}
+
+int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, float* ms, const char** names, int32_t* count) {
+	if (!ctx || !ms || !count) return TDVMC_ERR_ARG;
+	int rc = check_opts(o);
+	if (rc) return rc;
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	std::vector<cudaEvent_t> ev;
+	std::vector<const char*> nm;
+	cudaEvent_t e0;
+	CK(cudaEventCreate(&e0));
+	CK(cudaStreamSynchronize(ctx->st));
+	CK(cudaEventRecord(e0, ctx->st));
+	ctx->prof = &ev;
+	ctx->prof_names = &nm;
+	rc = run_stage_any(ctx, o);
+	ctx->prof = nullptr;
+	ctx->prof_names = nullptr;
+	cudaError_t se = cudaStreamSynchronize(ctx->st);
+	int nk = 0;
+	cudaEvent_t prev = e0;
+	for (size_t i = 0; i < ev.size() && nk < 16; i++, nk++) {
+		float t = 0.f;
+		cudaEventElapsedTime(&t, prev, ev[i]);
+		ms[nk] = t;
+		if (names) names[nk] = nm[i];
+		prev = ev[i];
+	}
+	for (auto e : ev) cudaEventDestroy(e);
+	cudaEventDestroy(e0);
+	*count = nk;
+	if (rc) return rc;
+	CK(se);
+	ctx->have_eval = true;
+	ctx->last_adj = o->use_adjoint != 0;
+	ctx->last_moves = o->moves_per_stage;
+	return TDVMC_OK;
+}
+
+int tdvmc_autotune(tdvmc_ctx* ctx, int32_t moves, double mc_step) {
+	if (!ctx || moves < 1) return TDVMC_ERR_ARG;
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	// candidates must not change the walkers: run on a copy and restore
+	const size_t bytes = (size_t)ctx->nw * ctx->sc.dim * ctx->sc.n * tsize(ctx->prec);
+	void* save = nullptr;
+	CK(cudaMalloc(&save, bytes));
+	CK(cudaMemcpyAsync(save, ctx->pos, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+	cudaEvent_t e0, e1;
+	CK(cudaEventCreate(&e0));
+	CK(cudaEventCreate(&e1));
+	Tiles best = ctx->tiles;
+	float best_s = 1e30f, best_e = 1e30f;
+	const int n = ctx->sc.n;
+	const int gs[3] = {8, 16, 32};
+	int rc = TDVMC_OK;
+	for (int gi = 0; gi < 3 && rc == TDVMC_OK; gi++) {
+		const int G = gs[gi];
+		if (slots_for(n, G) < 0 || (G > 8 && n < G / 2)) continue;
+		for (int gpb : {1, 2, 4, 8}) {
+			if (G * gpb > 128) continue;
+			ctx->tiles.sg = G;
+			ctx->tiles.sgpb = gpb;
+			rc = ctx->prec == TDVMC_PREC_FP64 ? launch_prep<double>(ctx) : launch_prep<float>(ctx);
+			if (rc) break;
+			CK(cudaEventRecord(e0, ctx->st));
+			rc = ctx->prec == TDVMC_PREC_FP64 ? launch_sample<double>(ctx, moves, mc_step, 7)
+			                                  : launch_sample<float>(ctx, moves, mc_step, 7);
+			CK(cudaEventRecord(e1, ctx->st));
+			CK(cudaEventSynchronize(e1));
+			float ms = 0;
+			cudaEventElapsedTime(&ms, e0, e1);
+			if (rc == TDVMC_OK && ms < best_s) {
+				best_s = ms;
+				best.sg = G;
+				best.sgpb = gpb;
+			}
+			rc = TDVMC_OK;
+			CK(cudaMemcpyAsync(ctx->pos, save, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+		}
+		for (int gpb : {1, 2, 4}) {
+			if (G * gpb > 128) continue;
+			const size_t smem = ctx->prec == TDVMC_PREC_FP64 ? eloc_smem<double>(ctx, G, gpb, true)
+			                                                 : eloc_smem<float>(ctx, G, gpb, true);
+			if (smem > 220 * 1024) continue;
+			ctx->tiles.eg = G;
+			ctx->tiles.egpb = gpb;
+			CK(cudaEventRecord(e0, ctx->st));
+			rc = ctx->prec == TDVMC_PREC_FP64 ? launch_eloc<double>(ctx, true) : launch_eloc<float>(ctx, true);
+			CK(cudaEventRecord(e1, ctx->st));
+			CK(cudaEventSynchronize(e1));
+			float ms = 0;
+			cudaEventElapsedTime(&ms, e0, e1);
+			if (rc == TDVMC_OK && ms < best_e) {
+				best_e = ms;
+				best.eg = G;
+				best.egpb = gpb;
+			}
+			rc = TDVMC_OK;
+		}
+	}
+	ctx->tiles = best;
+	for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+	ctx->graphs.clear();
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(save);
+	CK(cudaStreamSynchronize(ctx->st));
+	return rc;
+}
+
+int tdvmc_get_tiles(tdvmc_ctx* ctx, int32_t* sl, int32_t* sw, int32_t* el, int32_t* ew) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	if (sl) *sl = ctx->tiles.sg;
+	if (sw) *sw = ctx->tiles.sgpb;
+	if (el) *el = ctx->tiles.eg;
+	if (ew) *ew = ctx->tiles.egpb;
+	return TDVMC_OK;
+}
+
+int64_t tdvmc_launch_count(tdvmc_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+}  // extern "C"

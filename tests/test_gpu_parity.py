@@ -1,0 +1,245 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerances (stated per test):
+  FP64 path   relative 1e-12 on ln psi, O_k, E_loc, the kinetic sums and
+              dE_loc/d alpha (scaled by the largest magnitude of the vector);
+  mixed path  relative 1e-5 per walker on the same quantities (FP32 pairs);
+  sampler     FP64: the same Philox stream gives the same chain as the oracle
+              (positions to 1e-9, identical acceptance counts); mixed: the
+              sampled averages agree with the reference's own chain within 3
+              sigma (E^R, E^I) and 4 sigma per O_k.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+EVAL_FILES = sorted(glob.glob(os.path.join(GOLD, "eval_*.npz")))
+
+pytestmark = pytest.mark.gpu
+
+
+def relmax(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def gpu_system(z, nw, precision, potential="square", sysp=None, hbar2_2m=1.0):
+    import tdvmc_gb300 as T
+    kn = z["knots"] if z["knots"].size else None
+    s = T.BosonsBulk(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), nw,
+                     system_params=z["sysp"] if sysp is None else sysp, potential=potential, user_knots=kn,
+                     hbar2_2m=hbar2_2m, precision=precision)
+    s.SetTime(float(z["time"]))
+    return s
+
+
+def oracle_system(z, pot_kind=orc.POT_SQUARE, sysp=None, hbar2_2m=1.0):
+    kn = z["knots"] if z["knots"].size else None
+    return orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), user_knots=kn, pot_kind=pot_kind,
+                            pot=z["sysp"] if sysp is None else sysp, time=float(z["time"]), hbar2_2m=hbar2_2m)
+
+
+def soa(cfgs):
+    """(ncfg, n, dim) particle-major -> walker SoA (ncfg, dim, n)."""
+    return np.ascontiguousarray(np.transpose(np.asarray(cfgs), (0, 2, 1)))
+
+
+CASES = [(f, prec, pot) for f in EVAL_FILES for prec in ("fp64", "mixed") for pot in ("square", "lj")]
+
+
+@pytest.mark.parametrize("path,precision,pot", CASES,
+                         ids=["%s-%s-%s" % (os.path.basename(c[0])[5:-4], c[1], c[2]) for c in CASES])
+def test_eval_and_adjoint_match_oracle(path, precision, pot):
+    z = np.load(path)
+    cfgs = z["cfgs"]
+    nw = len(cfgs)
+    sysp = z["sysp"] if pot == "square" else np.array([1.0, 1.0])
+    s = gpu_system(z, nw, precision, potential=pot, sysp=sysp, hbar2_2m=0.09)
+    o = oracle_system(z, pot_kind=orc.POT_SQUARE if pot == "square" else orc.POT_LJ, sysp=sysp, hbar2_2m=0.09)
+    s.SetParameters(z["uR"], z["uI"], float(z["phiR"]), float(z["phiI"]))
+    s.SetWalkers(soa(cfgs))
+    fwd = s.CalculateExpectationValues()
+    dE = s.CalculateLocalEnergyAdjoint()
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    for c, R in enumerate(cfgs):
+        r = o.eval(z["uR"], z["uI"], R, adjoint=True)
+        scale_lnpsi = max(abs(r["lnpsi"]), np.abs(z["uR"]).max() * len(R))
+        assert abs(fwd["lnpsi"][c] - r["lnpsi"]) < tol * scale_lnpsi
+        assert relmax(fwd["O"][c], r["O"]) < tol
+        scaleE = max(np.abs(r["other"]).max(), 1.0)
+        assert np.abs(fwd["eloc"][c] - r["eloc"]).max() < tol * scaleE
+        assert np.abs(fwd["other"][c] - r["other"]).max() < tol * scaleE
+        scaled = max(np.abs(r["dE"]).max(), 1.0)
+        assert np.abs(dE[c] - r["dE"]).max() < (tol if precision == "fp64" else 3e-5) * scaled
+
+
+def test_sampler_follows_oracle_chain_fp64():
+    """Same Philox stream, same move rule: the FP64 chain equals the oracle's."""
+    z = np.load(os.path.join(GOLD, "eval_d3_n64_p10.npz"))
+    nw = 24
+    rng = np.random.default_rng(8)
+    R0 = np.concatenate([soa(z["cfgs"])] * 2)[:nw] + rng.normal(0, 0.01, size=(nw, 3, 64))
+    R0 = np.array([[[orc.lib().orc_nic_coord(v, float(z["L"])) for v in row] for row in w] for w in R0])
+    s = gpu_system(z, nw, "fp64")
+    o = oracle_system(z)
+    uR = np.asarray(z["uR"]) * 0.5
+    s.SetParameters(uR, z["uI"])
+    s.SetWalkers(R0)
+    acc_gpu = s.DoMetropolisSteps(2 * 64, 0.3, seed=1234, pass_id=7)
+    Ro = R0.copy()
+    acc_orc = o.sample(uR, Ro, 2 * 64, 0.3, seed=1234, pass_id=7)
+    assert acc_gpu == acc_orc
+    assert np.abs(s.GetWalkers() - Ro).max() < 1e-9
+
+
+def test_sampler_matches_reference_chain_mixed():
+    """FP32 chain vs the reference's mt19937 chain (tests/golden/sample_d3_n27.npz)."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "sample_d3_n27.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    blocks = z["blocks"]
+    ref_mean = blocks.mean(0)
+    ref_err = blocks.std(0, ddof=1) / np.sqrt(len(blocks))
+    nw = 4096
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=z["sysp"], potential="square", precision="mixed")
+    s.SetParameters(z["uR"], z["uI"])
+    R = np.repeat(z["R0"].T[None], nw, axis=0) + np.random.default_rng(2).normal(0, 0.05, size=(nw, dim, n))
+    s.SetWalkers(R)
+    s.DoMetropolisSteps(50 * n, float(z["step"]), seed=5, pass_id=0)
+    rows = []
+    acc = 0
+    nsamp = 8
+    for k in range(nsamp):
+        acc += s.DoMetropolisSteps(n, float(z["step"]), seed=5, pass_id=k + 1)
+        f = s.CalculateExpectationValues()
+        rows.append(np.concatenate([f["eloc"], f["O"]], axis=1))
+    per_walker = np.array(rows).mean(0)
+    mean = per_walker.mean(0)
+    err = per_walker.std(0, ddof=1) / np.sqrt(nw)
+    comb = np.sqrt(err ** 2 + ref_err[1:3 + p] ** 2)
+    diff = np.abs(mean - ref_mean[1:3 + p])
+    assert np.all(diff[comb == 0] < 1e-6)
+    dev = np.where(comb > 0, diff / np.where(comb > 0, comb, 1), 0)
+    assert dev[0] < 3 and dev[1] < 3, dev
+    assert np.all(dev[2:] < 4), dev
+    rate = acc / (nsamp * n * nw)
+    assert abs(rate - ref_mean[0]) < 3 * ref_err[0] + 0.01
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_reduction_and_solve_match_oracle(precision):
+    z = np.load(os.path.join(GOLD, "eval_d3_n64_p10.npz"))
+    nw = 1000
+    rng = np.random.default_rng(4)
+    R = np.concatenate([soa(z["cfgs"])] * (nw // len(z["cfgs"]) + 1))[:nw] + rng.normal(0, 0.05, size=(nw, 3, 64))
+    s = gpu_system(z, nw, precision, potential="lj", sysp=(1.0, 1.0), hbar2_2m=0.09)
+    s.SetParameters(z["uR"], z["uI"], 0.3, -0.1)
+    s.SetWalkers(R)
+    f = s.CalculateExpectationValues()
+    st = s.ReduceStatistics()
+    O, E = f["O"], f["eloc"]
+    Oc = O - O.mean(0)
+    tolS = 1e-12 if precision == "fp64" else 2e-6
+    assert relmax(st["O"], O.mean(0)) < 1e-12
+    assert abs(st["energy"][0] - E[:, 0].mean()) < 1e-12 * np.abs(E[:, 0]).max()
+    assert relmax(st["S"], Oc.T @ Oc / nw) < tolS
+    assert relmax(st["cov_OER"], Oc.T @ (E[:, 0] - E[:, 0].mean()) / nw) < 1e-10
+    assert relmax(st["cov_OEI"], Oc.T @ (E[:, 1] - E[:, 1].mean()) / nw) < 1e-10
+    for imag in (0, 1):
+        for pre in (0, 1):
+            for lin in (0, 1):
+                g = s.SolveForParametersDot(imag, pre, lin)
+                # the device solve against the oracle's, on the device's own moments: 1e-10
+                r = orc.solve_centred(st["O"], st["energy"][0], st["energy"][1], st["S"], st["cov_OER"],
+                                      st["cov_OEI"], imag, pre, lin)
+                assert relmax(g[0], r[0]) < 1e-10
+                assert relmax(g[1], r[1]) < 1e-10
+                assert abs(g[2] - r[2]) < 1e-10 * max(1, abs(r[2]))
+                assert abs(g[3] - r[3]) < 1e-10 * max(1, abs(r[3]))
+                assert g[4] == r[4]
+
+
+@pytest.mark.parametrize("ode", [2, 0])
+def test_tdvp_step_matches_oracle_fp64(ode):
+    """A full RK4 (or Euler) step: sampling, evaluation, reduction, solve, update."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "sample_d3_n27.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    nw, moves, step, dt, seed, pass0 = 64, 2 * n, 0.35, 0.01, 77, 3
+    rng = np.random.default_rng(9)
+    R0 = np.repeat(z["R0"].T[None], nw, axis=0) + rng.normal(0, 0.05, size=(nw, dim, n))
+    R0 = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(R0)
+    uR, uI = np.asarray(z["uR"]), np.asarray(z["uI"])
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=0.09, precision="fp64")
+    s.SetParameters(uR, uI, 0.0, 0.0)
+    s.SetWalkers(R0)
+    s.DoMetropolisSteps(0, step, seed, pass0)  # sets the Philox pass counter
+    td = T.TDVP(s, dt, moves, step, seed=seed, ode_solver=ode)
+    td.step()
+    gR, gI, gpR, gpI = s.GetParameters()
+
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0), hbar2_2m=0.09)
+    base = np.concatenate([uR, uI, [0.0, 0.0]])
+    cur = base.copy()
+    Ro = R0.copy()
+    ks = []
+    nst = 4 if ode == 2 else 1
+    for k in range(nst):
+        out = o.stage(cur[:p], cur[p:2 * p], Ro, moves, step, seed, pass0 + k, threads=4, adjoint=False)
+        m = orc.centred(out["O"], out["eloc"])
+        dR, dI, pR, pI, _ = orc.solve_centred(m["O"], m["ER"], m["EI"], m["S"], m["cOER"], m["cOEI"])
+        kv = np.concatenate([dR, dI, [pR, pI]])
+        ks.append(kv)
+        if ode == 2 and k < 3:
+            cur = base + kv * (dt / 2 if k < 2 else dt)
+    if ode == 2:
+        new = orc.rk4_combine(base, ks, dt)
+    else:
+        new = base + ks[0] * dt
+    assert np.abs(s.GetWalkers() - Ro).max() < 1e-9
+    got = np.concatenate([gR, gI, [gpR, gpI]])
+    assert relmax(got, new) < 1e-9
+
+
+def test_errors_and_call_order():
+    import tdvmc_gb300 as T
+    from tdvmc_gb300 import _native as N
+    with pytest.raises(N.TdvmcError):
+        T.BosonsBulk(3, 8, 3, 4.0, 4)  # too few parameters
+    with pytest.raises(N.TdvmcError):
+        T.BosonsBulk(4, 8, 10, 4.0, 4)  # DIM out of range
+    s = T.BosonsBulk(3, 8, 10, 4.0, 4)
+    with pytest.raises(N.TdvmcError) as e:
+        s.CalculateExpectationValues()  # no walkers yet
+    assert e.value.code == N.ERR_STATE
+    with pytest.raises(AssertionError):
+        s.SetWalkers(np.zeros((5, 3, 8)))
+
+
+@pytest.mark.parametrize("nw,n,dim", [(1, 2, 1), (3, 5, 2), (37, 33, 3), (5, 97, 3)])
+def test_ragged_sizes_match_oracle(nw, n, dim):
+    """Walker counts that do not fill a block, particle counts that do not fill a lane group."""
+    import tdvmc_gb300 as T
+    p, L = 8, 3.0 + n ** (1.0 / dim)
+    rng = np.random.default_rng(n)
+    uR, uI = rng.normal(0, 0.2, p), rng.normal(0, 0.1, p)
+    R = rng.uniform(-L / 2, L / 2, size=(nw, dim, n))
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", precision="fp64")
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R)
+    f = s.CalculateExpectationValues()
+    dE = s.CalculateLocalEnergyAdjoint()
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0))
+    for w in range(nw):
+        r = o.eval(uR, uI, R[w].T, adjoint=True)
+        assert relmax(f["O"][w], r["O"]) < 1e-12 or np.abs(r["O"]).max() == 0
+        sc = max(np.abs(r["other"]).max(), 1.0)
+        assert np.abs(f["eloc"][w] - r["eloc"]).max() < 1e-12 * sc
+        assert np.abs(dE[w] - r["dE"]).max() < 1e-12 * max(np.abs(r["dE"]).max(), 1.0)
