@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""TDVP steps/s on 3D N=343 Lennard-Jones bosons with 65,536 walkers.
+
+Workload (one "step" = one RK4 TDVP time step = 4 stages, each: 2 Metropolis
+sweeps per walker (686 single-particle moves), local energy + O_k + adjoint
+dE_loc/d alpha per walker, walker reduction to <O>, S, force, FP64 Cholesky
+solve and stage update):
+  D=3, N=343 on a 7x7x7 simple-cubic start with 10% jitter, density 0.365
+  (L = 9.7949), LJ eps = sigma = 1, hbar^2/2m = 0.09, 30 uniform knots on
+  [0, L/2] (P = 30), McMillan-like initial Jastrow, dt = 5e-4, real time.
+  Synthetic inputs (no dataset exists for this metric).  The walker array
+  (270 MB in FP32) is larger than L2, so no flush is needed between steps.
+
+Arms:
+  default             mixed precision (FP32 pairs, FP64 centring/solve/RK4)
+  --impl reference    the reference algorithm on the host cores: the FP64 CPU
+                      port in oracle/ (the reference sources themselves are not
+                      on the GPU host), bounded sample, extrapolated.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIM, N, P, RHO = 3, 343, 30, 0.365
+L = (N / RHO) ** (1.0 / DIM)
+NW = 65536
+DT = 5e-4
+SWEEPS = 2
+MOVES = SWEEPS * N
+MC_STEP = 0.18
+HBAR2_2M = 0.09
+METRIC = "TDVP steps/s (3D N=343, 64k walkers): mixed+adjoint vs FP64 GPU, |ΔE/N|<1e-5"
+
+# algorithmic FLOP convention (per pair evaluation; FMA = 2 FLOP)
+FLOP_MOVE_PAIR = 32     # one Metropolis pair evaluation
+FLOP_ELOC_PAIR = 110    # one unordered pair of the local-energy pass
+FLOP_ADJ_PAIR = 90      # one unordered pair of the reverse (adjoint) sweep
+
+
+def flop_sample_launch(nw=NW):
+    return float(nw) * MOVES * 2 * (N - 1) * FLOP_MOVE_PAIR
+
+
+def flop_eloc_launch(nw=NW, adjoint=True):
+    pairs = float(nw) * N * (N - 1) / 2
+    return pairs * (FLOP_ELOC_PAIR + (FLOP_ADJ_PAIR if adjoint else 0))
+
+
+def flop_step(nw=NW):
+    return 4 * (flop_sample_launch(nw) + flop_eloc_launch(nw))
+
+
+def initial_params():
+    """McMillan-like pair Jastrow u(r) = -(b/r)^5 / 2, b = 1.1 sigma, on the knot abscissae."""
+    r = np.linspace(0.0, L / 2, P)
+    uR = -0.5 * (1.1 / np.maximum(r, 0.85)) ** 5
+    uR -= uR[-1]
+    return uR, np.zeros(P)
+
+
+def initial_walkers(nw, seed=20261203):
+    """7x7x7 simple-cubic lattice, jitter U(-1/2, 1/2) * spacing / 10 (TDVMC.cpp:725-739)."""
+    m = 7
+    l = L / m
+    idx = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 3)
+    rng = np.random.default_rng(seed)
+    R = idx[None, :, :] * l + (rng.uniform(size=(nw, N, DIM)) - 0.5) * l / 10.0 - L / 2
+    return np.ascontiguousarray(np.transpose(R, (0, 2, 1)))
+
+
+class Clocks:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "%s_traffic.txt" % kernel)
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_workload:"):
+                return float(line.split(":")[1])
+    except Exception:
+        pass
+    return None
+
+
+def cpu_port_rate(threads, walkers_per_thread=1, seed=11):
+    """The reference algorithm (FP64 CPU port) on a bounded sample: one stage
+    (sampling pass + evaluation + adjoint) of threads*walkers_per_thread walkers.
+    Returns (steps/s extrapolated to the full workload, seconds, walkers)."""
+    from oracle import oracle as orc
+    s = orc.OracleSystem(DIM, N, P, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0), hbar2_2m=HBAR2_2M)
+    nws = threads * walkers_per_thread
+    R = initial_walkers(nws, seed=seed)
+    uR, uI = initial_params()
+    t0 = time.perf_counter()
+    s.stage(uR, uI, R, MOVES, MC_STEP, seed=1, pass_id=0, threads=threads, adjoint=True)
+    t = time.perf_counter() - t0
+    walker_stages_per_s = nws / t
+    return walker_stages_per_s / (4.0 * NW), t, nws
+
+
+def run_reference(args):
+    threads = os.cpu_count() or 1
+    rates = []
+    for _ in range(args.warmup):
+        cpu_port_rate(threads, 1)
+    t_all = 0.0
+    nws = 0
+    for k in range(args.steps):
+        r, t, nws = cpu_port_rate(threads, 1, seed=100 + k)
+        rates.append(r)
+        t_all += t
+    v = float(np.mean(rates))
+    line = {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3D N=343 LJ bosons rho=0.365, P=30, 65536 walkers, RK4 dt=5e-4, "
+                                   "2 sweeps/stage, adjoint", "walkers": NW, "particles": N, "params": P},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": "per step: one RK stage (686 moves + E_loc + adjoint) of %d walkers "
+                                       "on %d threads, extrapolated x4 stages x65536 walkers" % (nws, threads)},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    try:
+        import torch
+        torch.cuda.set_device(local)
+        sync = torch.cuda.synchronize
+    except Exception:
+        torch = None
+
+        def sync():
+            pass
+    import tdvmc_gb300 as T
+    from tdvmc_gb300 import _native as Nat
+
+    lib = Nat.load()
+    uR, uI = initial_params()
+    R0 = initial_walkers(NW)
+    sysm = T.BosonsBulk(DIM, N, P, L, NW, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
+                        precision="mixed")
+    sysm.SetParameters(uR, uI)
+    sysm.SetWalkers(R0)
+    td = T.TDVP(sysm, DT, MOVES, MC_STEP, seed=1, use_adjoint=1)
+    if args.autotune:
+        sysm.Autotune(MOVES, MC_STEP)
+    launches0 = sysm.LaunchCount()
+    # warm-up steps (thermalise the walkers, build and warm the graphs)
+    td.time_steps(args.warmup)
+    sync()
+    clocks = Clocks()
+    clocks.start()
+    launches_a = sysm.LaunchCount()
+    ms = td.time_steps(args.steps)
+    sync()
+    launches_b = sysm.LaunchCount()
+    clk = clocks.stop()
+    value_rank = args.steps / (ms / 1000.0)
+
+    # per-kernel device times of one eager stage (CUDA events around each kernel)
+    prof = td.profile_stage()
+    kt = {k: v for k, v in prof}
+    top = max(prof, key=lambda kv: kv[1])
+
+    # end-to-end through the C ABI with host buffers: parameters in, statistics
+    # and parameters out, every step
+    uRh, uIh, pRh, pIh = sysm.GetParameters()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sysm.SetParameters(uRh, uIh, pRh, pIh)
+        td.step(1)
+        uRh, uIh, pRh, pIh = sysm.GetParameters()
+    sync()
+    e2e_s = time.perf_counter() - t0
+    e2e = args.steps / e2e_s
+    h2d = (2 * P + 2) * 8 * 2 + 4
+    d2h = (3 * P + 12) * 8 + 24 + (2 * P + 2) * 8
+
+    # |dE/N| gate: FP64 evaluation of the same walkers (subset) vs the mixed path
+    nsub = 4096
+    Rm = sysm.GetWalkers()[:nsub]
+    fm = sysm.CalculateExpectationValues()
+    gp = sysm.GetParameters()
+    s64 = T.BosonsBulk(DIM, N, P, L, nsub, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
+                       precision="fp64")
+    s64.SetParameters(gp[0], gp[1], gp[2], gp[3])
+    s64.SetWalkers(Rm)
+    f64 = s64.CalculateExpectationValues()
+    dE_per_N = abs(fm["eloc"][:nsub, 0].mean() - f64["eloc"][:, 0].mean()) / N
+
+    # plain FP64 GPU path, same kernels in double, on nsub walkers, scaled
+    s64.SetWalkers(R0[:nsub])
+    s64.SetParameters(uR, uI)
+    td64 = T.TDVP(s64, DT, MOVES, MC_STEP, seed=1, use_adjoint=1)
+    td64.time_steps(1)
+    ms64 = td64.time_steps(1)
+    fp64_steps_s = (1000.0 / ms64) * nsub / NW
+
+    # FP32 pipe ceiling and roofline of the dominant kernel
+    pk = C_double = None
+    import ctypes as C
+    pk = C.c_double()
+    Nat.check(lib.tdvmc_measure_fp32_peak(C.byref(pk)), "tdvmc_measure_fp32_peak")
+    fp32_peak = pk.value
+    if top[0] == "k_sample":
+        fl = flop_sample_launch()
+    elif top[0].startswith("k_eloc"):
+        fl = flop_eloc_launch(adjoint=top[0].endswith("adjoint"))
+    else:
+        fl = 0.0
+    achieved = fl / (top[1] * 1e-3) / 1e12
+    traffic = ncu_traffic(top[0])
+
+    # CPU baseline: the reference algorithm (FP64 port) on the host cores, bounded sample
+    threads = os.cpu_count() or 1
+    cpu_v, cpu_t, cpu_w = cpu_port_rate(threads, 1)
+
+    if world > 1 and torch is not None:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl")
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms / 1000.0)
+    peaks = measured_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "3D N=343 LJ bosons rho=0.365, P=30, 65536 walkers, RK4 dt=5e-4, 2 sweeps/stage, "
+                               "adjoint", "walkers": NW, "particles": N, "params": P, "moves_per_stage": MOVES,
+                   "mc_step": MC_STEP, "l2": "inputs larger than L2 (walkers 270 MB)",
+                   "parallelism": "single GPU" if world == 1 else "replicas"},
+        "e2e": {"value": e2e * world, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches_b - launches_a),
+        "roofline": {"bound": "fp32", "kernel": top[0], "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,
+                     "peak_source": "measured FP32 FMA loop (tdvmc_measure_fp32_peak)",
+                     "traffic": traffic, "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "kernels_ms_per_stage": kt,
+        "fp64_gpu": {"value": fp64_steps_s, "unit": "steps/s", "walkers_timed": nsub, "scaled_to": NW,
+                     "speedup_mixed_over_fp64": value / world / fp64_steps_s},
+        "gate": {"dE_per_N": dE_per_N, "pass": bool(dE_per_N < 1e-5), "walkers": nsub},
+        "cpu_baseline": {"value": cpu_v, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": "one RK stage (686 moves + E_loc + adjoint) of %d walkers on %d threads "
+                                   "(%.1f s), extrapolated x4 stages x65536 walkers" % (cpu_w, threads, cpu_t)},
+        "algorithmic_tflop_per_step": flop_step() / 1e12,
+        "achieved_tflops_step": flop_step() / (ms / args.steps * 1e-3) / 1e12,
+        "clocks": clk,
+        "energy_per_particle": float(fm["eloc"][:, 0].mean() / N),
+        "tiles": sysm.Tiles(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--autotune", type=int, default=0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -162,6 +162,11 @@ int tdvmc_tdvp_rhs(tdvmc_ctx* ctx, int32_t imaginary_time, int32_t precondition,
  * Philox pass counter advances by one per stage. */
 int tdvmc_step(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, tdvmc_stats* stats);
 
+/* Walker means <O_k> (p values) and the FP64 means of the first stage of the
+ * last step (the localOperators the reference records per step,
+ * TDVMC.cpp:3750). */
+int tdvmc_get_step_operators(tdvmc_ctx* ctx, double* O_mean);
+
 /* `nsteps` steps back to back without host synchronisation (benchmarking
  * and long runs); statistics of the last step's first stage in *stats. */
 int tdvmc_run_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, int32_t nsteps, tdvmc_stats* stats);
@@ -186,6 +191,11 @@ int tdvmc_autotune(tdvmc_ctx* ctx, int32_t moves, double mc_step);
  * sampler and the evaluation kernels. */
 int tdvmc_get_tiles(tdvmc_ctx* ctx, int32_t* sample_lanes, int32_t* sample_walkers_per_block,
                     int32_t* eval_lanes, int32_t* eval_walkers_per_block);
+
+/* Measurement utility: FP32 FMA throughput of the current device in
+ * TFLOP/s (dependent-free FMA loop on every SM), the ceiling of the
+ * CUDA-core-bound sampling and evaluation kernels.  No reference counterpart. */
+int tdvmc_measure_fp32_peak(double* tflops);
 
 /* Number of kernel launches issued by this context since creation. */
 int64_t tdvmc_launch_count(tdvmc_ctx* ctx);

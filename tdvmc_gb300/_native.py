@@ -19,7 +19,8 @@ POT_NONE, POT_SQUARE, POT_GAUSS, POT_LJ = 0, 1, 2, 3
 EXPORTS = ("tdvmc_status_string", "tdvmc_create", "tdvmc_destroy", "tdvmc_get_stream", "tdvmc_set_time",
            "tdvmc_set_params", "tdvmc_get_params", "tdvmc_set_walkers", "tdvmc_get_walkers", "tdvmc_sample",
            "tdvmc_eval_local", "tdvmc_eval_local_adjoint", "tdvmc_reduce_stats", "tdvmc_tdvp_rhs", "tdvmc_step",
-           "tdvmc_run_steps", "tdvmc_time_steps", "tdvmc_profile_stage", "tdvmc_autotune", "tdvmc_get_tiles", "tdvmc_launch_count")
+           "tdvmc_get_step_operators", "tdvmc_run_steps", "tdvmc_time_steps", "tdvmc_profile_stage", "tdvmc_autotune", "tdvmc_get_tiles", "tdvmc_launch_count",
+           "tdvmc_measure_fp32_peak")
 
 
 class SystemDesc(C.Structure):
@@ -78,6 +79,7 @@ def load(build_if_missing: bool = True):
     L.tdvmc_reduce_stats.argtypes = [C.c_void_p, P(Stats), d, d, d, d, d]
     L.tdvmc_tdvp_rhs.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, d, d, P(C.c_double), P(C.c_double)]
     L.tdvmc_step.argtypes = [C.c_void_p, P(StepOpts), P(Stats)]
+    L.tdvmc_get_step_operators.argtypes = [C.c_void_p, d]
     L.tdvmc_run_steps.argtypes = [C.c_void_p, P(StepOpts), C.c_int32, P(Stats)]
     L.tdvmc_time_steps.argtypes = [C.c_void_p, P(StepOpts), C.c_int32, P(C.c_float)]
     L.tdvmc_profile_stage.argtypes = [C.c_void_p, P(StepOpts), P(C.c_float), P(C.c_char_p), P(C.c_int32)]
@@ -85,6 +87,7 @@ def load(build_if_missing: bool = True):
     L.tdvmc_get_tiles.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32), P(C.c_int32)]
     L.tdvmc_launch_count.argtypes = [C.c_void_p]
     L.tdvmc_launch_count.restype = C.c_int64
+    L.tdvmc_measure_fp32_peak.argtypes = [P(C.c_double)]
     _lib = L
     return L
 

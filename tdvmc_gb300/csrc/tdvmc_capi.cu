@@ -823,6 +823,13 @@ int tdvmc_run_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, td
 	return status_code(st);
 }
 
+int tdvmc_get_step_operators(tdvmc_ctx* ctx, double* O_mean) {
+	if (!ctx || !O_mean) return TDVMC_ERR_ARG;
+	CK(cudaMemcpyAsync(O_mean, ctx->means0, ctx->sc.p * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+	CK(cudaStreamSynchronize(ctx->st));
+	return TDVMC_OK;
+}
+
 int tdvmc_step(tdvmc_ctx* ctx, const tdvmc_step_opts* o, tdvmc_stats* stats) {
 	return tdvmc_run_steps(ctx, o, 1, stats);
 }
