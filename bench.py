@@ -234,9 +234,10 @@ def run_ours(args):
     # and parameters out, every step
     uRh, uIh, pRh, pIh = sysm.GetParameters()
     t0 = time.perf_counter()
+    last = None
     for _ in range(args.steps):
         sysm.SetParameters(uRh, uIh, pRh, pIh)
-        td.step(1)
+        last = td.step(1)
         uRh, uIh, pRh, pIh = sysm.GetParameters()
     sync()
     e2e_s = time.perf_counter() - t0
@@ -265,7 +266,6 @@ def run_ours(args):
     fp64_steps_s = (1000.0 / ms64) * nsub / NW
 
     # FP32 pipe ceiling and roofline of the dominant kernel
-    pk = C_double = None
     import ctypes as C
     pk = C.c_double()
     Nat.check(lib.tdvmc_measure_fp32_peak(C.byref(pk)), "tdvmc_measure_fp32_peak")
@@ -281,7 +281,7 @@ def run_ours(args):
 
     # CPU baseline: the reference algorithm (FP64 port) on the host cores, bounded sample
     threads = os.cpu_count() or 1
-    cpu_v, cpu_t, cpu_w = cpu_port_rate(threads, 1)
+    cpu_v, cpu_t, cpu_w = cpu_port_rate(threads, 4)
 
     if world > 1 and torch is not None:
         import torch.distributed as dist
@@ -317,6 +317,7 @@ def run_ours(args):
         "achieved_tflops_step": flop_step() / (ms / args.steps * 1e-3) / 1e12,
         "clocks": clk,
         "energy_per_particle": float(fm["eloc"][:, 0].mean() / N),
+        "accept_rate": last["accept_rate"] if last else None,
         "tiles": sysm.Tiles(),
     }
     if rank == 0:
