@@ -7,7 +7,9 @@ dE_loc/d alpha per walker, walker reduction to <O>, S, force, FP64 Cholesky
 solve and stage update):
   D=3, N=343 on a 7x7x7 simple-cubic start with 10% jitter, density 0.365
   (L = 9.7949), LJ eps = sigma = 1, hbar^2/2m = 0.09, 30 uniform knots on
-  [0, L/2] (P = 30), McMillan-like initial Jastrow, dt = 5e-4, real time.
+  [0, L/2] (P = 30), McMillan-like initial Jastrow u(r) = -(1.1/r)^5 / 2
+  (flat below 0.5 sigma), Gaussian moves of width 0.24 (~53% acceptance),
+  dt = 5e-4, real time.
   Synthetic inputs (no dataset exists for this metric).  The walker array
   (270 MB in FP32) is larger than L2, so no flush is needed between steps.
 
@@ -38,7 +40,7 @@ NW = 65536
 DT = 5e-4
 SWEEPS = 2
 MOVES = SWEEPS * N
-MC_STEP = 0.18
+MC_STEP = 0.24
 HBAR2_2M = 0.09
 METRIC = "TDVP steps/s (3D N=343, 64k walkers): mixed+adjoint vs FP64 GPU, |ΔE/N|<1e-5"
 
@@ -64,7 +66,7 @@ def flop_step(nw=NW):
 def initial_params():
     """McMillan-like pair Jastrow u(r) = -(b/r)^5 / 2, b = 1.1 sigma, on the knot abscissae."""
     r = np.linspace(0.0, L / 2, P)
-    uR = -0.5 * (1.1 / np.maximum(r, 0.85)) ** 5
+    uR = -0.5 * (1.1 / np.maximum(r, 0.5)) ** 5
     uR -= uR[-1]
     return uR, np.zeros(P)
 

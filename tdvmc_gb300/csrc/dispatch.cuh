@@ -19,14 +19,14 @@ int sample_slots_for(int n, int lanes);
 
 SampleFn<float> pick_sample_f32(int lanes, int slots);
 SampleFn<double> pick_sample_f64(int lanes, int slots);
-ElocFn<float> pick_eloc_f32(int lanes, bool adj);
-ElocFn<double> pick_eloc_f64(int lanes, bool adj);
+ElocFn<float> pick_eloc_f32(int lanes, bool adj, int hist);
+ElocFn<double> pick_eloc_f64(int lanes, bool adj, int hist);
 
 template <typename T> SampleFn<T> pick_sample(int lanes, int slots);
 template <> inline SampleFn<float> pick_sample<float>(int g, int s) { return pick_sample_f32(g, s); }
 template <> inline SampleFn<double> pick_sample<double>(int g, int s) { return pick_sample_f64(g, s); }
-template <typename T> ElocFn<T> pick_eloc(int lanes, bool adj);
-template <> inline ElocFn<float> pick_eloc<float>(int g, bool a) { return pick_eloc_f32(g, a); }
-template <> inline ElocFn<double> pick_eloc<double>(int g, bool a) { return pick_eloc_f64(g, a); }
+template <typename T> ElocFn<T> pick_eloc(int lanes, bool adj, int hist);
+template <> inline ElocFn<float> pick_eloc<float>(int g, bool a, int h) { return pick_eloc_f32(g, a, h); }
+template <> inline ElocFn<double> pick_eloc<double>(int g, bool a, int h) { return pick_eloc_f64(g, a, h); }
 
 }  // namespace tdvmc

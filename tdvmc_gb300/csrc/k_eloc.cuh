@@ -29,6 +29,56 @@ namespace tdvmc {
 constexpr int kFwdMoments = 4;     // sum t^c, c = 0..3
 constexpr int kFwdMomentsAdj = 7;  // + sum t^c / r, c = 0..2
 constexpr int kRevMoments = 6;     // complex sum g t^c, c = 0..2
+constexpr int kHistSlots = 8;      // histogram slots per interval and lane (max of the above, padded)
+
+// Histogram update modes of the lane-private moment histograms:
+//   0  scalar read-modify-write      hist[(j*8 + m)*G + lane]
+//   1  float4 read-modify-write      hist4[(j*2 + m/4)*G + lane].{x,y,z,w}[m%4]
+//   2  shared-memory atomic add      same layout as 0 (no contention: lane-private)
+template <int HIST, typename T, int G>
+__device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane, const T (&v)[8], int nv) {
+	if (HIST == 1) {
+		Q4<T>* h4 = reinterpret_cast<Q4<T>*>(hist) + ((size_t)j * 2) * G + lane;
+		Q4<T> a = h4[0];
+		a.x += v[0];
+		a.y += v[1];
+		a.z += v[2];
+		a.w += v[3];
+		h4[0] = a;
+		if (nv > 4) {
+			Q4<T> b = h4[G];
+			b.x += v[4];
+			b.y += v[5];
+			b.z += v[6];
+			if (nv > 7) b.w += v[7];
+			h4[G] = b;
+		}
+	} else {
+		T* hp = hist + (size_t)j * kHistSlots * G + lane;
+#pragma unroll
+		for (int m = 0; m < 8; m++) {
+			if (m >= nv) break;
+			if (HIST == 2) atomicAdd(hp + m * G, v[m]);
+			else hp[m * G] += v[m];
+		}
+	}
+}
+
+// value of moment m of interval j summed over the group's lanes
+template <int HIST, typename T, int G>
+__device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) {
+	T s = T(0);
+	if (HIST == 1) {
+		const T* h = hist + (((size_t)j * 2 + m / 4) * G) * 4 + (m & 3);
+#pragma unroll 8
+		for (int l = 0; l < G; l++) s += h[l * 4];
+	} else {
+		const T* h = hist + ((size_t)j * kHistSlots + m) * G;
+#pragma unroll 8
+		for (int l = 0; l < G; l++) s += h[l];
+	}
+	return s;
+}
 
 // Shared memory layout:
 //   CTA:   coefC[2*nbin] (uR, uI cubics) | kb[nbin] | hv[nbin] | lut[ncell]
@@ -41,9 +91,9 @@ __host__ __device__ inline size_t eloc_cta_bytes(int nbin, int ncell) {
 template <typename T>
 __host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G, bool adj) {
 	int nm = adj ? kFwdMomentsAdj : kFwdMoments;
-	int nmh = nm > kRevMoments ? nm : kRevMoments;
+	int nmh = kHistSlots;
 	size_t b = (size_t)n * sizeof(Q4<T>);
-	if (adj) b += (size_t)n * 6 * sizeof(T);
+	if (adj) b += (size_t)((n * 6 + 7) & ~7) * sizeof(T);  // keeps the histogram 32-byte aligned
 	b += (size_t)nbin * nmh * G * sizeof(T);
 	b += (size_t)nbin * (nm + (adj ? kRevMoments : 0)) * sizeof(T);
 	b += (size_t)ns * 4 * sizeof(T) + 16 * sizeof(T);
@@ -59,17 +109,19 @@ __device__ __forceinline__ T group_sum(T v, unsigned gmask) {
 
 // Pair kernel of the forward sweep for partners [i0, i1).
 // ON: 0 = no pair statistics, 1 = all lanes count the pair, 2 = count iff i < nrow.
-template <typename T, int G, int ON, bool ADJ>
+template <typename T, int G, int ON, bool ADJ, int HIST>
 __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
-                                           const Q4<T>* xs, const Q4<T>* coefC, const T* kb, const T* hv,
-                                           const int* lut, T* hist, int lane, T pa, T pb,
+                                           const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
+                                           const T* __restrict__ kb, const T* __restrict__ hv,
+                                           const int* __restrict__ lut, T* __restrict__ hist, int lane, T pa, T pb,
                                            KSum<T>* acc /* gRx gRy gRz gIx gIy gIz lR lI */, KSum<T>& vsum, int& nout) {
-	constexpr int NM = ADJ ? kFwdMomentsAdj : kFwdMoments;
 	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax, dm1 = (T)(sc.dim - 1);
+	const T hu = (T)sc.hinv;
 	for (int c0 = i0; c0 < i1; c0 += 32) {
 		const int c1 = (c0 + 32 < i1) ? c0 + 32 : i1;
 		T a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 		T vb = T(0);
+#pragma unroll 2
 		for (int i = c0; i < c1; i++) {
 			const Q4<T> xi = xs[i];
 			const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
@@ -82,7 +134,7 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 			const int j = locate<T>(sc, r, kb, hv, lut, t);
 			const Q4<T> cR = coefC[2 * j];
 			const Q4<T> cI = coefC[2 * j + 1];
-			const T hj = sc.uniform ? (T)sc.hinv : hv[j];
+			const T hj = sc.uniform ? hu : hv[j];
 			const T d1R = (cR.y + t * (T(2) * cR.z + T(3) * t * cR.w)) * hj;
 			const T d1I = (cI.y + t * (T(2) * cI.z + T(3) * t * cI.w)) * hj;
 			const T d2R = (T(2) * cR.z + T(6) * t * cR.w) * (hj * hj);
@@ -100,20 +152,11 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 			if (ON != 0) {
 				const bool cnt = (ON == 1) ? true : (i < nrow);
 				const bool on = in && cnt;
-				const T one = on ? T(1) : T(0);
 				const T ts = on ? t : T(0);  // t is NaN for the self pair
 				const T t2 = ts * ts;
-				T* hp = hist + (size_t)j * NM * G + lane;
-				hp[0 * G] += one;
-				hp[1 * G] += ts;
-				hp[2 * G] += t2;
-				hp[3 * G] += t2 * ts;
-				if (ADJ) {
-					const T q = on ? rinv : T(0);
-					hp[4 * G] += q;
-					hp[5 * G] += q * ts;
-					hp[6 * G] += q * t2;
-				}
+				const T q = on ? rinv : T(0);
+				T v[8] = {on ? T(1) : T(0), ts, t2, t2 * ts, q, q * ts, q * t2, T(0)};
+				hist_add8<HIST, T, G>(hist, j, lane, v, ADJ ? kFwdMomentsAdj : kFwdMoments);
 				vb += on ? pair_pot<T>(sc.pot_kind, r, rinv, pa, pb) : T(0);
 				nout += (rowok && notself && cnt && !(r <= rmax)) ? 1 : 0;
 			}
@@ -125,11 +168,13 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 }
 
 // Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1).
-template <typename T, int G, bool DIAG>
+template <typename T, int G, bool DIAG, int HIST>
 __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
-                                           const T* gn, const Q4<T>* xs, const T* Gs, const T* kb, const T* hv,
-                                           const int* lut, T* hist, int lane) {
+                                           const T* gn, const Q4<T>* __restrict__ xs, const T* __restrict__ Gs,
+                                           const T* __restrict__ kb, const T* __restrict__ hv,
+                                           const int* __restrict__ lut, T* __restrict__ hist, int lane) {
 	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax;
+#pragma unroll 2
 	for (int i = i0; i < i1; i++) {
 		const Q4<T> xi = xs[i];
 		const T* gi = Gs + (size_t)i * 6;
@@ -144,33 +189,23 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 		const T s = on ? rinv : T(0);
 		const T gR = ((gn[0] - gi[0]) * dx + (gn[1] - gi[1]) * dy + (gn[2] - gi[2]) * dz) * s;
 		const T gI = ((gn[3] - gi[3]) * dx + (gn[4] - gi[4]) * dy + (gn[5] - gi[5]) * dz) * s;
-		T* hp = hist + (size_t)j * kRevMoments * G + lane;
-		hp[0 * G] += gR;
-		hp[1 * G] += gR * t;
-		hp[2 * G] += gR * t * t;
-		hp[3 * G] += gI;
-		hp[4 * G] += gI * t;
-		hp[5 * G] += gI * t * t;
+		const T t2 = t * t;
+		T v[8] = {gR, gR * t, gR * t2, gI, gI * t, gI * t2, T(0), T(0)};
+		hist_add8<HIST, T, G>(hist, j, lane, v, kRevMoments);
 	}
 }
 
-// Sum lane-private histograms [nbin][nm][G] into red[nbin*nm] and clear them.
-template <typename T, int G>
+// Sum lane-private histograms into red[nbin*nm] and clear them.
+template <typename T, int G, int HIST>
 __device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, int lane, unsigned gmask) {
 	__syncwarp(gmask);
-	for (int e = lane; e < nbin * nm; e += G) {
-		T* hp = hist + (size_t)e * G;
-		T s = T(0);
-#pragma unroll 8
-		for (int l = 0; l < G; l++) s += hp[l];
-		red[e] = s;
-	}
+	for (int e = lane; e < nbin * nm; e += G) red[e] = hist_sum<HIST, T, G>(hist, e / nm, e % nm);
 	__syncwarp(gmask);
-	for (int e = lane; e < nbin * nm * G; e += G) hist[e] = T(0);
+	for (int e = lane; e < nbin * kHistSlots * G; e += G) hist[e] = T(0);
 	__syncwarp(gmask);
 }
 
-template <typename T, int G, bool ADJ>
+template <typename T, int G, bool ADJ, int HIST>
 __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
                                               const T* __restrict__ kb_g, const T* __restrict__ hv_g,
                                               const int* __restrict__ lut_g, const T* __restrict__ loc_g,
@@ -179,7 +214,7 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
                                               T* __restrict__ O_o, T* __restrict__ eloc_o, T* __restrict__ other_o,
                                               T* __restrict__ dE_o) {
 	constexpr int NM = ADJ ? kFwdMomentsAdj : kFwdMoments;
-	constexpr int NMH = NM > kRevMoments ? NM : kRevMoments;
+	constexpr int NMH = kHistSlots;
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
 	Q4<T>* coefC = reinterpret_cast<Q4<T>*>(smem_raw);
@@ -205,7 +240,7 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 	unsigned char* gbase = smem_raw + cta_b + (size_t)gib * grp_b;
 	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
 	T* Gs = reinterpret_cast<T*>(xs + n);
-	T* hist = Gs + (ADJ ? (size_t)n * 6 : 0);
+	T* hist = Gs + (ADJ ? (size_t)((n * 6 + 7) & ~7) : 0);
 	T* red = hist + (size_t)nbin * NMH * G;
 	T* redr = red + (size_t)nbin * NM;
 	T* spl = redr + (ADJ ? (size_t)nbin * kRevMoments : 0);  // [ns][4]: S, Lsp, AR, AI
@@ -236,9 +271,9 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 			KSum<T> acc[8];
 			const int base = s * G;
 			const int dend = (base + G < n) ? base + G : n;
-			fwd_region<T, G, 1, ADJ>(sc, 0, base, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
-			fwd_region<T, G, 2, ADJ>(sc, base, dend, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
-			fwd_region<T, G, 0, ADJ>(sc, dend, n, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			fwd_region<T, G, 1, ADJ, HIST>(sc, 0, base, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			fwd_region<T, G, 2, ADJ, HIST>(sc, base, dend, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			fwd_region<T, G, 0, ADJ, HIST>(sc, dend, n, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
 			const T gRx = acc[0].value(), gRy = acc[1].value(), gRz = acc[2].value();
 			const T gIx = acc[3].value(), gIy = acc[4].value(), gIz = acc[5].value();
 			if (rowok) {
@@ -269,7 +304,7 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 #pragma unroll
 		for (int o = G / 2; o > 0; o >>= 1) nout_all += __shfl_xor_sync(gmask, nout_all, o, G);
 
-		hist_reduce<T, G>(hist, red, nbin, NM, lane, gmask);
+		hist_reduce<T, G, HIST>(hist, red, nbin, NM, lane, gmask);
 
 		if (ADJ) {
 			for (int s = 0; s < nslot; s++) {
@@ -281,10 +316,10 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 					for (int k = 0; k < 6; k++) gn[k] = Gs[(size_t)nrow * 6 + k];
 				const int base = s * G;
 				const int dend = (base + G < n) ? base + G : n;
-				rev_region<T, G, false>(sc, 0, base, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
-				rev_region<T, G, true>(sc, base, dend, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
+				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
+				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
 			}
-			hist_reduce<T, G>(hist, redr, nbin, kRevMoments, lane, gmask);
+			hist_reduce<T, G, HIST>(hist, redr, nbin, kRevMoments, lane, gmask);
 		}
 
 		// moments -> spline values: spline sp = j + 3 - q on interval j

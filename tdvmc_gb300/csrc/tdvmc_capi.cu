@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -31,6 +32,7 @@ struct Tiles {
 	int sgpb = 4;    // sampler walkers per block
 	int eg = 32;     // evaluation lanes per walker
 	int egpb = 1;    // evaluation walkers per block
+	int hist = 0;    // histogram update mode of the evaluation kernel (full-warp groups)
 };
 
 struct GraphKey {
@@ -74,6 +76,7 @@ struct tdvmc_ctx {
 	void* gramws = nullptr;
 	DynState* dyn = nullptr;
 	int nblk1 = 0, nblk2 = 0, chunk2 = 0, nblkS = 0;
+	bool gram_tc = false;  // S on the tensor cores (mixed precision only)
 	std::map<GraphKey, cudaGraphExec_t> graphs;
 	std::string err;
 	// eager profiling: events recorded after every kernel when set
@@ -203,7 +206,7 @@ size_t eloc_smem(tdvmc_ctx* ctx, int G, int gpb, bool adj) {
 template <typename T>
 int launch_eloc(tdvmc_ctx* ctx, bool adj) {
 	const int G = ctx->tiles.eg, gpb = ctx->tiles.egpb;
-	ElocFn<T> fn = pick_eloc<T>(G, adj);
+	ElocFn<T> fn = pick_eloc<T>(G, adj, G == 32 ? ctx->tiles.hist : 0);
 	if (!fn) return TDVMC_ERR_ARG;
 	const int threads = G * gpb;
 	const size_t smem = eloc_smem<T>(ctx, G, gpb, adj);
@@ -232,7 +235,7 @@ int launch_reduce(tdvmc_ctx* ctx, bool adj) {
 	mark(ctx, "k_finalize1");
 	ctx->launches += 2;
 	CK(cudaGetLastError());
-	const bool tc = (ctx->prec == TDVMC_PREC_MIXED) && gram_supported(P);
+	const bool tc = ctx->gram_tc;
 	const size_t sm2 = (size_t)ctx->chunk2 * (P + 2) * sizeof(double);
 	CK(cudaFuncSetAttribute((const void*)k_reduce2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
 	k_reduce2<T><<<ctx->nblk2, 256, sm2, ctx->st>>>(P, ctx->nw, ctx->chunk2, (const T*)ctx->O, (const T*)ctx->eloc,
@@ -267,7 +270,7 @@ int launch_solve(tdvmc_ctx* ctx, int imag, int pre, int lin, int mode, int norm,
 	a.mode = mode;
 	a.normalize = norm;
 	a.dt = dt;
-	const bool tc = (ctx->prec == TDVMC_PREC_MIXED) && gram_supported(P);
+	const bool tc = ctx->gram_tc;
 	const double* S = tc ? ctx->Sg : ctx->C2;
 	a.ldS = tc ? P : P + 2;
 	a.ldC = P + 2;
@@ -334,7 +337,7 @@ int get_graph(tdvmc_ctx* ctx, const tdvmc_step_opts* o, cudaGraphExec_t* out) {
 
 int kernels_per_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
 	int k = 1 + (o->moves_per_stage > 0 ? 1 : 0) + 1 + 4 + 1;
-	if (ctx->prec == TDVMC_PREC_MIXED && gram_supported(ctx->sc.p)) k += 2;
+	if (ctx->gram_tc) k += 2;
 	return k;
 }
 
@@ -518,6 +521,12 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	c.chunk2 = (int)std::max<int64_t>(1, std::min<int64_t>(128, (96 * 1024) / ((P + 2) * 8)));
 	c.nblk2 = (int)((nw + c.chunk2 - 1) / c.chunk2);
 	c.nblkS = gram_blocks(nw, c.nsm);
+	{
+		// S = Oc^T Oc on the tensor cores in mixed precision when TDVMC_GRAM=tc
+		const char* g = std::getenv("TDVMC_GRAM");
+		const bool want_tc = g && std::strcmp(g, "tc") == 0;
+		c.gram_tc = (c.prec == TDVMC_PREC_MIXED) && want_tc && gram_supported(P);
+	}
 	bool ok = true;
 	auto A = [&](void** p, size_t bytes) {
 		if (!ok) return;
@@ -600,6 +609,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	c.tiles.sgpb = 128 / c.tiles.sg;
 	c.tiles.eg = c.tiles.sg;
 	c.tiles.egpb = std::max(1, 32 / c.tiles.eg);
+	if (const char* h = std::getenv("TDVMC_HIST")) c.tiles.hist = std::max(0, std::min(2, std::atoi(h)));
 	*out = ctx;
 	return TDVMC_OK;
 }
@@ -753,7 +763,7 @@ int tdvmc_reduce_stats(tdvmc_ctx* ctx, tdvmc_stats* stats, double* O_mean, doubl
 	CK(cudaMemcpyAsync(c2.data(), ctx->C2, c2.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
 	CK(cudaMemcpyAsync(sg.data(), ctx->Sg, sg.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
 	CK(cudaStreamSynchronize(ctx->st));
-	const bool tc = (ctx->prec == TDVMC_PREC_MIXED) && gram_supported(P);
+	const bool tc = ctx->gram_tc;
 	if (stats) {
 		fill_stats(ctx, m, ctx->last_moves, stats);
 		stats->status = 0;
