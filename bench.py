@@ -206,8 +206,9 @@ def run_ours(args):
 
     lib = Nat.load()
     uR, uI = initial_params()
-    R0 = initial_walkers(NW)
-    sysm = T.BosonsBulk(DIM, N, P, L, NW, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
+    nw = args.walkers
+    R0 = initial_walkers(nw)
+    sysm = T.BosonsBulk(DIM, N, P, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
                         precision="mixed")
     sysm.SetParameters(uR, uI)
     sysm.SetWalkers(R0)
@@ -226,6 +227,11 @@ def run_ours(args):
     launches_b = sysm.LaunchCount()
     clk = clocks.stop()
     value_rank = args.steps / (ms / 1000.0)
+    if args.no_extras:
+        # profiling runs: the timed steps only
+        if rank == 0:
+            print(json.dumps({"walkers": nw, "steps": args.steps, "ms_per_step": ms / args.steps}))
+        return
 
     # per-kernel device times of one eager stage (CUDA events around each kernel)
     prof = td.profile_stage()
@@ -333,6 +339,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--autotune", type=int, default=0)
+    ap.add_argument("--walkers", type=int, default=NW, help="walkers (default: the 65,536 of the workload)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="time the steps only (no e2e, FP64, CPU or gate legs): for profiler runs on a small case")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

@@ -29,7 +29,9 @@ namespace tdvmc {
 constexpr int kFwdMoments = 4;     // sum t^c, c = 0..3
 constexpr int kFwdMomentsAdj = 7;  // + sum t^c / r, c = 0..2
 constexpr int kRevMoments = 6;     // complex sum g t^c, c = 0..2
-constexpr int kHistSlots = 8;      // histogram slots per interval and lane (max of the above, padded)
+constexpr int kHistSlots = 8;      // histogram slots per interval and lane in the float4 mode
+// slots per interval and lane: the largest moment count (7), or 8 for the float4 mode
+template <int HIST> struct HistSlots { static constexpr int value = HIST == 1 ? 8 : 7; };
 
 // Histogram update modes of the lane-private moment histograms:
 //   0  scalar read-modify-write      hist[(j*8 + m)*G + lane]
@@ -54,7 +56,7 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 			h4[G] = b;
 		}
 	} else {
-		T* hp = hist + (size_t)j * kHistSlots * G + lane;
+		T* hp = hist + (size_t)j * HistSlots<HIST>::value * G + lane;
 #pragma unroll
 		for (int m = 0; m < 8; m++) {
 			if (m >= nv) break;
@@ -73,7 +75,7 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 #pragma unroll 8
 		for (int l = 0; l < G; l++) s += h[l * 4];
 	} else {
-		const T* h = hist + ((size_t)j * kHistSlots + m) * G;
+		const T* h = hist + ((size_t)j * HistSlots<HIST>::value + m) * G;
 #pragma unroll 8
 		for (int l = 0; l < G; l++) s += h[l];
 	}
@@ -89,9 +91,9 @@ __host__ __device__ inline size_t eloc_cta_bytes(int nbin, int ncell) {
 	return (b + 31) & ~(size_t)31;
 }
 template <typename T>
-__host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G, bool adj) {
+__host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G, bool adj, int hist_mode = 0) {
 	int nm = adj ? kFwdMomentsAdj : kFwdMoments;
-	int nmh = kHistSlots;
+	int nmh = hist_mode == 1 ? 8 : 7;
 	size_t b = (size_t)n * sizeof(Q4<T>);
 	if (adj) b += (size_t)((n * 6 + 7) & ~7) * sizeof(T);  // keeps the histogram 32-byte aligned
 	b += (size_t)nbin * nmh * G * sizeof(T);
@@ -201,7 +203,7 @@ __device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, i
 	__syncwarp(gmask);
 	for (int e = lane; e < nbin * nm; e += G) red[e] = hist_sum<HIST, T, G>(hist, e / nm, e % nm);
 	__syncwarp(gmask);
-	for (int e = lane; e < nbin * kHistSlots * G; e += G) hist[e] = T(0);
+	for (int e = lane; e < nbin * HistSlots<HIST>::value * G; e += G) hist[e] = T(0);
 	__syncwarp(gmask);
 }
 
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
                                               T* __restrict__ O_o, T* __restrict__ eloc_o, T* __restrict__ other_o,
                                               T* __restrict__ dE_o) {
 	constexpr int NM = ADJ ? kFwdMomentsAdj : kFwdMoments;
-	constexpr int NMH = kHistSlots;
+	constexpr int NMH = HistSlots<HIST>::value;
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
 	Q4<T>* coefC = reinterpret_cast<Q4<T>*>(smem_raw);
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 	T* hv = kb + nbin;
 	int* lut = reinterpret_cast<int*>(hv + nbin);
 	const size_t cta_b = eloc_cta_bytes<T>(nbin, sc.ncell);
-	const size_t grp_b = eloc_group_bytes<T>(n, nbin, ns, G, ADJ);
+	const size_t grp_b = eloc_group_bytes<T>(n, nbin, ns, G, ADJ, HIST);
 
 	for (int i = threadIdx.x; i < 2 * nbin; i += blockDim.x) coefC[i] = coefC_g[i];
 	for (int i = threadIdx.x; i < nbin; i += blockDim.x) {

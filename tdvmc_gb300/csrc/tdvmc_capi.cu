@@ -200,7 +200,7 @@ int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed) {
 template <typename T>
 size_t eloc_smem(tdvmc_ctx* ctx, int G, int gpb, bool adj) {
 	return eloc_cta_bytes<T>(ctx->sc.nbin, ctx->sc.ncell) +
-	       (size_t)gpb * eloc_group_bytes<T>(ctx->sc.n, ctx->sc.nbin, ctx->sc.ns, G, adj);
+	       (size_t)gpb * eloc_group_bytes<T>(ctx->sc.n, ctx->sc.nbin, ctx->sc.ns, G, adj, G == 32 ? ctx->tiles.hist : 0);
 }
 
 template <typename T>
@@ -522,9 +522,10 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	c.nblk2 = (int)((nw + c.chunk2 - 1) / c.chunk2);
 	c.nblkS = gram_blocks(nw, c.nsm);
 	{
-		// S = Oc^T Oc on the tensor cores in mixed precision when TDVMC_GRAM=tc
+		// S = Oc^T Oc on the tensor cores in mixed precision (TDVMC_GRAM=fp64 selects
+		// the FP64 CUDA-core contraction instead)
 		const char* g = std::getenv("TDVMC_GRAM");
-		const bool want_tc = g && std::strcmp(g, "tc") == 0;
+		const bool want_tc = !(g && std::strcmp(g, "fp64") == 0);
 		c.gram_tc = (c.prec == TDVMC_PREC_MIXED) && want_tc && gram_supported(P);
 	}
 	bool ok = true;
