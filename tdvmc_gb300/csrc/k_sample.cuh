@@ -24,22 +24,43 @@ template <typename T> struct alignas(4 * sizeof(T)) Q4 {
 	T x, y, z, w;
 };
 
+// Pair function at squared distance r2.  coef holds nbin + 1 cubics; entry
+// nbin is the constant outer-pair value uR[p-1] (coefficients (u, 0, 0, 0)),
+// selected for r >= r_max by the clamp of the interval index.
 template <typename T>
-__device__ __forceinline__ T pair_u(const SysConst& sc, T r2, const Q4<T>* coef, const T* kb, const T* hv,
-                                    const int* lut, T uout) {
-	T rinv = rsqrt_(r2);
-	T r = r2 * rinv;
+__device__ __forceinline__ T pair_u(const SysConst& sc, T r2, const Q4<T>* __restrict__ coef,
+                                    const T* __restrict__ kb, const T* __restrict__ hv,
+                                    const int* __restrict__ lut) {
+	const T rinv = rsqrt_(r2);
+	const T r = r2 * rinv;
 	T t;
-	int j = locate<T>(sc, r, kb, hv, lut, t);
-	Q4<T> c = coef[j];
-	T u = c.x + t * (c.y + t * (c.z + t * c.w));
-	return r <= (T)sc.rmax ? u : uout;
+	int j;
+	if (sc.uniform) {
+		const T x = r * (T)sc.hinv;
+		T jf;
+		j = floor_clamp(x, sc.nbin, jf);
+		t = x - jf;
+	} else {
+		j = locate<T>(sc, r, kb, hv, lut, t);
+		j = r < (T)sc.rmax ? j : sc.nbin;
+	}
+	const Q4<T> c = coef[j];
+	return c.x + t * (c.y + t * (c.z + t * c.w));
+}
+
+// squared minimum-image distance of two positions inside [-L/2, L/2]:
+// per axis min(|d|, L - |d|), exact for |d| <= L (Sterbenz)
+template <typename T>
+__device__ __forceinline__ T mi_r2(T dx, T dy, T dz, T L) {
+	const T ax = fabs(dx), ay = fabs(dy), az = fabs(dz);
+	const T mx = fmin(ax, L - ax), my = fmin(ay, L - ay), mz = fmin(az, L - az);
+	return mx * mx + my * my + mz * mz;
 }
 
 // Shared memory: coef[nbin] | kb[nbin] | hv[nbin] | lut[ncell] | mirror[groups][n]
 template <typename T>
 __host__ __device__ inline size_t sample_smem_bytes(int nbin, int ncell, int n, int groups) {
-	size_t b = (size_t)nbin * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+	size_t b = (size_t)(nbin + 1) * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
 	b = (b + 31) & ~(size_t)31;
 	return b + (size_t)groups * n * sizeof(Q4<T>);
 }
@@ -52,15 +73,15 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
                                                 int* __restrict__ acc_out) {
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	Q4<T>* coef = reinterpret_cast<Q4<T>*>(smem_raw);
-	T* kb = reinterpret_cast<T*>(coef + sc.nbin);
+	T* kb = reinterpret_cast<T*>(coef + sc.nbin + 1);
 	T* hv = kb + sc.nbin;
 	int* lut = reinterpret_cast<int*>(hv + sc.nbin);
-	size_t off = (size_t)sc.nbin * sizeof(Q4<T>) + 2 * (size_t)sc.nbin * sizeof(T) + (size_t)sc.ncell * sizeof(int);
+	size_t off = (size_t)(sc.nbin + 1) * sizeof(Q4<T>) + 2 * (size_t)sc.nbin * sizeof(T) + (size_t)sc.ncell * sizeof(int);
 	off = (off + 31) & ~(size_t)31;
 	Q4<T>* mirror_all = reinterpret_cast<Q4<T>*>(smem_raw + off);
 
+	for (int i = threadIdx.x; i <= sc.nbin; i += blockDim.x) coef[i] = coef_g[i];
 	for (int i = threadIdx.x; i < sc.nbin; i += blockDim.x) {
-		coef[i] = coef_g[i];
 		kb[i] = kb_g[i];
 		hv[i] = hv_g[i];
 	}
@@ -76,8 +97,8 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
 	Q4<T>* xs = mirror_all + (size_t)gib * n;
 	const T L = (T)sc.L, Lr = (T)sc.Lr;
-	const T uout = *uout_g;
 	const uint32_t pass = *pass_ptr;
+	(void)uout_g;
 
 	for (int64_t w = (int64_t)blockIdx.x * gpb + gib; w < nw; w += (int64_t)gridDim.x * gpb) {
 		T* pw = pos + (size_t)w * sc.dim * n;
@@ -87,9 +108,10 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 			int i = s * G + lane;
 			x[s] = y[s] = z[s] = T(0);
 			if (i < n) {
-				x[s] = pw[i];
-				if (sc.dim > 1) y[s] = pw[n + i];
-				if (sc.dim > 2) z[s] = pw[2 * n + i];
+				// positions into [-L/2, L/2] (AlignCoordinates, TDVMC.cpp:2569-2582)
+				x[s] = nic(pw[i], L, Lr);
+				if (sc.dim > 1) y[s] = nic(pw[n + i], L, Lr);
+				if (sc.dim > 2) z[s] = nic(pw[2 * n + i], L, Lr);
 				xs[i] = Q4<T>{x[s], y[s], z[s], T(0)};
 			}
 		}
@@ -115,17 +137,17 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 				const T xn0 = nic(xo.x + e0, L, Lr);
 				const T xn1 = nic(xo.y + e1, L, Lr);
 				const T xn2 = nic(xo.z + e2, L, Lr);
+				// the moved particle's own slot in this lane, -1 elsewhere
+				const int self_slot = (lane == (p & (G - 1))) ? p / G : -1;
 				T dsum = T(0);
 #pragma unroll
 				for (int s = 0; s < SLOTS; s++) {
-					const int i = s * G + lane;
-					const bool valid = (i < n) && (i != p);
-					T a0 = nic(x[s] - xn0, L, Lr), a1 = nic(y[s] - xn1, L, Lr), a2 = nic(z[s] - xn2, L, Lr);
-					T b0 = nic(x[s] - xo.x, L, Lr), b1 = nic(y[s] - xo.y, L, Lr), b2 = nic(z[s] - xo.z, L, Lr);
-					T r2n = a0 * a0 + a1 * a1 + a2 * a2;
-					T r2o = b0 * b0 + b1 * b1 + b2 * b2;
-					T un = pair_u<T>(sc, r2n, coef, kb, hv, lut, uout);
-					T uo = pair_u<T>(sc, r2o, coef, kb, hv, lut, uout);
+					bool valid = (s != self_slot);
+					if (s == SLOTS - 1) valid = valid && (s * G + lane < n);
+					const T r2n = mi_r2(x[s] - xn0, y[s] - xn1, z[s] - xn2, L);
+					const T r2o = mi_r2(x[s] - xo.x, y[s] - xo.y, z[s] - xo.z, L);
+					const T un = pair_u<T>(sc, r2n, coef, kb, hv, lut);
+					const T uo = pair_u<T>(sc, r2o, coef, kb, hv, lut);
 					dsum += valid ? (un - uo) : T(0);
 				}
 #pragma unroll

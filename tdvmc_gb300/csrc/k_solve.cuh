@@ -291,7 +291,12 @@ __global__ void __launch_bounds__(128) k_prep(int p, int ns, int nbin, const dou
 			coefC[j * 8 + 4 + c] = (T)ci[c];
 		}
 	}
-	if (threadIdx.x == 0) *uout = (T)params[p - 1];
+	if (threadIdx.x == 0) {
+		*uout = (T)params[p - 1];
+		// entry nbin of the sampler table: the constant outer-pair value
+		coefU[nbin * 4 + 0] = (T)params[p - 1];
+		coefU[nbin * 4 + 1] = coefU[nbin * 4 + 2] = coefU[nbin * 4 + 3] = (T)0;
+	}
 }
 
 }  // namespace tdvmc

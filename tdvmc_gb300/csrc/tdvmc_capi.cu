@@ -546,7 +546,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	A((void**)&c.rhs, np * sizeof(double));
 	A((void**)&c.loc_d, c.loc.size() * sizeof(double));
 	A((void**)&c.fold_d, c.fold.size() * sizeof(double));
-	A(&c.coefU, (size_t)s.nbin * 4 * ts);
+	A(&c.coefU, (size_t)(s.nbin + 1) * 4 * ts);
 	A(&c.coefC, (size_t)s.nbin * 8 * ts);
 	A(&c.uout, 32);
 	A(&c.kb, (size_t)s.nbin * ts);
