@@ -24,28 +24,37 @@ template <typename T> struct alignas(4 * sizeof(T)) Q4 {
 	T x, y, z, w;
 };
 
-// Pair function at squared distance r2.  coef holds nbin + 1 cubics; entry
-// nbin is the constant outer-pair value uR[p-1] (coefficients (u, 0, 0, 0)),
-// selected for r >= r_max by the clamp of the interval index.
+// Pair function at squared distance r2.  coef holds nbin + 1 cubics in the
+// centred local coordinate tau = t - 1/2 (better conditioned and one
+// operation shorter); entry nbin is the constant outer-pair value uR[p-1]
+// (coefficients (u, 0, 0, 0)), selected for r >= r_max by the clamp of the
+// interval index.
 template <typename T>
 __device__ __forceinline__ T pair_u(const SysConst& sc, T r2, const Q4<T>* __restrict__ coef,
                                     const T* __restrict__ kb, const T* __restrict__ hv,
                                     const int* __restrict__ lut) {
 	const T rinv = rsqrt_(r2);
 	const T r = r2 * rinv;
-	T t;
+	T tau;
 	int j;
 	if (sc.uniform) {
-		const T x = r * (T)sc.hinv;
-		T jf;
-		j = floor_clamp(x, sc.nbin, jf);
-		t = x - jf;
+		// floor(x) = round(x - 1/2), x = r / h, without conversions (see nic)
+		const T xm = fma(r, (T)sc.hinv, T(-0.5));
+		const T R = sizeof(T) == 4 ? (T)kRoundF : (T)kRoundD;
+		T y = xm + R;
+		y = fmin(y, R + (T)sc.nbin);
+		const T jf = y - R;
+		tau = xm - jf;
+		if (sizeof(T) == 4) j = __float_as_int((float)y) - __float_as_int(kRoundF);
+		else j = (int)(__double_as_longlong((double)y) - __double_as_longlong(kRoundD));
 	} else {
+		T t;
 		j = locate<T>(sc, r, kb, hv, lut, t);
 		j = r < (T)sc.rmax ? j : sc.nbin;
+		tau = t - T(0.5);
 	}
 	const Q4<T> c = coef[j];
-	return c.x + t * (c.y + t * (c.z + t * c.w));
+	return c.x + tau * (c.y + tau * (c.z + tau * c.w));
 }
 
 // squared minimum-image distance of two positions inside [-L/2, L/2]:

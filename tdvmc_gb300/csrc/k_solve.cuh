@@ -224,7 +224,12 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 	__syncthreads();
 
 	if (a.mode == 0) {
-		if (tid == 0 && bad) dyn->status |= kStatusNotPD;
+		if (tid == 0) {
+			int st = bad ? kStatusNotPD : 0;
+			for (int i = 0; i < np; i++)
+				if (!isfinite(rhs_out[i])) st |= kStatusNonFinite;
+			dyn->status |= st;
+		}
 		return;
 	}
 	if (a.mode == 2 || stage == 3) {
@@ -286,10 +291,14 @@ __global__ void __launch_bounds__(128) k_prep(int p, int ns, int nbin, const dou
 			}
 		}
 		for (int c = 0; c < 4; c++) {
-			coefU[j * 4 + c] = (T)cr[c];
 			coefC[j * 8 + c] = (T)cr[c];
 			coefC[j * 8 + 4 + c] = (T)ci[c];
 		}
+		// sampler table: the real cubic in tau = t - 1/2 (Taylor shift by 1/2)
+		coefU[j * 4 + 0] = (T)(cr[0] + 0.5 * cr[1] + 0.25 * cr[2] + 0.125 * cr[3]);
+		coefU[j * 4 + 1] = (T)(cr[1] + cr[2] + 0.75 * cr[3]);
+		coefU[j * 4 + 2] = (T)(cr[2] + 1.5 * cr[3]);
+		coefU[j * 4 + 3] = (T)cr[3];
 	}
 	if (threadIdx.x == 0) {
 		*uout = (T)params[p - 1];

@@ -1,0 +1,125 @@
+"""GPU: determinism of the mixed path, failure reporting, the native host
+driver on a reference-style config, and a full-size property check."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _system(precision="mixed", nw=512, n=64, p=12, L=6.0, seed=0):
+    import tdvmc_gb300 as T
+    rng = np.random.default_rng(seed)
+    s = T.BosonsBulk(3, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=0.09, precision=precision)
+    r = np.linspace(0, L / 2, p)
+    uR = -0.5 * (1.1 / np.maximum(r, 0.5)) ** 5
+    uR -= uR[-1]
+    s.SetParameters(uR, 0.01 * rng.normal(size=p))
+    m = round(n ** (1 / 3))
+    l = L / m
+    idx = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    R = idx[None] * l + (rng.uniform(size=(nw, n, 3)) - 0.5) * l / 10 - L / 2
+    s.SetWalkers(np.ascontiguousarray(np.transpose(R, (0, 2, 1))))
+    return s
+
+
+def test_mixed_step_is_deterministic():
+    import tdvmc_gb300 as T
+    outs = []
+    for _ in range(2):
+        s = _system()
+        td = T.TDVP(s, 1e-3, 128, 0.25, seed=7, use_adjoint=1)
+        td.step(2)
+        outs.append((s.GetParameters(), s.GetWalkers()))
+        s.close()
+    (p1, w1), (p2, w2) = outs
+    assert np.array_equal(p1[0], p2[0]) and np.array_equal(p1[1], p2[1])
+    assert p1[2] == p2[2] and p1[3] == p2[3]
+    assert np.array_equal(w1, w2)
+
+
+def test_zero_variance_parameter_with_preconditioning_is_reported():
+    """O_0 has no pair in its support, so S_00 = 0; the reference's diagonal
+    scaling divides by zero (TDVMC.cpp:1690-1699).  The device reports the
+    non-finite result through the status instead of continuing silently."""
+    from tdvmc_gb300 import _native as N
+    s = _system(precision="fp64", nw=256)
+    s.CalculateExpectationValues()
+    st = s.ReduceStatistics()
+    assert st["S"][0, 0] == 0.0
+    P = s.p
+    import ctypes as C
+    uR, uI = np.zeros(P), np.zeros(P)
+    pr, pi = C.c_double(), C.c_double()
+    code = s.lib.tdvmc_tdvp_rhs(s.h, 0, 1, 0, uR.ctypes.data_as(C.c_void_p), uI.ctypes.data_as(C.c_void_p),
+                                C.byref(pr), C.byref(pi))
+    assert code == N.ERR_NONFINITE
+    # without preconditioning the regularised system is fine
+    r = s.SolveForParametersDot(0, 0, 0)
+    assert np.all(np.isfinite(r[0])) and not r[4]
+
+
+def test_native_driver_runs_a_reference_config(tmp_path):
+    from tdvmc_gb300 import build as B
+    B.build()
+    cfg = {
+        "CONFIG_VERSION": "0.24", "SYSTEM_TYPE": "BosonsBulk", "N": 27, "LBOX": 3.6, "DIM": 3, "N_PARAM": 10,
+        "MC_STEP": 0.3, "MC_NSTEPS": 256, "MC_NTHERMSTEPS": 54, "MC_VERY_FIRST_NINITIALIZATIONSTEPS": 270,
+        "TIMESTEP": 0.001, "TOTALTIME": 0.0025, "IMAGINARY_TIME": 1, "ODE_SOLVER_TYPE": 2,
+        "LINEAR_EQUATION_SOLVER_TYPE": 0, "USE_PRECONDITIONING": 0, "USE_NORMALIZE_WF": 1,
+        "WRITE_EVERY_NTH_STEP_TO_FILE": 1, "USE_NURBS": 0, "NURBS_GRID": [0.0], "SYSTEM_PARAMS": [0.6, 1.0],
+        "PARAMS_REAL": [-2.0, -2.0, -1.0, -0.5, -0.2, -0.1, -0.05, 0.0, 0.0, 0.0], "PARAMS_IMAGINARY": [0.0],
+        "PARAM_PHIR": 0.0, "PARAM_PHII": 0.0, "GPU_PRECISION": "fp64",
+    }
+    path = tmp_path / "run.config"
+    path.write_text(json.dumps(cfg))
+    out = tmp_path / "out"
+    r = subprocess.run([B.RUNNER, str(path), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    for name in ("timesSystem", "LocalEnergyR", "LocalEnergyI", "LocalOperators", "OtherExpectationValues",
+                 "ParametersR", "ParametersI", "AllLocalEnergyR", "AllParametersR"):
+        assert (out / (name + ".dat")).exists(), name
+    er = np.loadtxt(out / "LocalEnergyR.dat")
+    assert er.size == 3 and np.all(np.isfinite(er))
+    pr = np.loadtxt(out / "ParametersR.dat")
+    assert pr.shape == (3, 11)
+    assert np.all(np.isfinite(pr))
+
+
+def test_full_size_mixed_step_energy_gate():
+    """The benchmark workload at full size (65,536 walkers): one RK4 step, then
+    the FP64 evaluation of the same walkers agrees with the mixed one to
+    |dE/N| < 1e-5 (the metric's gate), and S is symmetric positive
+    semi-definite."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    import tdvmc_gb300 as T
+    s = T.BosonsBulk(3, 343, 30, bench.L, bench.NW, system_params=(1.0, 1.0), potential="lj",
+                     hbar2_2m=bench.HBAR2_2M, precision="mixed")
+    uR, uI = bench.initial_params()
+    s.SetParameters(uR, uI)
+    s.SetWalkers(bench.initial_walkers(bench.NW))
+    td = T.TDVP(s, bench.DT, bench.MOVES, bench.MC_STEP, seed=1, use_adjoint=1)
+    out = td.step()
+    assert out["status"] == 0
+    f = s.CalculateExpectationValues()
+    st = s.ReduceStatistics()
+    ev = np.linalg.eigvalsh(st["S"])
+    assert ev.min() > -1e-9 * ev.max()
+    nsub = 2048
+    R = s.GetWalkers()[:nsub]
+    g = s.GetParameters()
+    s64 = T.BosonsBulk(3, 343, 30, bench.L, nsub, system_params=(1.0, 1.0), potential="lj",
+                       hbar2_2m=bench.HBAR2_2M, precision="fp64")
+    s64.SetParameters(*g)
+    s64.SetWalkers(R)
+    f64 = s64.CalculateExpectationValues()
+    dE = abs(f["eloc"][:nsub, 0].mean() - f64["eloc"][:, 0].mean()) / 343
+    assert dE < 1e-5
+    assert np.abs(f["eloc"][:nsub, 0] - f64["eloc"][:, 0]).max() < 1e-4 * np.abs(f64["eloc"][:, 0]).max()
