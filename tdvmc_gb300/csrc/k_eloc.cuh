@@ -5,22 +5,20 @@
 // CalculateOtherLocalOperators and CalculateExpectationValues
 // (BosonsBulk.cpp:179-218, 220-336, 349-458, 522-545).
 //
-// One group of G lanes owns one walker.  Rows n = s*G + lane (slot s) are
-// lane-owned; each lane walks the half shell of partners i = n + t (mod N),
-// t = 1..(N-1)/2 (N even: t = N/2 only for n < N/2), so every unordered pair
-// is visited exactly once.  The row's complex gradient G_n and the Laplacian
-// accumulate in registers with compensated block sums.  The partner's share
-// -g d of G_i travels systolically: the partner accumulator of lane l holds
-// the sum for target base + l + t, shifts one lane down per step, and lane 0
-// flushes the completed target to shared memory, so no two lanes ever write
-// the same entry.  Pair statistics that are linear in the spline basis
-// (O_k, and for the adjoint the alpha-independent Laplacian of O_k) are
-// accumulated as per-interval moments sum t^c (and sum t^c / r) in
-// lane-private shared histograms.  Reverse sweep (adjoint): the same half
-// shell once more, recomputing minimum-image distances and accumulating
-// sum t^c g with g = (G_n - G_i) . rhat_ni; no pair table is stored.
-// Moments are turned into spline values with the local piece polynomials
-// and folded to the p parameters at the end.
+// One group of G lanes owns one walker.  Forward sweep: lane l owns row
+// particle n = s*G + l of slot s and loops over all partners i (the partner
+// coordinate is a shared-memory broadcast), accumulating the complex
+// gradient G_n and Laplacian of ln psi in registers with compensated block
+// sums.  Pair statistics that are linear in the spline basis (O_k, and for
+// the adjoint the alpha-independent Laplacian of O_k) are accumulated as
+// per-interval moments sum t^c (and sum t^c / r) in lane-private shared
+// histograms; partners below the slot base are counted once per unordered
+// pair with warp-uniform control flow (the diagonal block is the only mixed
+// region).  Reverse sweep (adjoint): one pass over unordered pairs that
+// recomputes minimum-image distances and accumulates sum t^c g with
+// g = (G_n - G_i) . rhat_ni; no pair table is stored.  Moments are turned
+// into spline values with the local piece polynomials and folded to the p
+// parameters at the end.
 #pragma once
 
 #include "common.cuh"
@@ -97,7 +95,7 @@ __host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int 
 	int nm = adj ? kFwdMomentsAdj : kFwdMoments;
 	int nmh = hist_mode == 1 ? 8 : 7;
 	size_t b = (size_t)n * sizeof(Q4<T>);
-	b += (size_t)n * 8 * sizeof(T);  // G_n: (Re xyz, pad, Im xyz, pad)
+	if (adj) b += (size_t)((n * 6 + 7) & ~7) * sizeof(T);  // keeps the histogram 32-byte aligned
 	b += (size_t)nbin * nmh * G * sizeof(T);
 	b += (size_t)nbin * (nm + (adj ? kRevMoments : 0)) * sizeof(T);
 	b += (size_t)ns * 4 * sizeof(T) + 16 * sizeof(T);
@@ -111,179 +109,140 @@ __device__ __forceinline__ T group_sum(T v, unsigned gmask) {
 	return v;
 }
 
-// Forward sweep of one slot over the half shell (see the file comment).
+// Geometry and spline derivatives of one (row, partner) pair of the forward sweep.
+template <typename T> struct FwdPair {
+	T dx, dy, dz, r, rinv, t;
+	T gR, gI, lR, lI;
+	int j;
+	bool in;
+};
+
+template <typename T>
+__device__ __forceinline__ FwdPair<T> fwd_pair(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
+                                               const Q4<T>* __restrict__ coefC, const T* __restrict__ kb,
+                                               const T* __restrict__ hv, const int* __restrict__ lut) {
+	FwdPair<T> q;
+	const T L = (T)sc.L, Lr = (T)sc.Lr;
+	q.dx = nic(xr.x - xi.x, L, Lr);
+	q.dy = nic(xr.y - xi.y, L, Lr);
+	q.dz = nic(xr.z - xi.z, L, Lr);
+	const T r2 = q.dx * q.dx + q.dy * q.dy + q.dz * q.dz;
+	q.rinv = rsqrt_(r2);
+	q.r = r2 * q.rinv;
+	q.in = ok && (q.r <= (T)sc.rmax);
+	q.j = locate<T>(sc, q.r, kb, hv, lut, q.t);
+	const Q4<T> cR = coefC[2 * q.j];
+	const Q4<T> cI = coefC[2 * q.j + 1];
+	const T hj = sc.uniform ? (T)sc.hinv : hv[q.j];
+	const T t = q.t;
+	const T d1R = (cR.y + t * (T(2) * cR.z + T(3) * t * cR.w)) * hj;
+	const T d1I = (cI.y + t * (T(2) * cI.z + T(3) * t * cI.w)) * hj;
+	const T d2R = (T(2) * cR.z + T(6) * t * cR.w) * (hj * hj);
+	const T d2I = (T(2) * cI.z + T(6) * t * cI.w) * (hj * hj);
+	const T dm1 = (T)(sc.dim - 1);
+	q.gR = q.in ? d1R * q.rinv : T(0);
+	q.gI = q.in ? d1I * q.rinv : T(0);
+	q.lR = q.in ? d2R + dm1 * q.gR : T(0);
+	q.lI = q.in ? d2I + dm1 * q.gI : T(0);
+	return q;
+}
+
+// Pair statistics of one counted (unordered) pair: moments and potential.
 template <typename T, int G, bool ADJ, int HIST>
-__device__ __forceinline__ void fwd_slot(const SysConst& sc, int base, int lane, unsigned gmask,
-                                         const Q4<T>* __restrict__ xs, Q4<T>* __restrict__ Gs,
-                                         const Q4<T>* __restrict__ coefC, const T* __restrict__ kb,
-                                         const T* __restrict__ hv, const int* __restrict__ lut,
-                                         T* __restrict__ hist, T pa, T pb, KSum<T>& e_lR, KSum<T>& e_lI,
-                                         KSum<T>& e_v, int& nout) {
-	const int n = sc.n;
-	const int nrow = base + lane;
-	const bool rowok = nrow < n;
-	const int nr = rowok ? nrow : 0;
-	const bool even = (n & 1) == 0;
-	const int tmax = even ? n / 2 : (n - 1) / 2;
-	const int trow = even ? (nrow < n / 2 ? n / 2 : n / 2 - 1) : tmax;
-	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax, dm1 = (T)(sc.dim - 1);
-	const T hu = (T)sc.hinv;
-	const Q4<T> xr = xs[nr];
-	KSum<T> acc[8];
-	// systolic partner accumulator: target index base + lane + t (mod n)
-	T p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
-	for (int c0 = 1; c0 <= tmax; c0 += 32) {
-		const int c1 = (c0 + 31 < tmax) ? c0 + 31 : tmax;
+__device__ __forceinline__ void fwd_stats(const SysConst& sc, const FwdPair<T>& q, bool on, T* __restrict__ hist,
+                                          int lane, T pa, T pb, T& vb) {
+	const T ts = on ? q.t : T(0);  // t is NaN for the self pair
+	const T t2 = ts * ts;
+	const T qq = on ? q.rinv : T(0);
+	T v[8] = {on ? T(1) : T(0), ts, t2, t2 * ts, qq, qq * ts, qq * t2, T(0)};
+	hist_add8<HIST, T, G>(hist, q.j, lane, v, ADJ ? kFwdMomentsAdj : kFwdMoments);
+	vb += on ? pair_pot<T>(sc.pot_kind, q.r, q.rinv, pa, pb) : T(0);
+}
+
+// Forward sweep of row nrow against partners [i0, i1), two partners per
+// iteration so the two dependency chains overlap.
+// ON: 0 = no pair statistics, 1 = all lanes count the pair, 2 = count iff i < nrow.
+template <typename T, int G, int ON, bool ADJ, int HIST>
+__device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
+                                           const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
+                                           const T* __restrict__ kb, const T* __restrict__ hv,
+                                           const int* __restrict__ lut, T* __restrict__ hist, int lane, T pa, T pb,
+                                           KSum<T>* acc /* gRx gRy gRz gIx gIy gIz lR lI */, KSum<T>& vsum, int& nout) {
+	const T rmax = (T)sc.rmax;
+	for (int c0 = i0; c0 < i1; c0 += 32) {
+		const int c1 = (c0 + 32 < i1) ? c0 + 32 : i1;
 		T a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 		T vb = T(0);
-		for (int t = c0; t <= c1; t++) {
-			int i = nr + t;
-			i -= (i >= n) ? n : 0;
-			const bool valid = rowok && (t <= trow);
-			const Q4<T> xi = xs[i];
+		for (int i = c0; i < c1; i += 2) {
+			const bool two = i + 1 < c1;
+			const int ib = two ? i + 1 : i;
+			const Q4<T> xa = xs[i];
+			const Q4<T> xb = xs[ib];
+			const FwdPair<T> qa = fwd_pair<T>(sc, xr, xa, rowok && i != nrow, coefC, kb, hv, lut);
+			const FwdPair<T> qb = fwd_pair<T>(sc, xr, xb, two && rowok && ib != nrow, coefC, kb, hv, lut);
+			a[0] += qa.gR * qa.dx + qb.gR * qb.dx;
+			a[1] += qa.gR * qa.dy + qb.gR * qb.dy;
+			a[2] += qa.gR * qa.dz + qb.gR * qb.dz;
+			a[3] += qa.gI * qa.dx + qb.gI * qb.dx;
+			a[4] += qa.gI * qa.dy + qb.gI * qb.dy;
+			a[5] += qa.gI * qa.dz + qb.gI * qb.dz;
+			a[6] += qa.lR + qb.lR;
+			a[7] += qa.lI + qb.lI;
+			if (ON != 0) {
+				const bool ca = (ON == 1) ? true : (i < nrow);
+				const bool cb = (ON == 1) ? two : (two && ib < nrow);
+				fwd_stats<T, G, ADJ, HIST>(sc, qa, qa.in && ca, hist, lane, pa, pb, vb);
+				fwd_stats<T, G, ADJ, HIST>(sc, qb, qb.in && cb, hist, lane, pa, pb, vb);
+				nout += (rowok && i != nrow && ca && !(qa.r <= rmax)) ? 1 : 0;
+				nout += (two && rowok && ib != nrow && cb && !(qb.r <= rmax)) ? 1 : 0;
+			}
+		}
+#pragma unroll
+		for (int k = 0; k < 8; k++) acc[k].add(a[k]);
+		if (ON != 0) vsum.add(vb);
+	}
+}
+
+// Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), two
+// partners per iteration.
+template <typename T, int G, bool DIAG, int HIST>
+__device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
+                                           const T* gn, const Q4<T>* __restrict__ xs, const T* __restrict__ Gs,
+                                           const T* __restrict__ kb, const T* __restrict__ hv,
+                                           const int* __restrict__ lut, T* __restrict__ hist, int lane) {
+	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax;
+	for (int i = i0; i < i1; i += 2) {
+		const bool two = i + 1 < i1;
+		const int ib = two ? i + 1 : i;
+		T v[2][8];
+		int jj[2];
+#pragma unroll
+		for (int h = 0; h < 2; h++) {
+			const int ii = h ? ib : i;
+			const Q4<T> xi = xs[ii];
+			const T* gi = Gs + (size_t)ii * 6;
 			const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
 			const T r2 = dx * dx + dy * dy + dz * dz;
 			const T rinv = rsqrt_(r2);
 			const T r = r2 * rinv;
-			const bool in = valid && (r <= rmax);
-			T tl;
-			const int j = locate<T>(sc, r, kb, hv, lut, tl);
-			const Q4<T> cR = coefC[2 * j];
-			const Q4<T> cI = coefC[2 * j + 1];
-			const T hj = sc.uniform ? hu : hv[j];
-			const T d1R = (cR.y + tl * (T(2) * cR.z + T(3) * tl * cR.w)) * hj;
-			const T d1I = (cI.y + tl * (T(2) * cI.z + T(3) * tl * cI.w)) * hj;
-			const T d2R = (T(2) * cR.z + T(6) * tl * cR.w) * (hj * hj);
-			const T d2I = (T(2) * cI.z + T(6) * tl * cI.w) * (hj * hj);
-			const T gR = in ? d1R * rinv : T(0);
-			const T gI = in ? d1I * rinv : T(0);
-			const T gRx = gR * dx, gRy = gR * dy, gRz = gR * dz;
-			const T gIx = gI * dx, gIy = gI * dy, gIz = gI * dz;
-			a[0] += gRx;
-			a[1] += gRy;
-			a[2] += gRz;
-			a[3] += gIx;
-			a[4] += gIy;
-			a[5] += gIz;
-			a[6] += in ? d2R + dm1 * gR : T(0);
-			a[7] += in ? d2I + dm1 * gI : T(0);
-			p0 -= gRx;
-			p1 -= gRy;
-			p2 -= gRz;
-			p3 -= gIx;
-			p4 -= gIy;
-			p5 -= gIz;
-			// lane 0 holds the completed target base + t: flush it
-			if (lane == 0) {
-				int k = base + t;
-				k -= (k >= n) ? n : 0;
-				k -= (k >= n) ? n : 0;
-				Q4<T> gr = Gs[2 * k], gi = Gs[2 * k + 1];
-				gr.x += p0;
-				gr.y += p1;
-				gr.z += p2;
-				gi.x += p3;
-				gi.y += p4;
-				gi.z += p5;
-				Gs[2 * k] = gr;
-				Gs[2 * k + 1] = gi;
-			}
-			// shift down one lane; lane G-1 starts a fresh target
-			p0 = __shfl_down_sync(gmask, p0, 1, G);
-			p1 = __shfl_down_sync(gmask, p1, 1, G);
-			p2 = __shfl_down_sync(gmask, p2, 1, G);
-			p3 = __shfl_down_sync(gmask, p3, 1, G);
-			p4 = __shfl_down_sync(gmask, p4, 1, G);
-			p5 = __shfl_down_sync(gmask, p5, 1, G);
-			if (lane == G - 1) p0 = p1 = p2 = p3 = p4 = p5 = T(0);
-			// pair statistics (every visited pair is an unordered pair)
-			const T ts = in ? tl : T(0);  // tl is not meaningful outside the cut-off
-			const T t2 = ts * ts;
-			const T q = in ? rinv : T(0);
-			T v[8] = {in ? T(1) : T(0), ts, t2, t2 * ts, q, q * ts, q * t2, T(0)};
-			hist_add8<HIST, T, G>(hist, j, lane, v, ADJ ? kFwdMomentsAdj : kFwdMoments);
-			vb += in ? pair_pot<T>(sc.pot_kind, r, rinv, pa, pb) : T(0);
-			nout += (valid && !(r <= rmax)) ? 1 : 0;
+			const bool on = (h ? two : true) && rowok && (r <= rmax) && (DIAG ? (ii < nrow) : true);
+			T t;
+			jj[h] = locate<T>(sc, r, kb, hv, lut, t);
+			t = on ? t : T(0);  // t is NaN for the self pair
+			const T sr = on ? rinv : T(0);
+			const T gR = ((gn[0] - gi[0]) * dx + (gn[1] - gi[1]) * dy + (gn[2] - gi[2]) * dz) * sr;
+			const T gI = ((gn[3] - gi[3]) * dx + (gn[4] - gi[4]) * dy + (gn[5] - gi[5]) * dz) * sr;
+			const T t2 = t * t;
+			v[h][0] = gR;
+			v[h][1] = gR * t;
+			v[h][2] = gR * t2;
+			v[h][3] = gI;
+			v[h][4] = gI * t;
+			v[h][5] = gI * t2;
+			v[h][6] = v[h][7] = T(0);
 		}
-#pragma unroll
-		for (int k = 0; k < 8; k++) acc[k].add(a[k]);
-		e_v.add(vb);
-	}
-	// the remaining partner targets base + lane + tmax + 1 (mod n), and the row
-	// itself; the targets are distinct across lanes when G <= n, otherwise the
-	// lanes flush one after the other
-	__syncwarp(gmask);
-	{
-		int k = base + lane + tmax + 1;
-		while (k >= n) k -= n;
-		for (int l = (G <= n ? lane : 0); l < (G <= n ? lane + 1 : G); l++) {
-			if (l == lane) {
-				Q4<T> gr = Gs[2 * k], gi = Gs[2 * k + 1];
-				gr.x += p0;
-				gr.y += p1;
-				gr.z += p2;
-				gi.x += p3;
-				gi.y += p4;
-				gi.z += p5;
-				Gs[2 * k] = gr;
-				Gs[2 * k + 1] = gi;
-			}
-			if (G > n) __syncwarp(gmask);
-		}
-	}
-	__syncwarp(gmask);
-	if (rowok) {
-		Q4<T> gr = Gs[2 * nrow], gi = Gs[2 * nrow + 1];
-		gr.x += acc[0].value();
-		gr.y += acc[1].value();
-		gr.z += acc[2].value();
-		gi.x += acc[3].value();
-		gi.y += acc[4].value();
-		gi.z += acc[5].value();
-		Gs[2 * nrow] = gr;
-		Gs[2 * nrow + 1] = gi;
-		// each unordered pair adds the same Laplacian term to both particles
-		e_lR.add(T(2) * acc[6].value());
-		e_lI.add(T(2) * acc[7].value());
-	}
-	__syncwarp(gmask);
-}
-
-// Reverse (adjoint) sweep of one slot over the half shell.
-template <typename T, int G, int HIST>
-__device__ __forceinline__ void rev_slot(const SysConst& sc, int base, int lane, const Q4<T>* __restrict__ xs,
-                                         const Q4<T>* __restrict__ Gs, const T* __restrict__ kb,
-                                         const T* __restrict__ hv, const int* __restrict__ lut,
-                                         T* __restrict__ hist) {
-	const int n = sc.n;
-	const int nrow = base + lane;
-	const bool rowok = nrow < n;
-	const int nr = rowok ? nrow : 0;
-	const bool even = (n & 1) == 0;
-	const int tmax = even ? n / 2 : (n - 1) / 2;
-	const int trow = even ? (nrow < n / 2 ? n / 2 : n / 2 - 1) : tmax;
-	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax;
-	const Q4<T> xr = xs[nr];
-	const Q4<T> gnr = Gs[2 * nr], gni = Gs[2 * nr + 1];
-	for (int t = 1; t <= tmax; t++) {
-		int i = nr + t;
-		i -= (i >= n) ? n : 0;
-		const Q4<T> xi = xs[i];
-		const Q4<T> gir = Gs[2 * i], gii = Gs[2 * i + 1];
-		const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
-		const T r2 = dx * dx + dy * dy + dz * dz;
-		const T rinv = rsqrt_(r2);
-		const T r = r2 * rinv;
-		const bool on = rowok && (t <= trow) && (r <= rmax);
-		T tl;
-		const int j = locate<T>(sc, r, kb, hv, lut, tl);
-		tl = on ? tl : T(0);
-		const T sr = on ? rinv : T(0);
-		const T gR = ((gnr.x - gir.x) * dx + (gnr.y - gir.y) * dy + (gnr.z - gir.z) * dz) * sr;
-		const T gI = ((gni.x - gii.x) * dx + (gni.y - gii.y) * dy + (gni.z - gii.z) * dz) * sr;
-		const T t2 = tl * tl;
-		T v[8] = {gR, gR * tl, gR * t2, gI, gI * tl, gI * t2, T(0), T(0)};
-		hist_add8<HIST, T, G>(hist, j, lane, v, kRevMoments);
+		hist_add8<HIST, T, G>(hist, jj[0], lane, v[0], kRevMoments);
+		hist_add8<HIST, T, G>(hist, jj[1], lane, v[1], kRevMoments);
 	}
 }
 
@@ -298,7 +257,7 @@ __device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, i
 }
 
 template <typename T, int G, bool ADJ, int HIST>
-__global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
+__global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
                                               const T* __restrict__ kb_g, const T* __restrict__ hv_g,
                                               const int* __restrict__ lut_g, const T* __restrict__ loc_g,
                                               const double* __restrict__ fold_g, const double* __restrict__ params,
@@ -331,11 +290,12 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
 	unsigned char* gbase = smem_raw + cta_b + (size_t)gib * grp_b;
 	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
-	Q4<T>* Gs = xs + n;  // 2 per particle: (Re xyz, -), (Im xyz, -)
-	T* hist = reinterpret_cast<T*>(Gs + 2 * n);
+	T* Gs = reinterpret_cast<T*>(xs + n);
+	T* hist = Gs + (ADJ ? (size_t)((n * 6 + 7) & ~7) : 0);
 	T* red = hist + (size_t)nbin * NMH * G;
 	T* redr = red + (size_t)nbin * NM;
 	T* spl = redr + (ADJ ? (size_t)nbin * kRevMoments : 0);  // [ns][4]: S, Lsp, AR, AI
+	T* misc = spl + (size_t)ns * 4;
 
 	for (int e = lane; e < nbin * NMH * G; e += G) hist[e] = T(0);
 	__syncthreads();
@@ -350,30 +310,47 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 			T x1 = sc.dim > 1 ? pw[n + i] : T(0);
 			T x2 = sc.dim > 2 ? pw[2 * n + i] : T(0);
 			xs[i] = Q4<T>{x0, x1, x2, T(0)};
-			Gs[2 * i] = Q4<T>{T(0), T(0), T(0), T(0)};
-			Gs[2 * i + 1] = Q4<T>{T(0), T(0), T(0), T(0)};
 		}
 		__syncwarp(gmask);
 
-		KSum<T> e_lR, e_lI, e_v;
+		KSum<T> e_r1, e_i1, e_r1i1, e_lR, e_lI, e_v;
 		int nout = 0;
-		for (int s = 0; s < nslot; s++)
-			fwd_slot<T, G, ADJ, HIST>(sc, s * G, lane, gmask, xs, Gs, coefC, kb, hv, lut, hist, pa, pb, e_lR, e_lI,
-			                          e_v, nout);
-		// kinetic sums of the final gradients (BosonsBulk.cpp:418-420)
-		KSum<T> e_r1, e_i1, e_r1i1;
-		for (int i = lane; i < n; i += G) {
-			const Q4<T> gr = Gs[2 * i], gi = Gs[2 * i + 1];
-			e_r1.add(gr.x * gr.x + gr.y * gr.y + gr.z * gr.z);
-			e_i1.add(gi.x * gi.x + gi.y * gi.y + gi.z * gi.z);
-			e_r1i1.add(T(2) * (gr.x * gi.x + gr.y * gi.y + gr.z * gi.z));
+		for (int s = 0; s < nslot; s++) {
+			const int nrow = s * G + lane;
+			const bool rowok = nrow < n;
+			const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
+			KSum<T> acc[8];
+			const int base = s * G;
+			const int dend = (base + G < n) ? base + G : n;
+			fwd_region<T, G, 1, ADJ, HIST>(sc, 0, base, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			fwd_region<T, G, 2, ADJ, HIST>(sc, base, dend, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			fwd_region<T, G, 0, ADJ, HIST>(sc, dend, n, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			const T gRx = acc[0].value(), gRy = acc[1].value(), gRz = acc[2].value();
+			const T gIx = acc[3].value(), gIy = acc[4].value(), gIz = acc[5].value();
+			if (rowok) {
+				e_r1.add(gRx * gRx + gRy * gRy + gRz * gRz);
+				e_i1.add(gIx * gIx + gIy * gIy + gIz * gIz);
+				e_r1i1.add(T(2) * (gRx * gIx + gRy * gIy + gRz * gIz));
+				e_lR.add(acc[6].value());
+				e_lI.add(acc[7].value());
+				if (ADJ) {
+					T* g = Gs + (size_t)nrow * 6;
+					g[0] = gRx;
+					g[1] = gRy;
+					g[2] = gRz;
+					g[3] = gIx;
+					g[4] = gIy;
+					g[5] = gIz;
+				}
+			}
 		}
-		const T sR1 = group_sum<T, G>(e_r1.value(), gmask);
-		const T sI1 = group_sum<T, G>(e_i1.value(), gmask);
-		const T sR1I1 = group_sum<T, G>(e_r1i1.value(), gmask);
-		const T sR2 = group_sum<T, G>(e_lR.value(), gmask);
-		const T sI2 = group_sum<T, G>(e_lI.value(), gmask);
-		const T vint = group_sum<T, G>(e_v.value(), gmask);
+		// group totals (compensated per lane, then a butterfly over lanes)
+		T sR1 = group_sum<T, G>(e_r1.value(), gmask);
+		T sI1 = group_sum<T, G>(e_i1.value(), gmask);
+		T sR1I1 = group_sum<T, G>(e_r1i1.value(), gmask);
+		T sR2 = group_sum<T, G>(e_lR.value(), gmask);
+		T sI2 = group_sum<T, G>(e_lI.value(), gmask);
+		T vint = group_sum<T, G>(e_v.value(), gmask);
 		int nout_all = nout;
 #pragma unroll
 		for (int o = G / 2; o > 0; o >>= 1) nout_all += __shfl_xor_sync(gmask, nout_all, o, G);
@@ -381,7 +358,18 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 		hist_reduce<T, G, HIST>(hist, red, nbin, NM, lane, gmask);
 
 		if (ADJ) {
-			for (int s = 0; s < nslot; s++) rev_slot<T, G, HIST>(sc, s * G, lane, xs, Gs, kb, hv, lut, hist);
+			for (int s = 0; s < nslot; s++) {
+				const int nrow = s * G + lane;
+				const bool rowok = nrow < n;
+				const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
+				T gn[6] = {0, 0, 0, 0, 0, 0};
+				if (rowok)
+					for (int k = 0; k < 6; k++) gn[k] = Gs[(size_t)nrow * 6 + k];
+				const int base = s * G;
+				const int dend = (base + G < n) ? base + G : n;
+				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
+				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
+			}
 			hist_reduce<T, G, HIST>(hist, redr, nbin, kRevMoments, lane, gmask);
 		}
 
@@ -453,6 +441,7 @@ __global__ void __launch_bounds__(128) k_eloc(SysConst sc, const DynState* __res
 		}
 		__syncwarp(gmask);
 	}
+	(void)misc;
 }
 
 }  // namespace tdvmc
