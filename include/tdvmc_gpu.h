@@ -197,6 +197,30 @@ int tdvmc_get_tiles(tdvmc_ctx* ctx, int32_t* sample_lanes, int32_t* sample_walke
  * CUDA-core-bound sampling and evaluation kernels.  No reference counterpart. */
 int tdvmc_measure_fp32_peak(double* tflops);
 
+/* Walker statistics without any device allocation.
+ *
+ * For callers that cannot allocate device memory, e.g. a host program that
+ * owns all GPU memory through its own pool allocator and forbids cudaMalloc /
+ * cudaFree while it runs: they pass device arrays they already own.  Computes
+ * from O[nw*p] (walker-major) and eloc[nw*2] (E^R, E^I) the same FP64 results
+ * as tdvmc_reduce_stats: O_mean[p], E_mean[2], the centred S[p*p] and
+ * cov_OER[p], cov_OEI[p].  All pointers are device pointers; the work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * call returns without waiting for it.
+ *
+ * Limit: p <= 32.  Larger p returns TDVMC_ERR_ARG.  The partial sums live in
+ * one fixed file-scope device array of about 0.6 MB that every device which
+ * loads this library keeps until the process exits; the call itself
+ * allocates nothing.  The first call on a device looks up that array's
+ * device address with the device current, so make the first call on each
+ * device before any stream capture.  All calls share the array: calls whose
+ * work overlaps on the GPU (other streams or host threads) race on it.
+ *
+ * No counterpart in the reference (its averages live in host vectors,
+ * TDVMC.cpp:1103-1109). */
+int tdvmc_reduce_walkers_noalloc(const double* O, const double* eloc, int64_t nw, int32_t p, double* O_mean,
+                                 double* E_mean, double* S, double* cov_OER, double* cov_OEI, void* stream);
+
 /* Number of kernel launches issued by this context since creation. */
 int64_t tdvmc_launch_count(tdvmc_ctx* ctx);
 

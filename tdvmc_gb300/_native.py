@@ -20,7 +20,7 @@ EXPORTS = ("tdvmc_status_string", "tdvmc_create", "tdvmc_destroy", "tdvmc_get_st
            "tdvmc_set_params", "tdvmc_get_params", "tdvmc_set_walkers", "tdvmc_get_walkers", "tdvmc_sample",
            "tdvmc_eval_local", "tdvmc_eval_local_adjoint", "tdvmc_reduce_stats", "tdvmc_tdvp_rhs", "tdvmc_step",
            "tdvmc_get_step_operators", "tdvmc_run_steps", "tdvmc_time_steps", "tdvmc_profile_stage", "tdvmc_autotune", "tdvmc_get_tiles", "tdvmc_launch_count",
-           "tdvmc_measure_fp32_peak")
+           "tdvmc_measure_fp32_peak", "tdvmc_reduce_walkers_noalloc")
 
 
 class SystemDesc(C.Structure):
@@ -88,6 +88,8 @@ def load(build_if_missing: bool = True):
     L.tdvmc_launch_count.argtypes = [C.c_void_p]
     L.tdvmc_launch_count.restype = C.c_int64
     L.tdvmc_measure_fp32_peak.argtypes = [P(C.c_double)]
+    L.tdvmc_reduce_walkers_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = L
     return L
 
