@@ -94,7 +94,9 @@ typedef struct tdvmc_step_opts {
 	int32_t moves_per_stage;   /* single-particle moves per walker per sampling pass (MC_NTHERMSTEPS) */
 	double mc_step;            /* MC_STEP: Gaussian displacement width */
 	uint64_t seed;             /* Philox key */
-	int32_t use_adjoint;       /* also compute <dE_loc/d alpha> each stage */
+	int32_t use_adjoint;       /* 1: also compute <dE_loc/d alpha> each stage; 2: in imaginary time
+	                              also drive the force with it, F_k = -(cov(O_k, E^R) + <dE_loc/d uR_k>/2),
+	                              i.e. -1/2 d<E>/d uR_k (no reference counterpart) */
 	int32_t reserved;
 } tdvmc_step_opts;
 

@@ -25,6 +25,8 @@ struct SolveArgs {
 	int mode;        // 0: right-hand side only, 1: RK4 stage, 2: Euler step
 	int normalize;   // USE_NORMALIZE_WF
 	int ldS, ldC;    // leading dimensions of S and of the covariance rows
+	int adj_force;   // imaginary time: add half the walker mean of dE_loc/d uR to the force
+	int dE_col;      // column of Re dE_loc/d uR_0 in means1 (pairs Re, Im per parameter)
 	double dt;
 };
 
@@ -71,6 +73,9 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 		} else {
 			fr = -cR;
 			fi = -(cI + Om[i] * EI);  // -<O E^I>, not centred in the reference
+			// adjoint-driven ground-state preparation: -1/2 d<E>/d uR_k with
+			// d<E>/d uR_k = 2 cov(O_k, E^R) + <dE_loc/d uR_k>
+			if (a.adj_force) fr -= 0.5 * means1[a.dE_col + 2 * i];
 		}
 		M[i * ld + P] = fr;
 		M[i * ld + P + 1] = fi;

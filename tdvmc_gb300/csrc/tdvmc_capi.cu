@@ -260,9 +260,11 @@ int launch_reduce(tdvmc_ctx* ctx, bool adj) {
 }
 
 template <typename T>
-int launch_solve(tdvmc_ctx* ctx, int imag, int pre, int lin, int mode, int norm, double dt) {
+int launch_solve(tdvmc_ctx* ctx, int imag, int pre, int lin, int mode, int norm, double dt, int adj_force = 0) {
 	const int P = ctx->sc.p;
 	SolveArgs a;
+	a.adj_force = adj_force;
+	a.dE_col = Cols1{P}.dE();
 	a.p = P;
 	a.imag = imag;
 	a.precond = pre;
@@ -293,7 +295,7 @@ int run_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
 	if ((rc = launch_eloc<T>(ctx, o->use_adjoint != 0))) return rc;
 	if ((rc = launch_reduce<T>(ctx, o->use_adjoint != 0))) return rc;
 	return launch_solve<T>(ctx, o->imaginary_time, o->precondition, o->lin_solver, o->ode_solver == 0 ? 2 : 1,
-	                       o->normalize_wf, o->dt);
+	                       o->normalize_wf, o->dt, (o->use_adjoint == 2 && o->imaginary_time) ? 1 : 0);
 }
 
 int run_stage_any(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
@@ -305,6 +307,7 @@ int check_opts(const tdvmc_step_opts* o) {
 	if (o->ode_solver != 0 && o->ode_solver != 2) return TDVMC_ERR_ARG;
 	if (o->lin_solver != 0 && o->lin_solver != 1) return TDVMC_ERR_ARG;
 	if (o->moves_per_stage < 0) return TDVMC_ERR_ARG;
+	if (o->use_adjoint < 0 || o->use_adjoint > 2) return TDVMC_ERR_ARG;
 	return TDVMC_OK;
 }
 

@@ -255,3 +255,38 @@ def test_ragged_sizes_match_oracle(nw, n, dim):
         sc = max(np.abs(r["other"]).max(), 1.0)
         assert np.abs(f["eloc"][w] - r["eloc"]).max() < 1e-12 * sc
         assert np.abs(dE[w] - r["dE"]).max() < 1e-12 * max(np.abs(r["dE"]).max(), 1.0)
+
+
+def test_adjoint_driven_imaginary_time_step_matches_oracle_fp64():
+    """Imaginary-time Euler step with the adjoint in the force:
+    F_k = -(cov(O_k, E^R) + <dE_loc/d uR_k> / 2), i.e. -1/2 d<E>/d uR_k."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "sample_d3_n27.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    nw, moves, step, dt, seed, pass0 = 96, 2 * n, 0.35, 0.01, 5, 11
+    rng = np.random.default_rng(12)
+    R0 = np.repeat(z["R0"].T[None], nw, axis=0) + rng.normal(0, 0.05, size=(nw, dim, n))
+    R0 = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(R0)
+    uR, uI = np.asarray(z["uR"]), np.zeros(p)
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=0.09, precision="fp64")
+    s.SetParameters(uR, uI, 0.0, 0.0)
+    s.SetWalkers(R0)
+    s.DoMetropolisSteps(0, step, seed, pass0)
+    td = T.TDVP(s, dt, moves, step, seed=seed, ode_solver=0, imaginary_time=1, use_adjoint=2)
+    td.step()
+    gR, gI, gpR, gpI = s.GetParameters()
+
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0), hbar2_2m=0.09)
+    Ro = R0.copy()
+    out = o.stage(uR, uI, Ro, moves, step, seed, pass0, threads=4, adjoint=True)
+    m = orc.centred(out["O"], out["eloc"])
+    dER = out["dE"][:, :, 0].mean(0)
+    dR, dI, pR, pI, _ = orc.solve_centred(m["O"], m["ER"], m["EI"], m["S"], m["cOER"] + 0.5 * dER, m["cOEI"],
+                                          imag=1)
+    base = np.concatenate([uR, uI, [0.0, 0.0]])
+    new = base + np.concatenate([dR, dI, [pR, pI]]) * dt
+    got = np.concatenate([gR, gI, [gpR, gpI]])
+    assert relmax(got, new) < 1e-9
+    # and it differs from the plain covariance force
+    dR0 = orc.solve_centred(m["O"], m["ER"], m["EI"], m["S"], m["cOER"], m["cOEI"], imag=1)[0]
+    assert relmax(dR0, dR) > 1e-9
