@@ -159,9 +159,11 @@ __device__ __forceinline__ void fwd_stats(const SysConst& sc, const FwdPair<T>& 
 	vb += on ? pair_pot<T>(sc.pot_kind, q.r, q.rinv, pa, pb) : T(0);
 }
 
-// Forward sweep of row nrow against partners [i0, i1), two partners per
-// iteration so the two dependency chains overlap.
+// Forward sweep of row nrow against partners [i0, i1), kNp partners per
+// iteration so their dependency chains overlap (one warp per SM sub-partition
+// is all the shared memory allows).
 // ON: 0 = no pair statistics, 1 = all lanes count the pair, 2 = count iff i < nrow.
+constexpr int kNp = 4;
 template <typename T, int G, int ON, bool ADJ, int HIST>
 __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
                                            const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
@@ -173,28 +175,39 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 		const int c1 = (c0 + 32 < i1) ? c0 + 32 : i1;
 		T a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 		T vb = T(0);
-		for (int i = c0; i < c1; i += 2) {
-			const bool two = i + 1 < c1;
-			const int ib = two ? i + 1 : i;
-			const Q4<T> xa = xs[i];
-			const Q4<T> xb = xs[ib];
-			const FwdPair<T> qa = fwd_pair<T>(sc, xr, xa, rowok && i != nrow, coefC, kb, hv, lut);
-			const FwdPair<T> qb = fwd_pair<T>(sc, xr, xb, two && rowok && ib != nrow, coefC, kb, hv, lut);
-			a[0] += qa.gR * qa.dx + qb.gR * qb.dx;
-			a[1] += qa.gR * qa.dy + qb.gR * qb.dy;
-			a[2] += qa.gR * qa.dz + qb.gR * qb.dz;
-			a[3] += qa.gI * qa.dx + qb.gI * qb.dx;
-			a[4] += qa.gI * qa.dy + qb.gI * qb.dy;
-			a[5] += qa.gI * qa.dz + qb.gI * qb.dz;
-			a[6] += qa.lR + qb.lR;
-			a[7] += qa.lI + qb.lI;
+		for (int i = c0; i < c1; i += kNp) {
+			FwdPair<T> q[kNp];
+			int ii[kNp];
+			bool have[kNp];
+#pragma unroll
+			for (int h = 0; h < kNp; h++) {
+				have[h] = i + h < c1;
+				ii[h] = have[h] ? i + h : i;
+			}
+			Q4<T> xp[kNp];
+#pragma unroll
+			for (int h = 0; h < kNp; h++) xp[h] = xs[ii[h]];
+#pragma unroll
+			for (int h = 0; h < kNp; h++)
+				q[h] = fwd_pair<T>(sc, xr, xp[h], have[h] && rowok && ii[h] != nrow, coefC, kb, hv, lut);
+#pragma unroll
+			for (int h = 0; h < kNp; h++) {
+				a[0] += q[h].gR * q[h].dx;
+				a[1] += q[h].gR * q[h].dy;
+				a[2] += q[h].gR * q[h].dz;
+				a[3] += q[h].gI * q[h].dx;
+				a[4] += q[h].gI * q[h].dy;
+				a[5] += q[h].gI * q[h].dz;
+				a[6] += q[h].lR;
+				a[7] += q[h].lI;
+			}
 			if (ON != 0) {
-				const bool ca = (ON == 1) ? true : (i < nrow);
-				const bool cb = (ON == 1) ? two : (two && ib < nrow);
-				fwd_stats<T, G, ADJ, HIST>(sc, qa, qa.in && ca, hist, lane, pa, pb, vb);
-				fwd_stats<T, G, ADJ, HIST>(sc, qb, qb.in && cb, hist, lane, pa, pb, vb);
-				nout += (rowok && i != nrow && ca && !(qa.r <= rmax)) ? 1 : 0;
-				nout += (two && rowok && ib != nrow && cb && !(qb.r <= rmax)) ? 1 : 0;
+#pragma unroll
+				for (int h = 0; h < kNp; h++) {
+					const bool c = have[h] && ((ON == 1) ? true : (ii[h] < nrow));
+					fwd_stats<T, G, ADJ, HIST>(sc, q[h], q[h].in && c, hist, lane, pa, pb, vb);
+					nout += (rowok && ii[h] != nrow && c && !(q[h].r <= rmax)) ? 1 : 0;
+				}
 			}
 		}
 #pragma unroll
@@ -203,7 +216,7 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 	}
 }
 
-// Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), two
+// Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), kNp
 // partners per iteration.
 template <typename T, int G, bool DIAG, int HIST>
 __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
@@ -211,21 +224,20 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
                                            const T* __restrict__ kb, const T* __restrict__ hv,
                                            const int* __restrict__ lut, T* __restrict__ hist, int lane) {
 	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax;
-	for (int i = i0; i < i1; i += 2) {
-		const bool two = i + 1 < i1;
-		const int ib = two ? i + 1 : i;
-		T v[2][8];
-		int jj[2];
+	for (int i = i0; i < i1; i += kNp) {
+		T v[kNp][8];
+		int jj[kNp];
 #pragma unroll
-		for (int h = 0; h < 2; h++) {
-			const int ii = h ? ib : i;
+		for (int h = 0; h < kNp; h++) {
+			const bool have = i + h < i1;
+			const int ii = have ? i + h : i;
 			const Q4<T> xi = xs[ii];
 			const T* gi = Gs + (size_t)ii * 6;
 			const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
 			const T r2 = dx * dx + dy * dy + dz * dz;
 			const T rinv = rsqrt_(r2);
 			const T r = r2 * rinv;
-			const bool on = (h ? two : true) && rowok && (r <= rmax) && (DIAG ? (ii < nrow) : true);
+			const bool on = have && rowok && (r <= rmax) && (DIAG ? (ii < nrow) : true);
 			T t;
 			jj[h] = locate<T>(sc, r, kb, hv, lut, t);
 			t = on ? t : T(0);  // t is NaN for the self pair
@@ -241,8 +253,8 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 			v[h][5] = gI * t2;
 			v[h][6] = v[h][7] = T(0);
 		}
-		hist_add8<HIST, T, G>(hist, jj[0], lane, v[0], kRevMoments);
-		hist_add8<HIST, T, G>(hist, jj[1], lane, v[1], kRevMoments);
+#pragma unroll
+		for (int h = 0; h < kNp; h++) hist_add8<HIST, T, G>(hist, jj[h], lane, v[h], kRevMoments);
 	}
 }
 

@@ -58,7 +58,7 @@ def min_pair_distance(R, L):
     return r[np.triu_indices(len(R), 1)].min()
 
 
-CASES = [(f, prec, pot) for f in EVAL_FILES for prec in ("fp64", "mixed") for pot in ("square", "lj")]
+CASES = [(f, prec, pot) for f in EVAL_FILES for prec in ("fp64", "mixed") for pot in ("square", "lj", "gauss")]
 
 
 @pytest.mark.parametrize("path,precision,pot", CASES,
@@ -67,9 +67,12 @@ def test_eval_and_adjoint_match_oracle(path, precision, pot):
     z = np.load(path)
     cfgs = z["cfgs"]
     nw = len(cfgs)
-    sysp = z["sysp"] if pot == "square" else np.array([1.0, 1.0])
+    # LJ in reduced units; square well and Gaussian soft core with the file's parameters
+    # (including the quench branch of eval_d1_n20_p10_quench)
+    sysp = np.array([1.0, 1.0]) if pot == "lj" else z["sysp"]
     s = gpu_system(z, nw, precision, potential=pot, sysp=sysp, hbar2_2m=0.09)
-    o = oracle_system(z, pot_kind=orc.POT_SQUARE if pot == "square" else orc.POT_LJ, sysp=sysp, hbar2_2m=0.09)
+    kind = {"square": orc.POT_SQUARE, "lj": orc.POT_LJ, "gauss": orc.POT_GAUSS}[pot]
+    o = oracle_system(z, pot_kind=kind, sysp=sysp, hbar2_2m=0.09)
     s.SetParameters(z["uR"], z["uI"], float(z["phiR"]), float(z["phiI"]))
     s.SetWalkers(soa(cfgs))
     fwd = s.CalculateExpectationValues()
