@@ -87,7 +87,7 @@ typedef struct tdvmc_stats {
 typedef struct tdvmc_step_opts {
 	double dt;                 /* TIMESTEP */
 	int32_t imaginary_time;    /* IMAGINARY_TIME: 0 real, 1 imaginary */
-	int32_t ode_solver;        /* ODE_SOLVER_TYPE: 0 Euler, 2 RK4 */
+	int32_t ode_solver;        /* ODE_SOLVER_TYPE: 0 Euler, 2 RK4, 3 RK4 on stored samples */
 	int32_t lin_solver;        /* LINEAR_EQUATION_SOLVER_TYPE: 0 Cholesky (+1e-3 I) */
 	int32_t precondition;      /* USE_PRECONDITIONING */
 	int32_t normalize_wf;      /* USE_NORMALIZE_WF: phiR <- -ln psi of walker 0 */
@@ -97,7 +97,9 @@ typedef struct tdvmc_step_opts {
 	int32_t use_adjoint;       /* 1: also compute <dE_loc/d alpha> each stage; 2: in imaginary time
 	                              also drive the force with it, F_k = -(cov(O_k, E^R) + <dE_loc/d uR_k>/2),
 	                              i.e. -1/2 d<E>/d uR_k (no reference counterpart) */
-	int32_t reserved;
+	int32_t update_every;      /* ode_solver 3: UPDATE_SAMPLES_EVERY_NTH_STEP; 0 samples every walker each step,
+	                              k > 0 refreshes a window of walkers every k-th step */
+	double update_percent;     /* ode_solver 3: UPDATE_SAMPLES_PERCENT, size of the refresh window in % of walkers */
 } tdvmc_step_opts;
 
 const char* tdvmc_status_string(int status);
@@ -141,6 +143,26 @@ int tdvmc_eval_local(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, dou
  * stored.  No counterpart exists in the reference (its force is the SR
  * covariance only, TDVMC.cpp:1527-1528). */
 int tdvmc_eval_local_adjoint(tdvmc_ctx* ctx, double* dE);
+
+/* Correlated sampling.  tdvmc_store_samples keeps, for every walker at its
+ * current position, the parameter-independent data of the local quantities
+ * (InitCorrelatedSamplingData + FillCorrelatedSamplingData,
+ * BosonsBulk.cpp:667-681; CSDataBulkSplines.h:9-16): per spline and particle
+ * sum_i B'(r) rhat, the summed B'' + (D-1)/r B', O_k, V_int and the outer-pair
+ * count.  About nw * (p+2) * 3 * n values of the working precision; the
+ * store is allocated on first use (TDVMC_ERR_NOMEM if it does not fit).
+ * Moving the walkers (tdvmc_set_walkers, tdvmc_sample, a resampling step)
+ * invalidates it. */
+int tdvmc_store_samples(tdvmc_ctx* ctx);
+
+/* Local quantities of the stored samples at the current parameters, without
+ * resampling (CalculateWavefunction + CalculateExpectationValues for an
+ * ICorrelatedSamplingData, BosonsBulk.cpp:468-472, 547-551).  Same outputs
+ * as tdvmc_eval_local, plus dE as tdvmc_eval_local_adjoint when dE is not
+ * NULL.  ln psi uses the sample's own outer-pair count (the reference uses
+ * that of the configuration it evaluated last).  TDVMC_ERR_STATE without a
+ * valid store. */
+int tdvmc_eval_stored(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, double* other7, double* dE);
 
 /* Walker-mean reduction of the last evaluation (ParallelUpdateExpectationValues,
  * TDVMC.cpp:1152-1220).  Optional outputs: O_mean[p], S[p*p] (centred),

@@ -18,7 +18,8 @@ POT_NONE, POT_SQUARE, POT_GAUSS, POT_LJ = 0, 1, 2, 3
 # every entry point of include/tdvmc_gpu.h
 EXPORTS = ("tdvmc_status_string", "tdvmc_create", "tdvmc_destroy", "tdvmc_get_stream", "tdvmc_set_time",
            "tdvmc_set_params", "tdvmc_get_params", "tdvmc_set_walkers", "tdvmc_get_walkers", "tdvmc_sample",
-           "tdvmc_eval_local", "tdvmc_eval_local_adjoint", "tdvmc_reduce_stats", "tdvmc_tdvp_rhs", "tdvmc_step",
+           "tdvmc_eval_local", "tdvmc_eval_local_adjoint", "tdvmc_store_samples", "tdvmc_eval_stored",
+           "tdvmc_reduce_stats", "tdvmc_tdvp_rhs", "tdvmc_step",
            "tdvmc_get_step_operators", "tdvmc_run_steps", "tdvmc_time_steps", "tdvmc_profile_stage", "tdvmc_autotune", "tdvmc_get_tiles", "tdvmc_launch_count",
            "tdvmc_measure_fp32_peak", "tdvmc_reduce_walkers_noalloc")
 
@@ -40,7 +41,7 @@ class StepOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("imaginary_time", C.c_int32), ("ode_solver", C.c_int32),
                 ("lin_solver", C.c_int32), ("precondition", C.c_int32), ("normalize_wf", C.c_int32),
                 ("moves_per_stage", C.c_int32), ("mc_step", C.c_double), ("seed", C.c_uint64),
-                ("use_adjoint", C.c_int32), ("reserved", C.c_int32)]
+                ("use_adjoint", C.c_int32), ("update_every", C.c_int32), ("update_percent", C.c_double)]
 
 
 _lib = None
@@ -76,6 +77,8 @@ def load(build_if_missing: bool = True):
     L.tdvmc_sample.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.c_uint64, C.c_uint32, P(C.c_int64)]
     L.tdvmc_eval_local.argtypes = [C.c_void_p, d, d, d, d]
     L.tdvmc_eval_local_adjoint.argtypes = [C.c_void_p, d]
+    L.tdvmc_store_samples.argtypes = [C.c_void_p]
+    L.tdvmc_eval_stored.argtypes = [C.c_void_p, d, d, d, d, d]
     L.tdvmc_reduce_stats.argtypes = [C.c_void_p, P(Stats), d, d, d, d, d]
     L.tdvmc_tdvp_rhs.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, d, d, P(C.c_double), P(C.c_double)]
     L.tdvmc_step.argtypes = [C.c_void_p, P(StepOpts), P(Stats)]

@@ -24,6 +24,7 @@ struct SysConst {
 	int uniform;  // 1: equal interval widths
 	int ncell;    // non-uniform: lookup cells
 	int pot_kind;
+	int ncoef;    // entries of the sampler's pair-function table (>= nbin + 1)
 	double L, Lr;
 	double rmax;
 	double hinv;      // uniform: 1 / interval width
@@ -39,7 +40,7 @@ struct DynState {
 	uint32_t pass;      // Philox pass counter of the next sampling pass
 	uint32_t stage;     // RK stage being computed
 	int32_t status;     // OR of TDVMC_ERR_* flags of the solves since last read
-	int32_t pad;
+	int32_t cs_start;   // first walker of the next stored-sample refresh
 };
 
 // Minimum image of one Cartesian difference: d - L * round(d / L)

@@ -8,8 +8,8 @@
 namespace tdvmc {
 
 template <typename T>
-using SampleFn = void (*)(SysConst, const Q4<T>*, const T*, const T*, const T*, const int*, T*, int64_t, int, T, uint2,
-                          const uint32_t*, int*);
+using SampleFn = void (*)(SysConst, const Q4<T>*, const T*, const T*, const T*, const int*, T*, int64_t, int64_t,
+                          const int32_t*, int, T, uint2, const uint32_t*, int*);
 template <typename T>
 using ElocFn = void (*)(SysConst, const DynState*, const Q4<T>*, const T*, const T*, const int*, const T*,
                         const double*, const double*, const T*, int64_t, T*, T*, T*, T*, T*);
@@ -18,6 +18,8 @@ using ElocFn = void (*)(SysConst, const DynState*, const Q4<T>*, const T*, const
 int sample_slots_for(int n, int lanes);
 
 SampleFn<float> pick_sample_f32(int lanes, int slots);
+// FP32, uniform knots: packed f32x2 pair arithmetic (null where not instantiated)
+SampleFn<float> pick_sample_f32_packed(int lanes, int slots);
 SampleFn<double> pick_sample_f64(int lanes, int slots);
 ElocFn<float> pick_eloc_f32(int lanes, bool adj, int hist);
 ElocFn<double> pick_eloc_f64(int lanes, bool adj, int hist);

@@ -15,4 +15,31 @@ int sample_slots_for(int n, int G) {
 		if (l[i] >= need) return l[i];
 	return -1;
 }
+
+SampleFn<float> pick_sample_f32_packed(int G, int slots) {
+	if (G == 32) {
+		switch (slots) {
+		case 1: return k_sample_f2<32, 1>;
+		case 2: return k_sample_f2<32, 2>;
+		case 4: return k_sample_f2<32, 4>;
+		case 8: return k_sample_f2<32, 8>;
+		case 11: return k_sample_f2<32, 11>;
+		case 16: return k_sample_f2<32, 16>;
+		}
+	} else if (G == 16) {
+		switch (slots) {
+		case 1: return k_sample_f2<16, 1>;
+		case 2: return k_sample_f2<16, 2>;
+		case 4: return k_sample_f2<16, 4>;
+		case 8: return k_sample_f2<16, 8>;
+		}
+	} else if (G == 8) {
+		switch (slots) {
+		case 1: return k_sample_f2<8, 1>;
+		case 2: return k_sample_f2<8, 2>;
+		case 4: return k_sample_f2<8, 4>;
+		}
+	}
+	return nullptr;
+}
 }  // namespace tdvmc

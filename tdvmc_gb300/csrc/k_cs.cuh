@@ -1,0 +1,345 @@
+// Correlated-sampling reuse: per-walker data that does not depend on the
+// variational parameters, stored once per sample and re-evaluated at other
+// parameters without resampling (BosonsBulk::FillCorrelatedSamplingData and
+// CalculateExpectationValues(ICorrelatedSamplingData*), BosonsBulk.cpp:468-472,
+// 675-681; CSDataBulkSplines.h:9-16; used by CalculateNextParametersRK4ReuseSamples,
+// TDVMC.cpp:2037-2103, and UpdateExpectationValuesForGivenSamples, 1222-1293).
+//
+// Stored per walker, at spline level (s = 0..ns-1, before the boundary fold):
+//   D[s][a][n] = sum_{i != n, r <= r_max} B_s'(r_ni) (x_n - x_i)_a / r_ni
+//   D2[s]      = sum_n sum_{i != n, r <= r_max} (B_s''(r_ni) + (D-1)/r_ni B_s'(r_ni))
+//   O[k]       = BC-folded sum_{i < n, r <= r_max} B_s(r_ni)
+//   V          = pair potential over i < n, r <= r_max;  n_out = #pairs beyond r_max
+// With per-spline complex weights w_s = sum_k alpha_k fold[k][s]:
+//   G_n = sum_s w_s D[s][.][n],  sum_n L_n = sum_s w_s D2[s],
+// which gives the same local energy, kinetic sums and adjoint as k_eloc.
+#pragma once
+
+#include "common.cuh"
+#include "k_eloc.cuh"
+
+namespace tdvmc {
+
+// piece table per knot interval j (36 values): for q = 0..3 (spline j+3-q)
+//   [0..11]  h l1, 2h l2, 3h l3        (dB/dr = a0 + t (a1 + t a2))
+//   [12..27] l0, l1, l2, l3            (B in the local coordinate t)
+//   [28..35] 2h^2 l2, 6h^2 l3          (d2B/dr2 = c0 + t c1)
+constexpr int kCsPiece = 36;
+
+// Shared memory of k_cs_store.
+//   CTA:   piece[nbin*36] | kb[nbin] | hv[nbin] | lut[ncell]
+//   group: xs[n] | drow[ns*3*G] | oacc[ns*G] | d2acc[ns*G]   (lane-private columns)
+template <typename T>
+__host__ __device__ inline size_t cs_cta_bytes(int nbin, int ncell) {
+	size_t b = (size_t)nbin * kCsPiece * sizeof(T) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+	return (b + 31) & ~(size_t)31;
+}
+template <typename T>
+__host__ __device__ inline size_t cs_group_bytes(int n, int ns, int G) {
+	size_t b = (size_t)n * sizeof(Q4<T>) + (size_t)ns * 5 * G * sizeof(T);
+	return (b + 31) & ~(size_t)31;
+}
+
+// One (row, partner) pair: the row's D columns always; with STATS also the
+// pair's O, D2, potential and outer count (unordered pairs, counted once).
+template <typename T, int G, bool STATS>
+__device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
+                                        const T* __restrict__ piece, const T* __restrict__ kb,
+                                        const T* __restrict__ hv, const int* __restrict__ lut, T* __restrict__ drow,
+                                        T* __restrict__ oacc, T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs,
+                                        int& nout) {
+	const T L = (T)sc.L, Lr = (T)sc.Lr;
+	const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
+	const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+	const T rinv = rsqrt_(r2);
+	const T r = r2 * rinv;
+	const bool in = ok && (r <= (T)sc.rmax);
+	T t;
+	const int j = locate<T>(sc, r, kb, hv, lut, t);
+	t = in ? t : T(0);  // t is NaN for the self pair
+	const T sr = in ? rinv : T(0);
+	const T* pc = piece + (size_t)j * kCsPiece;
+	const int s0 = j + 3;  // spline of piece q is s0 - q
+#pragma unroll
+	for (int q = 0; q < 4; q++) {
+		const T b1 = fma(t, fma(t, pc[3 * q + 2], pc[3 * q + 1]), pc[3 * q]) * sr;  // B'(r) / r
+		T* dq = drow + (size_t)(s0 - q) * 3 * G + lane;
+		dq[0] = fma(b1, dx, dq[0]);
+		dq[G] = fma(b1, dy, dq[G]);
+		dq[2 * G] = fma(b1, dz, dq[2 * G]);
+	}
+	if (STATS) {
+		const T on = in ? T(1) : T(0);
+		const T dm1 = (T)(sc.dim - 1);
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const T* l = pc + 12 + 4 * q;
+			const T b = fma(t, fma(t, fma(t, l[3], l[2]), l[1]), l[0]) * on;
+			const T b1 = fma(t, fma(t, pc[3 * q + 2], pc[3 * q + 1]), pc[3 * q]);
+			const T b2 = fma(t, pc[28 + 2 * q + 1], pc[28 + 2 * q]);
+			const T lap = (b2 + dm1 * b1 * sr) * on;
+			oacc[(size_t)(s0 - q) * G + lane] += b;
+			d2acc[(size_t)(s0 - q) * G + lane] += T(2) * lap;  // both orderings of the pair
+		}
+		vs.add(in ? pair_pot<T>(sc.pot_kind, r, rinv, pa, pb) : T(0));
+		nout += (ok && !(r <= (T)sc.rmax)) ? 1 : 0;
+	}
+}
+
+// Stores the correlated-sampling data of walkers (start + w) mod nw_total,
+// w < count (start from *wstart when given, else 0).
+template <typename T, int G>
+__global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* __restrict__ dyn,
+                                                  const T* __restrict__ piece_g, const T* __restrict__ kb_g,
+                                                  const T* __restrict__ hv_g, const int* __restrict__ lut_g,
+                                                  const double* __restrict__ fold_g, const T* __restrict__ pos,
+                                                  int64_t count, int64_t nw_total, const int32_t* __restrict__ wstart,
+                                                  T* __restrict__ D_o, T* __restrict__ D2_o, T* __restrict__ O_o,
+                                                  T* __restrict__ V_o, int32_t* __restrict__ nout_o) {
+	extern __shared__ __align__(32) unsigned char smem_raw[];
+	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
+	T* piece = reinterpret_cast<T*>(smem_raw);
+	T* kb = piece + (size_t)nbin * kCsPiece;
+	T* hv = kb + nbin;
+	int* lut = reinterpret_cast<int*>(hv + nbin);
+	for (int i = threadIdx.x; i < nbin * kCsPiece; i += blockDim.x) piece[i] = piece_g[i];
+	for (int i = threadIdx.x; i < nbin; i += blockDim.x) {
+		kb[i] = kb_g[i];
+		hv[i] = hv_g[i];
+	}
+	for (int i = threadIdx.x; i < sc.ncell; i += blockDim.x) lut[i] = lut_g[i];
+
+	const int tid = threadIdx.x;
+	const int lane = tid & (G - 1);
+	const int gib = tid / G;
+	const int gpb = blockDim.x / G;
+	const unsigned wl = tid & 31;
+	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
+	unsigned char* gbase = smem_raw + cs_cta_bytes<T>(nbin, sc.ncell) + (size_t)gib * cs_group_bytes<T>(n, ns, G);
+	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
+	T* drow = reinterpret_cast<T*>(xs + n);
+	T* oacc = drow + (size_t)ns * 3 * G;
+	T* d2acc = oacc + (size_t)ns * G;
+	__syncthreads();
+
+	const T pa = (T)dyn->pa, pb = (T)dyn->pb;
+	const T L = (T)sc.L, Lr = (T)sc.Lr;
+	const int64_t w0 = wstart ? (int64_t)*wstart : 0;
+	const int nslot = (n + G - 1) / G;
+
+	for (int64_t wi = (int64_t)blockIdx.x * gpb + gib; wi < count; wi += (int64_t)gridDim.x * gpb) {
+		int64_t w = w0 + wi;
+		if (w >= nw_total) w -= nw_total;
+		const T* pw = pos + (size_t)w * sc.dim * n;
+		for (int i = lane; i < n; i += G) {
+			const T x0 = nic(pw[i], L, Lr);
+			const T x1 = sc.dim > 1 ? nic(pw[n + i], L, Lr) : T(0);
+			const T x2 = sc.dim > 2 ? nic(pw[2 * n + i], L, Lr) : T(0);
+			xs[i] = Q4<T>{x0, x1, x2, T(0)};
+		}
+		for (int e = lane; e < ns * G; e += G) {
+			oacc[e] = T(0);
+			d2acc[e] = T(0);
+		}
+		__syncwarp(gmask);
+		KSum<T> vs;
+		int nout = 0;
+		T* Dw = D_o + (size_t)w * ns * 3 * n;
+		for (int s = 0; s < nslot; s++) {
+			const int nrow = s * G + lane;
+			const bool rowok = nrow < n;
+			const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
+			for (int e = lane; e < ns * 3 * G; e += G) drow[e] = T(0);
+			const int base = s * G;
+			const int dend = (base + G < n) ? base + G : n;
+			// partners below the slot: every lane's pair is counted once (i < nrow)
+			for (int i = 0; i < base; i++)
+				cs_pair<T, G, true>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
+			// the slot's own block: counted iff i < nrow
+			for (int i = base; i < dend; i++) {
+				if (i < nrow)
+					cs_pair<T, G, true>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs,
+					                    nout);
+				else
+					cs_pair<T, G, false>(sc, xr, xs[i], rowok && i != nrow, piece, kb, hv, lut, drow, oacc, d2acc, lane,
+					                     pa, pb, vs, nout);
+			}
+			// partners above the slot: D only
+			for (int i = dend; i < n; i++)
+				cs_pair<T, G, false>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
+			if (rowok)
+				for (int e = 0; e < ns * 3; e++) Dw[(size_t)e * n + nrow] = drow[(size_t)e * G + lane];
+		}
+		__syncwarp(gmask);
+		// lane-ordered sums of the lane-private accumulators
+		for (int sp = lane; sp < ns; sp += G) {
+			T so = T(0), s2 = T(0);
+			for (int l = 0; l < G; l++) {
+				so += oacc[(size_t)sp * G + l];
+				s2 += d2acc[(size_t)sp * G + l];
+			}
+			drow[sp] = so;
+			drow[ns + sp] = s2;
+			D2_o[(size_t)w * ns + sp] = s2;
+		}
+		__syncwarp(gmask);
+		for (int k = lane; k < P; k += G) {
+			double o = 0.0;
+			for (int sp = 0; sp < ns; sp++) o += fold_g[(size_t)k * ns + sp] * (double)drow[sp];
+			O_o[(size_t)w * P + k] = (T)o;
+		}
+		const T v = group_sum<T, G>(vs.value(), gmask);
+		int nall = nout;
+#pragma unroll
+		for (int o = G / 2; o > 0; o >>= 1) nall += __shfl_xor_sync(gmask, nall, o, G);
+		if (lane == 0) {
+			V_o[w] = v;
+			nout_o[w] = nall;
+		}
+		__syncwarp(gmask);
+	}
+}
+
+// Local quantities of every stored walker at the current stage parameters:
+// same outputs as k_eloc (ln psi, O, E_loc, kinetic sums, dE/d alpha).
+// One warp per walker; D is streamed once for G_n and, with ADJ, once more
+// for sum_n G_n . D[s][.][n].
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __restrict__ params,
+                                                 const double* __restrict__ fold_g, const T* __restrict__ D,
+                                                 const T* __restrict__ D2, const T* __restrict__ Os,
+                                                 const T* __restrict__ Vs, const int32_t* __restrict__ nouts,
+                                                 int64_t nw, T* __restrict__ lnpsi_o, T* __restrict__ O_o,
+                                                 T* __restrict__ eloc_o, T* __restrict__ other_o, T* __restrict__ dE_o) {
+	extern __shared__ __align__(32) unsigned char smem_raw[];
+	const int n = sc.n, ns = sc.ns, P = sc.p;
+	T* wR = reinterpret_cast<T*>(smem_raw);
+	T* wI = wR + ns;
+	T* gs_all = wI + ns;  // per warp: [n][6] gradients (adjoint), then [2*ns] spline sums
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int wpb = blockDim.x >> 5;
+	for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+		double r = 0.0, im = 0.0;
+		for (int k = 0; k < P; k++) {
+			const double f = fold_g[(size_t)k * ns + s];
+			r += params[k] * f;
+			im += params[P + k] * f;
+		}
+		wR[s] = (T)r;
+		wI[s] = (T)im;
+	}
+	__syncthreads();
+	T* gs = gs_all + (size_t)warp * ((size_t)n * 6 + 2 * ns);
+	T* asum = gs + (size_t)n * 6;
+	const double c = sc.hbar2_2m;
+
+	for (int64_t w = (int64_t)blockIdx.x * wpb + warp; w < nw; w += (int64_t)gridDim.x * wpb) {
+		const T* Dw = D + (size_t)w * ns * 3 * n;
+		KSum<T> r1, i1, r1i1;
+		for (int i = lane; i < n; i += 32) {
+			T gr0 = 0, gr1 = 0, gr2 = 0, gi0 = 0, gi1 = 0, gi2 = 0;
+			for (int s = 0; s < ns; s++) {
+				const T* d = Dw + (size_t)s * 3 * n + i;
+				const T d0 = d[0], d1 = d[n], d2 = d[2 * n];
+				const T a = wR[s], b = wI[s];
+				gr0 = fma(a, d0, gr0);
+				gr1 = fma(a, d1, gr1);
+				gr2 = fma(a, d2, gr2);
+				gi0 = fma(b, d0, gi0);
+				gi1 = fma(b, d1, gi1);
+				gi2 = fma(b, d2, gi2);
+			}
+			r1.add(gr0 * gr0 + gr1 * gr1 + gr2 * gr2);
+			i1.add(gi0 * gi0 + gi1 * gi1 + gi2 * gi2);
+			r1i1.add(T(2) * (gr0 * gi0 + gr1 * gi1 + gr2 * gi2));
+			if (ADJ) {
+				T* g = gs + (size_t)i * 6;
+				g[0] = gr0;
+				g[1] = gr1;
+				g[2] = gr2;
+				g[3] = gi0;
+				g[4] = gi1;
+				g[5] = gi2;
+			}
+		}
+		T l2r = T(0), l2i = T(0);
+		for (int s = lane; s < ns; s += 32) {
+			const T v = D2[(size_t)w * ns + s];
+			l2r = fma(wR[s], v, l2r);
+			l2i = fma(wI[s], v, l2i);
+		}
+		const T sR1 = group_sum<T, 32>(r1.value(), 0xffffffffu);
+		const T sI1 = group_sum<T, 32>(i1.value(), 0xffffffffu);
+		const T sR1I1 = group_sum<T, 32>(r1i1.value(), 0xffffffffu);
+		const T sR2 = group_sum<T, 32>(l2r, 0xffffffffu);
+		const T sI2 = group_sum<T, 32>(l2i, 0xffffffffu);
+		const T vint = Vs[w];
+		double lnp = 0.0;
+		for (int k = lane; k < P; k += 32) {
+			const T o = Os[(size_t)w * P + k];
+			O_o[(size_t)w * P + k] = o;
+			lnp += params[k] * (double)o;
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) lnp += __shfl_xor_sync(0xffffffffu, lnp, o);
+		if (lane == 0) {
+			lnp += params[P - 1] * (double)nouts[w];
+			const double kinR = -((double)sR1 - (double)sI1 + (double)sR2) * c;
+			const double kinI = -((double)sR1I1 + (double)sI2) * c;
+			lnpsi_o[w] = (T)lnp;
+			eloc_o[2 * w + 0] = (T)(kinR + (double)vint);
+			eloc_o[2 * w + 1] = (T)kinI;
+			T* ot = other_o + (size_t)w * 7;
+			ot[0] = (T)kinR;
+			ot[1] = vint;
+			ot[2] = sR1;
+			ot[3] = sI1;
+			ot[4] = sR2;
+			ot[5] = sI2;
+			ot[6] = sR1I1;
+		}
+		if (ADJ) {
+			__syncwarp();
+			// A_s = sum_n G_n . D[s][.][n] (complex), then fold with D2
+			for (int s = 0; s < ns; s++) {
+				const T* d = Dw + (size_t)s * 3 * n;
+				T ar = T(0), ai = T(0);
+				for (int i = lane; i < n; i += 32) {
+					const T* g = gs + (size_t)i * 6;
+					const T d0 = d[i], d1 = d[n + i], d2 = d[2 * n + i];
+					ar = fma(g[0], d0, fma(g[1], d1, fma(g[2], d2, ar)));
+					ai = fma(g[3], d0, fma(g[4], d1, fma(g[5], d2, ai)));
+				}
+				ar = group_sum<T, 32>(ar, 0xffffffffu);
+				ai = group_sum<T, 32>(ai, 0xffffffffu);
+				if (lane == 0) {
+					asum[2 * s] = ar;
+					asum[2 * s + 1] = ai;
+				}
+			}
+			__syncwarp();
+			for (int k = lane; k < P; k += 32) {
+				double dR = 0.0, dI = 0.0;
+				for (int s = 0; s < ns; s++) {
+					const double f = fold_g[(size_t)k * ns + s];
+					if (f == 0.0) continue;
+					dR += f * (2.0 * (double)asum[2 * s] + (double)D2[(size_t)w * ns + s]);
+					dI += f * (2.0 * (double)asum[2 * s + 1]);
+				}
+				dE_o[((size_t)w * P + k) * 2 + 0] = (T)(-c * dR);
+				dE_o[((size_t)w * P + k) * 2 + 1] = (T)(-c * dI);
+			}
+		}
+		__syncwarp();
+	}
+}
+
+// Next refresh window: start <- (start + count) mod nw.
+__global__ void k_cs_advance(DynState* dyn, int64_t count, int64_t nw) {
+	if (threadIdx.x == 0 && blockIdx.x == 0) {
+		int64_t s = (int64_t)dyn->cs_start + count;
+		dyn->cs_start = (int32_t)(s % nw);
+	}
+}
+
+}  // namespace tdvmc

@@ -9,15 +9,15 @@
 // particle n = s*G + l of slot s and loops over all partners i (the partner
 // coordinate is a shared-memory broadcast), accumulating the complex
 // gradient G_n and Laplacian of ln psi in registers with compensated block
-// sums.  Pair statistics that are linear in the spline basis (O_k, and for
-// the adjoint the alpha-independent Laplacian of O_k) are accumulated as
-// per-interval moments sum t^c (and sum t^c / r) in lane-private shared
-// histograms; partners below the slot base are counted once per unordered
-// pair with warp-uniform control flow (the diagonal block is the only mixed
-// region).  Reverse sweep (adjoint): one pass over unordered pairs that
-// recomputes minimum-image distances and accumulates sum t^c g with
-// g = (G_n - G_i) . rhat_ni; no pair table is stored.  Moments are turned
-// into spline values with the local piece polynomials and folded to the p
+// sums.  O_k is linear in the spline basis and is accumulated as
+// per-interval moments sum t^c in lane-private shared histograms; partners
+// below the slot base are counted once per unordered pair with warp-uniform
+// control flow (the diagonal block is the only mixed region).  Reverse sweep
+// (adjoint): one pass over unordered pairs that recomputes minimum-image
+// distances and accumulates sum t^c g with g = (G_n - G_i) . rhat_ni, plus
+// the (D-1)/r term of the Laplacian of O_k, which enters the adjoint in the
+// same B' combination; no pair table is stored.  Moments are turned into
+// spline values with the local piece polynomials and folded to the p
 // parameters at the end.
 #pragma once
 
@@ -26,21 +26,22 @@
 
 namespace tdvmc {
 
-constexpr int kFwdMoments = 4;     // sum t^c, c = 0..3
-constexpr int kFwdMomentsAdj = 7;  // + sum t^c / r, c = 0..2
-constexpr int kRevMoments = 6;     // complex sum g t^c, c = 0..2
-constexpr int kHistSlots = 8;      // histogram slots per interval and lane in the float4 mode
-// slots per interval and lane: the largest moment count (7), or 8 for the float4 mode
-template <int HIST> struct HistSlots { static constexpr int value = HIST == 1 ? 8 : 7; };
+constexpr int kFwdMoments = 4;  // sum t^c, c = 0..3
+constexpr int kRevMoments = 6;  // complex sum g t^c, c = 0..2 (real part with (D-1)/r)
+// slots per interval and lane: the largest moment count of the kernel's
+// sweeps (4, or 6 with the adjoint), rounded to whole float4s in that mode
+template <int HIST, bool ADJ> struct HistSlots {
+	static constexpr int value = ADJ ? (HIST == 1 ? 8 : 6) : 4;
+};
 
-// Histogram update modes of the lane-private moment histograms:
-//   0  scalar read-modify-write      hist[(j*8 + m)*G + lane]
-//   1  float4 read-modify-write      hist4[(j*2 + m/4)*G + lane].{x,y,z,w}[m%4]
+// Histogram update modes of the lane-private moment histograms (NMH slots):
+//   0  scalar read-modify-write      hist[(j*NMH + m)*G + lane]
+//   1  float4 read-modify-write      hist4[(j*NMH/4 + m/4)*G + lane].{x,y,z,w}[m%4]
 //   2  shared-memory atomic add      same layout as 0 (no contention: lane-private)
-template <int HIST, typename T, int G>
+template <int HIST, int NMH, typename T, int G>
 __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane, const T (&v)[8], int nv) {
 	if (HIST == 1) {
-		Q4<T>* h4 = reinterpret_cast<Q4<T>*>(hist) + ((size_t)j * 2) * G + lane;
+		Q4<T>* h4 = reinterpret_cast<Q4<T>*>(hist) + ((size_t)j * (NMH / 4)) * G + lane;
 		Q4<T> a = h4[0];
 		a.x += v[0];
 		a.y += v[1];
@@ -56,7 +57,7 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 			h4[G] = b;
 		}
 	} else {
-		T* hp = hist + (size_t)j * HistSlots<HIST>::value * G + lane;
+		T* hp = hist + (size_t)j * NMH * G + lane;
 #pragma unroll
 		for (int m = 0; m < 8; m++) {
 			if (m >= nv) break;
@@ -67,15 +68,15 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 }
 
 // value of moment m of interval j summed over the group's lanes
-template <int HIST, typename T, int G>
+template <int HIST, int NMH, typename T, int G>
 __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) {
 	T s = T(0);
 	if (HIST == 1) {
-		const T* h = hist + (((size_t)j * 2 + m / 4) * G) * 4 + (m & 3);
+		const T* h = hist + (((size_t)j * (NMH / 4) + m / 4) * G) * 4 + (m & 3);
 #pragma unroll 8
 		for (int l = 0; l < G; l++) s += h[l * 4];
 	} else {
-		const T* h = hist + ((size_t)j * HistSlots<HIST>::value + m) * G;
+		const T* h = hist + ((size_t)j * NMH + m) * G;
 #pragma unroll 8
 		for (int l = 0; l < G; l++) s += h[l];
 	}
@@ -83,22 +84,27 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 }
 
 // Shared memory layout:
-//   CTA:   coefC[2*nbin] (uR, uI cubics) | kb[nbin] | hv[nbin] | lut[ncell]
-//   group: xs[n] | Gs[n*6] (adjoint) | hist[nbin*NM*G] | red[nbin*NMtot] | spl[ns*4] | misc[16]
+//   CTA:   coefC[3*nbin] (u', u'' coefficients) | kb[nbin] | hv[nbin] | lut[ncell]
+//   group: xs[n] {x, y, z, gRx} | (adjoint) g4[n] {gRy, gRz, gIx, gIy} | gz[n] {gIz}
+//          | hist[nbin*NMH*G] | red[nbin*4] | (adjoint) redr[nbin*6]
+// The spline values [ns][4] of the last step borrow the start of the (then
+// empty) histogram and are cleared after use.
 template <typename T>
 __host__ __device__ inline size_t eloc_cta_bytes(int nbin, int ncell) {
-	size_t b = 2 * (size_t)nbin * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+	size_t b = 3 * (size_t)nbin * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
 	return (b + 31) & ~(size_t)31;
+}
+__host__ __device__ inline int eloc_hist_slots(bool adj, int hist_mode) {
+	return adj ? (hist_mode == 1 ? 8 : 6) : 4;
 }
 template <typename T>
 __host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G, bool adj, int hist_mode = 0) {
-	int nm = adj ? kFwdMomentsAdj : kFwdMoments;
-	int nmh = hist_mode == 1 ? 8 : 7;
 	size_t b = (size_t)n * sizeof(Q4<T>);
-	if (adj) b += (size_t)((n * 6 + 7) & ~7) * sizeof(T);  // keeps the histogram 32-byte aligned
-	b += (size_t)nbin * nmh * G * sizeof(T);
-	b += (size_t)nbin * (nm + (adj ? kRevMoments : 0)) * sizeof(T);
-	b += (size_t)ns * 4 * sizeof(T) + 16 * sizeof(T);
+	if (adj) b += (size_t)n * sizeof(Q4<T>) + (size_t)((n + 7) & ~7) * sizeof(T);  // keeps the histogram 32-byte aligned
+	size_t h = (size_t)nbin * eloc_hist_slots(adj, hist_mode) * G;
+	if (h < (size_t)ns * 4) h = (size_t)ns * 4;
+	b += h * sizeof(T);
+	b += (size_t)nbin * (kFwdMoments + (adj ? kRevMoments : 0)) * sizeof(T);
 	return (b + 31) & ~(size_t)31;
 }
 
@@ -131,14 +137,14 @@ __device__ __forceinline__ FwdPair<T> fwd_pair(const SysConst& sc, const Q4<T>& 
 	q.r = r2 * q.rinv;
 	q.in = ok && (q.r <= (T)sc.rmax);
 	q.j = locate<T>(sc, q.r, kb, hv, lut, q.t);
-	const Q4<T> cR = coefC[2 * q.j];
-	const Q4<T> cI = coefC[2 * q.j + 1];
-	const T hj = sc.uniform ? (T)sc.hinv : hv[q.j];
+	const Q4<T> cR = coefC[3 * q.j];
+	const Q4<T> cI = coefC[3 * q.j + 1];
+	const Q4<T> c2 = coefC[3 * q.j + 2];
 	const T t = q.t;
-	const T d1R = (cR.y + t * (T(2) * cR.z + T(3) * t * cR.w)) * hj;
-	const T d1I = (cI.y + t * (T(2) * cI.z + T(3) * t * cI.w)) * hj;
-	const T d2R = (T(2) * cR.z + T(6) * t * cR.w) * (hj * hj);
-	const T d2I = (T(2) * cI.z + T(6) * t * cI.w) * (hj * hj);
+	const T d1R = fma(t, fma(t, cR.z, cR.y), cR.x);
+	const T d1I = fma(t, fma(t, cI.z, cI.y), cI.x);
+	const T d2R = fma(t, c2.x, cR.w);
+	const T d2I = fma(t, c2.y, cI.w);
 	const T dm1 = (T)(sc.dim - 1);
 	q.gR = q.in ? d1R * q.rinv : T(0);
 	q.gI = q.in ? d1I * q.rinv : T(0);
@@ -153,9 +159,8 @@ __device__ __forceinline__ void fwd_stats(const SysConst& sc, const FwdPair<T>& 
                                           int lane, T pa, T pb, T& vb) {
 	const T ts = on ? q.t : T(0);  // t is NaN for the self pair
 	const T t2 = ts * ts;
-	const T qq = on ? q.rinv : T(0);
-	T v[8] = {on ? T(1) : T(0), ts, t2, t2 * ts, qq, qq * ts, qq * t2, T(0)};
-	hist_add8<HIST, T, G>(hist, q.j, lane, v, ADJ ? kFwdMomentsAdj : kFwdMoments);
+	T v[8] = {on ? T(1) : T(0), ts, t2, t2 * ts, T(0), T(0), T(0), T(0)};
+	hist_add8<HIST, HistSlots<HIST, ADJ>::value, T, G>(hist, q.j, lane, v, kFwdMoments);
 	vb += on ? pair_pot<T>(sc.pot_kind, q.r, q.rinv, pa, pb) : T(0);
 }
 
@@ -163,7 +168,7 @@ __device__ __forceinline__ void fwd_stats(const SysConst& sc, const FwdPair<T>& 
 // iteration so their dependency chains overlap (one warp per SM sub-partition
 // is all the shared memory allows).
 // ON: 0 = no pair statistics, 1 = all lanes count the pair, 2 = count iff i < nrow.
-constexpr int kNp = 4;
+constexpr int kNp = 2;
 template <typename T, int G, int ON, bool ADJ, int HIST>
 __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
                                            const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
@@ -220,10 +225,12 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 // partners per iteration.
 template <typename T, int G, bool DIAG, int HIST>
 __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
-                                           const T* gn, const Q4<T>* __restrict__ xs, const T* __restrict__ Gs,
-                                           const T* __restrict__ kb, const T* __restrict__ hv,
-                                           const int* __restrict__ lut, T* __restrict__ hist, int lane) {
+                                           const T* gn, const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ g4,
+                                           const T* __restrict__ gz, const T* __restrict__ kb,
+                                           const T* __restrict__ hv, const int* __restrict__ lut,
+                                           T* __restrict__ hist, int lane) {
 	const T L = (T)sc.L, Lr = (T)sc.Lr, rmax = (T)sc.rmax;
+	const T dm1 = (T)(sc.dim - 1);
 	for (int i = i0; i < i1; i += kNp) {
 		T v[kNp][8];
 		int jj[kNp];
@@ -231,8 +238,9 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 		for (int h = 0; h < kNp; h++) {
 			const bool have = i + h < i1;
 			const int ii = have ? i + h : i;
-			const Q4<T> xi = xs[ii];
-			const T* gi = Gs + (size_t)ii * 6;
+			const Q4<T> xi = xs[ii];  // .w = gRx of the partner
+			const Q4<T> gi = g4[ii];
+			const T giz = gz[ii];
 			const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
 			const T r2 = dx * dx + dy * dy + dz * dz;
 			const T rinv = rsqrt_(r2);
@@ -242,8 +250,9 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 			jj[h] = locate<T>(sc, r, kb, hv, lut, t);
 			t = on ? t : T(0);  // t is NaN for the self pair
 			const T sr = on ? rinv : T(0);
-			const T gR = ((gn[0] - gi[0]) * dx + (gn[1] - gi[1]) * dy + (gn[2] - gi[2]) * dz) * sr;
-			const T gI = ((gn[3] - gi[3]) * dx + (gn[4] - gi[4]) * dy + (gn[5] - gi[5]) * dz) * sr;
+			// (G_n - G_i) . rhat plus the (D-1)/r of the Laplacian of B (real part only)
+			const T gR = ((gn[0] - xi.w) * dx + (gn[1] - gi.x) * dy + (gn[2] - gi.y) * dz + dm1) * sr;
+			const T gI = ((gn[3] - gi.z) * dx + (gn[4] - gi.w) * dy + (gn[5] - giz) * dz) * sr;
 			const T t2 = t * t;
 			v[h][0] = gR;
 			v[h][1] = gR * t;
@@ -254,17 +263,17 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 			v[h][6] = v[h][7] = T(0);
 		}
 #pragma unroll
-		for (int h = 0; h < kNp; h++) hist_add8<HIST, T, G>(hist, jj[h], lane, v[h], kRevMoments);
+		for (int h = 0; h < kNp; h++) hist_add8<HIST, HistSlots<HIST, true>::value, T, G>(hist, jj[h], lane, v[h], kRevMoments);
 	}
 }
 
 // Sum lane-private histograms into red[nbin*nm] and clear them.
-template <typename T, int G, int HIST>
+template <typename T, int G, int HIST, int NMH>
 __device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, int lane, unsigned gmask) {
 	__syncwarp(gmask);
-	for (int e = lane; e < nbin * nm; e += G) red[e] = hist_sum<HIST, T, G>(hist, e / nm, e % nm);
+	for (int e = lane; e < nbin * nm; e += G) red[e] = hist_sum<HIST, NMH, T, G>(hist, e / nm, e % nm);
 	__syncwarp(gmask);
-	for (int e = lane; e < nbin * HistSlots<HIST>::value * G; e += G) hist[e] = T(0);
+	for (int e = lane; e < nbin * NMH * G; e += G) hist[e] = T(0);
 	__syncwarp(gmask);
 }
 
@@ -276,18 +285,18 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
                                               const T* __restrict__ pos, int64_t nw, T* __restrict__ lnpsi_o,
                                               T* __restrict__ O_o, T* __restrict__ eloc_o, T* __restrict__ other_o,
                                               T* __restrict__ dE_o) {
-	constexpr int NM = ADJ ? kFwdMomentsAdj : kFwdMoments;
-	constexpr int NMH = HistSlots<HIST>::value;
+	constexpr int NM = kFwdMoments;
+	constexpr int NMH = HistSlots<HIST, ADJ>::value;
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
 	Q4<T>* coefC = reinterpret_cast<Q4<T>*>(smem_raw);
-	T* kb = reinterpret_cast<T*>(coefC + 2 * nbin);
+	T* kb = reinterpret_cast<T*>(coefC + 3 * nbin);
 	T* hv = kb + nbin;
 	int* lut = reinterpret_cast<int*>(hv + nbin);
 	const size_t cta_b = eloc_cta_bytes<T>(nbin, sc.ncell);
 	const size_t grp_b = eloc_group_bytes<T>(n, nbin, ns, G, ADJ, HIST);
 
-	for (int i = threadIdx.x; i < 2 * nbin; i += blockDim.x) coefC[i] = coefC_g[i];
+	for (int i = threadIdx.x; i < 3 * nbin; i += blockDim.x) coefC[i] = coefC_g[i];
 	for (int i = threadIdx.x; i < nbin; i += blockDim.x) {
 		kb[i] = kb_g[i];
 		hv[i] = hv_g[i];
@@ -302,14 +311,15 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
 	unsigned char* gbase = smem_raw + cta_b + (size_t)gib * grp_b;
 	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
-	T* Gs = reinterpret_cast<T*>(xs + n);
-	T* hist = Gs + (ADJ ? (size_t)((n * 6 + 7) & ~7) : 0);
-	T* red = hist + (size_t)nbin * NMH * G;
+	Q4<T>* g4 = xs + (ADJ ? n : 0);
+	T* gz = reinterpret_cast<T*>(xs + (ADJ ? 2 * n : n));
+	T* hist = gz + (ADJ ? (size_t)((n + 7) & ~7) : 0);
+	const size_t hist_len = (size_t)nbin * NMH * G > (size_t)ns * 4 ? (size_t)nbin * NMH * G : (size_t)ns * 4;
+	T* red = hist + hist_len;
 	T* redr = red + (size_t)nbin * NM;
-	T* spl = redr + (ADJ ? (size_t)nbin * kRevMoments : 0);  // [ns][4]: S, Lsp, AR, AI
-	T* misc = spl + (size_t)ns * 4;
+	T* spl = hist;  // [ns][4]: S, Lsp, AR, AI, while the histogram is empty
 
-	for (int e = lane; e < nbin * NMH * G; e += G) hist[e] = T(0);
+	for (size_t e = lane; e < hist_len; e += G) hist[e] = T(0);
 	__syncthreads();
 
 	const T pa = (T)dyn->pa, pb = (T)dyn->pb;
@@ -346,13 +356,9 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				e_lR.add(acc[6].value());
 				e_lI.add(acc[7].value());
 				if (ADJ) {
-					T* g = Gs + (size_t)nrow * 6;
-					g[0] = gRx;
-					g[1] = gRy;
-					g[2] = gRz;
-					g[3] = gIx;
-					g[4] = gIy;
-					g[5] = gIz;
+					xs[nrow].w = gRx;
+					g4[nrow] = Q4<T>{gRy, gRz, gIx, gIy};
+					gz[nrow] = gIz;
 				}
 			}
 		}
@@ -367,7 +373,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 #pragma unroll
 		for (int o = G / 2; o > 0; o >>= 1) nout_all += __shfl_xor_sync(gmask, nout_all, o, G);
 
-		hist_reduce<T, G, HIST>(hist, red, nbin, NM, lane, gmask);
+		hist_reduce<T, G, HIST, NMH>(hist, red, nbin, NM, lane, gmask);
 
 		if (ADJ) {
 			for (int s = 0; s < nslot; s++) {
@@ -375,18 +381,24 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				const bool rowok = nrow < n;
 				const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
 				T gn[6] = {0, 0, 0, 0, 0, 0};
-				if (rowok)
-					for (int k = 0; k < 6; k++) gn[k] = Gs[(size_t)nrow * 6 + k];
+				if (rowok) {
+					const Q4<T> a = g4[nrow];
+					gn[0] = xr.w;
+					gn[1] = a.x;
+					gn[2] = a.y;
+					gn[3] = a.z;
+					gn[4] = a.w;
+					gn[5] = gz[nrow];
+				}
 				const int base = s * G;
 				const int dend = (base + G < n) ? base + G : n;
-				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
-				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, Gs, kb, hv, lut, hist, lane);
+				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
 			}
-			hist_reduce<T, G, HIST>(hist, redr, nbin, kRevMoments, lane, gmask);
+			hist_reduce<T, G, HIST, NMH>(hist, redr, nbin, kRevMoments, lane, gmask);
 		}
 
 		// moments -> spline values: spline sp = j + 3 - q on interval j
-		const T dm1 = (T)(sc.dim - 1);
 		for (int sp = lane; sp < ns; sp += G) {
 			T S = T(0), Lsp = T(0), AR = T(0), AI = T(0);
 #pragma unroll
@@ -399,8 +411,8 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				S += l0 * m[0] + l1 * m[1] + l2 * m[2] + l3 * m[3];
 				if (ADJ) {
 					const T hj = sc.uniform ? (T)sc.hinv : hv[j];
-					Lsp += T(2) * (hj * hj * (T(2) * l2 * m[0] + T(6) * l3 * m[1]) +
-					               dm1 * hj * (l1 * m[4] + T(2) * l2 * m[5] + T(3) * l3 * m[6]));
+					// B'' part of the Laplacian of O_k; its (D-1)/r B' part is in g[0..2]
+					Lsp += T(2) * hj * hj * (T(2) * l2 * m[0] + T(6) * l3 * m[1]);
 					const T* g = redr + (size_t)j * kRevMoments;
 					AR += hj * (l1 * g[0] + T(2) * l2 * g[1] + T(3) * l3 * g[2]);
 					AI += hj * (l1 * g[3] + T(2) * l2 * g[4] + T(3) * l3 * g[5]);
@@ -433,6 +445,8 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 			}
 			lnp += params[k] * Ok;
 		}
+		__syncwarp(gmask);
+		for (int e = lane; e < ns * 4; e += G) spl[e] = T(0);  // the histogram starts empty
 #pragma unroll
 		for (int o = G / 2; o > 0; o >>= 1) lnp += __shfl_xor_sync(gmask, lnp, o, G);
 		if (lane == 0) {
@@ -453,7 +467,6 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 		}
 		__syncwarp(gmask);
 	}
-	(void)misc;
 }
 
 }  // namespace tdvmc

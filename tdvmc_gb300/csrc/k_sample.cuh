@@ -3,7 +3,7 @@
 // BosonsBulk::CalculateWFChange / CalculateWFQuotient, BosonsBulk.cpp:553-657).
 //
 // One group of G lanes owns one walker at a time (persistent grid-stride
-// loop over walkers).  Particle i of the walker lives in lane i % G, slot
+// loop over walkers (start + w) mod nw_total, w < nw, start = *wstart or 0).  Particle i of the walker lives in lane i % G, slot
 // i / G, in registers; a shared-memory mirror serves the random reads of the
 // moved particle.  Per move every lane evaluates u(r) at the old and new
 // position against its own particles; a butterfly reduction gives
@@ -24,11 +24,10 @@ template <typename T> struct alignas(4 * sizeof(T)) Q4 {
 	T x, y, z, w;
 };
 
-// Pair function at squared distance r2.  coef holds nbin + 1 cubics in the
+// Pair function at squared distance r2.  coef holds the nbin cubics in the
 // centred local coordinate tau = t - 1/2 (better conditioned and one
-// operation shorter); entry nbin is the constant outer-pair value uR[p-1]
-// (coefficients (u, 0, 0, 0)), selected for r >= r_max by the clamp of the
-// interval index.
+// operation shorter); entries nbin .. ncoef-1 are the constant outer-pair
+// value uR[p-1] (coefficients (u, 0, 0, 0)), selected for r >= r_max.
 template <typename T>
 __device__ __forceinline__ T pair_u(const SysConst& sc, T r2, const Q4<T>* __restrict__ coef,
                                     const T* __restrict__ kb, const T* __restrict__ hv,
@@ -63,13 +62,13 @@ template <typename T>
 __device__ __forceinline__ T mi_r2(T dx, T dy, T dz, T L) {
 	const T ax = fabs(dx), ay = fabs(dy), az = fabs(dz);
 	const T mx = fmin(ax, L - ax), my = fmin(ay, L - ay), mz = fmin(az, L - az);
-	return mx * mx + my * my + mz * mz;
+	return fma(mz, mz, fma(my, my, mx * mx));
 }
 
-// Shared memory: coef[nbin] | kb[nbin] | hv[nbin] | lut[ncell] | mirror[groups][n]
+// Shared memory: coef[ncoef] | kb[nbin] | hv[nbin] | lut[ncell] | mirror[groups][n]
 template <typename T>
-__host__ __device__ inline size_t sample_smem_bytes(int nbin, int ncell, int n, int groups) {
-	size_t b = (size_t)(nbin + 1) * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+__host__ __device__ inline size_t sample_smem_bytes(int ncoef, int nbin, int ncell, int n, int groups) {
+	size_t b = (size_t)ncoef * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
 	b = (b + 31) & ~(size_t)31;
 	return b + (size_t)groups * n * sizeof(Q4<T>);
 }
@@ -77,19 +76,20 @@ __host__ __device__ inline size_t sample_smem_bytes(int nbin, int ncell, int n, 
 template <typename T, int G, int SLOTS>
 __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __restrict__ coef_g, const T* __restrict__ uout_g,
                                                 const T* __restrict__ kb_g, const T* __restrict__ hv_g,
-                                                const int* __restrict__ lut_g, T* __restrict__ pos, int64_t nw, int moves,
+                                                const int* __restrict__ lut_g, T* __restrict__ pos, int64_t nw,
+                                                int64_t nw_total, const int32_t* __restrict__ wstart, int moves,
                                                 T step, uint2 key, const uint32_t* __restrict__ pass_ptr,
                                                 int* __restrict__ acc_out) {
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	Q4<T>* coef = reinterpret_cast<Q4<T>*>(smem_raw);
-	T* kb = reinterpret_cast<T*>(coef + sc.nbin + 1);
+	T* kb = reinterpret_cast<T*>(coef + sc.ncoef);
 	T* hv = kb + sc.nbin;
 	int* lut = reinterpret_cast<int*>(hv + sc.nbin);
-	size_t off = (size_t)(sc.nbin + 1) * sizeof(Q4<T>) + 2 * (size_t)sc.nbin * sizeof(T) + (size_t)sc.ncell * sizeof(int);
+	size_t off = (size_t)sc.ncoef * sizeof(Q4<T>) + 2 * (size_t)sc.nbin * sizeof(T) + (size_t)sc.ncell * sizeof(int);
 	off = (off + 31) & ~(size_t)31;
 	Q4<T>* mirror_all = reinterpret_cast<Q4<T>*>(smem_raw + off);
 
-	for (int i = threadIdx.x; i <= sc.nbin; i += blockDim.x) coef[i] = coef_g[i];
+	for (int i = threadIdx.x; i < sc.ncoef; i += blockDim.x) coef[i] = coef_g[i];
 	for (int i = threadIdx.x; i < sc.nbin; i += blockDim.x) {
 		kb[i] = kb_g[i];
 		hv[i] = hv_g[i];
@@ -107,9 +107,12 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 	Q4<T>* xs = mirror_all + (size_t)gib * n;
 	const T L = (T)sc.L, Lr = (T)sc.Lr;
 	const uint32_t pass = *pass_ptr;
+	const int64_t w0 = wstart ? (int64_t)*wstart : 0;
 	(void)uout_g;
 
-	for (int64_t w = (int64_t)blockIdx.x * gpb + gib; w < nw; w += (int64_t)gridDim.x * gpb) {
+	for (int64_t wi = (int64_t)blockIdx.x * gpb + gib; wi < nw; wi += (int64_t)gridDim.x * gpb) {
+		int64_t w = w0 + wi;
+		if (w >= nw_total) w -= nw_total;
 		T* pw = pos + (size_t)w * sc.dim * n;
 		T x[SLOTS], y[SLOTS], z[SLOTS];
 #pragma unroll
@@ -189,6 +192,226 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 				pw[i] = x[s];
 				if (sc.dim > 1) pw[n + i] = y[s];
 				if (sc.dim > 2) pw[2 * n + i] = z[s];
+			}
+		}
+		if (lane == 0) acc_out[w] = nacc;
+		__syncwarp(gmask);
+	}
+}
+
+// ---- packed FP32 pairs (f32x2 arithmetic of sm_100 and later) --------------
+// One 64-bit register holds two floats; add/sub/mul/fma.rn.f32x2 round each
+// half exactly like the scalar instruction, in one issue slot.
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_make(float lo, float hi) {
+	f2_t r;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+	return r;
+}
+__device__ __forceinline__ void f2_split(f2_t v, float& lo, float& hi) {
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
+	f2_t d;
+	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+	return d;
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b) {
+	f2_t d;
+	asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+	return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+	f2_t d;
+	asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+	return d;
+}
+// a * b + c
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+	f2_t d;
+	asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+	return d;
+}
+__device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
+	Q4<float> c;
+	asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(c.x), "=f"(c.y), "=f"(c.z), "=f"(c.w) : "r"(addr));
+	return c;
+}
+
+// FP32 sampler for uniform knots with packed pair arithmetic.  It walks the
+// same chain as k_sample<float>, bit for bit: same random numbers, moves and
+// acceptance rule, and every pair term and partial sum rounded the same way.
+// Per register slot the distances of the slot's particle to the proposed and
+// to the old position of the moved particle are one f32x2 instruction stream
+// (differences, r^2, r, the interval index by the float-rounding trick, the
+// local coordinate); the per-axis minimum image min(|d|, L - |d|) stays
+// scalar so its min runs on the ALU pipe beside the FMA pipe.  The table
+// holds the outer-pair constant for every index up to sqrt(D) L/2, so the
+// index needs no clamp (the clamped scalar lookup reads the same constant).
+// The moved particle's own slot (old distance 0, kept finite by a 1e-30
+// floor on r^2, which is below the rounding of any other r^2) and slots past
+// n are left out of the sum by predication.  Table indices
+// stay in range because every coordinate used lies in [-L/2, L/2]: a walker
+// with a coordinate outside after wrapping (non-finite or too large to wrap
+// exactly) makes no moves, as in the scalar sampler where every quotient of
+// such a walker is rejected, and a proposal outside is rejected.
+template <int G, int SLOTS>
+__global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
+                                                   const float* __restrict__ uout_g, const float* __restrict__ kb_g,
+                                                   const float* __restrict__ hv_g, const int* __restrict__ lut_g,
+                                                   float* __restrict__ pos, int64_t nw, int64_t nw_total,
+                                                   const int32_t* __restrict__ wstart, int moves, float step, uint2 key,
+                                                   const uint32_t* __restrict__ pass_ptr, int* __restrict__ acc_out) {
+	extern __shared__ __align__(32) unsigned char smem_raw[];
+	Q4<float>* coef = reinterpret_cast<Q4<float>*>(smem_raw);
+	size_t off = (size_t)sc.ncoef * sizeof(Q4<float>) + 2 * (size_t)sc.nbin * sizeof(float) + (size_t)sc.ncell * sizeof(int);
+	off = (off + 31) & ~(size_t)31;
+	Q4<float>* mirror_all = reinterpret_cast<Q4<float>*>(smem_raw + off);
+	for (int i = threadIdx.x; i < sc.ncoef; i += blockDim.x) coef[i] = coef_g[i];
+	__syncthreads();
+	(void)uout_g;
+	(void)kb_g;
+	(void)hv_g;
+	(void)lut_g;
+
+	// byte address of entry j is coef_a + (bits(y) << 4) with y = kRoundF + j
+	const uint32_t coef_a =
+	    (uint32_t)__cvta_generic_to_shared(coef) - ((uint32_t)__float_as_uint(kRoundF) << 4);
+	const int n = sc.n;
+	const int tid = threadIdx.x;
+	const int lane = tid & (G - 1);
+	const int gib = tid / G;
+	const int gpb = blockDim.x / G;
+	const unsigned wl = tid & 31;
+	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
+	Q4<float>* xs = mirror_all + (size_t)gib * n;
+	const float L = (float)sc.L, Lr = (float)sc.Lr;
+	const f2_t R2 = f2_make(kRoundF, kRoundF);
+	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mhalf2 = f2_make(-0.5f, -0.5f);
+	const f2_t tiny2 = f2_make(1e-30f, 1e-30f);
+	const uint32_t pass = *pass_ptr;
+	const bool last_ok = (SLOTS - 1) * G + lane < n;
+	const float half = 0.5f * L * (1.f + 1e-5f);
+	const int64_t w0 = wstart ? (int64_t)*wstart : 0;
+
+	for (int64_t wi = (int64_t)blockIdx.x * gpb + gib; wi < nw; wi += (int64_t)gridDim.x * gpb) {
+		int64_t w = w0 + wi;
+		if (w >= nw_total) w -= nw_total;
+		float* pw = pos + (size_t)w * sc.dim * n;
+		// each coordinate twice: one half meets the proposed, one the old position
+		f2_t X[SLOTS], Y[SLOTS], Z[SLOTS];
+		bool inside = true;
+#pragma unroll
+		for (int s = 0; s < SLOTS; s++) {
+			const int i = s * G + lane;
+			float x = 0.f, y = 0.f, z = 0.f;
+			if (i < n) {
+				// positions into [-L/2, L/2] (AlignCoordinates, TDVMC.cpp:2569-2582)
+				x = nic(pw[i], L, Lr);
+				if (sc.dim > 1) y = nic(pw[n + i], L, Lr);
+				if (sc.dim > 2) z = nic(pw[2 * n + i], L, Lr);
+				inside = inside && fabsf(x) <= half && fabsf(y) <= half && fabsf(z) <= half;
+				xs[i] = Q4<float>{x, y, z, 0.f};
+			}
+			X[s] = f2_make(x, x);
+			Y[s] = f2_make(y, y);
+			Z[s] = f2_make(z, z);
+		}
+		const bool walker_ok = __all_sync(gmask, inside);
+		__syncwarp(gmask);
+		int nacc = 0;
+		for (int mb = 0; walker_ok && mb < moves; mb += G) {
+			MoveRand<float> rl;
+			rl.part = 0;
+			rl.u = 1.f;
+			rl.z0 = rl.z1 = rl.z2 = 0.f;
+			if (mb + lane < moves) rl = move_rand<float>((uint32_t)(mb + lane), (uint32_t)w, pass, key, n, sc.dim);
+			const float lu = logf(rl.u);
+			const float dz0 = step * rl.z0, dz1 = step * rl.z1, dz2 = step * rl.z2;
+			const int nb = (moves - mb) < G ? (moves - mb) : G;
+			for (int jm = 0; jm < nb; jm++) {
+				const int p = __shfl_sync(gmask, rl.part, jm, G);
+				const float lum = __shfl_sync(gmask, lu, jm, G);
+				const float e0 = __shfl_sync(gmask, dz0, jm, G);
+				const float e1 = __shfl_sync(gmask, dz1, jm, G);
+				const float e2 = __shfl_sync(gmask, dz2, jm, G);
+				const Q4<float> xo = xs[p];
+				const float xn0 = nic(xo.x + e0, L, Lr);
+				const float xn1 = nic(xo.y + e1, L, Lr);
+				const float xn2 = nic(xo.z + e2, L, Lr);
+				if (!(fabsf(xn0) <= half && fabsf(xn1) <= half && fabsf(xn2) <= half)) continue;  // uniform over the group
+				const f2_t XN = f2_make(xn0, xo.x), YN = f2_make(xn1, xo.y), ZN = f2_make(xn2, xo.z);
+				const int self_slot = (lane == (p & (G - 1))) ? p / G : -1;
+				float dsum = 0.f;
+#pragma unroll
+				for (int s = 0; s < SLOTS; s++) {
+					float an, ao, bn, bo, cn, co;
+					f2_split(f2_sub(X[s], XN), an, ao);
+					f2_split(f2_sub(Y[s], YN), bn, bo);
+					f2_split(f2_sub(Z[s], ZN), cn, co);
+					const f2_t mx = f2_make(fminf(fabsf(an), L - fabsf(an)), fminf(fabsf(ao), L - fabsf(ao)));
+					const f2_t my = f2_make(fminf(fabsf(bn), L - fabsf(bn)), fminf(fabsf(bo), L - fabsf(bo)));
+					const f2_t mz = f2_make(fminf(fabsf(cn), L - fabsf(cn)), fminf(fabsf(co), L - fabsf(co)));
+					const f2_t r2 = f2_fma(mz, mz, f2_fma(my, my, f2_fma(mx, mx, tiny2)));
+					float ra, rb;
+					f2_split(r2, ra, rb);
+					const f2_t r = f2_mul(r2, f2_make(rsqrtf(ra), rsqrtf(rb)));
+					// floor(x) = round(x - 1/2), x = r / h (see nic)
+					const f2_t xm = f2_fma(r, H2, mhalf2);
+					const f2_t yv = f2_add(xm, R2);
+					const f2_t tau = f2_sub(xm, f2_sub(yv, R2));
+					float ya, yb, ta, tb;
+					f2_split(yv, ya, yb);
+					f2_split(tau, ta, tb);
+					const Q4<float> ca = lds_q4(coef_a + (__float_as_uint(ya) << 4));
+					const Q4<float> cb = lds_q4(coef_a + (__float_as_uint(yb) << 4));
+					const float un = fmaf(ta, fmaf(ta, fmaf(ta, ca.w, ca.z), ca.y), ca.x);
+					const float uo = fmaf(tb, fmaf(tb, fmaf(tb, cb.w, cb.z), cb.y), cb.x);
+					const bool ok = (s == SLOTS - 1) ? (last_ok && s != self_slot) : (s != self_slot);
+					const float du = un - uo;
+					if (ok) dsum += du;
+				}
+#pragma unroll
+				for (int o = G / 2; o > 0; o >>= 1) dsum += __shfl_xor_sync(gmask, dsum, o, G);
+				// exp(2 delta) >= U; a non-finite or overflowing quotient rejects (TDVMC.cpp:886-915)
+				const float two = 2.f * dsum;
+				const bool accept = isfinite(two) && (two >= lum) && ((double)two < kLogDblMax);
+				if (accept) {
+					if (lane == (p & (G - 1))) {
+						xs[p] = Q4<float>{xn0, xn1, xn2, 0.f};
+						const f2_t nx = f2_make(xn0, xn0), ny = f2_make(xn1, xn1), nz = f2_make(xn2, xn2);
+						switch (p / G) {
+#define TDVMC_SET_SLOT(S)                  \
+	case S:                                \
+		if (S < SLOTS) {                   \
+			X[S < SLOTS ? S : 0] = nx;     \
+			Y[S < SLOTS ? S : 0] = ny;     \
+			Z[S < SLOTS ? S : 0] = nz;     \
+		}                                  \
+		break;
+							TDVMC_SET_SLOT(0) TDVMC_SET_SLOT(1) TDVMC_SET_SLOT(2) TDVMC_SET_SLOT(3)
+							TDVMC_SET_SLOT(4) TDVMC_SET_SLOT(5) TDVMC_SET_SLOT(6) TDVMC_SET_SLOT(7)
+							TDVMC_SET_SLOT(8) TDVMC_SET_SLOT(9) TDVMC_SET_SLOT(10) TDVMC_SET_SLOT(11)
+							TDVMC_SET_SLOT(12) TDVMC_SET_SLOT(13) TDVMC_SET_SLOT(14) TDVMC_SET_SLOT(15)
+#undef TDVMC_SET_SLOT
+						}
+					}
+					nacc++;
+				}
+				__syncwarp(gmask);
+			}
+		}
+#pragma unroll
+		for (int s = 0; s < SLOTS && walker_ok; s++) {
+			const int i = s * G + lane;
+			if (i < n) {
+				float x, y, z, dummy;
+				f2_split(X[s], x, dummy);
+				pw[i] = x;
+				f2_split(Y[s], y, dummy);
+				if (sc.dim > 1) pw[n + i] = y;
+				f2_split(Z[s], z, dummy);
+				if (sc.dim > 2) pw[2 * n + i] = z;
 			}
 		}
 		if (lane == 0) acc_out[w] = nacc;

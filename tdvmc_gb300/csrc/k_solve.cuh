@@ -267,10 +267,12 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 
 // Stage coefficient tables from the current stage parameters: per-spline
 // complex weights w_s = sum_k alpha_k fold[k][s], then per knot interval j the
-// cubic sum_q w_{j+3-q} loc[j][q][.] (real part for the sampler; real and
-// imaginary parts for the evaluation) and the outer-pair value uR[p-1].
+// cubic sum_q w_{j+3-q} loc[j][q][.]: the real cubic for the sampler, the
+// first and second r-derivatives of the complex cubic for the evaluation,
+// and the outer-pair value uR[p-1].
 template <typename T>
-__global__ void __launch_bounds__(128) k_prep(int p, int ns, int nbin, const double* __restrict__ params,
+__global__ void __launch_bounds__(128) k_prep(int p, int ns, int nbin, int ncoef, int uniform, double hinv,
+                                              const T* __restrict__ hv, const double* __restrict__ params,
                                               const double* __restrict__ fold, const double* __restrict__ loc,
                                               T* __restrict__ coefU, T* __restrict__ coefC, T* __restrict__ uout) {
 	__shared__ double wR[kMaxSplines], wI[kMaxSplines];
@@ -295,21 +297,33 @@ __global__ void __launch_bounds__(128) k_prep(int p, int ns, int nbin, const dou
 				ci[c] += wI[s] * l[c];
 			}
 		}
-		for (int c = 0; c < 4; c++) {
-			coefC[j * 8 + c] = (T)cr[c];
-			coefC[j * 8 + 4 + c] = (T)ci[c];
-		}
+		// evaluation table: du/dr = a0 + t (a1 + t a2), d2u/dr2 = b0 + t b1 with
+		// the interval's 1/h folded in; per interval three 4-vectors
+		// {a0R a1R a2R b0R} {a0I a1I a2I b0I} {b1R b1I 0 0}
+		const double hj = uniform ? hinv : (double)hv[j];
+		T* e = coefC + (size_t)j * 12;
+		e[0] = (T)(cr[1] * hj);
+		e[1] = (T)(2.0 * cr[2] * hj);
+		e[2] = (T)(3.0 * cr[3] * hj);
+		e[3] = (T)(2.0 * cr[2] * hj * hj);
+		e[4] = (T)(ci[1] * hj);
+		e[5] = (T)(2.0 * ci[2] * hj);
+		e[6] = (T)(3.0 * ci[3] * hj);
+		e[7] = (T)(2.0 * ci[2] * hj * hj);
+		e[8] = (T)(6.0 * cr[3] * hj * hj);
+		e[9] = (T)(6.0 * ci[3] * hj * hj);
+		e[10] = e[11] = (T)0;
 		// sampler table: the real cubic in tau = t - 1/2 (Taylor shift by 1/2)
 		coefU[j * 4 + 0] = (T)(cr[0] + 0.5 * cr[1] + 0.25 * cr[2] + 0.125 * cr[3]);
 		coefU[j * 4 + 1] = (T)(cr[1] + cr[2] + 0.75 * cr[3]);
 		coefU[j * 4 + 2] = (T)(cr[2] + 1.5 * cr[3]);
 		coefU[j * 4 + 3] = (T)cr[3];
 	}
-	if (threadIdx.x == 0) {
-		*uout = (T)params[p - 1];
-		// entry nbin of the sampler table: the constant outer-pair value
-		coefU[nbin * 4 + 0] = (T)params[p - 1];
-		coefU[nbin * 4 + 1] = coefU[nbin * 4 + 2] = coefU[nbin * 4 + 3] = (T)0;
+	if (threadIdx.x == 0) *uout = (T)params[p - 1];
+	// entries nbin.. of the sampler table: the constant outer-pair value
+	for (int j = nbin + threadIdx.x; j < ncoef; j += blockDim.x) {
+		coefU[j * 4 + 0] = (T)params[p - 1];
+		coefU[j * 4 + 1] = coefU[j * 4 + 2] = coefU[j * 4 + 3] = (T)0;
 	}
 }
 

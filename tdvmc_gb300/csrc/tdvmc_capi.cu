@@ -5,6 +5,7 @@
 
 #include "common.cuh"
 #include "dispatch.cuh"
+#include "k_cs.cuh"
 #include "k_eloc.cuh"
 #include "k_gram_tf32.cuh"
 #include "k_sample.cuh"
@@ -39,10 +40,19 @@ struct GraphKey {
 	double dt, mc_step;
 	int imag, ode, lin, pre, norm, moves, adj;
 	uint64_t seed;
+	int kind;       // stage kind of the stored-sample solver (CsStage), 0 otherwise
+	int64_t count;  // walkers refreshed by a CsStage::kRefresh stage
 	bool operator<(const GraphKey& o) const {
-		return std::tie(dt, mc_step, imag, ode, lin, pre, norm, moves, adj, seed) <
-		       std::tie(o.dt, o.mc_step, o.imag, o.ode, o.lin, o.pre, o.norm, o.moves, o.adj, o.seed);
+		return std::tie(dt, mc_step, imag, ode, lin, pre, norm, moves, adj, seed, kind, count) <
+		       std::tie(o.dt, o.mc_step, o.imag, o.ode, o.lin, o.pre, o.norm, o.moves, o.adj, o.seed, o.kind, o.count);
 	}
+};
+
+// Stages of ODE_SOLVER_TYPE 3 (RK4 on stored samples)
+enum CsStage : int {
+	kCsFull = 1,     // sample every walker, store, evaluate the stored samples
+	kCsRefresh = 2,  // sample and store a rotating window of walkers, evaluate all
+	kCsReuse = 3,    // evaluate the stored samples at the stage parameters
 };
 
 }  // namespace
@@ -77,7 +87,15 @@ struct tdvmc_ctx {
 	DynState* dyn = nullptr;
 	int nblk1 = 0, nblk2 = 0, chunk2 = 0, nblkS = 0;
 	bool gram_tc = false;  // S on the tensor cores (mixed precision only)
+	bool packed_sampler = true;  // FP32 uniform-knot sampler with f32x2 pair arithmetic
 	std::map<GraphKey, cudaGraphExec_t> graphs;
+	std::map<GraphKey, int> graph_kernels;  // kernels launched by one replay
+	// stored samples (correlated-sampling reuse), allocated on first use
+	void *csD = nullptr, *csD2 = nullptr, *csO = nullptr, *csV = nullptr, *cs_piece = nullptr;
+	int32_t* csN = nullptr;
+	bool cs_valid = false;      // the store matches the walkers
+	int64_t cs_steps = 0;       // stored-sample steps since the last full store
+	int64_t cs_last_count = 0;  // walkers sampled by the last refresh
 	std::string err;
 	// eager profiling: events recorded after every kernel when set
 	std::vector<cudaEvent_t>* prof = nullptr;
@@ -169,28 +187,35 @@ int grid_for(tdvmc_ctx* ctx, const void* fn, int threads, size_t smem, int64_t w
 
 template <typename T>
 int launch_prep(tdvmc_ctx* ctx) {
-	k_prep<T><<<1, 128, 0, ctx->st>>>(ctx->sc.p, ctx->sc.ns, ctx->sc.nbin, ctx->stage, ctx->fold_d, ctx->loc_d,
-	                                  (T*)ctx->coefU, (T*)ctx->coefC, (T*)ctx->uout);
+	k_prep<T><<<1, 128, 0, ctx->st>>>(ctx->sc.p, ctx->sc.ns, ctx->sc.nbin, ctx->sc.ncoef, ctx->sc.uniform, ctx->sc.hinv,
+	                                  (const T*)ctx->hv, ctx->stage, ctx->fold_d, ctx->loc_d, (T*)ctx->coefU,
+	                                  (T*)ctx->coefC, (T*)ctx->uout);
 	ctx->launches++;
 	mark(ctx, "k_prep");
 	CK(cudaGetLastError());
 	return TDVMC_OK;
 }
 
+// Samples walkers (start + w) mod nw, w < count; start = *wstart (device) or 0.
 template <typename T>
-int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed) {
+int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed, int64_t count = -1,
+                  const int32_t* wstart = nullptr) {
+	if (count < 0) count = ctx->nw;
 	const int G = ctx->tiles.sg, gpb = ctx->tiles.sgpb;
 	const int slots = slots_for(ctx->sc.n, G);
-	SampleFn<T> fn = pick_sample<T>(G, slots);
+	SampleFn<T> fn = nullptr;
+	if constexpr (std::is_same<T, float>::value)
+		if (ctx->packed_sampler && ctx->sc.uniform) fn = pick_sample_f32_packed(G, slots);
+	if (!fn) fn = pick_sample<T>(G, slots);
 	if (!fn) return TDVMC_ERR_ARG;
 	const int threads = G * gpb;
-	const size_t smem = sample_smem_bytes<T>(ctx->sc.nbin, ctx->sc.ncell, ctx->sc.n, gpb);
+	const size_t smem = sample_smem_bytes<T>(ctx->sc.ncoef, ctx->sc.nbin, ctx->sc.ncell, ctx->sc.n, gpb);
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, gpb);
+	const int grid = grid_for(ctx, (const void*)fn, threads, smem, count, gpb);
 	uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
 	fn<<<grid, threads, smem, ctx->st>>>(ctx->sc, (const Q4<T>*)ctx->coefU, (const T*)ctx->uout, (const T*)ctx->kb,
-	                                     (const T*)ctx->hv, ctx->lut, (T*)ctx->pos, ctx->nw, moves, (T)step, key,
-	                                     &ctx->dyn->pass, ctx->acc);
+	                                     (const T*)ctx->hv, ctx->lut, (T*)ctx->pos, count, ctx->nw, wstart, moves,
+	                                     (T)step, key, &ctx->dyn->pass, ctx->acc);
 	ctx->launches++;
 	mark(ctx, "k_sample");
 	CK(cudaGetLastError());
@@ -287,6 +312,91 @@ int launch_solve(tdvmc_ctx* ctx, int imag, int pre, int lin, int mode, int norm,
 	return TDVMC_OK;
 }
 
+// ---- stored samples (correlated-sampling reuse, ODE_SOLVER_TYPE 3) --------
+int cs_alloc(tdvmc_ctx* ctx) {
+	if (ctx->csD) return TDVMC_OK;
+	const size_t ts = tsize(ctx->prec);
+	const size_t nw = (size_t)ctx->nw, ns = (size_t)ctx->sc.ns, n = (size_t)ctx->sc.n, P = (size_t)ctx->sc.p;
+	bool ok = cudaMalloc(&ctx->csD, nw * ns * 3 * n * ts) == cudaSuccess &&
+	          cudaMalloc(&ctx->csD2, nw * ns * ts) == cudaSuccess && cudaMalloc(&ctx->csO, nw * P * ts) == cudaSuccess &&
+	          cudaMalloc(&ctx->csV, nw * ts) == cudaSuccess &&
+	          cudaMalloc((void**)&ctx->csN, nw * sizeof(int32_t)) == cudaSuccess;
+	if (!ok) {
+		void* b[] = {ctx->csD, ctx->csD2, ctx->csO, ctx->csV, ctx->csN};
+		for (void* x : b)
+			if (x) cudaFree(x);
+		ctx->csD = ctx->csD2 = ctx->csO = ctx->csV = nullptr;
+		ctx->csN = nullptr;
+		cudaGetLastError();  // out of memory is not sticky
+		return TDVMC_ERR_NOMEM;
+	}
+	return TDVMC_OK;
+}
+
+// Stores walkers (start + w) mod nw, w < count (start = *wstart or 0).
+template <typename T>
+int launch_cs_store(tdvmc_ctx* ctx, int64_t count, const int32_t* wstart) {
+	constexpr int G = 32;
+	const SysConst& s = ctx->sc;
+	const size_t smem = cs_cta_bytes<T>(s.nbin, s.ncell) + cs_group_bytes<T>(s.n, s.ns, G);
+	auto fn = k_cs_store<T, G>;
+	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const int grid = grid_for(ctx, (const void*)fn, G, smem, count, 1);
+	fn<<<grid, G, smem, ctx->st>>>(s, ctx->dyn, (const T*)ctx->cs_piece, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut,
+	                               ctx->fold_d, (const T*)ctx->pos, count, ctx->nw, wstart, (T*)ctx->csD,
+	                               (T*)ctx->csD2, (T*)ctx->csO, (T*)ctx->csV, ctx->csN);
+	ctx->launches++;
+	mark(ctx, "k_cs_store");
+	CK(cudaGetLastError());
+	return TDVMC_OK;
+}
+
+template <typename T>
+int launch_cs_eval(tdvmc_ctx* ctx, bool adj) {
+	const SysConst& s = ctx->sc;
+	const int threads = 128, wpb = threads / 32;
+	const size_t smem = ((size_t)2 * s.ns + (size_t)wpb * ((size_t)s.n * 6 + 2 * s.ns)) * sizeof(T);
+	auto fn = adj ? k_cs_eval<T, true> : k_cs_eval<T, false>;
+	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, wpb);
+	fn<<<grid, threads, smem, ctx->st>>>(s, ctx->stage, ctx->fold_d, (const T*)ctx->csD, (const T*)ctx->csD2,
+	                                     (const T*)ctx->csO, (const T*)ctx->csV, ctx->csN, ctx->nw, (T*)ctx->lnpsi,
+	                                     (T*)ctx->O, (T*)ctx->eloc, (T*)ctx->other7, (T*)ctx->dE);
+	ctx->launches++;
+	mark(ctx, adj ? "k_cs_eval_adjoint" : "k_cs_eval");
+	CK(cudaGetLastError());
+	return TDVMC_OK;
+}
+
+// One RK stage on stored samples (CalculateNextParametersRK4ReuseSamples,
+// TDVMC.cpp:2037-2103, with the sample update of TDVMC.cpp:3654-3677 at the
+// first stage of a step).
+template <typename T>
+int run_cs_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int kind, int64_t count) {
+	int rc;
+	const bool adj = o->use_adjoint != 0;
+	if (kind == kCsFull || kind == kCsRefresh) {
+		const bool all = kind == kCsFull;
+		const int64_t cnt = all ? ctx->nw : count;
+		const int32_t* ws = all ? nullptr : &ctx->dyn->cs_start;
+		if ((rc = launch_prep<T>(ctx))) return rc;
+		if (!all) CK(cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->nw * sizeof(int), ctx->st));
+		if (o->moves_per_stage > 0 && (rc = launch_sample<T>(ctx, o->moves_per_stage, o->mc_step, o->seed, cnt, ws)))
+			return rc;
+		if ((rc = launch_cs_store<T>(ctx, cnt, ws))) return rc;
+		if (!all) {
+			k_cs_advance<<<1, 32, 0, ctx->st>>>(ctx->dyn, cnt, ctx->nw);
+			ctx->launches++;
+			mark(ctx, "k_cs_advance");
+			CK(cudaGetLastError());
+		}
+	}
+	if ((rc = launch_cs_eval<T>(ctx, adj))) return rc;
+	if ((rc = launch_reduce<T>(ctx, adj))) return rc;
+	return launch_solve<T>(ctx, o->imaginary_time, o->precondition, o->lin_solver, 1, o->normalize_wf, o->dt,
+	                       (o->use_adjoint == 2 && o->imaginary_time) ? 1 : 0);
+}
+
 template <typename T>
 int run_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
 	int rc;
@@ -298,32 +408,41 @@ int run_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
 	                       o->normalize_wf, o->dt, (o->use_adjoint == 2 && o->imaginary_time) ? 1 : 0);
 }
 
-int run_stage_any(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
+int run_stage_any(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int kind = 0, int64_t count = 0) {
+	if (kind)
+		return ctx->prec == TDVMC_PREC_FP64 ? run_cs_stage<double>(ctx, o, kind, count)
+		                                    : run_cs_stage<float>(ctx, o, kind, count);
 	return ctx->prec == TDVMC_PREC_FP64 ? run_stage<double>(ctx, o) : run_stage<float>(ctx, o);
 }
 
 int check_opts(const tdvmc_step_opts* o) {
 	if (!o || !(o->dt == o->dt)) return TDVMC_ERR_ARG;
-	if (o->ode_solver != 0 && o->ode_solver != 2) return TDVMC_ERR_ARG;
+	if (o->ode_solver != 0 && o->ode_solver != 2 && o->ode_solver != 3) return TDVMC_ERR_ARG;
+	if (o->ode_solver == 3 && (o->update_every < 0 || !(o->update_percent >= 0.0 && o->update_percent <= 100.0)))
+		return TDVMC_ERR_ARG;
 	if (o->lin_solver != 0 && o->lin_solver != 1) return TDVMC_ERR_ARG;
 	if (o->moves_per_stage < 0) return TDVMC_ERR_ARG;
 	if (o->use_adjoint < 0 || o->use_adjoint > 2) return TDVMC_ERR_ARG;
 	return TDVMC_OK;
 }
 
-int get_graph(tdvmc_ctx* ctx, const tdvmc_step_opts* o, cudaGraphExec_t* out) {
+// Graph of one stage; `kernels` = kernels one replay launches.
+int get_graph(tdvmc_ctx* ctx, const tdvmc_step_opts* o, cudaGraphExec_t* out, int* kernels, int kind = 0,
+              int64_t count = 0) {
 	GraphKey k{o->dt, o->mc_step, o->imaginary_time, o->ode_solver, o->lin_solver, o->precondition,
-	           o->normalize_wf, o->moves_per_stage, o->use_adjoint, o->seed};
+	           o->normalize_wf, o->moves_per_stage, o->use_adjoint, o->seed, kind, count};
 	auto it = ctx->graphs.find(k);
 	if (it != ctx->graphs.end()) {
 		*out = it->second;
+		*kernels = ctx->graph_kernels[k];
 		return TDVMC_OK;
 	}
 	cudaGraph_t g;
 	CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
 	const int64_t l0 = ctx->launches;
-	int rc = run_stage_any(ctx, o);
+	int rc = run_stage_any(ctx, o, kind, count);
 	cudaError_t e = cudaStreamEndCapture(ctx->st, &g);
+	const int nk = (int)(ctx->launches - l0);
 	ctx->launches = l0;  // counted when the graph runs
 	if (rc) return rc;
 	if (e != cudaSuccess) {
@@ -334,14 +453,72 @@ int get_graph(tdvmc_ctx* ctx, const tdvmc_step_opts* o, cudaGraphExec_t* out) {
 	CK(cudaGraphInstantiate(&ex, g, 0));
 	cudaGraphDestroy(g);
 	ctx->graphs[k] = ex;
+	ctx->graph_kernels[k] = nk;
 	*out = ex;
+	*kernels = nk;
 	return TDVMC_OK;
 }
 
-int kernels_per_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
-	int k = 1 + (o->moves_per_stage > 0 ? 1 : 0) + 1 + 4 + 1;
-	if (ctx->gram_tc) k += 2;
-	return k;
+// Stage kind of the first stage of the next stored-sample step and the size of
+// its refresh window.  UPDATE_SAMPLES_EVERY_NTH_STEP = 0 samples every walker
+// each step (TDVMC.cpp:3654); otherwise every update_every-th step refreshes
+// floor(nw * UPDATE_SAMPLES_PERCENT / 100) consecutive walkers
+// (UpdateSamplesConsecutive, TDVMC.cpp:975-983, 3406-3408, 3665-3675).
+void cs_plan(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int* kind, int64_t* count) {
+	int64_t c = (int64_t)std::floor((double)ctx->nw * o->update_percent / 100.0);
+	c = std::max<int64_t>(0, std::min<int64_t>(c, ctx->nw));
+	*count = 0;
+	if (!ctx->cs_valid || o->update_every <= 0) *kind = kCsFull;
+	else if (ctx->cs_steps % o->update_every == 0 && c > 0) {
+		*kind = c >= ctx->nw ? kCsFull : kCsRefresh;
+		if (*kind == kCsRefresh) *count = c;
+	} else
+		*kind = kCsReuse;
+}
+
+// Enqueues nsteps steps (graph replays) on the context's stream.
+int enqueue_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps) {
+	int rc;
+	if (o->ode_solver != 3) {
+		cudaGraphExec_t g;
+		int nk = 0;
+		if ((rc = get_graph(ctx, o, &g, &nk))) return rc;
+		const int nst = o->ode_solver == 0 ? 1 : 4;
+		for (int s = 0; s < nsteps; s++)
+			for (int k = 0; k < nst; k++) {
+				CK(cudaGraphLaunch(g, ctx->st));
+				ctx->launches += nk;
+			}
+		if (nsteps > 0 && o->moves_per_stage > 0) ctx->cs_valid = false;
+		return TDVMC_OK;
+	}
+	if ((rc = cs_alloc(ctx))) return rc;
+	cudaGraphExec_t gr;
+	int nkr = 0;
+	if ((rc = get_graph(ctx, o, &gr, &nkr, kCsReuse))) return rc;
+	for (int s = 0; s < nsteps; s++) {
+		int kind;
+		int64_t cnt;
+		cs_plan(ctx, o, &kind, &cnt);
+		cudaGraphExec_t g0 = gr;
+		int nk0 = nkr;
+		if (kind != kCsReuse && (rc = get_graph(ctx, o, &g0, &nk0, kind, cnt))) return rc;
+		CK(cudaGraphLaunch(g0, ctx->st));
+		ctx->launches += nk0;
+		for (int k = 1; k < 4; k++) {
+			CK(cudaGraphLaunch(gr, ctx->st));
+			ctx->launches += nkr;
+		}
+		if (kind == kCsFull) {
+			ctx->cs_valid = true;
+			ctx->cs_steps = 1;
+			ctx->cs_last_count = ctx->nw;
+		} else {
+			ctx->cs_steps++;
+			if (kind == kCsRefresh) ctx->cs_last_count = cnt;
+		}
+	}
+	return TDVMC_OK;
 }
 
 template <typename T>
@@ -508,6 +685,14 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		s.ncell = 0;
 		s.cell_inv = 0.0;
 	}
+	// sampler table: the nbin cubics, then the outer-pair constant for every
+	// interval index a minimum-image distance can reach (up to sqrt(D) L/2), so
+	// the uniform lookup needs no clamp
+	s.ncoef = s.nbin + 1;
+	if (s.uniform) {
+		const double xmax = std::sqrt((double)s.dim) * 0.5 * s.L * s.hinv * (1.0 + 1e-6);
+		s.ncoef = std::max(s.ncoef, (int)std::floor(xmax) + 2);
+	}
 
 	cudaGetDevice(&c.device);
 	cudaDeviceGetAttribute(&c.nsm, cudaDevAttrMultiProcessorCount, c.device);
@@ -549,12 +734,13 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	A((void**)&c.rhs, np * sizeof(double));
 	A((void**)&c.loc_d, c.loc.size() * sizeof(double));
 	A((void**)&c.fold_d, c.fold.size() * sizeof(double));
-	A(&c.coefU, (size_t)(s.nbin + 1) * 4 * ts);
-	A(&c.coefC, (size_t)s.nbin * 8 * ts);
+	A(&c.coefU, (size_t)s.ncoef * 4 * ts);
+	A(&c.coefC, (size_t)s.nbin * 12 * ts);
 	A(&c.uout, 32);
 	A(&c.kb, (size_t)s.nbin * ts);
 	A(&c.hv, (size_t)s.nbin * ts);
 	A(&c.locT, c.loc.size() * ts);
+	A(&c.cs_piece, (size_t)s.nbin * kCsPiece * ts);
 	A((void**)&c.lut, (size_t)std::max(1, s.ncell) * sizeof(int));
 	A((void**)&c.part1, (size_t)c.nblk1 * K1 * sizeof(double));
 	A((void**)&c.means1, K1 * sizeof(double));
@@ -583,6 +769,25 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		if (c.prec == TDVMC_PREC_FP64) ((double*)locT.data())[i] = c.loc[i];
 		else ((float*)locT.data())[i] = (float)c.loc[i];
 	}
+	// stored-sample piece table: dB/dr, B and d2B/dr2 of the four pieces per interval
+	std::vector<double> piece((size_t)s.nbin * kCsPiece, 0.0);
+	for (int j = 0; j < s.nbin; j++)
+		for (int q = 0; q < 4; q++) {
+			const double* l = &c.loc[((size_t)j * 4 + q) * 4];
+			const double h = hv[j];
+			double* pc = &piece[(size_t)j * kCsPiece];
+			pc[3 * q + 0] = h * l[1];
+			pc[3 * q + 1] = 2.0 * h * l[2];
+			pc[3 * q + 2] = 3.0 * h * l[3];
+			for (int cc = 0; cc < 4; cc++) pc[12 + 4 * q + cc] = l[cc];
+			pc[28 + 2 * q + 0] = 2.0 * h * h * l[2];
+			pc[28 + 2 * q + 1] = 6.0 * h * h * l[3];
+		}
+	std::vector<char> pieceT(piece.size() * ts);
+	for (size_t i = 0; i < piece.size(); i++) {
+		if (c.prec == TDVMC_PREC_FP64) ((double*)pieceT.data())[i] = piece[i];
+		else ((float*)pieceT.data())[i] = (float)piece[i];
+	}
 	DynState dy{};
 	c.time = 0.0;
 	apply_quench(ctx, dy.pa, dy.pb);
@@ -590,6 +795,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	bool cp = cudaMemcpy(c.kb, kbT.data(), kbT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.hv, hvT.data(), hvT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.locT, locT.data(), locT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.cs_piece, pieceT.data(), pieceT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.loc_d, c.loc.data(), c.loc.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.fold_d, c.fold.data(), c.fold.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.dyn, &dy, sizeof(dy), cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -614,6 +820,8 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	c.tiles.eg = c.tiles.sg;
 	c.tiles.egpb = std::max(1, 32 / c.tiles.eg);
 	if (const char* h = std::getenv("TDVMC_HIST")) c.tiles.hist = std::max(0, std::min(2, std::atoi(h)));
+	// TDVMC_SAMPLER=scalar selects the scalar FP32 sampler
+	if (const char* sm = std::getenv("TDVMC_SAMPLER")) c.packed_sampler = std::strcmp(sm, "scalar") != 0;
 	*out = ctx;
 	return TDVMC_OK;
 }
@@ -625,7 +833,7 @@ int tdvmc_destroy(tdvmc_ctx* ctx) {
 	void* bufs[] = {ctx->pos, ctx->lnpsi, ctx->O, ctx->eloc, ctx->other7, ctx->dE, ctx->acc, ctx->base, ctx->stage,
 	                ctx->kdot, ctx->rhs, ctx->loc_d, ctx->fold_d, ctx->coefU, ctx->coefC, ctx->uout, ctx->kb, ctx->hv,
 	                ctx->locT, ctx->lut, ctx->part1, ctx->means1, ctx->means0, ctx->part2, ctx->C2, ctx->partS, ctx->Sg,
-	                ctx->dyn, ctx->gramws};
+	                ctx->dyn, ctx->gramws, ctx->csD, ctx->csD2, ctx->csO, ctx->csV, ctx->csN, ctx->cs_piece};
 	for (void* b : bufs)
 		if (b) cudaFree(b);
 	if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -691,6 +899,7 @@ int tdvmc_set_walkers(tdvmc_ctx* ctx, const double* x, int64_t nw) {
 		CK(cudaStreamSynchronize(ctx->st));
 	}
 	ctx->have_walkers = true;
+	ctx->cs_valid = false;
 	return TDVMC_OK;
 }
 
@@ -708,6 +917,7 @@ int tdvmc_sample(tdvmc_ctx* ctx, int32_t moves, double mc_step, uint64_t seed, u
 	rc = ctx->prec == TDVMC_PREC_FP64 ? launch_sample<double>(ctx, moves, mc_step, seed)
 	                                  : launch_sample<float>(ctx, moves, mc_step, seed);
 	if (rc) return rc;
+	if (moves > 0) ctx->cs_valid = false;
 	ctx->last_moves = moves;
 	std::vector<int> a((size_t)ctx->nw);
 	CK(cudaMemcpyAsync(a.data(), ctx->acc, a.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
@@ -740,6 +950,38 @@ int tdvmc_eval_local(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, dou
 	if ((rc = copy_out_any(ctx, ctx->O, O, nw * ctx->sc.p))) return rc;
 	if ((rc = copy_out_any(ctx, ctx->eloc, eloc, nw * 2))) return rc;
 	if ((rc = copy_out_any(ctx, ctx->other7, other7, nw * 7))) return rc;
+	CK(cudaStreamSynchronize(ctx->st));
+	return TDVMC_OK;
+}
+
+int tdvmc_store_samples(tdvmc_ctx* ctx) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	int rc = cs_alloc(ctx);
+	if (rc) return rc;
+	rc = ctx->prec == TDVMC_PREC_FP64 ? launch_cs_store<double>(ctx, ctx->nw, nullptr)
+	                                  : launch_cs_store<float>(ctx, ctx->nw, nullptr);
+	if (rc) return rc;
+	CK(cudaStreamSynchronize(ctx->st));
+	ctx->cs_valid = true;
+	ctx->cs_steps = 0;
+	return TDVMC_OK;
+}
+
+int tdvmc_eval_stored(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, double* other7, double* dE) {
+	if (!ctx) return TDVMC_ERR_ARG;
+	if (!ctx->cs_valid) return TDVMC_ERR_STATE;
+	const bool adj = dE != nullptr;
+	int rc = ctx->prec == TDVMC_PREC_FP64 ? launch_cs_eval<double>(ctx, adj) : launch_cs_eval<float>(ctx, adj);
+	if (rc) return rc;
+	ctx->have_eval = true;
+	ctx->last_adj = adj;
+	const size_t nw = (size_t)ctx->nw;
+	if ((rc = copy_out_any(ctx, ctx->lnpsi, lnpsi, nw))) return rc;
+	if ((rc = copy_out_any(ctx, ctx->O, O, nw * ctx->sc.p))) return rc;
+	if ((rc = copy_out_any(ctx, ctx->eloc, eloc, nw * 2))) return rc;
+	if ((rc = copy_out_any(ctx, ctx->other7, other7, nw * 7))) return rc;
+	if (adj && (rc = copy_out_any(ctx, ctx->dE, dE, nw * 2 * ctx->sc.p))) return rc;
 	CK(cudaStreamSynchronize(ctx->st));
 	return TDVMC_OK;
 }
@@ -811,15 +1053,7 @@ int tdvmc_run_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, td
 	int rc = check_opts(o);
 	if (rc) return rc;
 	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
-	cudaGraphExec_t g;
-	if ((rc = get_graph(ctx, o, &g))) return rc;
-	const int nst = o->ode_solver == 0 ? 1 : 4;
-	const int kps = kernels_per_stage(ctx, o);
-	for (int s = 0; s < nsteps; s++)
-		for (int k = 0; k < nst; k++) {
-			CK(cudaGraphLaunch(g, ctx->st));
-			ctx->launches += kps;
-		}
+	if ((rc = enqueue_steps(ctx, o, nsteps))) return rc;
 	ctx->have_eval = true;
 	ctx->last_adj = o->use_adjoint != 0;
 	ctx->last_moves = o->moves_per_stage;
@@ -831,6 +1065,9 @@ int tdvmc_run_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, td
 		CK(cudaMemcpyAsync(m.data(), ctx->means0, m.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
 		CK(cudaStreamSynchronize(ctx->st));
 		fill_stats(ctx, m, o->moves_per_stage, stats);
+		// stored samples: the rate of the walkers the last refresh moved
+		if (o->ode_solver == 3 && ctx->cs_last_count > 0)
+			stats->accept_rate *= (double)ctx->nw / (double)ctx->cs_last_count;
 	}
 	if ((rc = read_status(ctx, &st))) return rc;
 	if (stats) stats->status = status_code(st);
@@ -853,20 +1090,27 @@ int tdvmc_time_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, f
 	int rc = check_opts(o);
 	if (rc) return rc;
 	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
-	cudaGraphExec_t g;
-	if ((rc = get_graph(ctx, o, &g))) return rc;
+	if (o->ode_solver == 3) {
+		// build the graphs (and the store) outside the timed region
+		if ((rc = cs_alloc(ctx))) return rc;
+		cudaGraphExec_t g;
+		int nk;
+		int kind;
+		int64_t cnt;
+		cs_plan(ctx, o, &kind, &cnt);
+		if ((rc = get_graph(ctx, o, &g, &nk, kCsReuse))) return rc;
+		if (kind != kCsReuse && (rc = get_graph(ctx, o, &g, &nk, kind, cnt))) return rc;
+	} else {
+		cudaGraphExec_t g;
+		int nk;
+		if ((rc = get_graph(ctx, o, &g, &nk))) return rc;
+	}
 	cudaEvent_t e0, e1;
 	CK(cudaEventCreate(&e0));
 	CK(cudaEventCreate(&e1));
-	const int nst = o->ode_solver == 0 ? 1 : 4;
-	const int kps = kernels_per_stage(ctx, o);
 	CK(cudaStreamSynchronize(ctx->st));
 	CK(cudaEventRecord(e0, ctx->st));
-	for (int s = 0; s < nsteps; s++)
-		for (int k = 0; k < nst; k++) {
-			CK(cudaGraphLaunch(g, ctx->st));
-			ctx->launches += kps;
-		}
+	if ((rc = enqueue_steps(ctx, o, nsteps))) return rc;
 	CK(cudaEventRecord(e1, ctx->st));
 	CK(cudaEventSynchronize(e1));
 	CK(cudaEventElapsedTime(ms, e0, e1));
@@ -891,7 +1135,23 @@ int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, float* ms, con
 	CK(cudaEventRecord(e0, ctx->st));
 	ctx->prof = &ev;
 	ctx->prof_names = &nm;
-	rc = run_stage_any(ctx, o);
+	if (o->ode_solver == 3) {
+		// one first stage of the next stored-sample step (the store is not advanced)
+		int kind;
+		int64_t cnt;
+		rc = cs_alloc(ctx);
+		if (!rc) {
+			cs_plan(ctx, o, &kind, &cnt);
+			rc = run_stage_any(ctx, o, kind, cnt);
+			if (!rc && kind == kCsFull) {
+				ctx->cs_valid = true;
+				ctx->cs_steps = 0;
+			}
+		}
+	} else {
+		rc = run_stage_any(ctx, o);
+		if (o->moves_per_stage > 0) ctx->cs_valid = false;
+	}
 	ctx->prof = nullptr;
 	ctx->prof_names = nullptr;
 	cudaError_t se = cudaStreamSynchronize(ctx->st);

@@ -128,6 +128,25 @@ class BosonsBulk:
         N.check(self.lib.tdvmc_eval_local_adjoint(self.h, _ptr(dE)), "tdvmc_eval_local_adjoint")
         return dE
 
+    def FillCorrelatedSamplingData(self):
+        """Store every walker's parameter-independent data (correlated sampling)."""
+        N.check(self.lib.tdvmc_store_samples(self.h), "tdvmc_store_samples")
+
+    def CalculateExpectationValuesForStoredSamples(self, adjoint=False):
+        """Local quantities of the stored samples at the current parameters (no
+        resampling); with adjoint=True also dE (n_walkers, p, 2)."""
+        lnpsi = np.zeros(self.nw)
+        O = np.zeros((self.nw, self.p))
+        eloc = np.zeros((self.nw, 2))
+        other = np.zeros((self.nw, 7))
+        dE = np.zeros((self.nw, self.p, 2)) if adjoint else None
+        N.check(self.lib.tdvmc_eval_stored(self.h, _ptr(lnpsi), _ptr(O), _ptr(eloc), _ptr(other),
+                                           _ptr(dE) if adjoint else None), "tdvmc_eval_stored")
+        out = dict(lnpsi=lnpsi, O=O, eloc=eloc, other=other)
+        if adjoint:
+            out["dE"] = dE
+        return out
+
     def ReduceStatistics(self):
         st = N.Stats()
         P = self.p
@@ -167,10 +186,12 @@ class BosonsBulk:
 
 
 class TDVP:
-    """One TDVP time step per call (ODE_SOLVER_TYPE 2 = RK4, 0 = Euler)."""
+    """One TDVP time step per call (ODE_SOLVER_TYPE 2 = RK4, 0 = Euler, 3 = RK4 on
+    stored samples with update_every / update_percent as UPDATE_SAMPLES_EVERY_NTH_STEP /
+    UPDATE_SAMPLES_PERCENT)."""
 
     def __init__(self, system: BosonsBulk, dt, moves_per_stage, mc_step, seed=1, imaginary_time=0, ode_solver=2,
-                 lin_solver=0, precondition=0, normalize_wf=0, use_adjoint=0):
+                 lin_solver=0, precondition=0, normalize_wf=0, use_adjoint=0, update_every=0, update_percent=100.0):
         self.sys = system
         o = N.StepOpts()
         o.dt = float(dt)
@@ -183,6 +204,8 @@ class TDVP:
         o.mc_step = float(mc_step)
         o.seed = int(seed)
         o.use_adjoint = int(use_adjoint)
+        o.update_every = int(update_every)
+        o.update_percent = float(update_percent)
         self.opts = o
 
     def time_steps(self, nsteps):

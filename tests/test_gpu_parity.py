@@ -293,3 +293,34 @@ def test_adjoint_driven_imaginary_time_step_matches_oracle_fp64():
     # and it differs from the plain covariance force
     dR0 = orc.solve_centred(m["O"], m["ER"], m["EI"], m["S"], m["cOER"], m["cOEI"], imag=1)[0]
     assert relmax(dR0, dR) > 1e-9
+
+
+def test_packed_sampler_follows_scalar_chain_mixed():
+    """The f32x2 FP32 sampler (uniform knots) walks the scalar FP32 sampler's
+    chain bit for bit: same Philox stream and update arithmetic, and every pair
+    term and partial sum rounded the same way.  Tolerance: identical walkers
+    and acceptance counts."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "eval_d3_n343_p30.npz"))
+    nw, n = 512, int(z["n"])
+    rng = np.random.default_rng(11)
+    R0 = np.concatenate([soa(z["cfgs"])] * (nw // 4)) + rng.normal(0, 0.02, size=(nw, 3, n))
+    uR = np.asarray(z["uR"])
+    out = {}
+    for mode in ("packed", "scalar"):
+        if mode == "scalar":
+            os.environ["TDVMC_SAMPLER"] = "scalar"
+        try:
+            s = T.BosonsBulk(3, n, int(z["p"]), float(z["L"]), nw, system_params=z["sysp"], precision="mixed")
+        finally:
+            os.environ.pop("TDVMC_SAMPLER", None)
+        s.SetParameters(uR, z["uI"])
+        s.SetWalkers(R0)
+        acc = s.DoMetropolisSteps(2 * n, 0.2, seed=99, pass_id=3)
+        out[mode] = (acc, s.GetWalkers())
+        s.close()
+    (a_p, R_p), (a_s, R_s) = out["packed"], out["scalar"]
+    same = np.all(R_p.reshape(nw, -1) == R_s.reshape(nw, -1), axis=1)
+    assert same.mean() == 1.0, same.mean()
+    assert a_p == a_s
+    assert 0.05 < a_p / (2 * n * nw) < 0.95
