@@ -273,6 +273,15 @@ def run_ours(args):
     ms64 = td64.time_steps(1)
     fp64_steps_s = (1000.0 / ms64) * nsub / NW
 
+    # RK4 on stored samples (ODE_SOLVER_TYPE 3, correlated-sampling reuse): the
+    # first stage of every step resamples a rotating quarter of the walkers, the
+    # other three stages re-evaluate the stored samples
+    td3 = T.TDVP(sysm, DT, MOVES, MC_STEP, seed=1, use_adjoint=1, ode_solver=3, update_every=1,
+                 update_percent=25.0)
+    td3.time_steps(2)  # stores every walker, then one refresh step
+    ms3 = td3.time_steps(args.steps)
+    prof3 = {k: v for k, v in td3.profile_stage()}
+
     # FP32 pipe ceiling and roofline of the dominant kernel
     import ctypes as C
     pk = C.c_double()
@@ -318,6 +327,8 @@ def run_ours(args):
         "fp64_gpu": {"value": fp64_steps_s, "unit": "steps/s", "walkers_timed": nsub, "scaled_to": NW,
                      "speedup_mixed_over_fp64": value / world / fp64_steps_s},
         "gate": {"dE_per_N": dE_per_N, "pass": bool(dE_per_N < 1e-5), "walkers": nsub},
+        "stored_sample_rk4": {"value": args.steps / (ms3 / 1000.0), "unit": "steps/s", "update_every": 1,
+                              "update_percent": 25.0, "kernels_ms_refresh_stage": prof3},
         "cpu_baseline": {"value": cpu_v, "unit": "steps/s", "cores": threads, "kind": "port",
                          "sample": "one RK stage (686 moves + E_loc + adjoint) of %d walkers on %d threads "
                                    "(%.1f s), extrapolated x4 stages x65536 walkers" % (cpu_w, threads, cpu_t)},

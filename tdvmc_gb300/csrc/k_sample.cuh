@@ -245,16 +245,15 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 // to the old position of the moved particle are one f32x2 instruction stream
 // (differences, r^2, r, the interval index by the float-rounding trick, the
 // local coordinate); the per-axis minimum image min(|d|, L - |d|) stays
-// scalar so its min runs on the ALU pipe beside the FMA pipe.  The table
-// holds the outer-pair constant for every index up to sqrt(D) L/2, so the
-// index needs no clamp (the clamped scalar lookup reads the same constant).
-// The moved particle's own slot (old distance 0, kept finite by a 1e-30
-// floor on r^2, which is below the rounding of any other r^2) and slots past
-// n are left out of the sum by predication.  Table indices
-// stay in range because every coordinate used lies in [-L/2, L/2]: a walker
-// with a coordinate outside after wrapping (non-finite or too large to wrap
-// exactly) makes no moves, as in the scalar sampler where every quotient of
-// such a walker is rejected, and a proposal outside is rejected.
+// scalar so its min runs on the ALU pipe beside the FMA pipe.  The interval
+// index is clamped to the outer-pair entry nbin with one integer min on the
+// float's bit pattern, so every pair beyond r_max reads the same (broadcast)
+// table entry.  The moved particle's own slot (old distance 0, kept finite by
+// a 1e-30 floor on r^2, which is below the rounding of any other r^2) and
+// slots past n are left out of the sum by predication.  A walker with a
+// coordinate outside [-L/2, L/2] after wrapping (non-finite or too large to
+// wrap exactly) makes no moves, as in the scalar sampler where every quotient
+// of such a walker is rejected, and a proposal outside is rejected.
 template <int G, int SLOTS>
 __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
                                                    const float* __restrict__ uout_g, const float* __restrict__ kb_g,
@@ -289,6 +288,7 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 	const f2_t R2 = f2_make(kRoundF, kRoundF);
 	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mhalf2 = f2_make(-0.5f, -0.5f);
 	const f2_t tiny2 = f2_make(1e-30f, 1e-30f);
+	const uint32_t ymax = __float_as_uint(kRoundF) + (uint32_t)sc.nbin;  // bit pattern of kRoundF + nbin
 	const uint32_t pass = *pass_ptr;
 	const bool last_ok = (SLOTS - 1) * G + lane < n;
 	const float half = 0.5f * L * (1.f + 1e-5f);
@@ -363,8 +363,8 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 					float ya, yb, ta, tb;
 					f2_split(yv, ya, yb);
 					f2_split(tau, ta, tb);
-					const Q4<float> ca = lds_q4(coef_a + (__float_as_uint(ya) << 4));
-					const Q4<float> cb = lds_q4(coef_a + (__float_as_uint(yb) << 4));
+					const Q4<float> ca = lds_q4(coef_a + (min(__float_as_uint(ya), ymax) << 4));
+					const Q4<float> cb = lds_q4(coef_a + (min(__float_as_uint(yb), ymax) << 4));
 					const float un = fmaf(ta, fmaf(ta, fmaf(ta, ca.w, ca.z), ca.y), ca.x);
 					const float uo = fmaf(tb, fmaf(tb, fmaf(tb, cb.w, cb.z), cb.y), cb.x);
 					const bool ok = (s == SLOTS - 1) ? (last_ok && s != self_slot) : (s != self_slot);

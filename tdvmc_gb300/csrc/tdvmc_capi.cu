@@ -685,14 +685,8 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		s.ncell = 0;
 		s.cell_inv = 0.0;
 	}
-	// sampler table: the nbin cubics, then the outer-pair constant for every
-	// interval index a minimum-image distance can reach (up to sqrt(D) L/2), so
-	// the uniform lookup needs no clamp
+	// sampler table: the nbin cubics, then the outer-pair constant
 	s.ncoef = s.nbin + 1;
-	if (s.uniform) {
-		const double xmax = std::sqrt((double)s.dim) * 0.5 * s.L * s.hinv * (1.0 + 1e-6);
-		s.ncoef = std::max(s.ncoef, (int)std::floor(xmax) + 2);
-	}
 
 	cudaGetDevice(&c.device);
 	cudaDeviceGetAttribute(&c.nsm, cudaDevAttrMultiProcessorCount, c.device);

@@ -1,0 +1,138 @@
+"""GPU: correlated-sampling reuse (stored samples, ODE_SOLVER_TYPE 3).
+
+Tolerances (stated per test):
+  stored vs direct evaluation at the same walkers and parameters: FP64
+      relative 1e-11, mixed 2e-5 on ln psi, O_k, E_loc, the kinetic sums and
+      dE/d alpha (scaled by the largest magnitude of each quantity);
+  RK4 on stored samples vs the FP64 oracle (sampling at the first stage,
+      evaluation of the fixed samples at the three others, a rotating
+      refresh window on later steps): parameters relative 1e-9, walkers 1e-9.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+
+pytestmark = pytest.mark.gpu
+
+
+def relmax(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def soa(cfgs):
+    return np.ascontiguousarray(np.transpose(np.asarray(cfgs), (0, 2, 1)))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 2e-5)])
+@pytest.mark.parametrize("golden,pot", [("eval_d3_n343_p30", "square"), ("eval_d2_n64_k20", "lj"),
+                                        ("eval_d1_n20_p10", "gauss")])
+def test_stored_eval_matches_direct_eval(precision, tol, golden, pot):
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, golden + ".npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    kn = z["knots"] if z["knots"].size else None
+    sysp = {"square": z["sysp"], "lj": (1.0, 1.0), "gauss": (0.5, 2.0)}[pot]
+    cfgs = soa(z["cfgs"])
+    nw = 4 * len(cfgs)
+    rng = np.random.default_rng(3)
+    R = np.concatenate([cfgs] * 4) + rng.normal(0, 0.01, size=(nw, dim, n))
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=sysp, potential=pot, user_knots=kn, hbar2_2m=0.09,
+                     precision=precision)
+    s.SetTime(float(z["time"]))
+    uR, uI = np.asarray(z["uR"]), np.asarray(z["uI"])
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R)
+    s.FillCorrelatedSamplingData()
+    for k, (a, b) in enumerate([(uR, uI), (1.1 * uR + 0.01, 0.5 * uI - 0.02)]):
+        s.SetParameters(a, b)
+        got = s.CalculateExpectationValuesForStoredSamples(adjoint=True)
+        ref = s.CalculateExpectationValues()
+        ref["dE"] = s.CalculateLocalEnergyAdjoint()
+        for key in ("lnpsi", "O", "eloc", "other", "dE"):
+            assert relmax(got[key], ref[key]) < tol, (k, key, relmax(got[key], ref[key]))
+
+
+def test_stored_sample_rk4_matches_oracle_fp64():
+    """Three RK4 steps on stored samples: the first samples every walker, the
+    next two refresh windows [0, nw/4) and [nw/4, nw/2) (UpdateSamplesConsecutive)."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "sample_d3_n27.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    nw, moves, step, dt, seed, pass0 = 64, 2 * n, 0.35, 1e-3, 21, 5
+    q = nw // 4
+    rng = np.random.default_rng(19)
+    R0 = np.repeat(z["R0"].T[None], nw, axis=0) + rng.normal(0, 0.05, size=(nw, dim, n))
+    R0 = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(R0)
+    uR, uI = np.asarray(z["uR"]), np.asarray(z["uI"])
+    sysp = tuple(z["sysp"])  # the square well the fixture was sampled with
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=sysp, potential="square", hbar2_2m=0.09, precision="fp64")
+    s.SetParameters(uR, uI, 0.0, 0.0)
+    s.SetWalkers(R0)
+    s.DoMetropolisSteps(0, step, seed, pass0)  # sets the Philox pass counter
+    td = T.TDVP(s, dt, moves, step, seed=seed, ode_solver=3, update_every=1, update_percent=25.0)
+
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_SQUARE, pot=sysp, hbar2_2m=0.09)
+    base = np.concatenate([uR, uI, [0.0, 0.0]])
+    Ro = R0.copy()
+    windows = [(0, nw), (0, q), (q, 2 * q)]
+    for st, (w0, w1) in enumerate(windows):
+        before = s.GetWalkers()
+        td.step()
+        after = s.GetWalkers()
+        moved = np.any(np.abs(after - before).reshape(nw, -1) > 0, axis=1)
+        assert not moved[:w0].any() and not moved[w1:].any()
+        pass_id = pass0 + 4 * st
+        o.sample(base[:p], Ro, moves, step, seed, pass_id, w0=w0, nw=w1 - w0) if st else \
+            o.sample(base[:p], Ro, moves, step, seed, pass_id)
+        cur = base.copy()
+        ks = []
+        for k in range(4):
+            out = o.stage(cur[:p], cur[p:2 * p], Ro, 0, step, seed, 0, threads=4, adjoint=False)
+            m = orc.centred(out["O"], out["eloc"])
+            dR, dI, pR, pI, _ = orc.solve_centred(m["O"], m["ER"], m["EI"], m["S"], m["cOER"], m["cOEI"])
+            kv = np.concatenate([dR, dI, [pR, pI]])
+            ks.append(kv)
+            if k < 3:
+                cur = base + kv * (dt / 2 if k < 2 else dt)
+        base = orc.rk4_combine(base, ks, dt)
+        assert np.all(np.isfinite(base))
+        assert np.abs(after - Ro).max() < 1e-9, st
+        gR, gI, gpR, gpI = s.GetParameters()
+        assert relmax(np.concatenate([gR, gI, [gpR, gpI]]), base) < 1e-9, st
+
+
+def test_store_state_rules():
+    import tdvmc_gb300 as T
+    from tdvmc_gb300 import _native as N
+    z = np.load(os.path.join(GOLD, "eval_d3_n64_p10.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    nw = 8
+    s = T.BosonsBulk(dim, n, p, L, nw, precision="fp64")
+    s.SetParameters(z["uR"], z["uI"])
+    R = np.concatenate([soa(z["cfgs"])] * 2)[:nw]
+    s.SetWalkers(R)
+    with pytest.raises(N.TdvmcError) as e:
+        s.CalculateExpectationValuesForStoredSamples()
+    assert e.value.code == N.ERR_STATE
+    s.FillCorrelatedSamplingData()
+    s.CalculateExpectationValuesForStoredSamples()
+    s.DoMetropolisSteps(4, 0.2, seed=1, pass_id=0)  # moving the walkers invalidates the store
+    with pytest.raises(N.TdvmcError) as e:
+        s.CalculateExpectationValuesForStoredSamples()
+    assert e.value.code == N.ERR_STATE
+    s.FillCorrelatedSamplingData()
+    s.SetWalkers(R)
+    with pytest.raises(N.TdvmcError) as e:
+        s.CalculateExpectationValuesForStoredSamples()
+    assert e.value.code == N.ERR_STATE
+    with pytest.raises(N.TdvmcError) as e:
+        T.TDVP(s, 0.01, 4, 0.2, ode_solver=3, update_every=1, update_percent=150.0).step()
+    assert e.value.code == N.ERR_ARG
