@@ -164,6 +164,21 @@ int tdvmc_store_samples(tdvmc_ctx* ctx);
  * valid store. */
 int tdvmc_eval_stored(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, double* other7, double* dE);
 
+/* Pair distribution and static structure factor of the current walkers,
+ * averaged over walkers (BosonsBulk::CalculateAdditionalSystemProperties,
+ * BosonsBulk.cpp:474-520; each walker is one sample of the running mean of
+ * CalculateAdditionalSystemProperties, TDVMC.cpp:1332-1388).
+ * g(r): the grid [0, r_max) with spacing r_max / gr_bins (GR_BIN_COUNT,
+ * BosonsBulk.cpp:145); gr[] receives *gr_count (<= gr_bins) values: pairs
+ * i < j with r < r_max, each adding D/(N-1) / (volume of its shell).
+ * S(k): kvec[nvec*dim] are the k vectors already scaled by 2 pi / L (the
+ * integer vectors of kVectors{D}D.json), shell s owns rows
+ * shell_off[s] .. shell_off[s+1]-1 (shell_off[0] = 0, nvec <= 4096);
+ * sk[s] = |sum over the shell's vectors and the particles of exp(i k.r)|^2 /
+ * (N * vectors in the shell).  nshell = 0 skips S(k). */
+int tdvmc_observables(tdvmc_ctx* ctx, int32_t gr_bins, int32_t nshell, const int32_t* shell_off, const double* kvec,
+                      double* gr, int32_t* gr_count, double* sk);
+
 /* Walker-mean reduction of the last evaluation (ParallelUpdateExpectationValues,
  * TDVMC.cpp:1152-1220).  Optional outputs: O_mean[p], S[p*p] (centred),
  * cov_OER[p], cov_OEI[p], dE_mean[2p] (zeros unless the last evaluation was

@@ -78,6 +78,8 @@ def lib():
         L.orc_solve.restype = C.c_int
         L.orc_solve_centred.argtypes = L.orc_solve.argtypes
         L.orc_solve_centred.restype = C.c_int
+        L.orc_observables.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, C.c_void_p, _dp, _dp, _dp]
+        L.orc_observables.restype = C.c_int
         _lib = L
     return _lib
 
@@ -152,6 +154,16 @@ class OracleSystem:
         if adjoint:
             res["dE"] = dE.reshape(self.p, 2)
         return res
+
+    def observables(self, R, gr_bins, shell_off, kvec):
+        """g(r) and S(k) of one configuration R (n, dim).  Returns (gr, sk)."""
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(-1)
+        off = np.ascontiguousarray(shell_off, dtype=np.int32)
+        kv = np.ascontiguousarray(kvec, dtype=np.float64).reshape(-1)
+        gr = np.zeros(int(gr_bins) + 1)
+        sk = np.zeros(max(len(off) - 1, 1))
+        cnt = lib().orc_observables(self.h, R, int(gr_bins), len(off) - 1, off.ctypes.data, kv, gr, sk)
+        return gr[:cnt], sk[:len(off) - 1]
 
     def move_delta(self, uR, R, p, newpos):
         return lib().orc_move_delta(self.h, np.ascontiguousarray(uR, dtype=np.float64),

@@ -18,11 +18,15 @@
 //                                -> uDotR[p] uDotI[p] phiDotR phiDotI rejected
 //   SAMPLE seed step nwarm nsamp ntherm nblock [cfg] -> per block averages
 //   NIC dim L ncase [ri rj]...   -> |d| and d (generic VectorDisplacementNIC)
+//   GRBINS nbins                 -> GR_BIN_COUNT of the next SYSTEM (default 50)
+//   ADDITIONAL ncfg [cfg]...     -> g(r) values, S(k) values and the k grid
+//                                   (BosonsBulk::CalculateAdditionalSystemProperties)
 #include "Constants.h"
 #include "SplineFactory.h"
 #include "Utils.h"
 #include "PhysicalSystems/BosonsBulk.h"
 #include "Potentials/LJ.h"
+#include "Observables/ObservableVsOnGrid.h"
 
 #include <cstdio>
 #include <iostream>
@@ -57,6 +61,7 @@ void DoMetropolisStep(vector<vector<double> >& R, vector<double>& uR, vector<dou
 void UpdateExpectationValues(vector<vector<double> >& R, vector<double>& uR, vector<double>& uI, double phiR, double phiI, bool intermediateStep);
 void SolveForParametersDot(vector<double>& uDotR, vector<double>& uDotI, double* phiDotR, double* phiDotI);
 
+static int g_grbins = 50;
 static vector<double> g_nodes;
 static double g_rmax = 0.0;
 static vector<double> g_uR, g_uI;
@@ -94,7 +99,7 @@ static void cmd_system()
 	WRITE_EVERY_NTH_STEP_TO_FILE = 1;
 	MC_NSTEP_MULTIPLICATION_FACTOR_FOR_WRITE_DATA = 1;
 	UPDATE_SAMPLES_EVERY_NTH_STEP = 0;
-	GR_BIN_COUNT = 50;
+	GR_BIN_COUNT = g_grbins;
 	isRootRank = true;
 
 	if (sys) delete sys;
@@ -293,6 +298,31 @@ static void cmd_nic()
 	}
 }
 
+static void cmd_additional()
+{
+	int ncfg;
+	cin >> ncfg;
+	for (int c = 0; c < ncfg; c++)
+	{
+		auto R = read_cfg();
+		sys->CalculateAdditionalSystemProperties(R, g_uR, g_uI, g_phiR, g_phiI);
+		auto oc = sys->GetAdditionalObservablesClone();
+		printf("ADD ");
+		for (int o = 0; o < 2; o++)
+		{
+			auto* g = dynamic_cast<Observables::ObservableVsOnGrid*>(oc.observables[o]);
+			const vector<double>& v = g->observablesV[0].values;
+			printf("%d ", (int)v.size());
+			for (double x : v) out(x);
+		}
+		auto* k = dynamic_cast<Observables::ObservableVsOnGrid*>(oc.observables[1]);
+		printf("%d ", (int)k->grid.grid.size());
+		for (double x : k->grid.grid) out(x);
+		endl_();
+		oc.Destroy();
+	}
+}
+
 int main(int argc, char** argv)
 {
 	configDirectory = argc > 1 ? string(argv[1]) : string("./");
@@ -308,6 +338,8 @@ int main(int argc, char** argv)
 		else if (cmd == "SOLVE") cmd_solve();
 		else if (cmd == "SAMPLE") cmd_sample();
 		else if (cmd == "NIC") cmd_nic();
+		else if (cmd == "GRBINS") cin >> g_grbins;
+		else if (cmd == "ADDITIONAL") cmd_additional();
 		else
 		{
 			fprintf(stderr, "unknown command %s\n", cmd.c_str());

@@ -897,3 +897,61 @@ static int solve_core(int P, int imag, int precond, int solver, const double* O,
 	free(sc);
 	return bad;
 }
+
+/* ------------------------------------------------------------------ */
+/* g(r) and S(k): BosonsBulk.cpp:474-520                               */
+/* ------------------------------------------------------------------ */
+int orc_observables(const orc_sys* s, const double* R, int gr_bins, int nshell, const int* shell_off,
+                    const double* kvec, double* gr, double* sk)
+{
+	const int D = s->dim, N = s->n;
+	/* grid [0, r_max) with spacing r_max / GR_BIN_COUNT (BosonsBulk.cpp:145,
+	 * Grid::Init: count = (max - min) / spacing, truncated) */
+	const double spacing = s->rmax / gr_bins;
+	const int count = (int)((s->rmax - 0.0) / spacing);
+	double* scale = (double*)malloc((size_t)(count > 0 ? count : 1) * sizeof(double));
+	/* InitScaling: shell volumes (ObservableVsOnGridWithScaling.cpp:19-44) */
+	for (int i = 0; i < count; i++)
+	{
+		if (D == 1) scale[i] = spacing;
+		else if (D == 3) scale[i] = 4.0 * M_PI * pow(spacing * (i + 1), 3.0) / 3.0;
+		else scale[i] = M_PI * pow(spacing * (i + 1), 2.0);
+	}
+	if (D > 1)
+		for (int i = count - 1; i > 0; i--) scale[i] = scale[i] - scale[i - 1];
+	for (int i = 0; i < count; i++) gr[i] = 0.0;
+	const double weight = 1.0 / ((double)(N - 1)) * D;
+	double d[3];
+	for (int i = 0; i < N; i++)
+		for (int j = 0; j < i; j++)
+		{
+			const double r = orc_nic_disp(R + i * D, R + j * D, D, s->L, d);
+			if (r < s->rmax)
+			{
+				const int bin = (int)floor(r / spacing); /* Grid::GetIndex */
+				if (bin < count) gr[bin] += weight / scale[bin];
+			}
+		}
+	free(scale);
+	/* structure factor: per shell the squared modulus of the sum over the
+	 * shell's vectors and the particles, over N * (vectors in the shell) */
+	double* sc = (double*)calloc((size_t)(nshell > 0 ? nshell : 1), sizeof(double));
+	double* ss = (double*)calloc((size_t)(nshell > 0 ? nshell : 1), sizeof(double));
+	for (int i = 0; i < N; i++)
+		for (int k = 0; k < nshell; k++)
+			for (int v = shell_off[k]; v < shell_off[k + 1]; v++)
+			{
+				double dot = 0.0;
+				for (int a = 0; a < D; a++) dot += kvec[v * D + a] * R[i * D + a];
+				sc[k] += cos(dot);
+				ss[k] += sin(dot);
+			}
+	for (int k = 0; k < nshell; k++)
+	{
+		const int nv = shell_off[k + 1] - shell_off[k];
+		sk[k] = nv > 0 ? (sc[k] * sc[k] + ss[k] * ss[k]) / ((double)(N * nv)) : 0.0;
+	}
+	free(sc);
+	free(ss);
+	return count;
+}

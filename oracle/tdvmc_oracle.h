@@ -100,6 +100,16 @@ int orc_solve_centred(int p, int imag, int precond, int solver, const double* O,
                       const double* S, const double* covOER, const double* covOEI,
                       double* uDotR, double* uDotI, double* phiDotR, double* phiDotI);
 
+/* Pair distribution and static structure factor of one configuration R
+ * (n x dim, AoS), BosonsBulk::CalculateAdditionalSystemProperties
+ * (BosonsBulk.cpp:474-520) with the grid of BosonsBulk.cpp:142-152 and
+ * Observables/Grid.cpp:15-70, ObservableVsOnGridWithScaling.cpp:19-52.
+ * gr_bins = GR_BIN_COUNT; returns the number of g(r) bins written to gr.
+ * kvec[nvec*dim] are the scaled k vectors, shell s = kvec rows
+ * shell_off[s] .. shell_off[s+1]-1; sk[nshell]. */
+int orc_observables(const orc_sys* s, const double* R, int gr_bins, int nshell, const int* shell_off,
+                    const double* kvec, double* gr, double* sk);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@ POT_NONE, POT_SQUARE, POT_GAUSS, POT_LJ = 0, 1, 2, 3
 EXPORTS = ("tdvmc_status_string", "tdvmc_create", "tdvmc_destroy", "tdvmc_get_stream", "tdvmc_set_time",
            "tdvmc_set_params", "tdvmc_get_params", "tdvmc_set_walkers", "tdvmc_get_walkers", "tdvmc_sample",
            "tdvmc_eval_local", "tdvmc_eval_local_adjoint", "tdvmc_store_samples", "tdvmc_eval_stored",
+           "tdvmc_observables",
            "tdvmc_reduce_stats", "tdvmc_tdvp_rhs", "tdvmc_step",
            "tdvmc_get_step_operators", "tdvmc_run_steps", "tdvmc_time_steps", "tdvmc_profile_stage", "tdvmc_autotune", "tdvmc_get_tiles", "tdvmc_launch_count",
            "tdvmc_measure_fp32_peak", "tdvmc_reduce_walkers_noalloc")
@@ -79,6 +80,7 @@ def load(build_if_missing: bool = True):
     L.tdvmc_eval_local_adjoint.argtypes = [C.c_void_p, d]
     L.tdvmc_store_samples.argtypes = [C.c_void_p]
     L.tdvmc_eval_stored.argtypes = [C.c_void_p, d, d, d, d, d]
+    L.tdvmc_observables.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, d, d, P(C.c_int32), d]
     L.tdvmc_reduce_stats.argtypes = [C.c_void_p, P(Stats), d, d, d, d, d]
     L.tdvmc_tdvp_rhs.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, d, d, P(C.c_double), P(C.c_double)]
     L.tdvmc_step.argtypes = [C.c_void_p, P(StepOpts), P(Stats)]

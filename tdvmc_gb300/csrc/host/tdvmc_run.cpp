@@ -10,6 +10,12 @@
 // (TDVMC.cpp:3939-3953) with 15 significant digits in 24-character columns
 // (Utils.h:25-28).
 //
+// With CALCULATE_ADDITIONAL_DATA_EVERY_NTH_STEP > 0 it appends g(r) and S(k)
+// to gr.dat and sk.dat and the time to timesAdditional.dat
+// (TDVMC.cpp:3471-3520), after MC_NADDITIONALTHERMSTEPS moves per walker;
+// the k shells are the first 50 of kVectors{D}D.json next to the config file
+// (BosonsBulk.cpp:55, 124-139).
+//
 // Extra keys (all optional): GPU_WALKERS (default MC_NSTEPS), GPU_PRECISION
 // ("mixed" or "fp64"), POTENTIAL ("square" as BosonsBulk, "gauss", "lj"),
 // HBAR2_2M (default 1.0, the reference's constant), GPU_ADJOINT (0/1),
@@ -193,6 +199,32 @@ void write_table(const std::string& name, const std::string& header, const std::
 	}
 }
 
+// k shells: rows of the "data" array of kVectors{D}D.json, scaled by 2 pi / L
+bool read_k_shells(const std::string& path, int dim, double L, int nshell, std::vector<int32_t>& off,
+                   std::vector<double>& kvec) {
+	std::ifstream in(path);
+	if (!in) return false;
+	std::stringstream ss;
+	ss << in.rdbuf();
+	std::string text = ss.str();
+	Json j;
+	Parser ps(text);
+	if (!ps.value(j) || j.kind != Json::OBJ) return false;
+	auto it = j.obj.find("data");
+	if (it == j.obj.end() || it->second.kind != Json::ARR) return false;
+	off.assign(1, 0);
+	kvec.clear();
+	const double f = 2.0 * M_PI / L;
+	for (size_t k = 0; k < it->second.arr.size() && (int)k < nshell; k++) {
+		for (auto& v : it->second.arr[k].arr) {
+			if (v.kind != Json::ARR || (int)v.arr.size() < dim) return false;
+			for (int a = 0; a < dim; a++) kvec.push_back(v.arr[a].num * f);
+		}
+		off.push_back((int32_t)(kvec.size() / dim));
+	}
+	return true;
+}
+
 bool file_exists(const std::string& p) {
 	struct stat st;
 	return stat(p.c_str(), &st) == 0;
@@ -241,6 +273,11 @@ int main(int argc, char** argv) {
 	const std::string prec = cfg.str("GPU_PRECISION", "mixed");
 	const std::string pot = cfg.str("POTENTIAL", "square");
 	const uint64_t seed = (uint64_t)cfg.num("GPU_SEED", 1);
+	const int ADD_NTH = (int)cfg.num("CALCULATE_ADDITIONAL_DATA_EVERY_NTH_STEP", 0);
+	const int ADD_THERM = (int)cfg.num("MC_NADDITIONALTHERMSTEPS", 0);
+	const int GR_BINS = (int)cfg.num("GR_BIN_COUNT", 50);
+	std::string cfg_dir = argv[1];
+	cfg_dir = cfg_dir.find_last_of("\\/") == std::string::npos ? "./" : cfg_dir.substr(0, cfg_dir.find_last_of("\\/")) + "/";
 
 	tdvmc_system_desc d{};
 	d.dim = DIM;
@@ -319,9 +356,34 @@ int main(int argc, char** argv) {
 	std::vector<std::vector<double>> allER, allEI, allO, allOther, allPR, allPI;
 	std::vector<double> times;
 	std::vector<double> O(P);
+	std::vector<int32_t> k_off;
+	std::vector<double> k_vec;
+	if (ADD_NTH > 0) {
+		const std::string kp = cfg_dir + "kVectors" + std::to_string(DIM) + "D.json";
+		if (!read_k_shells(kp, DIM, LBOX, 50, k_off, k_vec)) {
+			std::fprintf(stderr, "cannot read the k vectors %s; S(k) is skipped\n", kp.c_str());
+			k_off.assign(1, 0);
+		}
+	}
 	int step = 0;
 	for (double t = 0.0; t <= TOTALTIME; t += TIMESTEP, step++) {
 		if ((rc = tdvmc_set_time(ctx, t))) return die("tdvmc_set_time", rc);
+		if (ADD_NTH > 0 && step % ADD_NTH == 0) {
+			// additional system properties of the current parameters (TDVMC.cpp:3471-3520)
+			if (ADD_THERM > 0 && (rc = tdvmc_sample(ctx, ADD_THERM, MC_STEP, seed, 0xFFFF0000u + (uint32_t)step, &acc)))
+				return die("tdvmc_sample", rc);
+			const int nshell = (int)k_off.size() - 1;
+			std::vector<double> gr(GR_BINS), sk(std::max(nshell, 1));
+			int32_t ngr = 0;
+			if ((rc = tdvmc_observables(ctx, GR_BINS, nshell, k_off.data(), k_vec.empty() ? nullptr : k_vec.data(),
+			                            gr.data(), &ngr, sk.data())))
+				return die("tdvmc_observables", rc);
+			gr.resize(ngr);
+			sk.resize(nshell);
+			append_line("timesAdditional", {t});
+			append_line("gr", gr);
+			if (nshell > 0) append_line("sk", sk);
+		}
 		std::vector<double> pR(P), pI(P);
 		double p0R, p0I;
 		tdvmc_get_params(ctx, pR.data(), pI.data(), &p0R, &p0I);

