@@ -7,6 +7,7 @@
 //
 // Stored per walker, at spline level (s = 0..ns-1, before the boundary fold):
 //   D[s][a][n] = sum_{i != n, r <= r_max} B_s'(r_ni) (x_n - x_i)_a / r_ni
+//                (rows padded to npad = n rounded up to 4; the padding is zero)
 //   D2[s]      = sum_n sum_{i != n, r <= r_max} (B_s''(r_ni) + (D-1)/r_ni B_s'(r_ni))
 //   O[k]       = BC-folded sum_{i < n, r <= r_max} B_s(r_ni)
 //   V          = pair potential over i < n, r <= r_max;  n_out = #pairs beyond r_max
@@ -25,6 +26,8 @@ namespace tdvmc {
 //   [12..27] l0, l1, l2, l3            (B in the local coordinate t)
 //   [28..35] 2h^2 l2, 6h^2 l3          (d2B/dr2 = c0 + t c1)
 constexpr int kCsPiece = 36;
+
+__host__ __device__ inline int cs_npad(int n) { return (n + 3) & ~3; }
 
 // Shared memory of k_cs_store.
 //   CTA:   piece[nbin*36] | kb[nbin] | hv[nbin] | lut[ncell]
@@ -144,7 +147,8 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 		__syncwarp(gmask);
 		KSum<T> vs;
 		int nout = 0;
-		T* Dw = D_o + (size_t)w * ns * 3 * n;
+		const int npad = cs_npad(n);
+		T* Dw = D_o + (size_t)w * ns * 3 * npad;
 		for (int s = 0; s < nslot; s++) {
 			const int nrow = s * G + lane;
 			const bool rowok = nrow < n;
@@ -168,7 +172,7 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 			for (int i = dend; i < n; i++)
 				cs_pair<T, G, false>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			if (rowok)
-				for (int e = 0; e < ns * 3; e++) Dw[(size_t)e * n + nrow] = drow[(size_t)e * G + lane];
+				for (int e = 0; e < ns * 3; e++) Dw[(size_t)e * npad + nrow] = drow[(size_t)e * G + lane];
 		}
 		__syncwarp(gmask);
 		// lane-ordered sums of the lane-private accumulators
@@ -202,8 +206,37 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 
 // Local quantities of every stored walker at the current stage parameters:
 // same outputs as k_eloc (ln psi, O, E_loc, kinetic sums, dE/d alpha).
-// One warp per walker; D is streamed once for G_n and, with ADJ, once more
-// for sum_n G_n . D[s][.][n].
+// One warp per walker; each lane takes V consecutive particles per 16-byte
+// load.  D is streamed once for G_n and, with ADJ, once more for
+// sum_n G_n . D[s][.][n] (G staged component-major in shared memory).
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+	using type = float4;
+	static constexpr int V = 4;
+	__device__ static void get(const type& v, float* o) {
+		o[0] = v.x;
+		o[1] = v.y;
+		o[2] = v.z;
+		o[3] = v.w;
+	}
+};
+template <> struct Vec16<double> {
+	using type = double2;
+	static constexpr int V = 2;
+	__device__ static void get(const type& v, double* o) {
+		o[0] = v.x;
+		o[1] = v.y;
+	}
+};
+
+// Shared memory of k_cs_eval: wR, wI [ns each, padded to 4] | per warp: G[6][npad] | A[2*ns, padded to 4]
+// (every region starts on a 16-byte boundary for the vector loads)
+__host__ __device__ inline int cs_ns2(int ns) { return (2 * ns + 3) & ~3; }
+template <typename T>
+__host__ __device__ inline size_t cs_eval_smem_bytes(int n, int ns, int warps) {
+	return ((size_t)cs_ns2(ns) + (size_t)warps * ((size_t)6 * cs_npad(n) + cs_ns2(ns))) * sizeof(T);
+}
+
 template <typename T, bool ADJ>
 __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __restrict__ params,
                                                  const double* __restrict__ fold_g, const T* __restrict__ D,
@@ -211,11 +244,14 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
                                                  const T* __restrict__ Vs, const int32_t* __restrict__ nouts,
                                                  int64_t nw, T* __restrict__ lnpsi_o, T* __restrict__ O_o,
                                                  T* __restrict__ eloc_o, T* __restrict__ other_o, T* __restrict__ dE_o) {
+	using VT = typename Vec16<T>::type;
+	constexpr int V = Vec16<T>::V;
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int n = sc.n, ns = sc.ns, P = sc.p;
+	const int npad = cs_npad(n);
 	T* wR = reinterpret_cast<T*>(smem_raw);
 	T* wI = wR + ns;
-	T* gs_all = wI + ns;  // per warp: [n][6] gradients (adjoint), then [2*ns] spline sums
+	T* gs_all = wR + cs_ns2(ns);  // per warp: G[6][npad] (adjoint), then [2*ns] spline sums
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int wpb = blockDim.x >> 5;
 	for (int s = threadIdx.x; s < ns; s += blockDim.x) {
@@ -229,37 +265,45 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 		wI[s] = (T)im;
 	}
 	__syncthreads();
-	T* gs = gs_all + (size_t)warp * ((size_t)n * 6 + 2 * ns);
-	T* asum = gs + (size_t)n * 6;
+	T* gs = gs_all + (size_t)warp * ((size_t)6 * npad + cs_ns2(ns));
+	T* asum = gs + (size_t)6 * npad;
 	const double c = sc.hbar2_2m;
 
 	for (int64_t w = (int64_t)blockIdx.x * wpb + warp; w < nw; w += (int64_t)gridDim.x * wpb) {
-		const T* Dw = D + (size_t)w * ns * 3 * n;
+		const T* Dw = D + (size_t)w * ns * 3 * npad;
 		KSum<T> r1, i1, r1i1;
-		for (int i = lane; i < n; i += 32) {
-			T gr0 = 0, gr1 = 0, gr2 = 0, gi0 = 0, gi1 = 0, gi2 = 0;
+		for (int c0 = lane * V; c0 < n; c0 += 32 * V) {
+			T gr[3][V], gi[3][V];
+#pragma unroll
+			for (int a = 0; a < 3; a++)
+#pragma unroll
+				for (int v = 0; v < V; v++) gr[a][v] = gi[a][v] = T(0);
 			for (int s = 0; s < ns; s++) {
-				const T* d = Dw + (size_t)s * 3 * n + i;
-				const T d0 = d[0], d1 = d[n], d2 = d[2 * n];
-				const T a = wR[s], b = wI[s];
-				gr0 = fma(a, d0, gr0);
-				gr1 = fma(a, d1, gr1);
-				gr2 = fma(a, d2, gr2);
-				gi0 = fma(b, d0, gi0);
-				gi1 = fma(b, d1, gi1);
-				gi2 = fma(b, d2, gi2);
+				const T a_ = wR[s], b_ = wI[s];
+#pragma unroll
+				for (int a = 0; a < 3; a++) {
+					T d[V];
+					Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + ((size_t)s * 3 + a) * npad + c0), d);
+#pragma unroll
+					for (int v = 0; v < V; v++) {
+						gr[a][v] = fma(a_, d[v], gr[a][v]);
+						gi[a][v] = fma(b_, d[v], gi[a][v]);
+					}
+				}
 			}
-			r1.add(gr0 * gr0 + gr1 * gr1 + gr2 * gr2);
-			i1.add(gi0 * gi0 + gi1 * gi1 + gi2 * gi2);
-			r1i1.add(T(2) * (gr0 * gi0 + gr1 * gi1 + gr2 * gi2));
-			if (ADJ) {
-				T* g = gs + (size_t)i * 6;
-				g[0] = gr0;
-				g[1] = gr1;
-				g[2] = gr2;
-				g[3] = gi0;
-				g[4] = gi1;
-				g[5] = gi2;
+#pragma unroll
+			for (int v = 0; v < V; v++) {
+				if (c0 + v < n) {
+					r1.add(gr[0][v] * gr[0][v] + gr[1][v] * gr[1][v] + gr[2][v] * gr[2][v]);
+					i1.add(gi[0][v] * gi[0][v] + gi[1][v] * gi[1][v] + gi[2][v] * gi[2][v]);
+					r1i1.add(T(2) * (gr[0][v] * gi[0][v] + gr[1][v] * gi[1][v] + gr[2][v] * gi[2][v]));
+				}
+				if (ADJ)
+#pragma unroll
+					for (int a = 0; a < 3; a++) {
+						gs[(size_t)a * npad + c0 + v] = gr[a][v];
+						gs[(size_t)(3 + a) * npad + c0 + v] = gi[a][v];
+					}
 			}
 		}
 		T l2r = T(0), l2i = T(0);
@@ -300,15 +344,23 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 		}
 		if (ADJ) {
 			__syncwarp();
-			// A_s = sum_n G_n . D[s][.][n] (complex), then fold with D2
+			// A_s = sum_n G_n . D[s][.][n] (complex), then fold with D2; the
+			// padding of D is zero, so whole vectors can be summed
 			for (int s = 0; s < ns; s++) {
-				const T* d = Dw + (size_t)s * 3 * n;
 				T ar = T(0), ai = T(0);
-				for (int i = lane; i < n; i += 32) {
-					const T* g = gs + (size_t)i * 6;
-					const T d0 = d[i], d1 = d[n + i], d2 = d[2 * n + i];
-					ar = fma(g[0], d0, fma(g[1], d1, fma(g[2], d2, ar)));
-					ai = fma(g[3], d0, fma(g[4], d1, fma(g[5], d2, ai)));
+				for (int c0 = lane * V; c0 < n; c0 += 32 * V) {
+#pragma unroll
+					for (int a = 0; a < 3; a++) {
+						T d[V], g[V], h[V];
+						Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + ((size_t)s * 3 + a) * npad + c0), d);
+						Vec16<T>::get(*reinterpret_cast<const VT*>(gs + (size_t)a * npad + c0), g);
+						Vec16<T>::get(*reinterpret_cast<const VT*>(gs + (size_t)(3 + a) * npad + c0), h);
+#pragma unroll
+						for (int v = 0; v < V; v++) {
+							ar = fma(g[v], d[v], ar);
+							ai = fma(h[v], d[v], ai);
+						}
+					}
 				}
 				ar = group_sum<T, 32>(ar, 0xffffffffu);
 				ai = group_sum<T, 32>(ai, 0xffffffffu);

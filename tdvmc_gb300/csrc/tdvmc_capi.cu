@@ -318,7 +318,8 @@ int cs_alloc(tdvmc_ctx* ctx) {
 	if (ctx->csD) return TDVMC_OK;
 	const size_t ts = tsize(ctx->prec);
 	const size_t nw = (size_t)ctx->nw, ns = (size_t)ctx->sc.ns, n = (size_t)ctx->sc.n, P = (size_t)ctx->sc.p;
-	bool ok = cudaMalloc(&ctx->csD, nw * ns * 3 * n * ts) == cudaSuccess &&
+	const size_t dbytes = nw * ns * 3 * (size_t)cs_npad((int)n) * ts;
+	bool ok = cudaMalloc(&ctx->csD, dbytes) == cudaSuccess &&
 	          cudaMalloc(&ctx->csD2, nw * ns * ts) == cudaSuccess && cudaMalloc(&ctx->csO, nw * P * ts) == cudaSuccess &&
 	          cudaMalloc(&ctx->csV, nw * ts) == cudaSuccess &&
 	          cudaMalloc((void**)&ctx->csN, nw * sizeof(int32_t)) == cudaSuccess;
@@ -331,6 +332,8 @@ int cs_alloc(tdvmc_ctx* ctx) {
 		cudaGetLastError();  // out of memory is not sticky
 		return TDVMC_ERR_NOMEM;
 	}
+	// the row padding of D must read as zero; the store writes rows < n only
+	CK(cudaMemsetAsync(ctx->csD, 0, dbytes, ctx->st));
 	return TDVMC_OK;
 }
 
@@ -339,11 +342,15 @@ template <typename T>
 int launch_cs_store(tdvmc_ctx* ctx, int64_t count, const int32_t* wstart) {
 	constexpr int G = 32;
 	const SysConst& s = ctx->sc;
-	const size_t smem = cs_cta_bytes<T>(s.nbin, s.ncell) + cs_group_bytes<T>(s.n, s.ns, G);
+	// up to four walkers per block share the piece table
+	const size_t cta = cs_cta_bytes<T>(s.nbin, s.ncell), grp = cs_group_bytes<T>(s.n, s.ns, G);
+	int gpb = 4;
+	while (gpb > 1 && cta + gpb * grp > 200 * 1024) gpb--;
+	const size_t smem = cta + gpb * grp;
 	auto fn = k_cs_store<T, G>;
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	const int grid = grid_for(ctx, (const void*)fn, G, smem, count, 1);
-	fn<<<grid, G, smem, ctx->st>>>(s, ctx->dyn, (const T*)ctx->cs_piece, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut,
+	const int grid = grid_for(ctx, (const void*)fn, G * gpb, smem, count, gpb);
+	fn<<<grid, G * gpb, smem, ctx->st>>>(s, ctx->dyn, (const T*)ctx->cs_piece, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut,
 	                               ctx->fold_d, (const T*)ctx->pos, count, ctx->nw, wstart, (T*)ctx->csD,
 	                               (T*)ctx->csD2, (T*)ctx->csO, (T*)ctx->csV, ctx->csN);
 	ctx->launches++;
@@ -356,7 +363,7 @@ template <typename T>
 int launch_cs_eval(tdvmc_ctx* ctx, bool adj) {
 	const SysConst& s = ctx->sc;
 	const int threads = 128, wpb = threads / 32;
-	const size_t smem = ((size_t)2 * s.ns + (size_t)wpb * ((size_t)s.n * 6 + 2 * s.ns)) * sizeof(T);
+	const size_t smem = cs_eval_smem_bytes<T>(s.n, s.ns, wpb);
 	auto fn = adj ? k_cs_eval<T, true> : k_cs_eval<T, false>;
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, wpb);
