@@ -24,6 +24,8 @@
 #include "common.cuh"
 #include "k_sample.cuh"
 
+#include <type_traits>
+
 namespace tdvmc {
 
 constexpr int kFwdMoments = 4;  // sum t^c, c = 0..3
@@ -221,6 +223,119 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 	}
 }
 
+// FP32 forward sweep with partners i and i+1 in one f32x2 instruction stream
+// (same pairs, masks and statistics as fwd_region): differences, minimum
+// image, r^2, r, the interval coordinate, the gradient products and the
+// accumulators are packed; the table-dependent derivative polynomials stay
+// scalar.  The local coordinate of a pair outside the support (NaN for the
+// self pair) is zeroed before the masks multiply.
+template <int G, int ON, bool ADJ, int HIST>
+__device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1, int nrow, bool rowok,
+                                              const Q4<float>& xr, const Q4<float>* __restrict__ xs,
+                                              const Q4<float>* __restrict__ coefC, const float* __restrict__ kb,
+                                              const float* __restrict__ hv, const int* __restrict__ lut,
+                                              float* __restrict__ hist, int lane, float pa, float pb,
+                                              KSum<float>* acc, KSum<float>& vsum, int& nout) {
+	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
+	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
+	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mh2 = f2_make(-0.5f, -0.5f);
+	const float dm1 = (float)(sc.dim - 1);
+	const f2_t dm12 = f2_make(dm1, dm1);
+	const float ymax = kRoundF + (float)(sc.nbin - 1);
+	for (int c0 = i0; c0 < i1; c0 += 32) {
+		const int c1 = (c0 + 32 < i1) ? c0 + 32 : i1;
+		f2_t a2[8];
+#pragma unroll
+		for (int k = 0; k < 8; k++) a2[k] = f2_make(0.f, 0.f);
+		float vb = 0.f;
+		for (int i = c0; i < c1; i += 2) {
+			const bool have1 = i + 1 < c1;
+			const int ib = have1 ? i + 1 : i;
+			const Q4<float> pA = xs[i], pB = xs[ib];
+			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
+			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
+			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
+			// minimum image: d - L rint(d / L) (see nic)
+			dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
+			dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
+			dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
+			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+			float ra, rb;
+			f2_split(r2, ra, rb);
+			const float qa = rsqrtf(ra), qb = rsqrtf(rb);
+			const f2_t r = f2_mul(r2, f2_make(qa, qb));
+			float rA, rB;
+			f2_split(r, rA, rB);
+			const bool okA = rowok && i != nrow, okB = have1 && rowok && ib != nrow;
+			const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
+			float tA, tB;
+			int jA, jB;
+			if (sc.uniform) {
+				// floor(x) = round(x - 1/2), x = r / h, clamped to the last interval
+				const f2_t x = f2_mul(r, H2);
+				float ya, yb;
+				f2_split(f2_add(f2_add(x, mh2), R2), ya, yb);
+				ya = fminf(ya, ymax);
+				yb = fminf(yb, ymax);
+				float xa, xb;
+				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
+				tA = xa;
+				tB = xb;
+				jA = __float_as_int(ya) - __float_as_int(kRoundF);
+				jB = __float_as_int(yb) - __float_as_int(kRoundF);
+			} else {
+				jA = locate<float>(sc, rA, kb, hv, lut, tA);
+				jB = locate<float>(sc, rB, kb, hv, lut, tB);
+			}
+			tA = inA ? tA : 0.f;
+			tB = inB ? tB : 0.f;
+			const Q4<float> cRA = coefC[3 * jA], cIA = coefC[3 * jA + 1], c2A = coefC[3 * jA + 2];
+			const Q4<float> cRB = coefC[3 * jB], cIB = coefC[3 * jB + 1], c2B = coefC[3 * jB + 2];
+			const f2_t d1R = f2_make(fmaf(tA, fmaf(tA, cRA.z, cRA.y), cRA.x), fmaf(tB, fmaf(tB, cRB.z, cRB.y), cRB.x));
+			const f2_t d1I = f2_make(fmaf(tA, fmaf(tA, cIA.z, cIA.y), cIA.x), fmaf(tB, fmaf(tB, cIB.z, cIB.y), cIB.x));
+			const f2_t d2R = f2_make(fmaf(tA, c2A.x, cRA.w), fmaf(tB, c2B.x, cRB.w));
+			const f2_t d2I = f2_make(fmaf(tA, c2A.y, cIA.w), fmaf(tB, c2B.y, cIB.w));
+			const f2_t sr = f2_make(inA ? qa : 0.f, inB ? qb : 0.f);
+			const f2_t on = f2_make(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
+			const f2_t gR = f2_mul(d1R, sr), gI = f2_mul(d1I, sr);
+			const f2_t lR = f2_fma(dm12, gR, f2_mul(d2R, on)), lI = f2_fma(dm12, gI, f2_mul(d2I, on));
+			a2[0] = f2_fma(gR, dx, a2[0]);
+			a2[1] = f2_fma(gR, dy, a2[1]);
+			a2[2] = f2_fma(gR, dz, a2[2]);
+			a2[3] = f2_fma(gI, dx, a2[3]);
+			a2[4] = f2_fma(gI, dy, a2[4]);
+			a2[5] = f2_fma(gI, dz, a2[5]);
+			a2[6] = f2_add(a2[6], lR);
+			a2[7] = f2_add(a2[7], lI);
+			if (ON != 0) {
+				const bool cA = (ON == 1) ? true : (i < nrow);
+				const bool cB = have1 && ((ON == 1) ? true : (ib < nrow));
+				FwdPair<float> q;
+				q.t = tA;
+				q.j = jA;
+				q.r = rA;
+				q.rinv = qa;
+				fwd_stats<float, G, ADJ, HIST>(sc, q, inA && cA, hist, lane, pa, pb, vb);
+				q.t = tB;
+				q.j = jB;
+				q.r = rB;
+				q.rinv = qb;
+				fwd_stats<float, G, ADJ, HIST>(sc, q, inB && cB, hist, lane, pa, pb, vb);
+				nout += (okA && cA && !(rA <= rmax)) ? 1 : 0;
+				nout += (okB && cB && !(rB <= rmax)) ? 1 : 0;
+			}
+		}
+#pragma unroll
+		for (int k = 0; k < 8; k++) {
+			float lo, hi;
+			f2_split(a2[k], lo, hi);
+			acc[k].add(lo + hi);
+		}
+		if (ON != 0) vsum.add(vb);
+	}
+}
+
 // Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), kNp
 // partners per iteration.
 template <typename T, int G, bool DIAG, int HIST>
@@ -344,9 +459,15 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 			KSum<T> acc[8];
 			const int base = s * G;
 			const int dend = (base + G < n) ? base + G : n;
-			fwd_region<T, G, 1, ADJ, HIST>(sc, 0, base, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
-			fwd_region<T, G, 2, ADJ, HIST>(sc, base, dend, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
-			fwd_region<T, G, 0, ADJ, HIST>(sc, dend, n, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			if constexpr (std::is_same<T, float>::value) {
+				fwd_region_f2<G, 1, ADJ, HIST>(sc, 0, base, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+				fwd_region_f2<G, 2, ADJ, HIST>(sc, base, dend, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+				fwd_region_f2<G, 0, ADJ, HIST>(sc, dend, n, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			} else {
+				fwd_region<T, G, 1, ADJ, HIST>(sc, 0, base, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+				fwd_region<T, G, 2, ADJ, HIST>(sc, base, dend, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+				fwd_region<T, G, 0, ADJ, HIST>(sc, dend, n, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, lane, pa, pb, acc, e_v, nout);
+			}
 			const T gRx = acc[0].value(), gRy = acc[1].value(), gRz = acc[2].value();
 			const T gIx = acc[3].value(), gIy = acc[4].value(), gIz = acc[5].value();
 			if (rowok) {
