@@ -223,12 +223,14 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 	}
 }
 
-// FP32 forward sweep with partners i and i+1 in one f32x2 instruction stream
-// (same pairs, masks and statistics as fwd_region): differences, minimum
-// image, r^2, r, the interval coordinate, the gradient products and the
-// accumulators are packed; the table-dependent derivative polynomials stay
-// scalar.  The local coordinate of a pair outside the support (NaN for the
-// self pair) is zeroed before the masks multiply.
+// FP32 forward sweep with partner pairs in f32x2 arithmetic (same pairs,
+// masks and statistics as fwd_region): kF2 pairs of partners per iteration,
+// each pair one packed instruction stream (differences, minimum image, r^2,
+// r, the interval coordinate, the gradient products and the accumulators);
+// the pairs are independent chains for the scheduler.  The table-dependent
+// derivative polynomials stay scalar.  The local coordinate of a pair outside
+// the support (NaN for the self pair) is zeroed before the masks multiply.
+constexpr int kF2 = 2;
 template <int G, int ON, bool ADJ, int HIST>
 __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1, int nrow, bool rowok,
                                               const Q4<float>& xr, const Q4<float>* __restrict__ xs,
@@ -249,81 +251,87 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 #pragma unroll
 		for (int k = 0; k < 8; k++) a2[k] = f2_make(0.f, 0.f);
 		float vb = 0.f;
-		for (int i = c0; i < c1; i += 2) {
-			const bool have1 = i + 1 < c1;
-			const int ib = have1 ? i + 1 : i;
-			const Q4<float> pA = xs[i], pB = xs[ib];
-			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
-			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
-			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
-			// minimum image: d - L rint(d / L) (see nic)
-			dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
-			dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
-			dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
-			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-			float ra, rb;
-			f2_split(r2, ra, rb);
-			const float qa = rsqrtf(ra), qb = rsqrtf(rb);
-			const f2_t r = f2_mul(r2, f2_make(qa, qb));
-			float rA, rB;
-			f2_split(r, rA, rB);
-			const bool okA = rowok && i != nrow, okB = have1 && rowok && ib != nrow;
-			const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
-			float tA, tB;
-			int jA, jB;
-			if (sc.uniform) {
-				// floor(x) = round(x - 1/2), x = r / h, clamped to the last interval
-				const f2_t x = f2_mul(r, H2);
-				float ya, yb;
-				f2_split(f2_add(f2_add(x, mh2), R2), ya, yb);
-				ya = fminf(ya, ymax);
-				yb = fminf(yb, ymax);
-				float xa, xb;
-				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
-				tA = xa;
-				tB = xb;
-				jA = __float_as_int(ya) - __float_as_int(kRoundF);
-				jB = __float_as_int(yb) - __float_as_int(kRoundF);
-			} else {
-				jA = locate<float>(sc, rA, kb, hv, lut, tA);
-				jB = locate<float>(sc, rB, kb, hv, lut, tB);
-			}
-			tA = inA ? tA : 0.f;
-			tB = inB ? tB : 0.f;
-			const Q4<float> cRA = coefC[3 * jA], cIA = coefC[3 * jA + 1], c2A = coefC[3 * jA + 2];
-			const Q4<float> cRB = coefC[3 * jB], cIB = coefC[3 * jB + 1], c2B = coefC[3 * jB + 2];
-			const f2_t d1R = f2_make(fmaf(tA, fmaf(tA, cRA.z, cRA.y), cRA.x), fmaf(tB, fmaf(tB, cRB.z, cRB.y), cRB.x));
-			const f2_t d1I = f2_make(fmaf(tA, fmaf(tA, cIA.z, cIA.y), cIA.x), fmaf(tB, fmaf(tB, cIB.z, cIB.y), cIB.x));
-			const f2_t d2R = f2_make(fmaf(tA, c2A.x, cRA.w), fmaf(tB, c2B.x, cRB.w));
-			const f2_t d2I = f2_make(fmaf(tA, c2A.y, cIA.w), fmaf(tB, c2B.y, cIB.w));
-			const f2_t sr = f2_make(inA ? qa : 0.f, inB ? qb : 0.f);
-			const f2_t on = f2_make(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
-			const f2_t gR = f2_mul(d1R, sr), gI = f2_mul(d1I, sr);
-			const f2_t lR = f2_fma(dm12, gR, f2_mul(d2R, on)), lI = f2_fma(dm12, gI, f2_mul(d2I, on));
-			a2[0] = f2_fma(gR, dx, a2[0]);
-			a2[1] = f2_fma(gR, dy, a2[1]);
-			a2[2] = f2_fma(gR, dz, a2[2]);
-			a2[3] = f2_fma(gI, dx, a2[3]);
-			a2[4] = f2_fma(gI, dy, a2[4]);
-			a2[5] = f2_fma(gI, dz, a2[5]);
-			a2[6] = f2_add(a2[6], lR);
-			a2[7] = f2_add(a2[7], lI);
-			if (ON != 0) {
-				const bool cA = (ON == 1) ? true : (i < nrow);
-				const bool cB = have1 && ((ON == 1) ? true : (ib < nrow));
-				FwdPair<float> q;
-				q.t = tA;
-				q.j = jA;
-				q.r = rA;
-				q.rinv = qa;
-				fwd_stats<float, G, ADJ, HIST>(sc, q, inA && cA, hist, lane, pa, pb, vb);
-				q.t = tB;
-				q.j = jB;
-				q.r = rB;
-				q.rinv = qb;
-				fwd_stats<float, G, ADJ, HIST>(sc, q, inB && cB, hist, lane, pa, pb, vb);
-				nout += (okA && cA && !(rA <= rmax)) ? 1 : 0;
-				nout += (okB && cB && !(rB <= rmax)) ? 1 : 0;
+		for (int i = c0; i < c1; i += 2 * kF2) {
+#pragma unroll
+			for (int h = 0; h < kF2; h++) {
+				const int iA = i + 2 * h, iB = iA + 1;
+				const bool haveA = iA < c1, haveB = iB < c1;
+				const int ia = haveA ? iA : i, ib = haveB ? iB : i;
+				const Q4<float> pA = xs[ia], pB = xs[ib];
+				f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
+				f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
+				f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
+				// minimum image: d - L rint(d / L) (see nic)
+				dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
+				dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
+				dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
+				const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+				float ra, rb;
+				f2_split(r2, ra, rb);
+				const float qa = rsqrtf(ra), qb = rsqrtf(rb);
+				const f2_t r = f2_mul(r2, f2_make(qa, qb));
+				float rA, rB;
+				f2_split(r, rA, rB);
+				const bool okA = haveA && rowok && ia != nrow, okB = haveB && rowok && ib != nrow;
+				const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
+				float tA, tB;
+				int jA, jB;
+				if (sc.uniform) {
+					// floor(x) = round(x - 1/2), x = r / h, clamped to the last interval
+					const f2_t x = f2_mul(r, H2);
+					float ya, yb;
+					f2_split(f2_add(f2_add(x, mh2), R2), ya, yb);
+					ya = fminf(ya, ymax);
+					yb = fminf(yb, ymax);
+					float xa, xb;
+					f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
+					tA = xa;
+					tB = xb;
+					jA = __float_as_int(ya) - __float_as_int(kRoundF);
+					jB = __float_as_int(yb) - __float_as_int(kRoundF);
+				} else {
+					jA = locate<float>(sc, rA, kb, hv, lut, tA);
+					jB = locate<float>(sc, rB, kb, hv, lut, tB);
+				}
+				tA = inA ? tA : 0.f;
+				tB = inB ? tB : 0.f;
+				const Q4<float> cRA = coefC[3 * jA], cIA = coefC[3 * jA + 1], c2A = coefC[3 * jA + 2];
+				const Q4<float> cRB = coefC[3 * jB], cIB = coefC[3 * jB + 1], c2B = coefC[3 * jB + 2];
+				const f2_t d1R =
+				    f2_make(fmaf(tA, fmaf(tA, cRA.z, cRA.y), cRA.x), fmaf(tB, fmaf(tB, cRB.z, cRB.y), cRB.x));
+				const f2_t d1I =
+				    f2_make(fmaf(tA, fmaf(tA, cIA.z, cIA.y), cIA.x), fmaf(tB, fmaf(tB, cIB.z, cIB.y), cIB.x));
+				const f2_t d2R = f2_make(fmaf(tA, c2A.x, cRA.w), fmaf(tB, c2B.x, cRB.w));
+				const f2_t d2I = f2_make(fmaf(tA, c2A.y, cIA.w), fmaf(tB, c2B.y, cIB.w));
+				const f2_t sr = f2_make(inA ? qa : 0.f, inB ? qb : 0.f);
+				const f2_t on = f2_make(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
+				const f2_t gR = f2_mul(d1R, sr), gI = f2_mul(d1I, sr);
+				const f2_t lR = f2_fma(dm12, gR, f2_mul(d2R, on)), lI = f2_fma(dm12, gI, f2_mul(d2I, on));
+				a2[0] = f2_fma(gR, dx, a2[0]);
+				a2[1] = f2_fma(gR, dy, a2[1]);
+				a2[2] = f2_fma(gR, dz, a2[2]);
+				a2[3] = f2_fma(gI, dx, a2[3]);
+				a2[4] = f2_fma(gI, dy, a2[4]);
+				a2[5] = f2_fma(gI, dz, a2[5]);
+				a2[6] = f2_add(a2[6], lR);
+				a2[7] = f2_add(a2[7], lI);
+				if (ON != 0) {
+					const bool cA = haveA && ((ON == 1) ? true : (ia < nrow));
+					const bool cB = haveB && ((ON == 1) ? true : (ib < nrow));
+					FwdPair<float> q;
+					q.t = tA;
+					q.j = jA;
+					q.r = rA;
+					q.rinv = qa;
+					fwd_stats<float, G, ADJ, HIST>(sc, q, inA && cA, hist, lane, pa, pb, vb);
+					q.t = tB;
+					q.j = jB;
+					q.r = rB;
+					q.rinv = qb;
+					fwd_stats<float, G, ADJ, HIST>(sc, q, inB && cB, hist, lane, pa, pb, vb);
+					nout += (okA && cA && !(rA <= rmax)) ? 1 : 0;
+					nout += (okB && cB && !(rB <= rmax)) ? 1 : 0;
+				}
 			}
 		}
 #pragma unroll
@@ -379,6 +387,93 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 		}
 #pragma unroll
 		for (int h = 0; h < kNp; h++) hist_add8<HIST, HistSlots<HIST, true>::value, T, G>(hist, jj[h], lane, v[h], kRevMoments);
+	}
+}
+
+// FP32 reverse sweep with partner pairs in f32x2 arithmetic (same pairs and
+// moments as rev_region): kF2 packed pairs per iteration.
+template <int G, bool DIAG, int HIST>
+__device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1, int nrow, bool rowok,
+                                              const Q4<float>& xr, const float* gn, const Q4<float>* __restrict__ xs,
+                                              const Q4<float>* __restrict__ g4, const float* __restrict__ gz,
+                                              const float* __restrict__ kb, const float* __restrict__ hv,
+                                              const int* __restrict__ lut, float* __restrict__ hist, int lane) {
+	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
+	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
+	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mh2 = f2_make(-0.5f, -0.5f);
+	const float dm1 = (float)(sc.dim - 1);
+	const f2_t dm12 = f2_make(dm1, dm1);
+	const float ymax = kRoundF + (float)(sc.nbin - 1);
+	f2_t GN[6];
+#pragma unroll
+	for (int k = 0; k < 6; k++) GN[k] = f2_make(gn[k], gn[k]);
+	for (int i = i0; i < i1; i += 2 * kF2) {
+#pragma unroll
+		for (int h = 0; h < kF2; h++) {
+			const int iA = i + 2 * h, iB = iA + 1;
+			const bool haveA = iA < i1, haveB = iB < i1;
+			const int ia = haveA ? iA : i, ib = haveB ? iB : i;
+			const Q4<float> pA = xs[ia], pB = xs[ib];  // .w = gRx of the partner
+			const Q4<float> gA = g4[ia], gB = g4[ib];
+			const float zA = gz[ia], zB = gz[ib];
+			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
+			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
+			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
+			dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
+			dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
+			dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
+			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+			float ra, rb;
+			f2_split(r2, ra, rb);
+			const float qa = rsqrtf(ra), qb = rsqrtf(rb);
+			const f2_t r = f2_mul(r2, f2_make(qa, qb));
+			float rA, rB;
+			f2_split(r, rA, rB);
+			const bool onA = haveA && rowok && (rA <= rmax) && (DIAG ? (ia < nrow) : true);
+			const bool onB = haveB && rowok && (rB <= rmax) && (DIAG ? (ib < nrow) : true);
+			float tA, tB;
+			int jA, jB;
+			if (sc.uniform) {
+				const f2_t x = f2_mul(r, H2);
+				float ya, yb;
+				f2_split(f2_add(f2_add(x, mh2), R2), ya, yb);
+				ya = fminf(ya, ymax);
+				yb = fminf(yb, ymax);
+				float xa, xb;
+				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
+				tA = xa;
+				tB = xb;
+				jA = __float_as_int(ya) - __float_as_int(kRoundF);
+				jB = __float_as_int(yb) - __float_as_int(kRoundF);
+			} else {
+				jA = locate<float>(sc, rA, kb, hv, lut, tA);
+				jB = locate<float>(sc, rB, kb, hv, lut, tB);
+			}
+			const f2_t t = f2_make(onA ? tA : 0.f, onB ? tB : 0.f);  // t is NaN for the self pair
+			const f2_t sr = f2_make(onA ? qa : 0.f, onB ? qb : 0.f);
+			// (G_n - G_i) . rhat plus the (D-1)/r of the Laplacian of B (real part only)
+			const f2_t gR = f2_mul(
+			    f2_fma(f2_sub(GN[2], f2_make(gA.y, gB.y)), dz,
+			           f2_fma(f2_sub(GN[1], f2_make(gA.x, gB.x)), dy,
+			                  f2_fma(f2_sub(GN[0], f2_make(pA.w, pB.w)), dx, dm12))),
+			    sr);
+			const f2_t gI = f2_mul(
+			    f2_fma(f2_sub(GN[5], f2_make(zA, zB)), dz,
+			           f2_fma(f2_sub(GN[4], f2_make(gA.w, gB.w)), dy, f2_mul(f2_sub(GN[3], f2_make(gA.z, gB.z)), dx))),
+			    sr);
+			const f2_t t2 = f2_mul(t, t);
+			float v[2][8];
+			f2_split(gR, v[0][0], v[1][0]);
+			f2_split(f2_mul(gR, t), v[0][1], v[1][1]);
+			f2_split(f2_mul(gR, t2), v[0][2], v[1][2]);
+			f2_split(gI, v[0][3], v[1][3]);
+			f2_split(f2_mul(gI, t), v[0][4], v[1][4]);
+			f2_split(f2_mul(gI, t2), v[0][5], v[1][5]);
+			v[0][6] = v[0][7] = v[1][6] = v[1][7] = 0.f;
+			hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, jA, lane, v[0], kRevMoments);
+			hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, jB, lane, v[1], kRevMoments);
+		}
 	}
 }
 
@@ -513,8 +608,13 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				}
 				const int base = s * G;
 				const int dend = (base + G < n) ? base + G : n;
-				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				if constexpr (std::is_same<T, float>::value) {
+					rev_region_f2<G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+					rev_region_f2<G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				} else {
+					rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+					rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				}
 			}
 			hist_reduce<T, G, HIST, NMH>(hist, redr, nbin, kRevMoments, lane, gmask);
 		}
