@@ -245,8 +245,9 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
 	const float ymax = kRoundF + (float)(sc.nbin - 1);
-	for (int c0 = i0; c0 < i1; c0 += 32) {
-		const int c1 = (c0 + 32 < i1) ? c0 + 32 : i1;
+	constexpr int kChunk = 16 * kF2;  // partners per compensated block sum, whole iterations
+	for (int c0 = i0; c0 < i1; c0 += kChunk) {
+		const int c1 = (c0 + kChunk < i1) ? c0 + kChunk : i1;
 		f2_t a2[8];
 #pragma unroll
 		for (int k = 0; k < 8; k++) a2[k] = f2_make(0.f, 0.f);
