@@ -171,7 +171,7 @@ def run_reference(args):
     t_all = 0.0
     nws = 0
     for k in range(args.steps):
-        r, t, nws = cpu_port_rate(threads, 1, seed=100 + k)
+        r, t, nws = cpu_port_rate(threads, 8, seed=100 + k)
         rates.append(r)
         t_all += t
     v = float(np.mean(rates))
@@ -298,7 +298,9 @@ def run_ours(args):
 
     # CPU baseline: the reference algorithm (FP64 port) on the host cores, bounded sample
     threads = os.cpu_count() or 1
-    cpu_v, cpu_t, cpu_w = cpu_port_rate(threads, 4)
+    _, t_probe, _ = cpu_port_rate(threads, 4)
+    wpt = int(min(1024, max(4, np.ceil(4 * 12.0 / max(t_probe, 1e-3)))))  # about 12 s of CPU work
+    cpu_v, cpu_t, cpu_w = cpu_port_rate(threads, wpt)
 
     if world > 1 and torch is not None:
         import torch.distributed as dist

@@ -324,3 +324,45 @@ def test_packed_sampler_follows_scalar_chain_mixed():
     assert same.mean() == 1.0, same.mean()
     assert a_p == a_s
     assert 0.05 < a_p / (2 * n * nw) < 0.95
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-5)])
+def test_maximum_size_matches_oracle(precision, tol):
+    """N = 1024 (the largest N the C ABI accepts) with p = 64: evaluation and
+    adjoint against the oracle (FP64 1e-12, mixed 1e-5 relative), and for FP64
+    the sampler chain (positions 1e-9, identical acceptance)."""
+    import tdvmc_gb300 as T
+    dim, n, p = 3, 1024, 64
+    L = float((n / 0.365) ** (1.0 / 3.0))
+    nw = 3
+    rng = np.random.default_rng(1024)
+    m = int(np.ceil(n ** (1 / 3)))
+    idx = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    cfgs = np.array([idx * (L / m) + rng.uniform(-0.1, 0.1, size=(n, 3)) * (L / m) - L / 2 for _ in range(nw)])
+    cfgs = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(cfgs)  # inside the box, as the sampler keeps them
+    r = np.linspace(0.0, L / 2, p)
+    uR = -0.5 * (1.1 / np.maximum(r, 0.5)) ** 5
+    uR -= uR[-1]
+    uI = 0.01 * rng.normal(size=p)
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=0.09,
+                     precision=precision)
+    s.SetParameters(uR, uI)
+    s.SetWalkers(soa(cfgs))
+    f = s.CalculateExpectationValues()
+    dE = s.CalculateLocalEnergyAdjoint()
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0), hbar2_2m=0.09)
+    for w in range(nw):
+        ref = o.eval(uR, uI, cfgs[w], adjoint=True)
+        assert relmax(f["O"][w], ref["O"]) < tol
+        assert relmax(f["eloc"][w], ref["eloc"]) < tol
+        assert relmax(f["other"][w], ref["other"]) < tol
+        assert relmax(dE[w], ref["dE"]) < tol
+        assert abs(f["lnpsi"][w] - ref["lnpsi"]) <= tol * max(abs(ref["lnpsi"]), 1.0)
+    if precision == "fp64":
+        R0 = soa(cfgs)
+        s.SetWalkers(R0)
+        acc = s.DoMetropolisSteps(256, 0.1, seed=3, pass_id=2)
+        Ro = R0.copy()
+        acc_o = o.sample(uR, Ro, 256, 0.1, seed=3, pass_id=2)
+        assert acc == acc_o
+        assert np.abs(s.GetWalkers() - Ro).max() < 1e-9
