@@ -69,6 +69,34 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 	}
 }
 
+// Two partners' moments into lane-private histogram slots (scalar mode): both
+// intervals' slots are loaded before anything is stored, so the loads overlap;
+// when the intervals coincide B's values go in with A's and B's stores are
+// skipped.
+template <int NMH, int NV, typename T, int G>
+__device__ __forceinline__ void hist_add_pair(T* __restrict__ hist, int jA, const T (&vA)[8], int jB,
+                                              const T (&vB)[8], int lane) {
+	T* hA = hist + (size_t)jA * NMH * G + lane;
+	T* hB = hist + (size_t)jB * NMH * G + lane;
+	T a[NV], b[NV];
+#pragma unroll
+	for (int m = 0; m < NV; m++) {
+		a[m] = hA[m * G];
+		b[m] = hB[m * G];
+	}
+	const bool same = jA == jB;
+#pragma unroll
+	for (int m = 0; m < NV; m++) {
+		a[m] += same ? (vA[m] + vB[m]) : vA[m];
+		b[m] += vB[m];
+	}
+#pragma unroll
+	for (int m = 0; m < NV; m++) hA[m * G] = a[m];
+	if (!same)
+#pragma unroll
+		for (int m = 0; m < NV; m++) hB[m * G] = b[m];
+}
+
 // value of moment m of interval j summed over the group's lanes
 template <int HIST, int NMH, typename T, int G>
 __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) {
@@ -319,17 +347,30 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 				if (ON != 0) {
 					const bool cA = haveA && ((ON == 1) ? true : (ia < nrow));
 					const bool cB = haveB && ((ON == 1) ? true : (ib < nrow));
-					FwdPair<float> q;
-					q.t = tA;
-					q.j = jA;
-					q.r = rA;
-					q.rinv = qa;
-					fwd_stats<float, G, ADJ, HIST>(sc, q, inA && cA, hist, lane, pa, pb, vb);
-					q.t = tB;
-					q.j = jB;
-					q.r = rB;
-					q.rinv = qb;
-					fwd_stats<float, G, ADJ, HIST>(sc, q, inB && cB, hist, lane, pa, pb, vb);
+					const bool sA = inA && cA, sB = inB && cB;
+					if (HIST == 0) {
+						// moments sum t^c of both counted pairs, one paired update
+						const float t2A = tA * tA, t2B = tB * tB;
+						const float vA[8] = {sA ? 1.f : 0.f, sA ? tA : 0.f, sA ? t2A : 0.f, sA ? t2A * tA : 0.f,
+						                     0.f, 0.f, 0.f, 0.f};
+						const float vB[8] = {sB ? 1.f : 0.f, sB ? tB : 0.f, sB ? t2B : 0.f, sB ? t2B * tB : 0.f,
+						                     0.f, 0.f, 0.f, 0.f};
+						hist_add_pair<HistSlots<HIST, ADJ>::value, kFwdMoments, float, G>(hist, jA, vA, jB, vB, lane);
+						vb += sA ? pair_pot<float>(sc.pot_kind, rA, qa, pa, pb) : 0.f;
+						vb += sB ? pair_pot<float>(sc.pot_kind, rB, qb, pa, pb) : 0.f;
+					} else {
+						FwdPair<float> q;
+						q.t = tA;
+						q.j = jA;
+						q.r = rA;
+						q.rinv = qa;
+						fwd_stats<float, G, ADJ, HIST>(sc, q, sA, hist, lane, pa, pb, vb);
+						q.t = tB;
+						q.j = jB;
+						q.r = rB;
+						q.rinv = qb;
+						fwd_stats<float, G, ADJ, HIST>(sc, q, sB, hist, lane, pa, pb, vb);
+					}
 					nout += (okA && cA && !(rA <= rmax)) ? 1 : 0;
 					nout += (okB && cB && !(rB <= rmax)) ? 1 : 0;
 				}
@@ -472,8 +513,12 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			f2_split(f2_mul(gI, t), v[0][4], v[1][4]);
 			f2_split(f2_mul(gI, t2), v[0][5], v[1][5]);
 			v[0][6] = v[0][7] = v[1][6] = v[1][7] = 0.f;
-			hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, jA, lane, v[0], kRevMoments);
-			hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, jB, lane, v[1], kRevMoments);
+			if (HIST == 0) {
+				hist_add_pair<HistSlots<HIST, true>::value, kRevMoments, float, G>(hist, jA, v[0], jB, v[1], lane);
+			} else {
+				hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, jA, lane, v[0], kRevMoments);
+				hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, jB, lane, v[1], kRevMoments);
+			}
 		}
 	}
 }
