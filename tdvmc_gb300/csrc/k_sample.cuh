@@ -243,9 +243,10 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 // acceptance rule, and every pair term and partial sum rounded the same way.
 // Per register slot the distances of the slot's particle to the proposed and
 // to the old position of the moved particle are one f32x2 instruction stream
-// (differences, r^2, r, the interval index by the float-rounding trick, the
-// local coordinate); the per-axis minimum image min(|d|, L - |d|) stays
-// scalar so its min runs on the ALU pipe beside the FMA pipe.  The interval
+// from r^2 on (r^2, r, the interval index by the float-rounding trick, the
+// local coordinate); the differences and the per-axis minimum image
+// min(|d|, L - |d|) stay scalar, so the min runs on the ALU pipe beside the
+// FMA pipe and each coordinate is held once.  The interval
 // index is clamped to the outer-pair entry nbin with one integer min on the
 // float's bit pattern, so every pair beyond r_max reads the same (broadcast)
 // table entry.  The moved particle's own slot (old distance 0, kept finite by
@@ -298,8 +299,7 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 		int64_t w = w0 + wi;
 		if (w >= nw_total) w -= nw_total;
 		float* pw = pos + (size_t)w * sc.dim * n;
-		// each coordinate twice: one half meets the proposed, one the old position
-		f2_t X[SLOTS], Y[SLOTS], Z[SLOTS];
+		float X[SLOTS], Y[SLOTS], Z[SLOTS];
 		bool inside = true;
 #pragma unroll
 		for (int s = 0; s < SLOTS; s++) {
@@ -313,9 +313,9 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 				inside = inside && fabsf(x) <= half && fabsf(y) <= half && fabsf(z) <= half;
 				xs[i] = Q4<float>{x, y, z, 0.f};
 			}
-			X[s] = f2_make(x, x);
-			Y[s] = f2_make(y, y);
-			Z[s] = f2_make(z, z);
+			X[s] = x;
+			Y[s] = y;
+			Z[s] = z;
 		}
 		const bool walker_ok = __all_sync(gmask, inside);
 		__syncwarp(gmask);
@@ -340,15 +340,13 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 				const float xn1 = nic(xo.y + e1, L, Lr);
 				const float xn2 = nic(xo.z + e2, L, Lr);
 				if (!(fabsf(xn0) <= half && fabsf(xn1) <= half && fabsf(xn2) <= half)) continue;  // uniform over the group
-				const f2_t XN = f2_make(xn0, xo.x), YN = f2_make(xn1, xo.y), ZN = f2_make(xn2, xo.z);
 				const int self_slot = (lane == (p & (G - 1))) ? p / G : -1;
 				float dsum = 0.f;
 #pragma unroll
 				for (int s = 0; s < SLOTS; s++) {
-					float an, ao, bn, bo, cn, co;
-					f2_split(f2_sub(X[s], XN), an, ao);
-					f2_split(f2_sub(Y[s], YN), bn, bo);
-					f2_split(f2_sub(Z[s], ZN), cn, co);
+					const float an = X[s] - xn0, ao = X[s] - xo.x;
+					const float bn = Y[s] - xn1, bo = Y[s] - xo.y;
+					const float cn = Z[s] - xn2, co = Z[s] - xo.z;
 					const f2_t mx = f2_make(fminf(fabsf(an), L - fabsf(an)), fminf(fabsf(ao), L - fabsf(ao)));
 					const f2_t my = f2_make(fminf(fabsf(bn), L - fabsf(bn)), fminf(fabsf(bo), L - fabsf(bo)));
 					const f2_t mz = f2_make(fminf(fabsf(cn), L - fabsf(cn)), fminf(fabsf(co), L - fabsf(co)));
@@ -379,7 +377,7 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 				if (accept) {
 					if (lane == (p & (G - 1))) {
 						xs[p] = Q4<float>{xn0, xn1, xn2, 0.f};
-						const f2_t nx = f2_make(xn0, xn0), ny = f2_make(xn1, xn1), nz = f2_make(xn2, xn2);
+						const float nx = xn0, ny = xn1, nz = xn2;
 						switch (p / G) {
 #define TDVMC_SET_SLOT(S)                  \
 	case S:                                \
@@ -405,13 +403,9 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 		for (int s = 0; s < SLOTS && walker_ok; s++) {
 			const int i = s * G + lane;
 			if (i < n) {
-				float x, y, z, dummy;
-				f2_split(X[s], x, dummy);
-				pw[i] = x;
-				f2_split(Y[s], y, dummy);
-				if (sc.dim > 1) pw[n + i] = y;
-				f2_split(Z[s], z, dummy);
-				if (sc.dim > 2) pw[2 * n + i] = z;
+				pw[i] = X[s];
+				if (sc.dim > 1) pw[n + i] = Y[s];
+				if (sc.dim > 2) pw[2 * n + i] = Z[s];
 			}
 		}
 		if (lane == 0) acc_out[w] = nacc;
