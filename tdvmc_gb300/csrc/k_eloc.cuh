@@ -37,9 +37,36 @@ template <int HIST, bool ADJ> struct HistSlots {
 };
 
 // Histogram update modes of the lane-private moment histograms (NMH slots):
-//   0  scalar read-modify-write      hist[(j*NMH + m)*G + lane]
+//   0  per-lane records, 2-vector read-modify-write   hist[(j*G + lane)*NMH + m]
 //   1  float4 read-modify-write      hist4[(j*NMH/4 + m/4)*G + lane].{x,y,z,w}[m%4]
-//   2  shared-memory atomic add      same layout as 0 (no contention: lane-private)
+//   2  shared-memory atomic add      layout of 0 (no contention: lane-private)
+// In mode 0 a lane's NMH moments of one interval are contiguous (NMH even), so
+// they move as 8-byte (FP32) or 16-byte (FP64) vectors; records of 24 or 48
+// bytes map the lanes of each access phase to distinct banks.
+template <typename T> struct V2;
+template <> struct V2<float> {
+	using type = float2;
+};
+template <> struct V2<double> {
+	using type = double2;
+};
+template <int NV, typename T>
+__device__ __forceinline__ void rec_load(const T* p, T* v) {
+	using VT = typename V2<T>::type;
+#pragma unroll
+	for (int m = 0; m < NV; m += 2) {
+		const VT a = *reinterpret_cast<const VT*>(p + m);
+		v[m] = a.x;
+		v[m + 1] = a.y;
+	}
+}
+template <int NV, typename T>
+__device__ __forceinline__ void rec_store(T* p, const T* v) {
+	using VT = typename V2<T>::type;
+#pragma unroll
+	for (int m = 0; m < NV; m += 2) *reinterpret_cast<VT*>(p + m) = VT{v[m], v[m + 1]};
+}
+
 template <int HIST, int NMH, typename T, int G>
 __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane, const T (&v)[8], int nv) {
 	if (HIST == 1) {
@@ -58,13 +85,26 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 			if (nv > 7) b.w += v[7];
 			h4[G] = b;
 		}
-	} else {
-		T* hp = hist + (size_t)j * NMH * G + lane;
+	} else if (HIST == 2) {
+		T* hp = hist + ((size_t)j * G + lane) * NMH;
 #pragma unroll
 		for (int m = 0; m < 8; m++) {
 			if (m >= nv) break;
-			if (HIST == 2) atomicAdd(hp + m * G, v[m]);
-			else hp[m * G] += v[m];
+			atomicAdd(hp + m, v[m]);
+		}
+	} else {
+		T* hp = hist + ((size_t)j * G + lane) * NMH;
+		T a[8];
+		if (nv == kRevMoments) {
+			rec_load<kRevMoments>(hp, a);
+#pragma unroll
+			for (int m = 0; m < kRevMoments; m++) a[m] += v[m];
+			rec_store<kRevMoments>(hp, a);
+		} else {
+			rec_load<kFwdMoments>(hp, a);
+#pragma unroll
+			for (int m = 0; m < kFwdMoments; m++) a[m] += v[m];
+			rec_store<kFwdMoments>(hp, a);
 		}
 	}
 }
@@ -76,25 +116,19 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 template <int NMH, int NV, typename T, int G>
 __device__ __forceinline__ void hist_add_pair(T* __restrict__ hist, int jA, const T (&vA)[8], int jB,
                                               const T (&vB)[8], int lane) {
-	T* hA = hist + (size_t)jA * NMH * G + lane;
-	T* hB = hist + (size_t)jB * NMH * G + lane;
+	T* hA = hist + ((size_t)jA * G + lane) * NMH;
+	T* hB = hist + ((size_t)jB * G + lane) * NMH;
 	T a[NV], b[NV];
-#pragma unroll
-	for (int m = 0; m < NV; m++) {
-		a[m] = hA[m * G];
-		b[m] = hB[m * G];
-	}
+	rec_load<NV>(hA, a);
+	rec_load<NV>(hB, b);
 	const bool same = jA == jB;
 #pragma unroll
 	for (int m = 0; m < NV; m++) {
 		a[m] += same ? (vA[m] + vB[m]) : vA[m];
 		b[m] += vB[m];
 	}
-#pragma unroll
-	for (int m = 0; m < NV; m++) hA[m * G] = a[m];
-	if (!same)
-#pragma unroll
-		for (int m = 0; m < NV; m++) hB[m * G] = b[m];
+	rec_store<NV>(hA, a);
+	if (!same) rec_store<NV>(hB, b);
 }
 
 // value of moment m of interval j summed over the group's lanes
@@ -106,9 +140,9 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 #pragma unroll 8
 		for (int l = 0; l < G; l++) s += h[l * 4];
 	} else {
-		const T* h = hist + ((size_t)j * NMH + m) * G;
+		const T* h = hist + (size_t)j * G * NMH + m;
 #pragma unroll 8
-		for (int l = 0; l < G; l++) s += h[l];
+		for (int l = 0; l < G; l++) s += h[(size_t)l * NMH];
 	}
 	return s;
 }
