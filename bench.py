@@ -289,8 +289,10 @@ def run_ours(args):
     fp32_peak = pk.value
     if top[0] == "k_sample":
         fl = flop_sample_launch()
+    elif top[0] == "k_eloc_rev":
+        fl = float(NW) * N * (N - 1) / 2 * FLOP_ADJ_PAIR
     elif top[0].startswith("k_eloc"):
-        fl = flop_eloc_launch(adjoint=top[0].endswith("adjoint"))
+        fl = flop_eloc_launch(adjoint=False)  # the forward kernel; the adjoint pass is k_eloc_rev
     else:
         fl = 0.0
     achieved = fl / (top[1] * 1e-3) / 1e12

@@ -12,7 +12,10 @@ using SampleFn = void (*)(SysConst, const Q4<T>*, const T*, const T*, const T*, 
                           const int32_t*, int, T, uint2, const uint32_t*, int*);
 template <typename T>
 using ElocFn = void (*)(SysConst, const DynState*, const Q4<T>*, const T*, const T*, const int*, const T*,
-                        const double*, const double*, const T*, int64_t, T*, T*, T*, T*, T*);
+                        const double*, const double*, const T*, int64_t, T*, T*, T*, T*, T*, T*);
+template <typename T>
+using RevFn = void (*)(SysConst, const T*, const T*, const int*, const T*, const double*, const T*, const T*, int64_t,
+                       T*);
 
 // register slots per lane available for `lanes` lanes per walker
 int sample_slots_for(int n, int lanes);
@@ -23,6 +26,8 @@ SampleFn<float> pick_sample_f32_packed(int lanes, int slots);
 SampleFn<double> pick_sample_f64(int lanes, int slots);
 ElocFn<float> pick_eloc_f32(int lanes, bool adj, int hist);
 ElocFn<double> pick_eloc_f64(int lanes, bool adj, int hist);
+RevFn<float> pick_eloc_rev_f32(int lanes, int hist);
+RevFn<double> pick_eloc_rev_f64(int lanes, int hist);
 
 template <typename T> SampleFn<T> pick_sample(int lanes, int slots);
 template <> inline SampleFn<float> pick_sample<float>(int g, int s) { return pick_sample_f32(g, s); }
@@ -30,5 +35,8 @@ template <> inline SampleFn<double> pick_sample<double>(int g, int s) { return p
 template <typename T> ElocFn<T> pick_eloc(int lanes, bool adj, int hist);
 template <> inline ElocFn<float> pick_eloc<float>(int g, bool a, int h) { return pick_eloc_f32(g, a, h); }
 template <> inline ElocFn<double> pick_eloc<double>(int g, bool a, int h) { return pick_eloc_f64(g, a, h); }
+template <typename T> RevFn<T> pick_eloc_rev(int lanes, int hist);
+template <> inline RevFn<float> pick_eloc_rev<float>(int g, int h) { return pick_eloc_rev_f32(g, h); }
+template <> inline RevFn<double> pick_eloc_rev<double>(int g, int h) { return pick_eloc_rev_f64(g, h); }
 
 }  // namespace tdvmc

@@ -147,10 +147,12 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 	return s;
 }
 
-// Shared memory layout:
+// Shared memory layout of the forward kernel k_eloc:
 //   CTA:   coefC[3*nbin] (u', u'' coefficients) | kb[nbin] | hv[nbin] | lut[ncell]
-//   group: xs[n] {x, y, z, gRx} | (adjoint) g4[n] {gRy, gRz, gIx, gIy} | gz[n] {gIz}
-//          | hist[nbin*NMH*G] | red[nbin*4] | (adjoint) redr[nbin*6]
+//   group: xs[n] {x, y, z, 0} | hist[nbin*4*G] | red[nbin*4]
+// and of the reverse (adjoint) kernel k_eloc_rev:
+//   CTA:   kb[nbin] | hv[nbin] | lut[ncell]
+//   group: xs[n] {x, y, z, gRx} | g4[n] {gRy, gRz, gIx, gIy} | gz[n] {gIz} | hist[nbin*NMH*G] | redr[nbin*6]
 // The spline values [ns][4] of the last step borrow the start of the (then
 // empty) histogram and are cleared after use.
 template <typename T>
@@ -161,14 +163,27 @@ __host__ __device__ inline size_t eloc_cta_bytes(int nbin, int ncell) {
 __host__ __device__ inline int eloc_hist_slots(bool adj, int hist_mode) {
 	return adj ? (hist_mode == 1 ? 8 : 6) : 4;
 }
+__host__ __device__ inline size_t eloc_hist_len(int nbin, int ns, int G, int slots) {
+	size_t h = (size_t)nbin * slots * G;
+	return h < (size_t)ns * 4 ? (size_t)ns * 4 : h;
+}
 template <typename T>
-__host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G, bool adj, int hist_mode = 0) {
+__host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G) {
 	size_t b = (size_t)n * sizeof(Q4<T>);
-	if (adj) b += (size_t)n * sizeof(Q4<T>) + (size_t)((n + 7) & ~7) * sizeof(T);  // keeps the histogram 32-byte aligned
-	size_t h = (size_t)nbin * eloc_hist_slots(adj, hist_mode) * G;
-	if (h < (size_t)ns * 4) h = (size_t)ns * 4;
-	b += h * sizeof(T);
-	b += (size_t)nbin * (kFwdMoments + (adj ? kRevMoments : 0)) * sizeof(T);
+	b += eloc_hist_len(nbin, ns, G, 4) * sizeof(T);
+	b += (size_t)nbin * kFwdMoments * sizeof(T);
+	return (b + 31) & ~(size_t)31;
+}
+template <typename T>
+__host__ __device__ inline size_t rev_cta_bytes(int nbin, int ncell) {
+	size_t b = 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+	return (b + 31) & ~(size_t)31;
+}
+template <typename T>
+__host__ __device__ inline size_t rev_group_bytes(int n, int nbin, int ns, int G, int hist_mode) {
+	size_t b = 2 * (size_t)n * sizeof(Q4<T>) + (size_t)((n + 7) & ~7) * sizeof(T);  // keeps the histogram 32-byte aligned
+	b += eloc_hist_len(nbin, ns, G, eloc_hist_slots(true, hist_mode)) * sizeof(T);
+	b += (size_t)nbin * kRevMoments * sizeof(T);
 	return (b + 31) & ~(size_t)31;
 }
 
@@ -224,7 +239,7 @@ __device__ __forceinline__ void fwd_stats(const SysConst& sc, const FwdPair<T>& 
 	const T ts = on ? q.t : T(0);  // t is NaN for the self pair
 	const T t2 = ts * ts;
 	T v[8] = {on ? T(1) : T(0), ts, t2, t2 * ts, T(0), T(0), T(0), T(0)};
-	hist_add8<HIST, HistSlots<HIST, ADJ>::value, T, G>(hist, q.j, lane, v, kFwdMoments);
+	hist_add8<HIST, HistSlots<HIST, false>::value, T, G>(hist, q.j, lane, v, kFwdMoments);
 	vb += on ? pair_pot<T>(sc.pot_kind, q.r, q.rinv, pa, pb) : T(0);
 }
 
@@ -389,7 +404,7 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 						                     0.f, 0.f, 0.f, 0.f};
 						const float vB[8] = {sB ? 1.f : 0.f, sB ? tB : 0.f, sB ? t2B : 0.f, sB ? t2B * tB : 0.f,
 						                     0.f, 0.f, 0.f, 0.f};
-						hist_add_pair<HistSlots<HIST, ADJ>::value, kFwdMoments, float, G>(hist, jA, vA, jB, vB, lane);
+						hist_add_pair<HistSlots<HIST, false>::value, kFwdMoments, float, G>(hist, jA, vA, jB, vB, lane);
 						vb += sA ? pair_pot<float>(sc.pot_kind, rA, qa, pa, pb) : 0.f;
 						vb += sB ? pair_pot<float>(sc.pot_kind, rB, qb, pa, pb) : 0.f;
 					} else {
@@ -567,6 +582,10 @@ __device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, i
 	__syncwarp(gmask);
 }
 
+// Forward kernel: ln psi, O_k, E_loc and the kinetic sums of every walker.
+// With ADJ it also writes every particle's complex gradient G_n to
+// gout[w][6][n] (gRx gRy gRz gIx gIy gIz) for k_eloc_rev and the B'' part of
+// dE_loc/d alpha to dE_o, which k_eloc_rev completes.
 template <typename T, int G, bool ADJ, int HIST>
 __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
                                               const T* __restrict__ kb_g, const T* __restrict__ hv_g,
@@ -574,9 +593,9 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
                                               const double* __restrict__ fold_g, const double* __restrict__ params,
                                               const T* __restrict__ pos, int64_t nw, T* __restrict__ lnpsi_o,
                                               T* __restrict__ O_o, T* __restrict__ eloc_o, T* __restrict__ other_o,
-                                              T* __restrict__ dE_o) {
+                                              T* __restrict__ dE_o, T* __restrict__ gout) {
 	constexpr int NM = kFwdMoments;
-	constexpr int NMH = HistSlots<HIST, ADJ>::value;
+	constexpr int NMH = HistSlots<HIST, false>::value;
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
 	Q4<T>* coefC = reinterpret_cast<Q4<T>*>(smem_raw);
@@ -584,7 +603,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 	T* hv = kb + nbin;
 	int* lut = reinterpret_cast<int*>(hv + nbin);
 	const size_t cta_b = eloc_cta_bytes<T>(nbin, sc.ncell);
-	const size_t grp_b = eloc_group_bytes<T>(n, nbin, ns, G, ADJ, HIST);
+	const size_t grp_b = eloc_group_bytes<T>(n, nbin, ns, G);
 
 	for (int i = threadIdx.x; i < 3 * nbin; i += blockDim.x) coefC[i] = coefC_g[i];
 	for (int i = threadIdx.x; i < nbin; i += blockDim.x) {
@@ -601,13 +620,10 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
 	unsigned char* gbase = smem_raw + cta_b + (size_t)gib * grp_b;
 	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
-	Q4<T>* g4 = xs + (ADJ ? n : 0);
-	T* gz = reinterpret_cast<T*>(xs + (ADJ ? 2 * n : n));
-	T* hist = gz + (ADJ ? (size_t)((n + 7) & ~7) : 0);
-	const size_t hist_len = (size_t)nbin * NMH * G > (size_t)ns * 4 ? (size_t)nbin * NMH * G : (size_t)ns * 4;
+	T* hist = reinterpret_cast<T*>(xs + n);
+	const size_t hist_len = eloc_hist_len(nbin, ns, G, NMH);
 	T* red = hist + hist_len;
-	T* redr = red + (size_t)nbin * NM;
-	T* spl = hist;  // [ns][4]: S, Lsp, AR, AI, while the histogram is empty
+	T* spl = hist;  // [ns][4]: S, Lsp, -, -, while the histogram is empty
 
 	for (size_t e = lane; e < hist_len; e += G) hist[e] = T(0);
 	__syncthreads();
@@ -627,6 +643,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 
 		KSum<T> e_r1, e_i1, e_r1i1, e_lR, e_lI, e_v;
 		int nout = 0;
+		T* gw = ADJ ? gout + (size_t)w * 6 * n : nullptr;
 		for (int s = 0; s < nslot; s++) {
 			const int nrow = s * G + lane;
 			const bool rowok = nrow < n;
@@ -652,9 +669,12 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				e_lR.add(acc[6].value());
 				e_lI.add(acc[7].value());
 				if (ADJ) {
-					xs[nrow].w = gRx;
-					g4[nrow] = Q4<T>{gRy, gRz, gIx, gIy};
-					gz[nrow] = gIz;
+					gw[nrow] = gRx;
+					gw[n + nrow] = gRy;
+					gw[2 * n + nrow] = gRz;
+					gw[3 * n + nrow] = gIx;
+					gw[4 * n + nrow] = gIy;
+					gw[5 * n + nrow] = gIz;
 				}
 			}
 		}
@@ -671,37 +691,9 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 
 		hist_reduce<T, G, HIST, NMH>(hist, red, nbin, NM, lane, gmask);
 
-		if (ADJ) {
-			for (int s = 0; s < nslot; s++) {
-				const int nrow = s * G + lane;
-				const bool rowok = nrow < n;
-				const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
-				T gn[6] = {0, 0, 0, 0, 0, 0};
-				if (rowok) {
-					const Q4<T> a = g4[nrow];
-					gn[0] = xr.w;
-					gn[1] = a.x;
-					gn[2] = a.y;
-					gn[3] = a.z;
-					gn[4] = a.w;
-					gn[5] = gz[nrow];
-				}
-				const int base = s * G;
-				const int dend = (base + G < n) ? base + G : n;
-				if constexpr (std::is_same<T, float>::value) {
-					rev_region_f2<G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-					rev_region_f2<G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-				} else {
-					rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-					rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-				}
-			}
-			hist_reduce<T, G, HIST, NMH>(hist, redr, nbin, kRevMoments, lane, gmask);
-		}
-
 		// moments -> spline values: spline sp = j + 3 - q on interval j
 		for (int sp = lane; sp < ns; sp += G) {
-			T S = T(0), Lsp = T(0), AR = T(0), AI = T(0);
+			T S = T(0), Lsp = T(0);
 #pragma unroll
 			for (int q = 0; q < 4; q++) {
 				const int j = sp - 3 + q;
@@ -712,37 +704,29 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				S += l0 * m[0] + l1 * m[1] + l2 * m[2] + l3 * m[3];
 				if (ADJ) {
 					const T hj = sc.uniform ? (T)sc.hinv : hv[j];
-					// B'' part of the Laplacian of O_k; its (D-1)/r B' part is in g[0..2]
+					// B'' part of the Laplacian of O_k; its (D-1)/r B' part comes from k_eloc_rev
 					Lsp += T(2) * hj * hj * (T(2) * l2 * m[0] + T(6) * l3 * m[1]);
-					const T* g = redr + (size_t)j * kRevMoments;
-					AR += hj * (l1 * g[0] + T(2) * l2 * g[1] + T(3) * l3 * g[2]);
-					AI += hj * (l1 * g[3] + T(2) * l2 * g[4] + T(3) * l3 * g[5]);
 				}
 			}
 			spl[sp * 4 + 0] = S;
 			spl[sp * 4 + 1] = Lsp;
-			spl[sp * 4 + 2] = AR;
-			spl[sp * 4 + 3] = AI;
 		}
 		__syncwarp(gmask);
 		// fold to the p parameters; ln psi in FP64 (BosonsBulk.cpp:522-539)
 		const double c = sc.hbar2_2m;
 		double lnp = 0.0;
 		for (int k = lane; k < P; k += G) {
-			double Ok = 0.0, dR = 0.0, dI = 0.0;
+			double Ok = 0.0, dR = 0.0;
 			for (int sp = 0; sp < ns; sp++) {
 				const double f = fold_g[(size_t)k * ns + sp];
 				if (f == 0.0) continue;
 				Ok += f * (double)spl[sp * 4 + 0];
-				if (ADJ) {
-					dR += f * (2.0 * (double)spl[sp * 4 + 2] + (double)spl[sp * 4 + 1]);
-					dI += f * (2.0 * (double)spl[sp * 4 + 3]);
-				}
+				if (ADJ) dR += f * (double)spl[sp * 4 + 1];
 			}
 			O_o[(size_t)w * P + k] = (T)Ok;
 			if (ADJ) {
 				dE_o[((size_t)w * P + k) * 2 + 0] = (T)(-c * dR);
-				dE_o[((size_t)w * P + k) * 2 + 1] = (T)(-c * dI);
+				dE_o[((size_t)w * P + k) * 2 + 1] = T(0);
 			}
 			lnp += params[k] * Ok;
 		}
@@ -766,6 +750,123 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 			ot[5] = sI2;
 			ot[6] = sR1I1;
 		}
+		__syncwarp(gmask);
+	}
+}
+
+// Reverse (adjoint) kernel: one pass over unordered pairs with the gradients
+// of k_eloc, accumulating sum t^c ((G_n - G_i) . rhat_ni + (D-1)/r) per
+// interval, then adds 2 sum_n G_n . sD_k + the (D-1)/r B' part of the
+// Laplacian of O_k to the dE_o that k_eloc started.
+template <typename T, int G, int HIST>
+__global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __restrict__ kb_g, const T* __restrict__ hv_g,
+                                                  const int* __restrict__ lut_g, const T* __restrict__ loc_g,
+                                                  const double* __restrict__ fold_g, const T* __restrict__ pos,
+                                                  const T* __restrict__ gin, int64_t nw, T* __restrict__ dE_o) {
+	constexpr int NMH = HistSlots<HIST, true>::value;
+	extern __shared__ __align__(32) unsigned char smem_raw[];
+	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
+	T* kb = reinterpret_cast<T*>(smem_raw);
+	T* hv = kb + nbin;
+	int* lut = reinterpret_cast<int*>(hv + nbin);
+	const size_t cta_b = rev_cta_bytes<T>(nbin, sc.ncell);
+	const int hist_mode = HIST;
+	const size_t grp_b = rev_group_bytes<T>(n, nbin, ns, G, hist_mode);
+	for (int i = threadIdx.x; i < nbin; i += blockDim.x) {
+		kb[i] = kb_g[i];
+		hv[i] = hv_g[i];
+	}
+	for (int i = threadIdx.x; i < sc.ncell; i += blockDim.x) lut[i] = lut_g[i];
+
+	const int tid = threadIdx.x;
+	const int lane = tid & (G - 1);
+	const int gib = tid / G;
+	const int gpb = blockDim.x / G;
+	const unsigned wl = tid & 31;
+	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
+	unsigned char* gbase = smem_raw + cta_b + (size_t)gib * grp_b;
+	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
+	Q4<T>* g4 = xs + n;
+	T* gz = reinterpret_cast<T*>(xs + 2 * n);
+	T* hist = gz + (size_t)((n + 7) & ~7);
+	const size_t hist_len = eloc_hist_len(nbin, ns, G, NMH);
+	T* redr = hist + hist_len;
+	T* spl = hist;  // [ns][4]: -, -, AR, AI, while the histogram is empty
+
+	for (size_t e = lane; e < hist_len; e += G) hist[e] = T(0);
+	__syncthreads();
+	const int nslot = (n + G - 1) / G;
+
+	for (int64_t w = (int64_t)blockIdx.x * gpb + gib; w < nw; w += (int64_t)gridDim.x * gpb) {
+		const T* pw = pos + (size_t)w * sc.dim * n;
+		const T* gw = gin + (size_t)w * 6 * n;
+		for (int i = lane; i < n; i += G) {
+			T x0 = pw[i];
+			T x1 = sc.dim > 1 ? pw[n + i] : T(0);
+			T x2 = sc.dim > 2 ? pw[2 * n + i] : T(0);
+			xs[i] = Q4<T>{x0, x1, x2, gw[i]};
+			g4[i] = Q4<T>{gw[n + i], gw[2 * n + i], gw[3 * n + i], gw[4 * n + i]};
+			gz[i] = gw[5 * n + i];
+		}
+		__syncwarp(gmask);
+		for (int s = 0; s < nslot; s++) {
+			const int nrow = s * G + lane;
+			const bool rowok = nrow < n;
+			const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
+			T gn[6] = {0, 0, 0, 0, 0, 0};
+			if (rowok) {
+				const Q4<T> a = g4[nrow];
+				gn[0] = xr.w;
+				gn[1] = a.x;
+				gn[2] = a.y;
+				gn[3] = a.z;
+				gn[4] = a.w;
+				gn[5] = gz[nrow];
+			}
+			const int base = s * G;
+			const int dend = (base + G < n) ? base + G : n;
+			if constexpr (std::is_same<T, float>::value) {
+				rev_region_f2<G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				rev_region_f2<G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+			} else {
+				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+			}
+		}
+		hist_reduce<T, G, HIST, NMH>(hist, redr, nbin, kRevMoments, lane, gmask);
+
+		for (int sp = lane; sp < ns; sp += G) {
+			T AR = T(0), AI = T(0);
+#pragma unroll
+			for (int q = 0; q < 4; q++) {
+				const int j = sp - 3 + q;
+				if (j < 0 || j >= nbin) continue;
+				const T* l = loc_g + ((size_t)j * 4 + q) * 4;
+				const T l1 = l[1], l2 = l[2], l3 = l[3];
+				const T hj = sc.uniform ? (T)sc.hinv : hv[j];
+				const T* g = redr + (size_t)j * kRevMoments;
+				AR += hj * (l1 * g[0] + T(2) * l2 * g[1] + T(3) * l3 * g[2]);
+				AI += hj * (l1 * g[3] + T(2) * l2 * g[4] + T(3) * l3 * g[5]);
+			}
+			spl[sp * 4 + 2] = AR;
+			spl[sp * 4 + 3] = AI;
+		}
+		__syncwarp(gmask);
+		const double c = sc.hbar2_2m;
+		for (int k = lane; k < P; k += G) {
+			double dR = 0.0, dI = 0.0;
+			for (int sp = 0; sp < ns; sp++) {
+				const double f = fold_g[(size_t)k * ns + sp];
+				if (f == 0.0) continue;
+				dR += f * (2.0 * (double)spl[sp * 4 + 2]);
+				dI += f * (2.0 * (double)spl[sp * 4 + 3]);
+			}
+			T* d = dE_o + ((size_t)w * P + k) * 2;
+			d[0] = (T)((double)d[0] - c * dR);
+			d[1] = (T)(-c * dI);
+		}
+		__syncwarp(gmask);
+		for (int e = lane; e < ns * 4; e += G) spl[e] = T(0);  // the histogram starts empty
 		__syncwarp(gmask);
 	}
 }

@@ -93,6 +93,7 @@ struct tdvmc_ctx {
 	std::map<GraphKey, int> graph_kernels;  // kernels launched by one replay
 	// stored samples (correlated-sampling reuse), allocated on first use
 	void *csD = nullptr, *csD2 = nullptr, *csO = nullptr, *csV = nullptr, *cs_piece = nullptr;
+	void* gbuf = nullptr;  // per-particle gradients [w][6][n] passed to the reverse (adjoint) kernel
 	int32_t* csN = nullptr;
 	bool cs_valid = false;      // the store matches the walkers
 	int64_t cs_steps = 0;       // stored-sample steps since the last full store
@@ -223,27 +224,60 @@ int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed, int64_t
 	return TDVMC_OK;
 }
 
+// shared memory of the forward (k_eloc) and, for adj, the larger of it and the reverse kernel
 template <typename T>
 size_t eloc_smem(tdvmc_ctx* ctx, int G, int gpb, bool adj) {
-	return eloc_cta_bytes<T>(ctx->sc.nbin, ctx->sc.ncell) +
-	       (size_t)gpb * eloc_group_bytes<T>(ctx->sc.n, ctx->sc.nbin, ctx->sc.ns, G, adj, G == 32 ? ctx->tiles.hist : 0);
+	const SysConst& s = ctx->sc;
+	const size_t f = eloc_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * eloc_group_bytes<T>(s.n, s.nbin, s.ns, G);
+	if (!adj) return f;
+	const size_t r =
+	    rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, G == 32 ? ctx->tiles.hist : 0);
+	return std::max(f, r);
 }
 
+// Gradient scratch of the adjoint (nw x 6 x n), allocated on first need and
+// always before a stream capture (allocation is not capturable).
+int ensure_gbuf(tdvmc_ctx* ctx) {
+	if (ctx->gbuf) return TDVMC_OK;
+	const size_t bytes = (size_t)ctx->nw * 6 * ctx->sc.n * tsize(ctx->prec);
+	if (cudaMalloc(&ctx->gbuf, bytes) != cudaSuccess) {
+		ctx->gbuf = nullptr;
+		cudaGetLastError();  // out of memory is not sticky
+		return TDVMC_ERR_NOMEM;
+	}
+	return TDVMC_OK;
+}
+
+// Forward evaluation; with adj also the reverse (adjoint) kernel, which reads
+// the per-particle gradients the forward kernel leaves in ctx->gbuf.
 template <typename T>
 int launch_eloc(tdvmc_ctx* ctx, bool adj) {
 	const int G = ctx->tiles.eg, gpb = ctx->tiles.egpb;
-	ElocFn<T> fn = pick_eloc<T>(G, adj, G == 32 ? ctx->tiles.hist : 0);
-	if (!fn) return TDVMC_ERR_ARG;
+	const int hist = G == 32 ? ctx->tiles.hist : 0;
+	ElocFn<T> fn = pick_eloc<T>(G, adj, hist);
+	RevFn<T> fr = adj ? pick_eloc_rev<T>(G, hist) : nullptr;
+	if (!fn || (adj && !fr)) return TDVMC_ERR_ARG;
+	const SysConst& s = ctx->sc;
+	if (adj && !ctx->gbuf) return TDVMC_ERR_STATE;  // ensure_gbuf was not called
 	const int threads = G * gpb;
-	const size_t smem = eloc_smem<T>(ctx, G, gpb, adj);
+	const size_t smem = eloc_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * eloc_group_bytes<T>(s.n, s.nbin, s.ns, G);
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, gpb);
-	fn<<<grid, threads, smem, ctx->st>>>(ctx->sc, ctx->dyn, (const Q4<T>*)ctx->coefC, (const T*)ctx->kb,
-	                                     (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT, ctx->fold_d, ctx->stage,
-	                                     (const T*)ctx->pos, ctx->nw, (T*)ctx->lnpsi, (T*)ctx->O, (T*)ctx->eloc,
-	                                     (T*)ctx->other7, (T*)ctx->dE);
+	fn<<<grid, threads, smem, ctx->st>>>(s, ctx->dyn, (const Q4<T>*)ctx->coefC, (const T*)ctx->kb, (const T*)ctx->hv,
+	                                     ctx->lut, (const T*)ctx->locT, ctx->fold_d, ctx->stage, (const T*)ctx->pos,
+	                                     ctx->nw, (T*)ctx->lnpsi, (T*)ctx->O, (T*)ctx->eloc, (T*)ctx->other7,
+	                                     (T*)ctx->dE, adj ? (T*)ctx->gbuf : nullptr);
 	ctx->launches++;
-	mark(ctx, adj ? "k_eloc_adjoint" : "k_eloc");
+	mark(ctx, "k_eloc");
+	CK(cudaGetLastError());
+	if (!adj) return TDVMC_OK;
+	const size_t smr = rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist);
+	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+	const int gridr = grid_for(ctx, (const void*)fr, threads, smr, ctx->nw, gpb);
+	fr<<<gridr, threads, smr, ctx->st>>>(s, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT,
+	                                      ctx->fold_d, (const T*)ctx->pos, (const T*)ctx->gbuf, ctx->nw, (T*)ctx->dE);
+	ctx->launches++;
+	mark(ctx, "k_eloc_rev");
 	CK(cudaGetLastError());
 	return TDVMC_OK;
 }
@@ -444,6 +478,10 @@ int get_graph(tdvmc_ctx* ctx, const tdvmc_step_opts* o, cudaGraphExec_t* out, in
 		*out = it->second;
 		*kernels = ctx->graph_kernels[k];
 		return TDVMC_OK;
+	}
+	if (o->use_adjoint) {
+		const int ra = ensure_gbuf(ctx);
+		if (ra) return ra;
 	}
 	cudaGraph_t g;
 	CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
@@ -835,7 +873,7 @@ int tdvmc_destroy(tdvmc_ctx* ctx) {
 	void* bufs[] = {ctx->pos, ctx->lnpsi, ctx->O, ctx->eloc, ctx->other7, ctx->dE, ctx->acc, ctx->base, ctx->stage,
 	                ctx->kdot, ctx->rhs, ctx->loc_d, ctx->fold_d, ctx->coefU, ctx->coefC, ctx->uout, ctx->kb, ctx->hv,
 	                ctx->locT, ctx->lut, ctx->part1, ctx->means1, ctx->means0, ctx->part2, ctx->C2, ctx->partS, ctx->Sg,
-	                ctx->dyn, ctx->gramws, ctx->csD, ctx->csD2, ctx->csO, ctx->csV, ctx->csN, ctx->cs_piece};
+	                ctx->dyn, ctx->gramws, ctx->csD, ctx->csD2, ctx->csO, ctx->csV, ctx->csN, ctx->cs_piece, ctx->gbuf};
 	for (void* b : bufs)
 		if (b) cudaFree(b);
 	if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -934,6 +972,10 @@ int tdvmc_sample(tdvmc_ctx* ctx, int32_t moves, double mc_step, uint64_t seed, u
 
 static int eval_common(tdvmc_ctx* ctx, bool adj) {
 	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
+	if (adj) {
+		const int ra = ensure_gbuf(ctx);
+		if (ra) return ra;
+	}
 	int rc = ctx->prec == TDVMC_PREC_FP64 ? launch_prep<double>(ctx) : launch_prep<float>(ctx);
 	if (rc) return rc;
 	rc = ctx->prec == TDVMC_PREC_FP64 ? launch_eloc<double>(ctx, adj) : launch_eloc<float>(ctx, adj);
@@ -1237,6 +1279,7 @@ int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, float* ms, con
 	CK(cudaEventCreate(&e0));
 	CK(cudaStreamSynchronize(ctx->st));
 	CK(cudaEventRecord(e0, ctx->st));
+	if (o->use_adjoint && (rc = ensure_gbuf(ctx))) return rc;
 	ctx->prof = &ev;
 	ctx->prof_names = &nm;
 	if (o->ode_solver == 3) {
@@ -1319,6 +1362,7 @@ int tdvmc_autotune(tdvmc_ctx* ctx, int32_t moves, double mc_step) {
 			rc = TDVMC_OK;
 			CK(cudaMemcpyAsync(ctx->pos, save, bytes, cudaMemcpyDeviceToDevice, ctx->st));
 		}
+		if ((rc = ensure_gbuf(ctx))) break;
 		for (int gpb : {1, 2, 4}) {
 			if (G * gpb > 128) continue;
 			const size_t smem = ctx->prec == TDVMC_PREC_FP64 ? eloc_smem<double>(ctx, G, gpb, true)
