@@ -262,6 +262,9 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj) {
 	const int threads = G * gpb;
 	const size_t smem = eloc_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * eloc_group_bytes<T>(s.n, s.nbin, s.ns, G);
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	// shared memory limits the residency: ask for the largest carve-out
+	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+	                        (int)cudaSharedmemCarveoutMaxShared));
 	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, gpb);
 	fn<<<grid, threads, smem, ctx->st>>>(s, ctx->dyn, (const Q4<T>*)ctx->coefC, (const T*)ctx->kb, (const T*)ctx->hv,
 	                                     ctx->lut, (const T*)ctx->locT, ctx->fold_d, ctx->stage, (const T*)ctx->pos,
@@ -273,6 +276,8 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj) {
 	if (!adj) return TDVMC_OK;
 	const size_t smr = rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist);
 	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributePreferredSharedMemoryCarveout,
+	                        (int)cudaSharedmemCarveoutMaxShared));
 	const int gridr = grid_for(ctx, (const void*)fr, threads, smr, ctx->nw, gpb);
 	fr<<<gridr, threads, smr, ctx->st>>>(s, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT,
 	                                      ctx->fold_d, (const T*)ctx->pos, (const T*)ctx->gbuf, ctx->nw, (T*)ctx->dE);
