@@ -94,6 +94,17 @@ struct tdvmc_ctx {
 	// stored samples (correlated-sampling reuse), allocated on first use
 	void *csD = nullptr, *csD2 = nullptr, *csO = nullptr, *csV = nullptr, *cs_piece = nullptr;
 	void* gbuf = nullptr;  // per-particle gradients [w][6][n] passed to the reverse (adjoint) kernel
+	// sampling / evaluation pipeline over walker chunks: the sampler runs on st,
+	// the evaluation of the previous chunk on st2 beside it.  Off by default:
+	// at N=343, 65,536 walkers it measured 380-416 ms per step (2-8 chunks)
+	// against 328 ms back to back, because the evaluation kernels lose more to
+	// the block slots left to the sampler than the sampler gains.
+	static constexpr int kMaxChunks = 16;
+	int pipeline = 1;  // chunks per stage; 1 runs sampling and evaluation back to back
+	cudaStream_t st2 = nullptr;
+	cudaEvent_t ev_s[kMaxChunks] = {};
+	cudaEvent_t ev_e = nullptr;
+	int32_t* chunk_starts = nullptr;  // device: first walker of every chunk
 	int32_t* csN = nullptr;
 	bool cs_valid = false;      // the store matches the walkers
 	int64_t cs_steps = 0;       // stored-sample steps since the last full store
@@ -178,9 +189,12 @@ void mark(tdvmc_ctx* ctx, const char* name) {
 	ctx->prof_names->push_back(name);
 }
 
-int grid_for(tdvmc_ctx* ctx, const void* fn, int threads, size_t smem, int64_t work_groups, int gpb) {
+// Persistent grid: resident blocks per SM x SMs, at most one block per work
+// group; free > 0 leaves that many block slots per SM to a concurrent kernel.
+int grid_for(tdvmc_ctx* ctx, const void* fn, int threads, size_t smem, int64_t work_groups, int gpb, int free = 0) {
 	int per_sm = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+	per_sm -= free;
 	if (per_sm < 1) per_sm = 1;
 	int64_t need = (work_groups + gpb - 1) / gpb;
 	int64_t g = (int64_t)per_sm * ctx->nsm;
@@ -250,8 +264,12 @@ int ensure_gbuf(tdvmc_ctx* ctx) {
 
 // Forward evaluation; with adj also the reverse (adjoint) kernel, which reads
 // the per-particle gradients the forward kernel leaves in ctx->gbuf.
+// Walkers [w0, w0 + count) on stream st; free block slots per SM as in grid_for.
 template <typename T>
-int launch_eloc(tdvmc_ctx* ctx, bool adj) {
+int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cudaStream_t st = nullptr,
+                int free = 0) {
+	if (count < 0) count = ctx->nw;
+	if (!st) st = ctx->st;
 	const int G = ctx->tiles.eg, gpb = ctx->tiles.egpb;
 	const int hist = G == 32 ? ctx->tiles.hist : 0;
 	ElocFn<T> fn = pick_eloc<T>(G, adj, hist);
@@ -265,11 +283,13 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj) {
 	// shared memory limits the residency: ask for the largest carve-out
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributePreferredSharedMemoryCarveout,
 	                        (int)cudaSharedmemCarveoutMaxShared));
-	const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, gpb);
-	fn<<<grid, threads, smem, ctx->st>>>(s, ctx->dyn, (const Q4<T>*)ctx->coefC, (const T*)ctx->kb, (const T*)ctx->hv,
-	                                     ctx->lut, (const T*)ctx->locT, ctx->fold_d, ctx->stage, (const T*)ctx->pos,
-	                                     ctx->nw, (T*)ctx->lnpsi, (T*)ctx->O, (T*)ctx->eloc, (T*)ctx->other7,
-	                                     (T*)ctx->dE, adj ? (T*)ctx->gbuf : nullptr);
+	const int grid = grid_for(ctx, (const void*)fn, threads, smem, count, gpb, free);
+	const size_t P = (size_t)s.p, dn = (size_t)s.dim * s.n;
+	T* gb = adj ? (T*)ctx->gbuf + (size_t)w0 * 6 * s.n : nullptr;
+	fn<<<grid, threads, smem, st>>>(s, ctx->dyn, (const Q4<T>*)ctx->coefC, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut,
+	                                (const T*)ctx->locT, ctx->fold_d, ctx->stage, (const T*)ctx->pos + w0 * dn, count,
+	                                (T*)ctx->lnpsi + w0, (T*)ctx->O + w0 * P, (T*)ctx->eloc + 2 * w0,
+	                                (T*)ctx->other7 + 7 * w0, (T*)ctx->dE + 2 * P * w0, gb);
 	ctx->launches++;
 	mark(ctx, "k_eloc");
 	CK(cudaGetLastError());
@@ -278,9 +298,9 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj) {
 	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
 	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributePreferredSharedMemoryCarveout,
 	                        (int)cudaSharedmemCarveoutMaxShared));
-	const int gridr = grid_for(ctx, (const void*)fr, threads, smr, ctx->nw, gpb);
-	fr<<<gridr, threads, smr, ctx->st>>>(s, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT,
-	                                      ctx->fold_d, (const T*)ctx->pos, (const T*)ctx->gbuf, ctx->nw, (T*)ctx->dE);
+	const int gridr = grid_for(ctx, (const void*)fr, threads, smr, count, gpb, free);
+	fr<<<gridr, threads, smr, st>>>(s, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT, ctx->fold_d,
+	                                 (const T*)ctx->pos + w0 * dn, gb, count, (T*)ctx->dE + 2 * P * w0);
 	ctx->launches++;
 	mark(ctx, "k_eloc_rev");
 	CK(cudaGetLastError());
@@ -447,6 +467,26 @@ int run_cs_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int kind, int64_t cou
 template <typename T>
 int run_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o) {
 	int rc;
+	const int K = (int)std::min<int64_t>(ctx->pipeline, ctx->nw);
+	if (K > 1 && o->moves_per_stage > 0 && !ctx->prof) {
+		// chunk k is evaluated on st2 while st samples chunk k+1; the evaluation
+		// kernels leave two block slots per SM to the sampler
+		if ((rc = launch_prep<T>(ctx))) return rc;
+		const bool adj = o->use_adjoint != 0;
+		for (int k = 0; k < K; k++) {
+			const int64_t a = ctx->nw * k / K, b = ctx->nw * (k + 1) / K;
+			if ((rc = launch_sample<T>(ctx, o->moves_per_stage, o->mc_step, o->seed, b - a, ctx->chunk_starts + k)))
+				return rc;
+			CK(cudaEventRecord(ctx->ev_s[k], ctx->st));
+			CK(cudaStreamWaitEvent(ctx->st2, ctx->ev_s[k], 0));
+			if ((rc = launch_eloc<T>(ctx, adj, a, b - a, ctx->st2, 2))) return rc;
+		}
+		CK(cudaEventRecord(ctx->ev_e, ctx->st2));
+		CK(cudaStreamWaitEvent(ctx->st, ctx->ev_e, 0));
+		if ((rc = launch_reduce<T>(ctx, adj))) return rc;
+		return launch_solve<T>(ctx, o->imaginary_time, o->precondition, o->lin_solver, o->ode_solver == 0 ? 2 : 1,
+		                       o->normalize_wf, o->dt, (o->use_adjoint == 2 && o->imaginary_time) ? 1 : 0);
+	}
 	if ((rc = launch_prep<T>(ctx))) return rc;
 	if (o->moves_per_stage > 0 && (rc = launch_sample<T>(ctx, o->moves_per_stage, o->mc_step, o->seed))) return rc;
 	if ((rc = launch_eloc<T>(ctx, o->use_adjoint != 0))) return rc;
@@ -741,10 +781,23 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 
 	cudaGetDevice(&c.device);
 	cudaDeviceGetAttribute(&c.nsm, cudaDevAttrMultiProcessorCount, c.device);
-	if (cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) != cudaSuccess) {
-		delete ctx;
+	if (cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) != cudaSuccess ||
+	    cudaStreamCreateWithFlags(&c.st2, cudaStreamNonBlocking) != cudaSuccess) {
+		tdvmc_destroy(ctx);
 		return TDVMC_ERR_CUDA;
 	}
+	for (int k = 0; k < tdvmc_ctx::kMaxChunks; k++)
+		if (cudaEventCreateWithFlags(&c.ev_s[k], cudaEventDisableTiming) != cudaSuccess) {
+			tdvmc_destroy(ctx);
+			return TDVMC_ERR_CUDA;
+		}
+	if (cudaEventCreateWithFlags(&c.ev_e, cudaEventDisableTiming) != cudaSuccess) {
+		tdvmc_destroy(ctx);
+		return TDVMC_ERR_CUDA;
+	}
+	// TDVMC_PIPELINE=k splits every sampling stage into k walker chunks (1 = off)
+	if (const char* pl = std::getenv("TDVMC_PIPELINE"))
+		c.pipeline = std::max(1, std::min(tdvmc_ctx::kMaxChunks, std::atoi(pl)));
 	const size_t ts = tsize(c.prec);
 	const int64_t nw = c.nw;
 	const int np = 2 * P + 2;
@@ -795,6 +848,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	A((void**)&c.partS, (size_t)c.nblkS * P * P * sizeof(float));
 	A((void**)&c.Sg, (size_t)P * P * sizeof(double));
 	A((void**)&c.dyn, sizeof(DynState));
+	A((void**)&c.chunk_starts, tdvmc_ctx::kMaxChunks * sizeof(int32_t));
 	if (!ok) {
 		tdvmc_destroy(ctx);
 		return TDVMC_ERR_NOMEM;
@@ -834,6 +888,11 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		else ((float*)pieceT.data())[i] = (float)piece[i];
 	}
 	DynState dy{};
+	std::vector<int32_t> starts(tdvmc_ctx::kMaxChunks, 0);
+	{
+		const int K = (int)std::min<int64_t>(c.pipeline, nw);
+		for (int k = 0; k < tdvmc_ctx::kMaxChunks; k++) starts[k] = (int32_t)(k < K ? nw * k / K : 0);
+	}
 	c.time = 0.0;
 	apply_quench(ctx, dy.pa, dy.pb);
 	std::vector<double> zeros((size_t)4 * np, 0.0);
@@ -844,6 +903,8 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	          cudaMemcpy(c.loc_d, c.loc.data(), c.loc.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.fold_d, c.fold.data(), c.fold.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.dyn, &dy, sizeof(dy), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.chunk_starts, starts.data(), starts.size() * sizeof(int32_t), cudaMemcpyHostToDevice) ==
+	              cudaSuccess &&
 	          cudaMemcpy(c.base, zeros.data(), np * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.stage, zeros.data(), np * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.kdot, zeros.data(), 4 * np * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -878,10 +939,15 @@ int tdvmc_destroy(tdvmc_ctx* ctx) {
 	void* bufs[] = {ctx->pos, ctx->lnpsi, ctx->O, ctx->eloc, ctx->other7, ctx->dE, ctx->acc, ctx->base, ctx->stage,
 	                ctx->kdot, ctx->rhs, ctx->loc_d, ctx->fold_d, ctx->coefU, ctx->coefC, ctx->uout, ctx->kb, ctx->hv,
 	                ctx->locT, ctx->lut, ctx->part1, ctx->means1, ctx->means0, ctx->part2, ctx->C2, ctx->partS, ctx->Sg,
-	                ctx->dyn, ctx->gramws, ctx->csD, ctx->csD2, ctx->csO, ctx->csV, ctx->csN, ctx->cs_piece, ctx->gbuf};
+	                ctx->dyn, ctx->gramws, ctx->csD, ctx->csD2, ctx->csO, ctx->csV, ctx->csN, ctx->cs_piece, ctx->gbuf,
+	                ctx->chunk_starts};
 	for (void* b : bufs)
 		if (b) cudaFree(b);
 	if (ctx->st) cudaStreamDestroy(ctx->st);
+	if (ctx->st2) cudaStreamDestroy(ctx->st2);
+	for (int k = 0; k < tdvmc_ctx::kMaxChunks; k++)
+		if (ctx->ev_s[k]) cudaEventDestroy(ctx->ev_s[k]);
+	if (ctx->ev_e) cudaEventDestroy(ctx->ev_e);
 	delete ctx;
 	return TDVMC_OK;
 }
