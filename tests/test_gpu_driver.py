@@ -43,6 +43,28 @@ def test_mixed_step_is_deterministic():
     assert np.array_equal(w1, w2)
 
 
+def test_chunk_pipeline_gives_the_same_step():
+    """TDVMC_PIPELINE=4 (chunks of walkers sampled on one stream and evaluated
+    on another) does the same per-walker work as the default back-to-back
+    stage, so parameters and walkers of two steps are bitwise equal."""
+    import tdvmc_gb300 as T
+    outs = []
+    for pipe in ("1", "4"):
+        os.environ["TDVMC_PIPELINE"] = pipe
+        try:
+            s = _system()
+        finally:
+            os.environ.pop("TDVMC_PIPELINE", None)
+        td = T.TDVP(s, 1e-3, 128, 0.25, seed=7, use_adjoint=1)
+        td.step(2)
+        outs.append((s.GetParameters(), s.GetWalkers()))
+        s.close()
+    (p1, w1), (p2, w2) = outs
+    assert np.array_equal(p1[0], p2[0]) and np.array_equal(p1[1], p2[1])
+    assert p1[2] == p2[2] and p1[3] == p2[3]
+    assert np.array_equal(w1, w2)
+
+
 def test_zero_variance_parameter_with_preconditioning_is_reported():
     """O_0 has no pair in its support, so S_00 = 0; the reference's diagonal
     scaling divides by zero (TDVMC.cpp:1690-1699).  The device reports the
