@@ -166,7 +166,9 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 				for (int o = G / 2; o > 0; o >>= 1) dsum += __shfl_xor_sync(gmask, dsum, o, G);
 				// exp(2 delta) >= U; a non-finite or overflowing quotient rejects (TDVMC.cpp:886-915)
 				const T two = T(2) * dsum;
-				const bool accept = isfinite(two) && (two >= lum) && ((double)two < kLogDblMax);
+				// the bound in T: no float lies between log(DBL_MAX) and its nearest float,
+				// so the comparison decides as the double one does
+				const bool accept = isfinite(two) && (two >= lum) && (two < (T)kLogDblMax);
 				if (accept) {
 					const int owner = p & (G - 1);
 					const int sp = p / G;
@@ -373,7 +375,7 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 				for (int o = G / 2; o > 0; o >>= 1) dsum += __shfl_xor_sync(gmask, dsum, o, G);
 				// exp(2 delta) >= U; a non-finite or overflowing quotient rejects (TDVMC.cpp:886-915)
 				const float two = 2.f * dsum;
-				const bool accept = isfinite(two) && (two >= lum) && ((double)two < kLogDblMax);
+				const bool accept = isfinite(two) && (two >= lum) && (two < (float)kLogDblMax);
 				if (accept) {
 					if (lane == (p & (G - 1))) {
 						xs[p] = Q4<float>{xn0, xn1, xn2, 0.f};
