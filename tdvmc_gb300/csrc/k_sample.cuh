@@ -253,10 +253,12 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 // float's bit pattern, so every pair beyond r_max reads the same (broadcast)
 // table entry.  The moved particle's own slot (old distance 0, kept finite by
 // a 1e-30 floor on r^2, which is below the rounding of any other r^2) and
-// slots past n are left out of the sum by predication.  A walker with a
-// coordinate outside [-L/2, L/2] after wrapping (non-finite or too large to
-// wrap exactly) makes no moves, as in the scalar sampler where every quotient
-// of such a walker is rejected, and a proposal outside is rejected.
+// slots past n are left out of the sum by predication.  Every table read is
+// in range for any input (r >= 0 puts the rounded index at 0 or above, the
+// integer min maps larger, infinite and NaN indices to entry nbin).  A walker
+// with a coordinate outside [-L/2, L/2] after wrapping (non-finite or too large
+// to wrap exactly) makes no moves, as in the scalar sampler where every
+// quotient of such a walker is rejected, and a proposal outside is rejected.
 template <int G, int SLOTS>
 __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
                                                    const float* __restrict__ uout_g, const float* __restrict__ kb_g,
