@@ -270,13 +270,18 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cu
                 int free = 0) {
 	if (count < 0) count = ctx->nw;
 	if (!st) st = ctx->st;
-	const int G = ctx->tiles.eg, gpb = ctx->tiles.egpb;
+	const int G = ctx->tiles.eg;
 	const int hist = G == 32 ? ctx->tiles.hist : 0;
 	ElocFn<T> fn = pick_eloc<T>(G, adj, hist);
 	RevFn<T> fr = adj ? pick_eloc_rev<T>(G, hist) : nullptr;
 	if (!fn || (adj && !fr)) return TDVMC_ERR_ARG;
 	const SysConst& s = ctx->sc;
 	if (adj && !ctx->gbuf) return TDVMC_ERR_STATE;  // ensure_gbuf was not called
+	// walkers per block: the tile value, fewer where a kernel's shared memory would not fit
+	constexpr size_t kSmemMax = 227 * 1024;
+	int gpb = ctx->tiles.egpb;
+	while (gpb > 1 && eloc_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * eloc_group_bytes<T>(s.n, s.nbin, s.ns, G) > kSmemMax)
+		gpb--;
 	const int threads = G * gpb;
 	const size_t smem = eloc_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * eloc_group_bytes<T>(s.n, s.nbin, s.ns, G);
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -294,12 +299,16 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cu
 	mark(ctx, "k_eloc");
 	CK(cudaGetLastError());
 	if (!adj) return TDVMC_OK;
-	const size_t smr = rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist);
+	int gpr = ctx->tiles.egpb;
+	while (gpr > 1 && rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpr * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist) > kSmemMax)
+		gpr--;
+	const int threads_r = G * gpr;
+	const size_t smr = rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpr * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist);
 	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
 	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributePreferredSharedMemoryCarveout,
 	                        (int)cudaSharedmemCarveoutMaxShared));
-	const int gridr = grid_for(ctx, (const void*)fr, threads, smr, count, gpb, free);
-	fr<<<gridr, threads, smr, st>>>(s, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT, ctx->fold_d,
+	const int gridr = grid_for(ctx, (const void*)fr, threads_r, smr, count, gpr, free);
+	fr<<<gridr, threads_r, smr, st>>>(s, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT, ctx->fold_d,
 	                                 (const T*)ctx->pos + w0 * dn, gb, count, (T*)ctx->dE + 2 * P * w0);
 	ctx->launches++;
 	mark(ctx, "k_eloc_rev");
@@ -925,6 +934,9 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	c.tiles.sgpb = 128 / c.tiles.sg;
 	c.tiles.eg = c.tiles.sg;
 	c.tiles.egpb = std::max(1, 32 / c.tiles.eg);
+	// TDVMC_EVAL_WALKERS_PER_BLOCK overrides the evaluation kernels' walkers per block
+	if (const char* e = std::getenv("TDVMC_EVAL_WALKERS_PER_BLOCK"))
+		c.tiles.egpb = std::max(1, std::min(128 / c.tiles.eg, std::atoi(e)));
 	if (const char* h = std::getenv("TDVMC_HIST")) c.tiles.hist = std::max(0, std::min(2, std::atoi(h)));
 	// TDVMC_SAMPLER=scalar selects the scalar FP32 sampler
 	if (const char* sm = std::getenv("TDVMC_SAMPLER")) c.packed_sampler = std::strcmp(sm, "scalar") != 0;
