@@ -227,7 +227,9 @@ int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, float* ms, 
  * walkers.  Results are kept in the context. */
 int tdvmc_autotune(tdvmc_ctx* ctx, int32_t moves, double mc_step);
 /* Report the chosen tiles: lanes per walker and walkers per block of the
- * sampler and the evaluation kernels. */
+ * sampler and the evaluation kernels (evaluation walkers per block 0: each
+ * evaluation kernel takes the count in {1, 2, 4} that keeps the most walkers
+ * resident per SM). */
 int tdvmc_get_tiles(tdvmc_ctx* ctx, int32_t* sample_lanes, int32_t* sample_walkers_per_block,
                     int32_t* eval_lanes, int32_t* eval_walkers_per_block);
 

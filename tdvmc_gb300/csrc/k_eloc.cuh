@@ -29,6 +29,7 @@
 namespace tdvmc {
 
 constexpr int kFwdMoments = 4;  // sum t^c, c = 0..3
+constexpr int G32 = 32;
 constexpr int kRevMoments = 6;  // complex sum g t^c, c = 0..2 (real part with (D-1)/r)
 // slots per interval and lane: the largest moment count of the kernel's
 // sweeps (4, or 6 with the adjoint), rounded to whole float4s in that mode
@@ -150,6 +151,8 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 // Shared memory layout of the forward kernel k_eloc:
 //   CTA:   coefC[3*nbin] (u', u'' coefficients) | kb[nbin] | hv[nbin] | lut[ncell]
 //   group: xs[n] {x, y, z, 0} | hist[nbin*4*G] | red[nbin*4]
+//   (FP32, 32-lane groups: xs[n].w and red, widened to [5][n], hold the row
+//   gradients of the half sweep until the histogram reduction)
 // and of the reverse (adjoint) kernel k_eloc_rev:
 //   CTA:   kb[nbin] | hv[nbin] | lut[ncell]
 //   group: xs[n] {x, y, z, gRx} | g4[n] {gRy, gRz, gIx, gIy} | gz[n] {gIz} | hist[nbin*NMH*G] | redr[nbin*6]
@@ -171,7 +174,9 @@ template <typename T>
 __host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G) {
 	size_t b = (size_t)n * sizeof(Q4<T>);
 	b += eloc_hist_len(nbin, ns, G, 4) * sizeof(T);
-	b += (size_t)nbin * kFwdMoments * sizeof(T);
+	size_t red = (size_t)nbin * kFwdMoments;
+	if (sizeof(T) == 4 && G == 32 && red < (size_t)5 * n) red = (size_t)5 * n;  // half sweep: gacc[5][n]
+	b += red * sizeof(T);
 	return (b + 31) & ~(size_t)31;
 }
 template <typename T>
@@ -435,6 +440,148 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 	}
 }
 
+// FP32 half sweep of the forward kernel for 32-lane groups: every unordered
+// pair once.  Rows come in slots of 32 (row s*32 + lane).  Slot s meets each
+// earlier slot sp in 32 rotation steps (at step k lane l pairs with row
+// sp*32 + (l + k) mod 32) and its own slot in steps 1..16 (step 16 for lanes
+// below 16 only), which meets every unordered pair exactly once.  The row's
+// gradient g d stays in registers; the partner's share (-g d) is collected in
+// a travelling sum trav that moves down the lanes with the rotation: before
+// step k lane l holds the sum for partner (l + k) mod 32, so after the 32
+// steps of a block it is back in the partner's lane (own slot: after 16 steps
+// it sits 17 lanes on).  kHalfSteps steps per iteration in two f32x2 streams;
+// the sum moves once per iteration, fed by one shuffle per step (p_j from
+// lane l + kHalfSteps - j), so its dependency chain is one shuffle long.  The
+// Laplacian enters the energy only as a total, twice the sum over pairs.
+constexpr int kHalfSteps = 4;
+template <bool DIAG, bool ADJ, int HIST>
+__device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n, int lane, bool rowok,
+                                               const Q4<float>& xr, const Q4<float>* __restrict__ xs,
+                                               const Q4<float>* __restrict__ coefC, const float* __restrict__ kb,
+                                               const float* __restrict__ hv, const int* __restrict__ lut,
+                                               float* __restrict__ hist, float pa, float pb, KSum<float>* own,
+                                               float* trav, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum,
+                                               int& nout) {
+	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
+	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
+	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mh2 = f2_make(-0.5f, -0.5f);
+	const float dm1 = (float)(sc.dim - 1);
+	const f2_t dm12 = f2_make(dm1, dm1);
+	const float ymax = kRoundF + (float)(sc.nbin - 1);
+	f2_t a2[6], l2R = f2_make(0.f, 0.f), l2I = f2_make(0.f, 0.f);
+#pragma unroll
+	for (int c = 0; c < 6; c++) a2[c] = f2_make(0.f, 0.f);
+	float vb = 0.f;
+	constexpr int k0 = DIAG ? 1 : 0, k1 = DIAG ? 17 : 32;
+	for (int k = k0; k < k1; k += kHalfSteps) {
+		float pj[kHalfSteps][6];  // g d of each step, R then I, x y z
+#pragma unroll
+		for (int h = 0; h < kHalfSteps / 2; h++) {
+			const int kA = k + 2 * h, kB = kA + 1;
+			const int ia = sp * 32 + ((lane + kA) & 31), ib = sp * 32 + ((lane + kB) & 31);
+			const bool okA = rowok && ia < n && (DIAG ? (kA < 16 || (kA == 16 && lane < 16)) : true);
+			const bool okB = rowok && ib < n && (DIAG ? (kB < 16 || (kB == 16 && lane < 16)) : true);
+			const Q4<float> pA = xs[ia < n ? ia : 0], pB = xs[ib < n ? ib : 0];
+			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
+			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
+			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
+			dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
+			dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
+			dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
+			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+			float ra, rb;
+			f2_split(r2, ra, rb);
+			const float qa = rsqrtf(ra), qb = rsqrtf(rb);
+			const f2_t r = f2_mul(r2, f2_make(qa, qb));
+			float rA, rB;
+			f2_split(r, rA, rB);
+			const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
+			float tA, tB;
+			int jA, jB;
+			if (sc.uniform) {
+				const f2_t x = f2_mul(r, H2);
+				float ya, yb;
+				f2_split(f2_add(f2_add(x, mh2), R2), ya, yb);
+				ya = fminf(ya, ymax);
+				yb = fminf(yb, ymax);
+				float xa, xb;
+				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
+				tA = xa;
+				tB = xb;
+				jA = __float_as_int(ya) - __float_as_int(kRoundF);
+				jB = __float_as_int(yb) - __float_as_int(kRoundF);
+			} else {
+				jA = locate<float>(sc, rA, kb, hv, lut, tA);
+				jB = locate<float>(sc, rB, kb, hv, lut, tB);
+			}
+			tA = inA ? tA : 0.f;
+			tB = inB ? tB : 0.f;
+			const Q4<float> cRA = coefC[3 * jA], cIA = coefC[3 * jA + 1], c2A = coefC[3 * jA + 2];
+			const Q4<float> cRB = coefC[3 * jB], cIB = coefC[3 * jB + 1], c2B = coefC[3 * jB + 2];
+			const f2_t d1R = f2_make(fmaf(tA, fmaf(tA, cRA.z, cRA.y), cRA.x), fmaf(tB, fmaf(tB, cRB.z, cRB.y), cRB.x));
+			const f2_t d1I = f2_make(fmaf(tA, fmaf(tA, cIA.z, cIA.y), cIA.x), fmaf(tB, fmaf(tB, cIB.z, cIB.y), cIB.x));
+			const f2_t d2R = f2_make(fmaf(tA, c2A.x, cRA.w), fmaf(tB, c2B.x, cRB.w));
+			const f2_t d2I = f2_make(fmaf(tA, c2A.y, cIA.w), fmaf(tB, c2B.y, cIB.w));
+			const f2_t sr = f2_make(inA ? qa : 0.f, inB ? qb : 0.f);
+			const f2_t on = f2_make(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
+			const f2_t gR = f2_mul(d1R, sr), gI = f2_mul(d1I, sr);
+			l2R = f2_add(l2R, f2_fma(dm12, gR, f2_mul(d2R, on)));
+			l2I = f2_add(l2I, f2_fma(dm12, gI, f2_mul(d2I, on)));
+			const f2_t q[6] = {f2_mul(gR, dx), f2_mul(gR, dy), f2_mul(gR, dz),
+			                   f2_mul(gI, dx), f2_mul(gI, dy), f2_mul(gI, dz)};
+#pragma unroll
+			for (int c = 0; c < 6; c++) {
+				a2[c] = f2_add(a2[c], q[c]);
+				f2_split(q[c], pj[2 * h][c], pj[2 * h + 1][c]);
+			}
+			// pair statistics: every pair met here is an unordered pair, counted once
+			if (HIST == 0) {
+				const float t2A = tA * tA, t2B = tB * tB;
+				const float vA[8] = {inA ? 1.f : 0.f, tA, t2A, t2A * tA, 0.f, 0.f, 0.f, 0.f};
+				const float vB[8] = {inB ? 1.f : 0.f, tB, t2B, t2B * tB, 0.f, 0.f, 0.f, 0.f};
+				hist_add_pair<HistSlots<HIST, false>::value, kFwdMoments, float, G32>(hist, jA, vA, jB, vB, lane);
+				vb += inA ? pair_pot<float>(sc.pot_kind, rA, qa, pa, pb) : 0.f;
+				vb += inB ? pair_pot<float>(sc.pot_kind, rB, qb, pa, pb) : 0.f;
+			} else {
+				FwdPair<float> fq;
+				fq.t = tA;
+				fq.j = jA;
+				fq.r = rA;
+				fq.rinv = qa;
+				fwd_stats<float, G32, ADJ, HIST>(sc, fq, inA, hist, lane, pa, pb, vb);
+				fq.t = tB;
+				fq.j = jB;
+				fq.r = rB;
+				fq.rinv = qb;
+				fwd_stats<float, G32, ADJ, HIST>(sc, fq, inB, hist, lane, pa, pb, vb);
+			}
+			nout += (okA && !(rA <= rmax)) ? 1 : 0;
+			nout += (okB && !(rB <= rmax)) ? 1 : 0;
+		}
+		// trav(l) <- trav(l + S) + p_0(l + S) + p_1(l + S - 1) + ... + p_{S-1}(l + 1), S = kHalfSteps
+#pragma unroll
+		for (int c = 0; c < 6; c++) {
+			float t = __shfl_sync(0xffffffffu, trav[c] + pj[0][c], (lane + kHalfSteps) & 31);
+#pragma unroll
+			for (int j = 1; j < kHalfSteps; j++) t += __shfl_sync(0xffffffffu, pj[j][c], (lane + kHalfSteps - j) & 31);
+			trav[c] = t;
+		}
+	}
+#pragma unroll
+	for (int c = 0; c < 6; c++) {
+		float lo, hi;
+		f2_split(a2[c], lo, hi);
+		own[c].add(lo + hi);
+	}
+	float lo, hi;
+	f2_split(l2R, lo, hi);
+	elR.add(2.f * (lo + hi));
+	f2_split(l2I, lo, hi);
+	elI.add(2.f * (lo + hi));
+	vsum.add(vb);
+}
+
 // Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), kNp
 // partners per iteration.
 template <typename T, int G, bool DIAG, int HIST>
@@ -644,6 +791,56 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 		KSum<T> e_r1, e_i1, e_r1i1, e_lR, e_lI, e_v;
 		int nout = 0;
 		T* gw = ADJ ? gout + (size_t)w * 6 * n : nullptr;
+		if constexpr (std::is_same<T, float>::value && G == 32) {
+			// half sweep; row gradients: gRx in xs[row].w, gRy..gIz in gacc[c-1][row] (the
+			// reduction area, free until the histogram reduction).  Lane l only touches rows = l mod 32.
+			float* gacc = red;
+			for (int i = lane; i < n; i += 32)
+#pragma unroll
+				for (int c = 0; c < 5; c++) gacc[c * n + i] = 0.f;
+			for (int s = 0; s < nslot; s++) {
+				const int nrow = s * 32 + lane;
+				const bool rowok = nrow < n;
+				const Q4<float> xr = rowok ? xs[nrow] : Q4<float>{0.f, 0.f, 0.f, 0.f};
+				KSum<float> own[6];
+				for (int sp = 0; sp < s; sp++) {
+					float trav[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+					half_block_f32<false, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
+					                                 own, trav, e_lR, e_lI, e_v, nout);
+					const int pr = sp * 32 + lane;  // the partners' shares are home
+					if (pr < n) {
+						xs[pr].w -= trav[0];
+#pragma unroll
+						for (int c = 1; c < 6; c++) gacc[(c - 1) * n + pr] -= trav[c];
+					}
+				}
+				float trav[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+				half_block_f32<true, ADJ, HIST>(sc, s, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
+				                                trav, e_lR, e_lI, e_v, nout);
+#pragma unroll
+				for (int c = 0; c < 6; c++) own[c].add(-__shfl_sync(0xffffffffu, trav[c], (lane + 15) & 31));
+				if (rowok) {  // later slots add their shares
+					xs[nrow].w = own[0].value();
+#pragma unroll
+					for (int c = 1; c < 6; c++) gacc[(c - 1) * n + nrow] = own[c].value();
+				}
+			}
+			for (int r = lane; r < n; r += 32) {
+				const float gRx = xs[r].w, gRy = gacc[r], gRz = gacc[n + r];
+				const float gIx = gacc[2 * n + r], gIy = gacc[3 * n + r], gIz = gacc[4 * n + r];
+				e_r1.add(gRx * gRx + gRy * gRy + gRz * gRz);
+				e_i1.add(gIx * gIx + gIy * gIy + gIz * gIz);
+				e_r1i1.add(2.f * (gRx * gIx + gRy * gIy + gRz * gIz));
+				if (ADJ) {
+					gw[r] = gRx;
+					gw[n + r] = gRy;
+					gw[2 * n + r] = gRz;
+					gw[3 * n + r] = gIx;
+					gw[4 * n + r] = gIy;
+					gw[5 * n + r] = gIz;
+				}
+			}
+		} else
 		for (int s = 0; s < nslot; s++) {
 			const int nrow = s * G + lane;
 			const bool rowok = nrow < n;

@@ -33,7 +33,7 @@ struct Tiles {
 	int sg = 32;     // sampler lanes per walker
 	int sgpb = 4;    // sampler walkers per block
 	int eg = 32;     // evaluation lanes per walker
-	int egpb = 1;    // evaluation walkers per block
+	int egpb = 0;    // evaluation walkers per block; 0: per kernel, the most walkers resident per SM
 	int hist = 0;    // histogram update mode of the evaluation kernel (full-warp groups)
 };
 
@@ -249,6 +249,36 @@ size_t eloc_smem(tdvmc_ctx* ctx, int G, int gpb, bool adj) {
 	return std::max(f, r);
 }
 
+// Walkers per block of an evaluation kernel (cta + gpb * grp bytes of shared
+// memory, G lanes per walker): `want` when positive, fewer where the shared
+// memory would not fit; else the count in {1, 2, 4} that keeps the most walkers
+// resident per SM (the smaller on a tie).  Sets the kernel's shared memory
+// attributes for the largest request; 0 if no count fits.
+int pick_gpb(const void* fn, int G, int want, size_t cta, size_t grp) {
+	constexpr size_t kSmemMax = 227 * 1024;
+	if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) != cudaSuccess ||
+	    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) !=
+	        cudaSuccess)
+		return 0;
+	if (want > 0) {
+		int g = want;
+		while (g > 1 && cta + (size_t)g * grp > kSmemMax) g--;
+		return cta + (size_t)g * grp <= kSmemMax ? g : 0;
+	}
+	int best = 0, best_w = 0;
+	for (int g : {1, 2, 4}) {
+		if (G * g > 128 || cta + (size_t)g * grp > kSmemMax) continue;
+		int blocks = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, G * g, cta + (size_t)g * grp) != cudaSuccess)
+			return 0;
+		if (blocks * g > best_w) {
+			best_w = blocks * g;
+			best = g;
+		}
+	}
+	return best;
+}
+
 // Gradient scratch of the adjoint (nw x 6 x n), allocated on first need and
 // always before a stream capture (allocation is not capturable).
 int ensure_gbuf(tdvmc_ctx* ctx) {
@@ -277,17 +307,11 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cu
 	if (!fn || (adj && !fr)) return TDVMC_ERR_ARG;
 	const SysConst& s = ctx->sc;
 	if (adj && !ctx->gbuf) return TDVMC_ERR_STATE;  // ensure_gbuf was not called
-	// walkers per block: the tile value, fewer where a kernel's shared memory would not fit
-	constexpr size_t kSmemMax = 227 * 1024;
-	int gpb = ctx->tiles.egpb;
-	while (gpb > 1 && eloc_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * eloc_group_bytes<T>(s.n, s.nbin, s.ns, G) > kSmemMax)
-		gpb--;
+	const size_t fcta = eloc_cta_bytes<T>(s.nbin, s.ncell), fgrp = eloc_group_bytes<T>(s.n, s.nbin, s.ns, G);
+	const int gpb = pick_gpb((const void*)fn, G, ctx->tiles.egpb, fcta, fgrp);
+	if (gpb < 1) return TDVMC_ERR_CUDA;
 	const int threads = G * gpb;
-	const size_t smem = eloc_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpb * eloc_group_bytes<T>(s.n, s.nbin, s.ns, G);
-	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	// shared memory limits the residency: ask for the largest carve-out
-	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributePreferredSharedMemoryCarveout,
-	                        (int)cudaSharedmemCarveoutMaxShared));
+	const size_t smem = fcta + (size_t)gpb * fgrp;
 	const int grid = grid_for(ctx, (const void*)fn, threads, smem, count, gpb, free);
 	const size_t P = (size_t)s.p, dn = (size_t)s.dim * s.n;
 	T* gb = adj ? (T*)ctx->gbuf + (size_t)w0 * 6 * s.n : nullptr;
@@ -299,14 +323,11 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cu
 	mark(ctx, "k_eloc");
 	CK(cudaGetLastError());
 	if (!adj) return TDVMC_OK;
-	int gpr = ctx->tiles.egpb;
-	while (gpr > 1 && rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpr * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist) > kSmemMax)
-		gpr--;
+	const size_t rcta = rev_cta_bytes<T>(s.nbin, s.ncell), rgrp = rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist);
+	const int gpr = pick_gpb((const void*)fr, G, ctx->tiles.egpb, rcta, rgrp);
+	if (gpr < 1) return TDVMC_ERR_CUDA;
 	const int threads_r = G * gpr;
-	const size_t smr = rev_cta_bytes<T>(s.nbin, s.ncell) + (size_t)gpr * rev_group_bytes<T>(s.n, s.nbin, s.ns, G, hist);
-	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
-	CK(cudaFuncSetAttribute((const void*)fr, cudaFuncAttributePreferredSharedMemoryCarveout,
-	                        (int)cudaSharedmemCarveoutMaxShared));
+	const size_t smr = rcta + (size_t)gpr * rgrp;
 	const int gridr = grid_for(ctx, (const void*)fr, threads_r, smr, count, gpr, free);
 	fr<<<gridr, threads_r, smr, st>>>(s, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut, (const T*)ctx->locT, ctx->fold_d,
 	                                 (const T*)ctx->pos + w0 * dn, gb, count, (T*)ctx->dE + 2 * P * w0);
@@ -933,7 +954,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	}
 	c.tiles.sgpb = 128 / c.tiles.sg;
 	c.tiles.eg = c.tiles.sg;
-	c.tiles.egpb = std::max(1, 32 / c.tiles.eg);
+	c.tiles.egpb = c.tiles.eg == 32 ? 0 : 32 / c.tiles.eg;
 	// TDVMC_EVAL_WALKERS_PER_BLOCK overrides the evaluation kernels' walkers per block
 	if (const char* e = std::getenv("TDVMC_EVAL_WALKERS_PER_BLOCK"))
 		c.tiles.egpb = std::max(1, std::min(128 / c.tiles.eg, std::atoi(e)));
@@ -1446,7 +1467,7 @@ int tdvmc_autotune(tdvmc_ctx* ctx, int32_t moves, double mc_step) {
 			CK(cudaMemcpyAsync(ctx->pos, save, bytes, cudaMemcpyDeviceToDevice, ctx->st));
 		}
 		if ((rc = ensure_gbuf(ctx))) break;
-		for (int gpb : {1, 2, 4}) {
+		for (int gpb : {0, 1, 2, 4}) {
 			if (G * gpb > 128) continue;
 			const size_t smem = ctx->prec == TDVMC_PREC_FP64 ? eloc_smem<double>(ctx, G, gpb, true)
 			                                                 : eloc_smem<float>(ctx, G, gpb, true);
