@@ -51,21 +51,38 @@ template <> struct V2<float> {
 template <> struct V2<double> {
 	using type = double2;
 };
-template <int NV, typename T>
+// A16: the record starts on a 16-byte boundary (FP32 records of 4k values move as float4)
+template <int NV, typename T, bool A16 = false>
 __device__ __forceinline__ void rec_load(const T* p, T* v) {
-	using VT = typename V2<T>::type;
+	if constexpr (A16 && sizeof(T) == 4 && NV % 4 == 0) {
 #pragma unroll
-	for (int m = 0; m < NV; m += 2) {
-		const VT a = *reinterpret_cast<const VT*>(p + m);
-		v[m] = a.x;
-		v[m + 1] = a.y;
+		for (int m = 0; m < NV; m += 4) {
+			const float4 a = *reinterpret_cast<const float4*>(p + m);
+			v[m] = a.x;
+			v[m + 1] = a.y;
+			v[m + 2] = a.z;
+			v[m + 3] = a.w;
+		}
+	} else {
+		using VT = typename V2<T>::type;
+#pragma unroll
+		for (int m = 0; m < NV; m += 2) {
+			const VT a = *reinterpret_cast<const VT*>(p + m);
+			v[m] = a.x;
+			v[m + 1] = a.y;
+		}
 	}
 }
-template <int NV, typename T>
+template <int NV, typename T, bool A16 = false>
 __device__ __forceinline__ void rec_store(T* p, const T* v) {
-	using VT = typename V2<T>::type;
+	if constexpr (A16 && sizeof(T) == 4 && NV % 4 == 0) {
 #pragma unroll
-	for (int m = 0; m < NV; m += 2) *reinterpret_cast<VT*>(p + m) = VT{v[m], v[m + 1]};
+		for (int m = 0; m < NV; m += 4) *reinterpret_cast<float4*>(p + m) = float4{v[m], v[m + 1], v[m + 2], v[m + 3]};
+	} else {
+		using VT = typename V2<T>::type;
+#pragma unroll
+		for (int m = 0; m < NV; m += 2) *reinterpret_cast<VT*>(p + m) = VT{v[m], v[m + 1]};
+	}
 }
 
 template <int HIST, int NMH, typename T, int G>
@@ -102,10 +119,10 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 			for (int m = 0; m < kRevMoments; m++) a[m] += v[m];
 			rec_store<kRevMoments>(hp, a);
 		} else {
-			rec_load<kFwdMoments>(hp, a);
+			rec_load<kFwdMoments, T, NMH % 4 == 0>(hp, a);
 #pragma unroll
 			for (int m = 0; m < kFwdMoments; m++) a[m] += v[m];
-			rec_store<kFwdMoments>(hp, a);
+			rec_store<kFwdMoments, T, NMH % 4 == 0>(hp, a);
 		}
 	}
 }
@@ -119,17 +136,18 @@ __device__ __forceinline__ void hist_add_pair(T* __restrict__ hist, int jA, cons
                                               const T (&vB)[8], int lane) {
 	T* hA = hist + ((size_t)jA * G + lane) * NMH;
 	T* hB = hist + ((size_t)jB * G + lane) * NMH;
+	constexpr bool A16 = NMH % 4 == 0;  // hist starts on a 16-byte boundary
 	T a[NV], b[NV];
-	rec_load<NV>(hA, a);
-	rec_load<NV>(hB, b);
+	rec_load<NV, T, A16>(hA, a);
+	rec_load<NV, T, A16>(hB, b);
 	const bool same = jA == jB;
 #pragma unroll
 	for (int m = 0; m < NV; m++) {
 		a[m] += same ? (vA[m] + vB[m]) : vA[m];
 		b[m] += vB[m];
 	}
-	rec_store<NV>(hA, a);
-	if (!same) rec_store<NV>(hB, b);
+	rec_store<NV, T, A16>(hA, a);
+	if (!same) rec_store<NV, T, A16>(hB, b);
 }
 
 // value of moment m of interval j summed over the group's lanes
@@ -454,6 +472,25 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 // lane l + kHalfSteps - j), so its dependency chain is one shuffle long.  The
 // Laplacian enters the energy only as a total, twice the sum over pairs.
 constexpr int kHalfSteps = 4;
+
+// Potential of two pairs into vb (pair_pot; Lennard-Jones in f32x2 with the
+// same operation order, the other kinds per pair).
+__device__ __forceinline__ void pair_pot2(int kind, float rA, float rB, float qa, float qb, bool inA, bool inB,
+                                          float pa, float pb, float& vb) {
+	float vA, vB;
+	if (kind == 3) {
+		f2_t s2 = f2_mul(f2_make(pa, pa), f2_make(qa, qb));
+		s2 = f2_mul(s2, s2);
+		const f2_t s6 = f2_mul(f2_mul(s2, s2), s2);
+		const float b4 = 4.f * pb;
+		f2_split(f2_mul(f2_mul(f2_make(b4, b4), s6), f2_sub(s6, f2_make(1.f, 1.f))), vA, vB);
+	} else {
+		vA = pair_pot<float>(kind, rA, qa, pa, pb);
+		vB = pair_pot<float>(kind, rB, qb, pa, pb);
+	}
+	vb += inA ? vA : 0.f;
+	vb += inB ? vB : 0.f;
+}
 template <bool DIAG, bool ADJ, int HIST>
 __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n, int lane, bool rowok,
                                                const Q4<float>& xr, const Q4<float>* __restrict__ xs,
@@ -479,10 +516,11 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 #pragma unroll
 		for (int h = 0; h < kHalfSteps / 2; h++) {
 			const int kA = k + 2 * h, kB = kA + 1;
+			// an earlier slot is full; the own slot may be the last, partial one
 			const int ia = sp * 32 + ((lane + kA) & 31), ib = sp * 32 + ((lane + kB) & 31);
-			const bool okA = rowok && ia < n && (DIAG ? (kA < 16 || (kA == 16 && lane < 16)) : true);
-			const bool okB = rowok && ib < n && (DIAG ? (kB < 16 || (kB == 16 && lane < 16)) : true);
-			const Q4<float> pA = xs[ia < n ? ia : 0], pB = xs[ib < n ? ib : 0];
+			const bool okA = DIAG ? (rowok && ia < n && (kA < 16 || (kA == 16 && lane < 16))) : rowok;
+			const bool okB = DIAG ? (rowok && ib < n && (kB < 16 || (kB == 16 && lane < 16))) : rowok;
+			const Q4<float> pA = xs[DIAG && ia >= n ? 0 : ia], pB = xs[DIAG && ib >= n ? 0 : ib];
 			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
 			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
@@ -541,8 +579,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 				const float vA[8] = {inA ? 1.f : 0.f, tA, t2A, t2A * tA, 0.f, 0.f, 0.f, 0.f};
 				const float vB[8] = {inB ? 1.f : 0.f, tB, t2B, t2B * tB, 0.f, 0.f, 0.f, 0.f};
 				hist_add_pair<HistSlots<HIST, false>::value, kFwdMoments, float, G32>(hist, jA, vA, jB, vB, lane);
-				vb += inA ? pair_pot<float>(sc.pot_kind, rA, qa, pa, pb) : 0.f;
-				vb += inB ? pair_pot<float>(sc.pot_kind, rB, qb, pa, pb) : 0.f;
+				pair_pot2(sc.pot_kind, rA, rB, qa, qb, inA, inB, pa, pb, vb);
 			} else {
 				FwdPair<float> fq;
 				fq.t = tA;
