@@ -76,7 +76,14 @@ __device__ __forceinline__ int floor_clamp(double x, int jmax, double& jf) {
 	return (int)(__double_as_longlong(y) - __double_as_longlong(kRoundD));
 }
 
-__device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
+// FP32: the hardware reciprocal square root (PTX rsqrt.approx.ftz.f32) without
+// handling for subnormal arguments: squared pair distances are either normal
+// or exactly 0 (a masked self pair, giving +inf as before).
+__device__ __forceinline__ float rsqrt_(float x) {
+	float r;
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return r;
+}
 __device__ __forceinline__ double rsqrt_(double x) { return rsqrt(x); }
 
 // Interval lookup over [0, r_max]: returns j (interval index; knot k_{j+3})

@@ -369,7 +369,7 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 				const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
 				float ra, rb;
 				f2_split(r2, ra, rb);
-				const float qa = rsqrtf(ra), qb = rsqrtf(rb);
+				const float qa = rsqrt_(ra), qb = rsqrt_(rb);
 				const f2_t r = f2_mul(r2, f2_make(qa, qb));
 				float rA, rB;
 				f2_split(r, rA, rB);
@@ -530,7 +530,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
 			float ra, rb;
 			f2_split(r2, ra, rb);
-			const float qa = rsqrtf(ra), qb = rsqrtf(rb);
+			const float qa = rsqrt_(ra), qb = rsqrt_(rb);
 			const f2_t r = f2_mul(r2, f2_make(qa, qb));
 			float rA, rB;
 			f2_split(r, rA, rB);
@@ -701,7 +701,7 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
 			float ra, rb;
 			f2_split(r2, ra, rb);
-			const float qa = rsqrtf(ra), qb = rsqrtf(rb);
+			const float qa = rsqrt_(ra), qb = rsqrt_(rb);
 			const f2_t r = f2_mul(r2, f2_make(qa, qb));
 			float rA, rB;
 			f2_split(r, rA, rB);

@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 					const f2_t r2 = f2_fma(mz, mz, f2_fma(my, my, f2_fma(mx, mx, tiny2)));
 					float ra, rb;
 					f2_split(r2, ra, rb);
-					const f2_t r = f2_mul(r2, f2_make(rsqrtf(ra), rsqrtf(rb)));
+					const f2_t r = f2_mul(r2, f2_make(rsqrt_(ra), rsqrt_(rb)));
 					// floor(x) = round(x - 1/2), x = r / h (see nic)
 					const f2_t xm = f2_fma(r, H2, mhalf2);
 					const f2_t yv = f2_add(xm, R2);
