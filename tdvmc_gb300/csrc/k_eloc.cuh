@@ -43,7 +43,11 @@ template <int HIST, bool ADJ> struct HistSlots {
 //   2  shared-memory atomic add      layout of 0 (no contention: lane-private)
 // In mode 0 a lane's NMH moments of one interval are contiguous (NMH even), so
 // they move as 8-byte (FP32) or 16-byte (FP64) vectors; records of 24 or 48
-// bytes map the lanes of each access phase to distinct banks.
+// bytes map the lanes of each access phase to distinct banks.  FP32 records
+// of 4 moments move as one float4; FP32 records of 6 moments are split per
+// interval into a float4 block and a float2 block,
+//   hist[j*6G + lane*4 + m] (m < 4),  hist[j*6G + 4G + lane*2 + m - 4] (m >= 4),
+// two accesses instead of three, still one bank group per lane.
 template <typename T> struct V2;
 template <> struct V2<float> {
 	using type = float2;
@@ -85,6 +89,28 @@ __device__ __forceinline__ void rec_store(T* p, const T* v) {
 	}
 }
 
+template <int G>
+__device__ __forceinline__ void rec6_load(const float* hist, int j, int lane, float* v) {
+	const float* b = hist + (size_t)j * 6 * G;
+	const float4 a = *reinterpret_cast<const float4*>(b + lane * 4);
+	const float2 c = *reinterpret_cast<const float2*>(b + 4 * G + lane * 2);
+	v[0] = a.x;
+	v[1] = a.y;
+	v[2] = a.z;
+	v[3] = a.w;
+	v[4] = c.x;
+	v[5] = c.y;
+}
+template <int G>
+__device__ __forceinline__ void rec6_store(float* hist, int j, int lane, const float* v) {
+	float* b = hist + (size_t)j * 6 * G;
+	*reinterpret_cast<float4*>(b + lane * 4) = float4{v[0], v[1], v[2], v[3]};
+	*reinterpret_cast<float2*>(b + 4 * G + lane * 2) = float2{v[4], v[5]};
+}
+// FP32 six-moment records in mode 0 use the split layout
+template <int HIST, int NMH, typename T>
+constexpr bool kSplit6 = HIST == 0 && NMH == 6 && sizeof(T) == 4;
+
 template <int HIST, int NMH, typename T, int G>
 __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane, const T (&v)[8], int nv) {
 	if (HIST == 1) {
@@ -110,6 +136,12 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 			if (m >= nv) break;
 			atomicAdd(hp + m, v[m]);
 		}
+	} else if constexpr (kSplit6<HIST, NMH, T>) {
+		float a[6];
+		rec6_load<G>(hist, j, lane, a);
+#pragma unroll
+		for (int m = 0; m < 6; m++) a[m] += m < nv ? v[m] : 0.f;
+		rec6_store<G>(hist, j, lane, a);
 	} else {
 		T* hp = hist + ((size_t)j * G + lane) * NMH;
 		T a[8];
@@ -136,6 +168,20 @@ __device__ __forceinline__ void hist_add_pair(T* __restrict__ hist, int jA, cons
                                               const T (&vB)[8], int lane) {
 	T* hA = hist + ((size_t)jA * G + lane) * NMH;
 	T* hB = hist + ((size_t)jB * G + lane) * NMH;
+	if constexpr (kSplit6<0, NMH, T> && NV == 6) {
+		float a[6], b[6];
+		rec6_load<G>(hist, jA, lane, a);
+		rec6_load<G>(hist, jB, lane, b);
+		const bool same = jA == jB;
+#pragma unroll
+		for (int m = 0; m < 6; m++) {
+			a[m] += same ? (vA[m] + vB[m]) : vA[m];
+			b[m] += vB[m];
+		}
+		rec6_store<G>(hist, jA, lane, a);
+		if (!same) rec6_store<G>(hist, jB, lane, b);
+		return;
+	}
 	constexpr bool A16 = NMH % 4 == 0;  // hist starts on a 16-byte boundary
 	T a[NV], b[NV];
 	rec_load<NV, T, A16>(hA, a);
@@ -158,6 +204,11 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 		const T* h = hist + (((size_t)j * (NMH / 4) + m / 4) * G) * 4 + (m & 3);
 #pragma unroll 8
 		for (int l = 0; l < G; l++) s += h[l * 4];
+	} else if constexpr (kSplit6<HIST, NMH, T>) {
+		const T* h = hist + (size_t)j * 6 * G + (m < 4 ? m : 4 * G + (m - 4));
+		const int st = m < 4 ? 4 : 2;
+#pragma unroll 8
+		for (int l = 0; l < G; l++) s += h[l * st];
 	} else {
 		const T* h = hist + (size_t)j * G * NMH + m;
 #pragma unroll 8
@@ -686,8 +737,9 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 	for (int i = i0; i < i1; i += 2 * kF2) {
 #pragma unroll
 		for (int h = 0; h < kF2; h++) {
+			// the off-diagonal range [0, s*G) is a whole number of iterations
 			const int iA = i + 2 * h, iB = iA + 1;
-			const bool haveA = iA < i1, haveB = iB < i1;
+			const bool haveA = DIAG ? iA < i1 : true, haveB = DIAG ? iB < i1 : true;
 			const int ia = haveA ? iA : i, ib = haveB ? iB : i;
 			const Q4<float> pA = xs[ia], pB = xs[ib];  // .w = gRx of the partner
 			const Q4<float> gA = g4[ia], gB = g4[ib];
