@@ -718,7 +718,11 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 
 // FP32 reverse sweep with partner pairs in f32x2 arithmetic (same pairs and
 // moments as rev_region): kF2 packed pairs per iteration.
-template <int G, bool DIAG, int HIST>
+// ROT (own slot, 32-lane groups): instead of the partners i < nrow of the
+// slot [i0, i1), lane l meets row i0 + (l + k) mod 32 at steps k = 1..16
+// (step 16 for lanes below 16 only), every unordered pair of the slot once
+// with no idle lanes; the pair terms do not depend on which row is first.
+template <int G, bool DIAG, int HIST, bool ROT = false>
 __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1, int nrow, bool rowok,
                                               const Q4<float>& xr, const float* gn, const Q4<float>* __restrict__ xs,
                                               const Q4<float>* __restrict__ g4, const float* __restrict__ gz,
@@ -734,13 +738,28 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 	f2_t GN[6];
 #pragma unroll
 	for (int k = 0; k < 6; k++) GN[k] = f2_make(gn[k], gn[k]);
-	for (int i = i0; i < i1; i += 2 * kF2) {
+	static_assert(!ROT || (DIAG && G == 32), "rotation only for the own slot of 32-lane groups");
+	for (int i = ROT ? 1 : i0; i < (ROT ? 17 : i1); i += 2 * kF2) {
 #pragma unroll
 		for (int h = 0; h < kF2; h++) {
-			// the off-diagonal range [0, s*G) is a whole number of iterations
-			const int iA = i + 2 * h, iB = iA + 1;
-			const bool haveA = DIAG ? iA < i1 : true, haveB = DIAG ? iB < i1 : true;
-			const int ia = haveA ? iA : i, ib = haveB ? iB : i;
+			int ia, ib;
+			bool haveA, haveB;
+			if (ROT) {
+				const int kA = i + 2 * h, kB = kA + 1;
+				ia = i0 + ((lane + kA) & 31);
+				ib = i0 + ((lane + kB) & 31);
+				haveA = ia < i1 && (kA < 16 || lane < 16);
+				haveB = ib < i1 && (kB < 16 || lane < 16);
+				ia = haveA ? ia : i0;
+				ib = haveB ? ib : i0;
+			} else {
+				// the off-diagonal range [0, s*G) is a whole number of iterations
+				const int iA = i + 2 * h, iB = iA + 1;
+				haveA = DIAG ? iA < i1 : true;
+				haveB = DIAG ? iB < i1 : true;
+				ia = haveA ? iA : i;
+				ib = haveB ? iB : i;
+			}
 			const Q4<float> pA = xs[ia], pB = xs[ib];  // .w = gRx of the partner
 			const Q4<float> gA = g4[ia], gB = g4[ib];
 			const float zA = gz[ia], zB = gz[ib];
@@ -757,8 +776,8 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			const f2_t r = f2_mul(r2, f2_make(qa, qb));
 			float rA, rB;
 			f2_split(r, rA, rB);
-			const bool onA = haveA && rowok && (rA <= rmax) && (DIAG ? (ia < nrow) : true);
-			const bool onB = haveB && rowok && (rB <= rmax) && (DIAG ? (ib < nrow) : true);
+			const bool onA = haveA && rowok && (rA <= rmax) && ((DIAG && !ROT) ? (ia < nrow) : true);
+			const bool onB = haveB && rowok && (rB <= rmax) && ((DIAG && !ROT) ? (ib < nrow) : true);
 			float tA, tB;
 			int jA, jB;
 			if (sc.uniform) {
@@ -1113,7 +1132,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __res
 			const int dend = (base + G < n) ? base + G : n;
 			if constexpr (std::is_same<T, float>::value) {
 				rev_region_f2<G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-				rev_region_f2<G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				rev_region_f2<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
 			} else {
 				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
 				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
