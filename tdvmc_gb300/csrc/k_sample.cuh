@@ -303,23 +303,29 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 		int64_t w = w0 + wi;
 		if (w >= nw_total) w -= nw_total;
 		float* pw = pos + (size_t)w * sc.dim * n;
-		float X[SLOTS], Y[SLOTS], Z[SLOTS];
+		// own particles in slot pairs (slot s: pair s / 2, half s % 2), so the
+		// differences of two slots to a moving particle are one f32x2 subtraction
+		constexpr int NP = (SLOTS + 1) / 2;
+		f2_t PX[NP], PY[NP], PZ[NP];
 		bool inside = true;
 #pragma unroll
-		for (int s = 0; s < SLOTS; s++) {
-			const int i = s * G + lane;
-			float x = 0.f, y = 0.f, z = 0.f;
-			if (i < n) {
-				// positions into [-L/2, L/2] (AlignCoordinates, TDVMC.cpp:2569-2582)
-				x = nic(pw[i], L, Lr);
-				if (sc.dim > 1) y = nic(pw[n + i], L, Lr);
-				if (sc.dim > 2) z = nic(pw[2 * n + i], L, Lr);
-				inside = inside && fabsf(x) <= half && fabsf(y) <= half && fabsf(z) <= half;
-				xs[i] = Q4<float>{x, y, z, 0.f};
+		for (int k = 0; k < NP; k++) {
+			float x[2] = {0.f, 0.f}, y[2] = {0.f, 0.f}, z[2] = {0.f, 0.f};
+#pragma unroll
+			for (int h = 0; h < 2; h++) {
+				const int i = (2 * k + h) * G + lane;
+				if (2 * k + h < SLOTS && i < n) {
+					// positions into [-L/2, L/2] (AlignCoordinates, TDVMC.cpp:2569-2582)
+					x[h] = nic(pw[i], L, Lr);
+					if (sc.dim > 1) y[h] = nic(pw[n + i], L, Lr);
+					if (sc.dim > 2) z[h] = nic(pw[2 * n + i], L, Lr);
+					inside = inside && fabsf(x[h]) <= half && fabsf(y[h]) <= half && fabsf(z[h]) <= half;
+					xs[i] = Q4<float>{x[h], y[h], z[h], 0.f};
+				}
 			}
-			X[s] = x;
-			Y[s] = y;
-			Z[s] = z;
+			PX[k] = f2_make(x[0], x[1]);
+			PY[k] = f2_make(y[0], y[1]);
+			PZ[k] = f2_make(z[0], z[1]);
 		}
 		const bool walker_ok = __all_sync(gmask, inside);
 		__syncwarp(gmask);
@@ -346,11 +352,26 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 				if (!(fabsf(xn0) <= half && fabsf(xn1) <= half && fabsf(xn2) <= half)) continue;  // uniform over the group
 				const int self_slot = (lane == (p & (G - 1))) ? p / G : -1;
 				float dsum = 0.f;
+				const f2_t N0 = f2_make(xn0, xn0), N1 = f2_make(xn1, xn1), N2 = f2_make(xn2, xn2);
+				const f2_t O0 = f2_make(xo.x, xo.x), O1 = f2_make(xo.y, xo.y), O2 = f2_make(xo.z, xo.z);
 #pragma unroll
 				for (int s = 0; s < SLOTS; s++) {
-					const float an = X[s] - xn0, ao = X[s] - xo.x;
-					const float bn = Y[s] - xn1, bo = Y[s] - xo.y;
-					const float cn = Z[s] - xn2, co = Z[s] - xo.z;
+					float an, ao, bn, bo, cn, co;
+					{
+						float d[2];
+						f2_split(f2_sub(PX[s / 2], N0), d[0], d[1]);
+						an = d[s & 1];
+						f2_split(f2_sub(PX[s / 2], O0), d[0], d[1]);
+						ao = d[s & 1];
+						f2_split(f2_sub(PY[s / 2], N1), d[0], d[1]);
+						bn = d[s & 1];
+						f2_split(f2_sub(PY[s / 2], O1), d[0], d[1]);
+						bo = d[s & 1];
+						f2_split(f2_sub(PZ[s / 2], N2), d[0], d[1]);
+						cn = d[s & 1];
+						f2_split(f2_sub(PZ[s / 2], O2), d[0], d[1]);
+						co = d[s & 1];
+					}
 					const f2_t mx = f2_make(fminf(fabsf(an), L - fabsf(an)), fminf(fabsf(ao), L - fabsf(ao)));
 					const f2_t my = f2_make(fminf(fabsf(bn), L - fabsf(bn)), fminf(fabsf(bo), L - fabsf(bo)));
 					const f2_t mz = f2_make(fminf(fabsf(cn), L - fabsf(cn)), fminf(fabsf(co), L - fabsf(co)));
@@ -383,13 +404,18 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 						xs[p] = Q4<float>{xn0, xn1, xn2, 0.f};
 						const float nx = xn0, ny = xn1, nz = xn2;
 						switch (p / G) {
-#define TDVMC_SET_SLOT(S)                  \
-	case S:                                \
-		if (S < SLOTS) {                   \
-			X[S < SLOTS ? S : 0] = nx;     \
-			Y[S < SLOTS ? S : 0] = ny;     \
-			Z[S < SLOTS ? S : 0] = nz;     \
-		}                                  \
+#define TDVMC_SET_SLOT(S)                                              \
+	case S:                                                            \
+		if (S < SLOTS) {                                               \
+			constexpr int k = S < SLOTS ? S / 2 : 0;                   \
+			float a0, a1;                                              \
+			f2_split(PX[k], a0, a1);                                   \
+			PX[k] = (S & 1) ? f2_make(a0, nx) : f2_make(nx, a1);       \
+			f2_split(PY[k], a0, a1);                                   \
+			PY[k] = (S & 1) ? f2_make(a0, ny) : f2_make(ny, a1);       \
+			f2_split(PZ[k], a0, a1);                                   \
+			PZ[k] = (S & 1) ? f2_make(a0, nz) : f2_make(nz, a1);       \
+		}                                                              \
 		break;
 							TDVMC_SET_SLOT(0) TDVMC_SET_SLOT(1) TDVMC_SET_SLOT(2) TDVMC_SET_SLOT(3)
 							TDVMC_SET_SLOT(4) TDVMC_SET_SLOT(5) TDVMC_SET_SLOT(6) TDVMC_SET_SLOT(7)
@@ -407,9 +433,13 @@ __global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>*
 		for (int s = 0; s < SLOTS && walker_ok; s++) {
 			const int i = s * G + lane;
 			if (i < n) {
-				pw[i] = X[s];
-				if (sc.dim > 1) pw[n + i] = Y[s];
-				if (sc.dim > 2) pw[2 * n + i] = Z[s];
+				float d[2];
+				f2_split(PX[s / 2], d[0], d[1]);
+				pw[i] = d[s & 1];
+				f2_split(PY[s / 2], d[0], d[1]);
+				if (sc.dim > 1) pw[n + i] = d[s & 1];
+				f2_split(PZ[s / 2], d[0], d[1]);
+				if (sc.dim > 2) pw[2 * n + i] = d[s & 1];
 			}
 		}
 		if (lane == 0) acc_out[w] = nacc;
