@@ -548,8 +548,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
                                                const Q4<float>* __restrict__ coefC, const float* __restrict__ kb,
                                                const float* __restrict__ hv, const int* __restrict__ lut,
                                                float* __restrict__ hist, float pa, float pb, KSum<float>* own,
-                                               float* trav, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum,
-                                               int& nout) {
+                                               float* trav, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum) {
 	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
@@ -644,8 +643,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 				fq.rinv = qb;
 				fwd_stats<float, G32, ADJ, HIST>(sc, fq, inB, hist, lane, pa, pb, vb);
 			}
-			nout += (okA && !(rA <= rmax)) ? 1 : 0;
-			nout += (okB && !(rB <= rmax)) ? 1 : 0;
+			// pairs beyond r_max are counted by the caller (all pairs less those in moment 0)
 		}
 		// trav(l) <- trav(l + S) + p_0(l + S) + p_1(l + S - 1) + ... + p_{S-1}(l + 1), S = kHalfSteps
 #pragma unroll
@@ -914,7 +912,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				for (int sp = 0; sp < s; sp++) {
 					float trav[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 					half_block_f32<false, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
-					                                 own, trav, e_lR, e_lI, e_v, nout);
+					                                 own, trav, e_lR, e_lI, e_v);
 					const int pr = sp * 32 + lane;  // the partners' shares are home
 					if (pr < n) {
 						xs[pr].w -= trav[0];
@@ -924,7 +922,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				}
 				float trav[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 				half_block_f32<true, ADJ, HIST>(sc, s, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
-				                                trav, e_lR, e_lI, e_v, nout);
+				                                trav, e_lR, e_lI, e_v);
 #pragma unroll
 				for (int c = 0; c < 6; c++) own[c].add(-__shfl_sync(0xffffffffu, trav[c], (lane + 15) & 31));
 				if (rowok) {  // later slots add their shares
@@ -995,6 +993,13 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 		for (int o = G / 2; o > 0; o >>= 1) nout_all += __shfl_xor_sync(gmask, nout_all, o, G);
 
 		hist_reduce<T, G, HIST, NMH>(hist, red, nbin, NM, lane, gmask);
+		if constexpr (std::is_same<T, float>::value && G == 32) {
+			// half sweep: pairs beyond r_max are all pairs less those in moment 0
+			// (integer counts below 2^24, exact in FP32)
+			float m0 = 0.f;
+			for (int j = 0; j < nbin; j++) m0 += red[j * NM];
+			nout_all = n * (n - 1) / 2 - (int)m0;
+		}
 
 		// moments -> spline values: spline sp = j + 3 - q on interval j
 		for (int sp = lane; sp < ns; sp += G) {
