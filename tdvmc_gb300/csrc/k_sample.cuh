@@ -246,9 +246,12 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 // Per register slot the distances of the slot's particle to the proposed and
 // to the old position of the moved particle are one f32x2 instruction stream
 // from r^2 on (r^2, r, the interval index by the float-rounding trick, the
-// local coordinate); the differences and the per-axis minimum image
-// min(|d|, L - |d|) stay scalar, so the min runs on the ALU pipe beside the
-// FMA pipe and each coordinate is held once.  The interval
+// local coordinate).  The lane's own coordinates are held once, in slot pairs,
+// so the differences of two slots to the moved particle are one f32x2
+// subtraction; the per-axis minimum image min(|d|, L - |d|) stays scalar, so
+// the min runs on the ALU pipe beside the FMA pipe.  Up to 11 slots the kernel
+// is compiled for 5 blocks per SM (a few spilled registers cost less than the
+// fifth block gains).  The interval
 // index is clamped to the outer-pair entry nbin with one integer min on the
 // float's bit pattern, so every pair beyond r_max reads the same (broadcast)
 // table entry.  The moved particle's own slot (old distance 0, kept finite by
@@ -260,7 +263,7 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 // to wrap exactly) makes no moves, as in the scalar sampler where every
 // quotient of such a walker is rejected, and a proposal outside is rejected.
 template <int G, int SLOTS>
-__global__ void __launch_bounds__(128) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
+__global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 4) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
                                                    const float* __restrict__ uout_g, const float* __restrict__ kb_g,
                                                    const float* __restrict__ hv_g, const int* __restrict__ lut_g,
                                                    float* __restrict__ pos, int64_t nw, int64_t nw_total,
