@@ -263,7 +263,7 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 // to wrap exactly) makes no moves, as in the scalar sampler where every
 // quotient of such a walker is rejected, and a proposal outside is rejected.
 template <int G, int SLOTS>
-__global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 1) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
+__global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
                                                    const float* __restrict__ uout_g, const float* __restrict__ kb_g,
                                                    const float* __restrict__ hv_g, const int* __restrict__ lut_g,
                                                    float* __restrict__ pos, int64_t nw, int64_t nw_total,
