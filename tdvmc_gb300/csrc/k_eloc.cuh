@@ -561,8 +561,25 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 	for (int c = 0; c < 6; c++) a2[c] = f2_make(0.f, 0.f);
 	float vb = 0.f;
 	constexpr int k0 = DIAG ? 1 : 0, k1 = DIAG ? 17 : 32;
+	// partner rows of the next iteration are loaded one iteration ahead
+	Q4<float> nxt[kHalfSteps];
+#pragma unroll
+	for (int j = 0; j < kHalfSteps; j++) {
+		const int i = sp * 32 + ((lane + k0 + j) & 31);
+		nxt[j] = xs[DIAG && i >= n ? 0 : i];
+	}
 	for (int k = k0; k < k1; k += kHalfSteps) {
 		float pj[kHalfSteps][6];  // g d of each step, R then I, x y z
+		Q4<float> cur[kHalfSteps];
+#pragma unroll
+		for (int j = 0; j < kHalfSteps; j++) cur[j] = nxt[j];
+		if (k + kHalfSteps < k1) {
+#pragma unroll
+			for (int j = 0; j < kHalfSteps; j++) {
+				const int i = sp * 32 + ((lane + k + kHalfSteps + j) & 31);
+				nxt[j] = xs[DIAG && i >= n ? 0 : i];
+			}
+		}
 #pragma unroll
 		for (int h = 0; h < kHalfSteps / 2; h++) {
 			const int kA = k + 2 * h, kB = kA + 1;
@@ -570,7 +587,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			const int ia = sp * 32 + ((lane + kA) & 31), ib = sp * 32 + ((lane + kB) & 31);
 			const bool okA = DIAG ? (rowok && ia < n && (kA < 16 || (kA == 16 && lane < 16))) : rowok;
 			const bool okB = DIAG ? (rowok && ib < n && (kB < 16 || (kB == 16 && lane < 16))) : rowok;
-			const Q4<float> pA = xs[DIAG && ia >= n ? 0 : ia], pB = xs[DIAG && ib >= n ? 0 : ib];
+			const Q4<float> pA = cur[2 * h], pB = cur[2 * h + 1];
 			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
 			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
