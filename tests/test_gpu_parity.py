@@ -260,6 +260,36 @@ def test_ragged_sizes_match_oracle(nw, n, dim):
         assert np.abs(dE[w] - r["dE"]).max() < 1e-12 * max(np.abs(r["dE"]).max(), 1.0)
 
 
+@pytest.mark.parametrize("n", [65, 80, 96, 111, 337])
+def test_half_sweep_slot_edges_mixed(n):
+    """FP32 32-lane evaluation (the half sweep of the forward kernel and the rotated
+    own slot of the adjoint) at particle counts that leave the last slot of 32 rows
+    with 1, 16, 32, 15 and 17 rows; tolerances as in the fixture cases (1e-5, dE 3e-5)."""
+    import tdvmc_gb300 as T
+    dim, p, nw = 3, 12, 9
+    L = (n / 0.4) ** (1.0 / dim)
+    rng = np.random.default_rng(n)
+    R = rng.uniform(-L / 2, L / 2, size=(nw, dim, n))
+    uR, uI = rng.normal(0, 0.2, p), rng.normal(0, 0.1, p)
+    sysp = (0.5, 2.0)
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=sysp, potential="gauss", hbar2_2m=0.09, precision="mixed")
+    assert s.Tiles()["eval_lanes"] == 32
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R)
+    f = s.CalculateExpectationValues()
+    dE = s.CalculateLocalEnergyAdjoint()
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_GAUSS, pot=sysp, hbar2_2m=0.09)
+    tol = 1e-5
+    for w in range(nw):
+        r = o.eval(uR, uI, R[w].T, adjoint=True)
+        assert abs(f["lnpsi"][w] - r["lnpsi"]) < tol * max(abs(r["lnpsi"]), np.abs(uR).max() * n)
+        assert relmax(f["O"][w], r["O"]) < tol
+        sc = max(np.abs(r["other"]).max(), 1.0)
+        assert np.abs(f["eloc"][w] - r["eloc"]).max() < tol * sc
+        assert np.abs(f["other"][w] - r["other"]).max() < tol * sc
+        assert np.abs(dE[w] - r["dE"]).max() < 3e-5 * max(np.abs(r["dE"]).max(), 1.0)
+
+
 def test_adjoint_driven_imaginary_time_step_matches_oracle_fp64():
     """Imaginary-time Euler step with the adjoint in the force:
     F_k = -(cov(O_k, E^R) + <dE_loc/d uR_k> / 2), i.e. -1/2 d<E>/d uR_k."""
