@@ -85,6 +85,15 @@ __device__ __forceinline__ float rsqrt_(float x) {
 	return r;
 }
 __device__ __forceinline__ double rsqrt_(double x) { return rsqrt(x); }
+// Pair distance from its square in the samplers: FP32 the hardware square root
+// (PTX sqrt.approx.ftz.f32, one instruction; r^2 is never subnormal there),
+// FP64 r^2 / sqrt(r^2) as r^2 * rsqrt(r^2).
+__device__ __forceinline__ float pair_r(float r2) {
+	float r;
+	asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(r2));
+	return r;
+}
+__device__ __forceinline__ double pair_r(double r2) { return r2 * rsqrt_(r2); }
 
 // Interval lookup over [0, r_max]: returns j (interval index; knot k_{j+3})
 // and the local coordinate t in [0, 1].  kb[j] = left knot, hv[j] = 1/width,

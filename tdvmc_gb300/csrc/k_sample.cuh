@@ -32,8 +32,7 @@ template <typename T>
 __device__ __forceinline__ T pair_u(const SysConst& sc, T r2, const Q4<T>* __restrict__ coef,
                                     const T* __restrict__ kb, const T* __restrict__ hv,
                                     const int* __restrict__ lut) {
-	const T rinv = rsqrt_(r2);
-	const T r = r2 * rinv;
+	const T r = pair_r(r2);
 	T tau;
 	int j;
 	if (sc.uniform) {
@@ -381,7 +380,7 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 					const f2_t r2 = f2_fma(mz, mz, f2_fma(my, my, f2_fma(mx, mx, tiny2)));
 					float ra, rb;
 					f2_split(r2, ra, rb);
-					const f2_t r = f2_mul(r2, f2_make(rsqrt_(ra), rsqrt_(rb)));
+					const f2_t r = f2_make(pair_r(ra), pair_r(rb));
 					// floor(x) = round(x - 1/2), x = r / h (see nic)
 					const f2_t xm = f2_fma(r, H2, mhalf2);
 					const f2_t yv = f2_add(xm, R2);
