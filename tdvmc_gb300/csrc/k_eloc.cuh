@@ -5,20 +5,22 @@
 // CalculateOtherLocalOperators and CalculateExpectationValues
 // (BosonsBulk.cpp:179-218, 220-336, 349-458, 522-545).
 //
-// One group of G lanes owns one walker.  Forward sweep: lane l owns row
-// particle n = s*G + l of slot s and loops over all partners i (the partner
-// coordinate is a shared-memory broadcast), accumulating the complex
-// gradient G_n and Laplacian of ln psi in registers with compensated block
-// sums.  O_k is linear in the spline basis and is accumulated as
-// per-interval moments sum t^c in lane-private shared histograms; partners
-// below the slot base are counted once per unordered pair with warp-uniform
-// control flow (the diagonal block is the only mixed region).  Reverse sweep
-// (adjoint): one pass over unordered pairs that recomputes minimum-image
-// distances and accumulates sum t^c g with g = (G_n - G_i) . rhat_ni, plus
-// the (D-1)/r term of the Laplacian of O_k, which enters the adjoint in the
-// same B' combination; no pair table is stored.  Moments are turned into
-// spline values with the local piece polynomials and folded to the p
-// parameters at the end.
+// One group of G lanes owns one walker; lane l owns row particle n = s*G + l
+// of slot s.  Forward sweep, FP32 with 32-lane groups (half_block_f32): every
+// unordered pair once in a rotation schedule; the row's complex gradient G_n
+// is accumulated in registers with compensated block sums and the partner's
+// share travels along the lanes back to the partner's row (the Laplacian of
+// ln psi enters only as a total).  Forward sweep otherwise (fwd_region_f2 in
+// FP32, fwd_region): each row loops over all partners i (a shared-memory
+// broadcast) and counts
+// the statistics of the pairs i < n.  O_k is linear in the spline basis and
+// is accumulated as per-interval moments sum t^c in lane-private shared
+// histograms.  Reverse sweep (adjoint): one pass over unordered pairs that
+// recomputes minimum-image distances and accumulates sum t^c g with
+// g = (G_n - G_i) . rhat_ni, plus the (D-1)/r term of the Laplacian of O_k,
+// which enters the adjoint in the same B' combination; no pair table is
+// stored.  Moments are turned into spline values with the local piece
+// polynomials and folded to the p parameters at the end.
 #pragma once
 
 #include "common.cuh"
