@@ -188,6 +188,32 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+class Ranks:
+    """Replica ranks under torchrun (one process per GPU, each running the whole
+    workload): a barrier and the maximum over ranks; no-ops for one rank."""
+
+    def __init__(self, world, backend="nccl"):
+        self.dist = None
+        self.device = "cuda" if backend == "nccl" else "cpu"
+        if world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
 def run_ours(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -201,6 +227,7 @@ def run_ours(args):
 
         def sync():
             pass
+    ranks = Ranks(world, "nccl")
     import tdvmc_gb300 as T
     from tdvmc_gb300 import _native as Nat
 
@@ -219,14 +246,18 @@ def run_ours(args):
     # warm-up steps (thermalise the walkers, build and warm the graphs)
     td.time_steps(args.warmup)
     sync()
+    ranks.barrier()
+    sync()
     clocks = Clocks()
     clocks.start()
     launches_a = sysm.LaunchCount()
-    ms = td.time_steps(args.steps)
+    ms = td.time_steps(args.steps)  # CUDA events on the library's stream around the K steps
+    sync()
+    ranks.barrier()
     sync()
     launches_b = sysm.LaunchCount()
     clk = clocks.stop()
-    value_rank = args.steps / (ms / 1000.0)
+    ms = ranks.max(ms)
     if args.no_extras:
         # profiling runs: the timed steps only
         if rank == 0:
@@ -241,6 +272,8 @@ def run_ours(args):
     # end-to-end through the C ABI with host buffers: parameters in, statistics
     # and parameters out, every step
     uRh, uIh, pRh, pIh = sysm.GetParameters()
+    sync()
+    ranks.barrier()
     t0 = time.perf_counter()
     last = None
     for _ in range(args.steps):
@@ -248,7 +281,7 @@ def run_ours(args):
         last = td.step(1)
         uRh, uIh, pRh, pIh = sysm.GetParameters()
     sync()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = ranks.max(time.perf_counter() - t0)
     e2e = args.steps / e2e_s
     h2d = (2 * P + 2) * 8 * 2 + 4
     d2h = (3 * P + 12) * 8 + 24 + (2 * P + 2) * 8
@@ -298,19 +331,18 @@ def run_ours(args):
     achieved = fl / (top[1] * 1e-3) / 1e12
     traffic = ncu_traffic(top[0])
 
-    # CPU baseline: the reference algorithm (FP64 port) on the host cores, bounded sample
+    # CPU baseline: the reference algorithm (FP64 port) on the host cores, bounded
+    # sample; one GPU only (replica ranks would share the host's cores)
     threads = os.cpu_count() or 1
-    _, t_probe, _ = cpu_port_rate(threads, 4)
-    wpt = int(min(1024, max(4, np.ceil(4 * 12.0 / max(t_probe, 1e-3)))))  # about 12 s of CPU work
-    cpu_v, cpu_t, cpu_w = cpu_port_rate(threads, wpt)
+    cpu_baseline = None
+    if world == 1:
+        _, t_probe, _ = cpu_port_rate(threads, 4)
+        wpt = int(min(1024, max(4, np.ceil(4 * 12.0 / max(t_probe, 1e-3)))))  # about 12 s of CPU work
+        cpu_v, cpu_t, cpu_w = cpu_port_rate(threads, wpt)
+        cpu_baseline = {"value": cpu_v, "unit": "steps/s", "cores": threads, "kind": "port",
+                        "sample": "one RK stage (686 moves + E_loc + adjoint) of %d walkers on %d threads "
+                                  "(%.1f s), extrapolated x4 stages x65536 walkers" % (cpu_w, threads, cpu_t)}
 
-    if world > 1 and torch is not None:
-        import torch.distributed as dist
-        if not dist.is_initialized():
-            dist.init_process_group("nccl")
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     value = world * args.steps / (ms / 1000.0)
     peaks = measured_peaks()
     line = {
@@ -333,9 +365,7 @@ def run_ours(args):
         "gate": {"dE_per_N": dE_per_N, "pass": bool(dE_per_N < 1e-5), "walkers": nsub},
         "stored_sample_rk4": {"value": args.steps / (ms3 / 1000.0), "unit": "steps/s", "update_every": 1,
                               "update_percent": 25.0, "kernels_ms_refresh_stage": prof3},
-        "cpu_baseline": {"value": cpu_v, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": "one RK stage (686 moves + E_loc + adjoint) of %d walkers on %d threads "
-                                   "(%.1f s), extrapolated x4 stages x65536 walkers" % (cpu_w, threads, cpu_t)},
+        "cpu_baseline": cpu_baseline,
         "algorithmic_tflop_per_step": flop_step() / 1e12,
         "achieved_tflops_step": flop_step() / (ms / args.steps * 1e-3) / 1e12,
         "clocks": clk,
