@@ -163,13 +163,11 @@ __device__ __forceinline__ void hist_add8(T* __restrict__ hist, int j, int lane,
 
 // Two partners' moments into lane-private histogram slots (scalar mode): both
 // intervals' slots are loaded before anything is stored, so the loads overlap;
-// when the intervals coincide B's values go in with A's and B's stores are
-// skipped.
+// B's record starts from A's updated record when the intervals coincide and is
+// stored last, so that one store holds both partners' moments.
 template <int NMH, int NV, typename T, int G>
 __device__ __forceinline__ void hist_add_pair(T* __restrict__ hist, int jA, const T (&vA)[8], int jB,
                                               const T (&vB)[8], int lane) {
-	T* hA = hist + ((size_t)jA * G + lane) * NMH;
-	T* hB = hist + ((size_t)jB * G + lane) * NMH;
 	if constexpr (kSplit6<0, NMH, T> && NV == 6) {
 		float a[6], b[6];
 		rec6_load<G>(hist, jA, lane, a);
@@ -177,13 +175,15 @@ __device__ __forceinline__ void hist_add_pair(T* __restrict__ hist, int jA, cons
 		const bool same = jA == jB;
 #pragma unroll
 		for (int m = 0; m < 6; m++) {
-			a[m] += same ? (vA[m] + vB[m]) : vA[m];
-			b[m] += vB[m];
+			a[m] += vA[m];
+			b[m] = (same ? a[m] : b[m]) + vB[m];
 		}
 		rec6_store<G>(hist, jA, lane, a);
-		if (!same) rec6_store<G>(hist, jB, lane, b);
+		rec6_store<G>(hist, jB, lane, b);
 		return;
 	}
+	T* hA = hist + ((size_t)jA * G + lane) * NMH;
+	T* hB = hist + ((size_t)jB * G + lane) * NMH;
 	constexpr bool A16 = NMH % 4 == 0;  // hist starts on a 16-byte boundary
 	T a[NV], b[NV];
 	rec_load<NV, T, A16>(hA, a);
@@ -191,11 +191,11 @@ __device__ __forceinline__ void hist_add_pair(T* __restrict__ hist, int jA, cons
 	const bool same = jA == jB;
 #pragma unroll
 	for (int m = 0; m < NV; m++) {
-		a[m] += same ? (vA[m] + vB[m]) : vA[m];
-		b[m] += vB[m];
+		a[m] += vA[m];
+		b[m] = (same ? a[m] : b[m]) + vB[m];
 	}
 	rec_store<NV, T, A16>(hA, a);
-	if (!same) rec_store<NV, T, A16>(hB, b);
+	rec_store<NV, T, A16>(hB, b);
 }
 
 // value of moment m of interval j summed over the group's lanes
