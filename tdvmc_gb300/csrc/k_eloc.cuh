@@ -6,7 +6,8 @@
 // (BosonsBulk.cpp:179-218, 220-336, 349-458, 522-545).
 //
 // One group of G lanes owns one walker; lane l owns row particle n = s*G + l
-// of slot s.  Forward sweep, FP32 with 32-lane groups (half_block_f32): every
+// of slot s.  Forward sweep with 32-lane groups (half_block_f32 in FP32,
+// half_block_s in FP64): every
 // unordered pair once in a rotation schedule; the row's complex gradient G_n
 // is accumulated in registers with compensated block sums and the partner's
 // share travels along the lanes back to the partner's row (the Laplacian of
@@ -222,7 +223,7 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 // Shared memory layout of the forward kernel k_eloc:
 //   CTA:   coefC[3*nbin] (u', u'' coefficients) | kb[nbin] | hv[nbin] | lut[ncell]
 //   group: xs[n] {x, y, z, 0} | hist[nbin*4*G] | red[nbin*4]
-//   (FP32, 32-lane groups: xs[n].w and red, widened to [5][n], hold the row
+//   (32-lane groups: xs[n].w and red, widened to [5][n], hold the row
 //   gradients of the half sweep until the histogram reduction)
 // and of the reverse (adjoint) kernel k_eloc_rev:
 //   CTA:   kb[nbin] | hv[nbin] | lut[ncell]
@@ -246,7 +247,7 @@ __host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int 
 	size_t b = (size_t)n * sizeof(Q4<T>);
 	b += eloc_hist_len(nbin, ns, G, 4) * sizeof(T);
 	size_t red = (size_t)nbin * kFwdMoments;
-	if (sizeof(T) == 4 && G == 32 && red < (size_t)5 * n) red = (size_t)5 * n;  // half sweep: gacc[5][n]
+	if (G == 32 && red < (size_t)5 * n) red = (size_t)5 * n;  // half sweep: gacc[5][n]
 	b += red * sizeof(T);
 	return (b + 31) & ~(size_t)31;
 }
@@ -687,6 +688,74 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 	vsum.add(vb);
 }
 
+// The half sweep of half_block_f32 in scalar arithmetic (FP64): the same
+// rotation schedule, travelling partner sums and statistics, two steps per
+// iteration as independent pairs.
+template <typename T, bool DIAG, bool ADJ, int HIST>
+__device__ __forceinline__ void half_block_s(const SysConst& sc, int sp, int n, int lane, bool rowok,
+                                             const Q4<T>& xr, const Q4<T>* __restrict__ xs,
+                                             const Q4<T>* __restrict__ coefC, const T* __restrict__ kb,
+                                             const T* __restrict__ hv, const int* __restrict__ lut,
+                                             T* __restrict__ hist, T pa, T pb, KSum<T>* own, T* trav, KSum<T>& elR,
+                                             KSum<T>& elI, KSum<T>& vsum) {
+	constexpr int S = 2;  // steps per iteration
+	T a[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+	T l2R = T(0), l2I = T(0), vb = T(0);
+	constexpr int k0 = DIAG ? 1 : 0, k1 = DIAG ? 17 : 32;
+	for (int k = k0; k < k1; k += S) {
+		T pj[S][6];
+		FwdPair<T> q[S];
+#pragma unroll
+		for (int h = 0; h < S; h++) {
+			const int kk = k + h;
+			const int i = sp * 32 + ((lane + kk) & 31);
+			const bool ok = DIAG ? (rowok && i < n && (kk < 16 || (kk == 16 && lane < 16))) : rowok;
+			q[h] = fwd_pair<T>(sc, xr, xs[DIAG && i >= n ? 0 : i], ok, coefC, kb, hv, lut);
+		}
+#pragma unroll
+		for (int h = 0; h < S; h++) {
+			pj[h][0] = q[h].gR * q[h].dx;
+			pj[h][1] = q[h].gR * q[h].dy;
+			pj[h][2] = q[h].gR * q[h].dz;
+			pj[h][3] = q[h].gI * q[h].dx;
+			pj[h][4] = q[h].gI * q[h].dy;
+			pj[h][5] = q[h].gI * q[h].dz;
+#pragma unroll
+			for (int c = 0; c < 6; c++) a[c] += pj[h][c];
+			l2R += q[h].lR;
+			l2I += q[h].lI;
+			fwd_stats<T, G32, ADJ, HIST>(sc, q[h], q[h].in, hist, lane, pa, pb, vb);
+		}
+		// trav(l) <- trav(l + S) + p_0(l + S) + p_1(l + S - 1) + ... + p_{S-1}(l + 1)
+#pragma unroll
+		for (int c = 0; c < 6; c++) {
+			T t = __shfl_sync(0xffffffffu, trav[c] + pj[0][c], (lane + S) & 31);
+#pragma unroll
+			for (int j = 1; j < S; j++) t += __shfl_sync(0xffffffffu, pj[j][c], (lane + S - j) & 31);
+			trav[c] = t;
+		}
+	}
+#pragma unroll
+	for (int c = 0; c < 6; c++) own[c].add(a[c]);
+	elR.add(T(2) * l2R);
+	elI.add(T(2) * l2I);
+	vsum.add(vb);
+}
+
+template <typename T, bool DIAG, bool ADJ, int HIST>
+__device__ __forceinline__ void half_block(const SysConst& sc, int sp, int n, int lane, bool rowok, const Q4<T>& xr,
+                                           const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
+                                           const T* __restrict__ kb, const T* __restrict__ hv,
+                                           const int* __restrict__ lut, T* __restrict__ hist, T pa, T pb,
+                                           KSum<T>* own, T* trav, KSum<T>& elR, KSum<T>& elI, KSum<T>& vsum) {
+	if constexpr (std::is_same<T, float>::value)
+		half_block_f32<DIAG, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own, trav,
+		                                elR, elI, vsum);
+	else
+		half_block_s<T, DIAG, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own, trav,
+		                                 elR, elI, vsum);
+}
+
 // Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), kNp
 // partners per iteration.
 template <typename T, int G, bool DIAG, int HIST>
@@ -916,22 +985,22 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 		KSum<T> e_r1, e_i1, e_r1i1, e_lR, e_lI, e_v;
 		int nout = 0;
 		T* gw = ADJ ? gout + (size_t)w * 6 * n : nullptr;
-		if constexpr (std::is_same<T, float>::value && G == 32) {
+		if constexpr (G == 32) {
 			// half sweep; row gradients: gRx in xs[row].w, gRy..gIz in gacc[c-1][row] (the
 			// reduction area, free until the histogram reduction).  Lane l only touches rows = l mod 32.
-			float* gacc = red;
+			T* gacc = red;
 			for (int i = lane; i < n; i += 32)
 #pragma unroll
-				for (int c = 0; c < 5; c++) gacc[c * n + i] = 0.f;
+				for (int c = 0; c < 5; c++) gacc[c * n + i] = T(0);
 			for (int s = 0; s < nslot; s++) {
 				const int nrow = s * 32 + lane;
 				const bool rowok = nrow < n;
-				const Q4<float> xr = rowok ? xs[nrow] : Q4<float>{0.f, 0.f, 0.f, 0.f};
-				KSum<float> own[6];
+				const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
+				KSum<T> own[6];
 				for (int sp = 0; sp < s; sp++) {
-					float trav[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-					half_block_f32<false, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
-					                                 own, trav, e_lR, e_lI, e_v);
+					T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+					half_block<T, false, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
+					                                own, trav, e_lR, e_lI, e_v);
 					const int pr = sp * 32 + lane;  // the partners' shares are home
 					if (pr < n) {
 						xs[pr].w -= trav[0];
@@ -939,9 +1008,9 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 						for (int c = 1; c < 6; c++) gacc[(c - 1) * n + pr] -= trav[c];
 					}
 				}
-				float trav[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-				half_block_f32<true, ADJ, HIST>(sc, s, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
-				                                trav, e_lR, e_lI, e_v);
+				T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+				half_block<T, true, ADJ, HIST>(sc, s, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
+				                               trav, e_lR, e_lI, e_v);
 #pragma unroll
 				for (int c = 0; c < 6; c++) own[c].add(-__shfl_sync(0xffffffffu, trav[c], (lane + 15) & 31));
 				if (rowok) {  // later slots add their shares
@@ -951,11 +1020,11 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				}
 			}
 			for (int r = lane; r < n; r += 32) {
-				const float gRx = xs[r].w, gRy = gacc[r], gRz = gacc[n + r];
-				const float gIx = gacc[2 * n + r], gIy = gacc[3 * n + r], gIz = gacc[4 * n + r];
+				const T gRx = xs[r].w, gRy = gacc[r], gRz = gacc[n + r];
+				const T gIx = gacc[2 * n + r], gIy = gacc[3 * n + r], gIz = gacc[4 * n + r];
 				e_r1.add(gRx * gRx + gRy * gRy + gRz * gRz);
 				e_i1.add(gIx * gIx + gIy * gIy + gIz * gIz);
-				e_r1i1.add(2.f * (gRx * gIx + gRy * gIy + gRz * gIz));
+				e_r1i1.add(T(2) * (gRx * gIx + gRy * gIy + gRz * gIz));
 				if (ADJ) {
 					gw[r] = gRx;
 					gw[n + r] = gRy;
@@ -1012,10 +1081,10 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 		for (int o = G / 2; o > 0; o >>= 1) nout_all += __shfl_xor_sync(gmask, nout_all, o, G);
 
 		hist_reduce<T, G, HIST, NMH>(hist, red, nbin, NM, lane, gmask);
-		if constexpr (std::is_same<T, float>::value && G == 32) {
+		if constexpr (G == 32) {
 			// half sweep: pairs beyond r_max are all pairs less those in moment 0
 			// (integer counts below 2^24, exact in FP32)
-			float m0 = 0.f;
+			T m0 = T(0);
 			for (int j = 0; j < nbin; j++) m0 += red[j * NM];
 			nout_all = n * (n - 1) / 2 - (int)m0;
 		}
