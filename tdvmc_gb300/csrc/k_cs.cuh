@@ -207,8 +207,11 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 // Local quantities of every stored walker at the current stage parameters:
 // same outputs as k_eloc (ln psi, O, E_loc, kinetic sums, dE/d alpha).
 // One warp per walker; each lane takes V consecutive particles per 16-byte
-// load.  D is streamed once for G_n and, with ADJ, once more for
-// sum_n G_n . D[s][.][n] (G staged component-major in shared memory).
+// load, 32 V particles per chunk.  D is streamed once for G_n; with ADJ each
+// chunk's G_n . D[s][.][n] follows right after its G_n, so the second read of
+// the chunk's D comes from L2, not HBM; the per-lane sums over the chunks
+// stay in shared memory (part[s][lane], complex) and are added over the lanes
+// once per walker.
 template <typename T> struct Vec16;
 template <> struct Vec16<float> {
 	using type = float4;
@@ -229,12 +232,15 @@ template <> struct Vec16<double> {
 	}
 };
 
-// Shared memory of k_cs_eval: wR, wI [ns each, padded to 4] | per warp: G[6][npad] | A[2*ns, padded to 4]
-// (every region starts on a 16-byte boundary for the vector loads)
+// Shared memory of k_cs_eval: wR, wI [ns each, padded to 4] | per warp:
+// part[ns][33][2] (lane-private complex partial sums; the row of 33 keeps the
+// per-spline sums over the lanes free of bank conflicts) | A[2*ns, padded to 4]
 __host__ __device__ inline int cs_ns2(int ns) { return (2 * ns + 3) & ~3; }
+constexpr int kCsPartRow = 33;
 template <typename T>
 __host__ __device__ inline size_t cs_eval_smem_bytes(int n, int ns, int warps) {
-	return ((size_t)cs_ns2(ns) + (size_t)warps * ((size_t)6 * cs_npad(n) + cs_ns2(ns))) * sizeof(T);
+	(void)n;
+	return ((size_t)cs_ns2(ns) + (size_t)warps * ((size_t)2 * kCsPartRow * ns + cs_ns2(ns))) * sizeof(T);
 }
 
 template <typename T, bool ADJ>
@@ -251,7 +257,7 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 	const int npad = cs_npad(n);
 	T* wR = reinterpret_cast<T*>(smem_raw);
 	T* wI = wR + ns;
-	T* gs_all = wR + cs_ns2(ns);  // per warp: G[6][npad] (adjoint), then [2*ns] spline sums
+	T* gs_all = wR + cs_ns2(ns);  // per warp: part[ns][33][2] (adjoint), then [2*ns] spline sums
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int wpb = blockDim.x >> 5;
 	for (int s = threadIdx.x; s < ns; s += blockDim.x) {
@@ -265,13 +271,18 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 		wI[s] = (T)im;
 	}
 	__syncthreads();
-	T* gs = gs_all + (size_t)warp * ((size_t)6 * npad + cs_ns2(ns));
-	T* asum = gs + (size_t)6 * npad;
+	T* part = gs_all + (size_t)warp * ((size_t)2 * kCsPartRow * ns + cs_ns2(ns));
+	T* asum = part + (size_t)2 * kCsPartRow * ns;
 	const double c = sc.hbar2_2m;
 
 	for (int64_t w = (int64_t)blockIdx.x * wpb + warp; w < nw; w += (int64_t)gridDim.x * wpb) {
 		const T* Dw = D + (size_t)w * ns * 3 * npad;
 		KSum<T> r1, i1, r1i1;
+		if (ADJ)
+			for (int s = 0; s < ns; s++) {
+				part[((size_t)s * kCsPartRow + lane) * 2] = T(0);
+				part[((size_t)s * kCsPartRow + lane) * 2 + 1] = T(0);
+			}
 		for (int c0 = lane * V; c0 < n; c0 += 32 * V) {
 			T gr[3][V], gi[3][V];
 #pragma unroll
@@ -298,12 +309,25 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 					i1.add(gi[0][v] * gi[0][v] + gi[1][v] * gi[1][v] + gi[2][v] * gi[2][v]);
 					r1i1.add(T(2) * (gr[0][v] * gi[0][v] + gr[1][v] * gi[1][v] + gr[2][v] * gi[2][v]));
 				}
-				if (ADJ)
+			}
+			if (ADJ) {
+				// this chunk's G_n . D[s][.][n] (the padding of D is zero)
+				for (int s = 0; s < ns; s++) {
+					T cr = T(0), ci = T(0);
 #pragma unroll
 					for (int a = 0; a < 3; a++) {
-						gs[(size_t)a * npad + c0 + v] = gr[a][v];
-						gs[(size_t)(3 + a) * npad + c0 + v] = gi[a][v];
+						T d[V];
+						Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + ((size_t)s * 3 + a) * npad + c0), d);
+#pragma unroll
+						for (int v = 0; v < V; v++) {
+							cr = fma(gr[a][v], d[v], cr);
+							ci = fma(gi[a][v], d[v], ci);
+						}
 					}
+					T* pp = part + ((size_t)s * kCsPartRow + lane) * 2;
+					pp[0] += cr;
+					pp[1] += ci;
+				}
 			}
 		}
 		T l2r = T(0), l2i = T(0);
@@ -344,30 +368,16 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 		}
 		if (ADJ) {
 			__syncwarp();
-			// A_s = sum_n G_n . D[s][.][n] (complex), then fold with D2; the
-			// padding of D is zero, so whole vectors can be summed
-			for (int s = 0; s < ns; s++) {
+			// A_s = sum_n G_n . D[s][.][n] (complex): the lanes' partial sums in lane order
+			for (int s = lane; s < ns; s += 32) {
 				T ar = T(0), ai = T(0);
-				for (int c0 = lane * V; c0 < n; c0 += 32 * V) {
-#pragma unroll
-					for (int a = 0; a < 3; a++) {
-						T d[V], g[V], h[V];
-						Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + ((size_t)s * 3 + a) * npad + c0), d);
-						Vec16<T>::get(*reinterpret_cast<const VT*>(gs + (size_t)a * npad + c0), g);
-						Vec16<T>::get(*reinterpret_cast<const VT*>(gs + (size_t)(3 + a) * npad + c0), h);
-#pragma unroll
-						for (int v = 0; v < V; v++) {
-							ar = fma(g[v], d[v], ar);
-							ai = fma(h[v], d[v], ai);
-						}
-					}
+				const T* pp = part + (size_t)s * kCsPartRow * 2;
+				for (int l = 0; l < 32; l++) {
+					ar += pp[2 * l];
+					ai += pp[2 * l + 1];
 				}
-				ar = group_sum<T, 32>(ar, 0xffffffffu);
-				ai = group_sum<T, 32>(ai, 0xffffffffu);
-				if (lane == 0) {
-					asum[2 * s] = ar;
-					asum[2 * s + 1] = ai;
-				}
+				asum[2 * s] = ar;
+				asum[2 * s + 1] = ai;
 			}
 			__syncwarp();
 			for (int k = lane; k < P; k += 32) {
