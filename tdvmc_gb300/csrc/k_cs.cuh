@@ -208,10 +208,11 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 // same outputs as k_eloc (ln psi, O, E_loc, kinetic sums, dE/d alpha).
 // One warp per walker; each lane takes V consecutive particles per 16-byte
 // load, 32 V particles per chunk.  D is streamed once for G_n; with ADJ each
-// chunk's G_n . D[s][.][n] follows right after its G_n, so the second read of
-// the chunk's D comes from L2, not HBM; the per-lane sums over the chunks
-// stay in shared memory (part[s][lane], complex) and are added over the lanes
-// once per walker.
+// chunk's G_n . D[s][.][n] follows right after its G_n (a second read of the
+// chunk's D: with a whole GPU of warps streaming, most of it comes from HBM
+// again), and the per-lane sums over the chunks stay in shared memory
+// (part[s][lane], complex) and are added over the lanes once per walker
+// instead of one butterfly per spline.
 template <typename T> struct Vec16;
 template <> struct Vec16<float> {
 	using type = float4;
