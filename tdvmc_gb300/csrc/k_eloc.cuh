@@ -223,8 +223,8 @@ __device__ __forceinline__ T hist_sum(const T* __restrict__ hist, int j, int m) 
 // Shared memory layout of the forward kernel k_eloc:
 //   CTA:   coefC[3*nbin] (u', u'' coefficients) | kb[nbin] | hv[nbin] | lut[ncell]
 //   group: xs[n] {x, y, z, 0} | hist[nbin*4*G] | red[nbin*4]
-//   (32-lane groups: xs[n].w and red, widened to [5][n], hold the row
-//   gradients of the half sweep until the histogram reduction)
+//   (32-lane groups: xs[n].w holds gRx of the half sweep's rows; gRy..gIz
+//   accumulate in the global gradient scratch)
 // and of the reverse (adjoint) kernel k_eloc_rev:
 //   CTA:   kb[nbin] | hv[nbin] | lut[ncell]
 //   group: xs[n] {x, y, z, gRx} | g4[n] {gRy, gRz, gIx, gIy} | gz[n] {gIz} | hist[nbin*NMH*G] | redr[nbin*6]
@@ -246,9 +246,7 @@ template <typename T>
 __host__ __device__ inline size_t eloc_group_bytes(int n, int nbin, int ns, int G) {
 	size_t b = (size_t)n * sizeof(Q4<T>);
 	b += eloc_hist_len(nbin, ns, G, 4) * sizeof(T);
-	size_t red = (size_t)nbin * kFwdMoments;
-	if (G == 32 && red < (size_t)5 * n) red = (size_t)5 * n;  // half sweep: gacc[5][n]
-	b += red * sizeof(T);
+	b += (size_t)nbin * kFwdMoments * sizeof(T);
 	return (b + 31) & ~(size_t)31;
 }
 template <typename T>
@@ -927,8 +925,11 @@ __device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, i
 // With ADJ it also writes every particle's complex gradient G_n to
 // gout[w][6][n] (gRx gRy gRz gIx gIy gIz) for k_eloc_rev and the B'' part of
 // dE_loc/d alpha to dE_o, which k_eloc_rev completes.
+// FP32 32-lane groups: at most 2 walkers (64 threads) per block and 5 blocks
+// per SM, so that registers (<= 204) and shared memory both allow 10 resident walkers.
 template <typename T, int G, bool ADJ, int HIST>
-__global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
+__global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 32 && sizeof(T) == 4) ? 5 : 1)
+    k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
                                               const T* __restrict__ kb_g, const T* __restrict__ hv_g,
                                               const int* __restrict__ lut_g, const T* __restrict__ loc_g,
                                               const double* __restrict__ fold_g, const double* __restrict__ params,
@@ -984,11 +985,12 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 
 		KSum<T> e_r1, e_i1, e_r1i1, e_lR, e_lI, e_v;
 		int nout = 0;
-		T* gw = ADJ ? gout + (size_t)w * 6 * n : nullptr;
+		T* gw = (ADJ || G == 32) ? gout + (size_t)w * 6 * n : nullptr;
 		if constexpr (G == 32) {
-			// half sweep; row gradients: gRx in xs[row].w, gRy..gIz in gacc[c-1][row] (the
-			// reduction area, free until the histogram reduction).  Lane l only touches rows = l mod 32.
-			T* gacc = red;
+			// half sweep; row gradients: gRx in xs[row].w, gRy..gIz in the walker's gradient
+			// scratch gw[c][row], c = 1..5 (L2-resident while the walker runs).  Lane l only
+			// touches rows = l mod 32, so its own reads see its own writes.
+			T* gacc = gw + n;
 			for (int i = lane; i < n; i += 32)
 #pragma unroll
 				for (int c = 0; c < 5; c++) gacc[c * n + i] = T(0);
@@ -998,15 +1000,17 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
 				KSum<T> own[6];
 				for (int sp = 0; sp < s; sp++) {
+					const int pr = sp * 32 + lane;  // an earlier slot is full: pr < n
+					T pacc[5];  // the partner row's sums so far, loaded before the block
+#pragma unroll
+					for (int c = 0; c < 5; c++) pacc[c] = gacc[c * n + pr];
 					T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
 					half_block<T, false, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
 					                                own, trav, e_lR, e_lI, e_v);
-					const int pr = sp * 32 + lane;  // the partners' shares are home
-					if (pr < n) {
-						xs[pr].w -= trav[0];
+					// the partners' shares are home
+					xs[pr].w -= trav[0];
 #pragma unroll
-						for (int c = 1; c < 6; c++) gacc[(c - 1) * n + pr] -= trav[c];
-					}
+					for (int c = 0; c < 5; c++) gacc[c * n + pr] = pacc[c] - trav[c + 1];
 				}
 				T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
 				half_block<T, true, ADJ, HIST>(sc, s, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
@@ -1025,14 +1029,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc(SysConst sc, const DynState* __
 				e_r1.add(gRx * gRx + gRy * gRy + gRz * gRz);
 				e_i1.add(gIx * gIx + gIy * gIy + gIz * gIz);
 				e_r1i1.add(T(2) * (gRx * gIx + gRy * gIy + gRz * gIz));
-				if (ADJ) {
-					gw[r] = gRx;
-					gw[n + r] = gRy;
-					gw[2 * n + r] = gRz;
-					gw[3 * n + r] = gIx;
-					gw[4 * n + r] = gIy;
-					gw[5 * n + r] = gIz;
-				}
+				if (ADJ) gw[r] = gRx;  // gRy..gIz are in place
 			}
 		} else
 		for (int s = 0; s < nslot; s++) {

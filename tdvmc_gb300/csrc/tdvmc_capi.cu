@@ -260,14 +260,17 @@ int pick_gpb(const void* fn, int G, int want, size_t cta, size_t grp) {
 	    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) !=
 	        cudaSuccess)
 		return 0;
+	cudaFuncAttributes fa;
+	if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return 0;
+	const int max_threads = fa.maxThreadsPerBlock < 128 ? fa.maxThreadsPerBlock : 128;
 	if (want > 0) {
 		int g = want;
-		while (g > 1 && cta + (size_t)g * grp > kSmemMax) g--;
+		while (g > 1 && (cta + (size_t)g * grp > kSmemMax || G * g > max_threads)) g--;
 		return cta + (size_t)g * grp <= kSmemMax ? g : 0;
 	}
 	int best = 0, best_w = 0;
 	for (int g : {1, 2, 4}) {
-		if (G * g > 128 || cta + (size_t)g * grp > kSmemMax) continue;
+		if (G * g > max_threads || cta + (size_t)g * grp > kSmemMax) continue;
 		int blocks = 0;
 		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, G * g, cta + (size_t)g * grp) != cudaSuccess)
 			return 0;
@@ -279,7 +282,8 @@ int pick_gpb(const void* fn, int G, int want, size_t cta, size_t grp) {
 	return best;
 }
 
-// Gradient scratch of the adjoint (nw x 6 x n), allocated on first need and
+// Gradient scratch (nw x 6 x n): the partner sums of the 32-lane forward
+// kernel and the adjoint's input, allocated on the first evaluation and
 // always before a stream capture (allocation is not capturable).
 int ensure_gbuf(tdvmc_ctx* ctx) {
 	if (ctx->gbuf) return TDVMC_OK;
@@ -306,7 +310,9 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cu
 	RevFn<T> fr = adj ? pick_eloc_rev<T>(G, hist) : nullptr;
 	if (!fn || (adj && !fr)) return TDVMC_ERR_ARG;
 	const SysConst& s = ctx->sc;
-	if (adj && !ctx->gbuf) return TDVMC_ERR_STATE;  // ensure_gbuf was not called
+	// the gradient scratch: the adjoint's input, and the 32-lane forward's partner sums
+	const bool need_g = adj || G == 32;
+	if (need_g && !ctx->gbuf) return TDVMC_ERR_STATE;  // ensure_gbuf was not called
 	const size_t fcta = eloc_cta_bytes<T>(s.nbin, s.ncell), fgrp = eloc_group_bytes<T>(s.n, s.nbin, s.ns, G);
 	const int gpb = pick_gpb((const void*)fn, G, ctx->tiles.egpb, fcta, fgrp);
 	if (gpb < 1) return TDVMC_ERR_CUDA;
@@ -314,7 +320,7 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cu
 	const size_t smem = fcta + (size_t)gpb * fgrp;
 	const int grid = grid_for(ctx, (const void*)fn, threads, smem, count, gpb, free);
 	const size_t P = (size_t)s.p, dn = (size_t)s.dim * s.n;
-	T* gb = adj ? (T*)ctx->gbuf + (size_t)w0 * 6 * s.n : nullptr;
+	T* gb = need_g ? (T*)ctx->gbuf + (size_t)w0 * 6 * s.n : nullptr;
 	fn<<<grid, threads, smem, st>>>(s, ctx->dyn, (const Q4<T>*)ctx->coefC, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut,
 	                                (const T*)ctx->locT, ctx->fold_d, ctx->stage, (const T*)ctx->pos + w0 * dn, count,
 	                                (T*)ctx->lnpsi + w0, (T*)ctx->O + w0 * P, (T*)ctx->eloc + 2 * w0,
@@ -554,8 +560,8 @@ int get_graph(tdvmc_ctx* ctx, const tdvmc_step_opts* o, cudaGraphExec_t* out, in
 		*kernels = ctx->graph_kernels[k];
 		return TDVMC_OK;
 	}
-	if (o->use_adjoint) {
-		const int ra = ensure_gbuf(ctx);
+	{
+		const int ra = ensure_gbuf(ctx);  // gradient scratch of the forward and adjoint kernels
 		if (ra) return ra;
 	}
 	cudaGraph_t g;
@@ -1076,7 +1082,7 @@ int tdvmc_sample(tdvmc_ctx* ctx, int32_t moves, double mc_step, uint64_t seed, u
 
 static int eval_common(tdvmc_ctx* ctx, bool adj) {
 	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
-	if (adj) {
+	{
 		const int ra = ensure_gbuf(ctx);
 		if (ra) return ra;
 	}
@@ -1383,7 +1389,7 @@ int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, float* ms, con
 	CK(cudaEventCreate(&e0));
 	CK(cudaStreamSynchronize(ctx->st));
 	CK(cudaEventRecord(e0, ctx->st));
-	if (o->use_adjoint && (rc = ensure_gbuf(ctx))) return rc;
+	if ((rc = ensure_gbuf(ctx))) return rc;
 	ctx->prof = &ev;
 	ctx->prof_names = &nm;
 	if (o->ode_solver == 3) {
