@@ -134,7 +134,10 @@ int tdvmc_sample(tdvmc_ctx* ctx, int32_t moves, double mc_step, uint64_t seed, u
 /* Forward evaluation at the current walkers (CalculateWavefunction +
  * CalculateExpectationValues, BosonsBulk.cpp:179-545).  Outputs (any may be
  * NULL): lnpsi[nw]; O[nw*p] walker-major; eloc[nw*2] = (E^R, E^I);
- * other7[nw*7] = {kineticR, V_int, sumR1, sumI1, sumR2, sumI2, sumR1I1}. */
+ * other7[nw*7] = {kineticR, V_int, sumR1, sumI1, sumR2, sumI2, sumR1I1}.
+ * The first evaluation of a context allocates its particle-gradient scratch
+ * (nw x 6 x n values; TDVMC_ERR_NOMEM if it does not fit), which the forward
+ * and adjoint sweeps share. */
 int tdvmc_eval_local(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, double* other7);
 
 /* Backward: the same forward pass plus one reverse sweep over the pairs,
