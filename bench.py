@@ -314,6 +314,12 @@ def run_ours(args):
     td3.time_steps(2)  # stores every walker, then one refresh step
     ms3 = td3.time_steps(args.steps)
     prof3 = {k: v for k, v in td3.profile_stage()}
+    # predictor-corrector on stored samples (ODE_SOLVER_TYPE 5): Euler predictor and
+    # 6 corrector passes, each re-evaluating the stored samples
+    td5 = T.TDVP(sysm, DT, MOVES, MC_STEP, seed=1, use_adjoint=1, ode_solver=5, update_every=1,
+                 update_percent=25.0)
+    td5.time_steps(1)
+    ms5 = td5.time_steps(args.steps)
 
     # FP32 pipe ceiling and roofline of the dominant kernel
     import ctypes as C
@@ -365,6 +371,8 @@ def run_ours(args):
         "gate": {"dE_per_N": dE_per_N, "pass": bool(dE_per_N < 1e-5), "walkers": nsub},
         "stored_sample_rk4": {"value": args.steps / (ms3 / 1000.0), "unit": "steps/s", "update_every": 1,
                               "update_percent": 25.0, "kernels_ms_refresh_stage": prof3},
+        "stored_sample_pc": {"value": args.steps / (ms5 / 1000.0), "unit": "steps/s", "update_every": 1,
+                             "update_percent": 25.0, "correctors": 6},
         "cpu_baseline": cpu_baseline,
         "algorithmic_tflop_per_step": flop_step() / 1e12,
         "achieved_tflops_step": flop_step() / (ms / args.steps * 1e-3) / 1e12,

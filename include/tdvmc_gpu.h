@@ -87,7 +87,9 @@ typedef struct tdvmc_stats {
 typedef struct tdvmc_step_opts {
 	double dt;                 /* TIMESTEP */
 	int32_t imaginary_time;    /* IMAGINARY_TIME: 0 real, 1 imaginary */
-	int32_t ode_solver;        /* ODE_SOLVER_TYPE: 0 Euler, 2 RK4, 3 RK4 on stored samples */
+	int32_t ode_solver;        /* ODE_SOLVER_TYPE: 0 Euler, 2 RK4, 3 RK4 on stored samples,
+	                              5 predictor-corrector on stored samples (Euler predictor,
+	                              6 trapezoidal corrector passes, CalculateNextParametersPCReuseSamples) */
 	int32_t lin_solver;        /* LINEAR_EQUATION_SOLVER_TYPE: 0 Cholesky (+1e-3 I) */
 	int32_t precondition;      /* USE_PRECONDITIONING */
 	int32_t normalize_wf;      /* USE_NORMALIZE_WF: phiR <- -ln psi of walker 0 */
@@ -97,9 +99,9 @@ typedef struct tdvmc_step_opts {
 	int32_t use_adjoint;       /* 1: also compute <dE_loc/d alpha> each stage; 2: in imaginary time
 	                              also drive the force with it, F_k = -(cov(O_k, E^R) + <dE_loc/d uR_k>/2),
 	                              i.e. -1/2 d<E>/d uR_k (no reference counterpart) */
-	int32_t update_every;      /* ode_solver 3: UPDATE_SAMPLES_EVERY_NTH_STEP; 0 samples every walker each step,
+	int32_t update_every;      /* ode_solver 3, 5: UPDATE_SAMPLES_EVERY_NTH_STEP; 0 samples every walker each step,
 	                              k > 0 refreshes a window of walkers every k-th step */
-	double update_percent;     /* ode_solver 3: UPDATE_SAMPLES_PERCENT, size of the refresh window in % of walkers */
+	double update_percent;     /* ode_solver 3, 5: UPDATE_SAMPLES_PERCENT, size of the refresh window in % of walkers */
 } tdvmc_step_opts;
 
 const char* tdvmc_status_string(int status);

@@ -342,13 +342,13 @@ int main(int argc, char** argv) {
 	o.mc_step = MC_STEP;
 	o.seed = seed;
 	o.use_adjoint = (int)cfg.num("GPU_ADJOINT", 0);
-	// ODE_SOLVER_TYPE 3: samples are refreshed on every step after the first
+	// ODE_SOLVER_TYPE 3 and 5: samples are refreshed on every step after the first
 	// whenever UPDATE_SAMPLES_EVERY_NTH_STEP > 0, because the reference's
 	// condition (TDVMC.cpp:3665) also holds for every parameter trial
 	o.update_every = (int)cfg.num("UPDATE_SAMPLES_EVERY_NTH_STEP", 0) > 0 ? 1 : 0;
 	o.update_percent = cfg.num("UPDATE_SAMPLES_PERCENT", 100.0);
-	if (o.ode_solver != 0 && o.ode_solver != 2 && o.ode_solver != 3) {
-		std::fprintf(stderr, "ODE_SOLVER_TYPE %d is not implemented on the GPU (0, 2 and 3 are)\n", o.ode_solver);
+	if (o.ode_solver != 0 && o.ode_solver != 2 && o.ode_solver != 3 && o.ode_solver != 5) {
+		std::fprintf(stderr, "ODE_SOLVER_TYPE %d is not implemented on the GPU (0, 2, 3 and 5 are)\n", o.ode_solver);
 		return 2;
 	}
 	const bool acceptance_check = (int)cfg.num("USE_PARAMETER_ACCEPTANCE_CHECK", 0) == 1;

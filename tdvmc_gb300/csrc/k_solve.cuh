@@ -4,7 +4,8 @@
 // diagonal preconditioning (1684-1701), the regularisation (1703-1711), the
 // Cholesky factorisation and solves (1560-1622) or a pivoted dense solve with
 // the mean of the solution removed (type 1, 1763-1827), CalculatePhiDot
-// (1658-1682), and the Euler / RK4 parameter updates (1834-1858, 1969-2035)
+// (1658-1682), and the Euler / RK4 / predictor-corrector parameter updates
+// (1834-1858, 1969-2035, 1912-1967)
 // with NormalizeWavefunction (2525-2529).
 //
 // Stage bookkeeping lives in DynState so the same captured graph serves all
@@ -22,13 +23,19 @@ struct SolveArgs {
 	int imag;        // IMAGINARY_TIME
 	int precond;     // USE_PRECONDITIONING
 	int solver;      // LINEAR_EQUATION_SOLVER_TYPE (0 Cholesky, 1 pivoted dense)
-	int mode;        // 0: right-hand side only, 1: RK4 stage, 2: Euler step
+	int mode;        // 0: right-hand side only, 1: RK4 stage, 2: Euler step, 3: predictor-corrector stage
 	int normalize;   // USE_NORMALIZE_WF
 	int ldS, ldC;    // leading dimensions of S and of the covariance rows
 	int adj_force;   // imaginary time: add half the walker mean of dE_loc/d uR to the force
 	int dE_col;      // column of Re dE_loc/d uR_0 in means1 (pairs Re, Im per parameter)
 	double dt;
 };
+
+// Corrector passes of the predictor-corrector on stored samples (PCsteps in
+// CalculateNextParametersPCReuseSamples, TDVMC.cpp:1912-1967): stage 0 is the
+// Euler predictor u + u'(u) dt, stage c = 1..kPcCorrectors sets
+// u + (u'(u) + u'(trial)) dt / 2 and the last one ends the step.
+constexpr int kPcCorrectors = 6;
 
 constexpr int kStatusNotPD = 1;
 constexpr int kStatusNonFinite = 2;
@@ -54,7 +61,7 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 	const int ld = P + 2;
 	if (tid == 0) {
 		bad = 0;
-		stage_s = (a.mode == 1) ? (int)dyn->stage : 0;
+		stage_s = (a.mode == 1 || a.mode == 3) ? (int)dyn->stage : 0;
 	}
 	const double* Om = means1;       // <O_k>
 	const double ER = means1[P];
@@ -202,7 +209,9 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 	__syncthreads();
 	const double phiDotR = tmp[0], phiDotI = tmp[1];
 	const int stage = stage_s;
-	double* kd = kdot + (size_t)stage * np;
+	// slot of this stage's derivative: RK4 one per stage; predictor-corrector: the
+	// predictor's in slot 0, the latest corrector's in slot 1
+	double* kd = kdot + (size_t)(a.mode == 3 ? (stage == 0 ? 0 : 1) : stage) * np;
 	for (int i = tid; i < P; i += blockDim.x) {
 		double r = sol[i], im = sol[P + i];
 		if (a.precond) {
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 			rhs_out[2 * P + 1] = phiDotI;
 		}
 	}
-	if (a.mode == 1 && stage == 0)
+	if ((a.mode == 1 || a.mode == 3) && stage == 0)
 		for (int i = tid; i < n_means; i += blockDim.x) means_step0[i] = means1[i];
 	__syncthreads();
 
@@ -237,11 +246,13 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 		}
 		return;
 	}
-	if (a.mode == 2 || stage == 3) {
+	const bool last = a.mode == 2 || (a.mode == 1 && stage == 3) || (a.mode == 3 && stage == kPcCorrectors);
+	if (last) {
 		// final update of the step
 		for (int i = tid; i < np; i += blockDim.x) {
 			double inc;
 			if (a.mode == 2) inc = kdot[i];
+			else if (a.mode == 3) inc = (kdot[i] + kdot[np + i]) / 2.0;
 			else inc = (kdot[i] + 2.0 * kdot[np + i] + 2.0 * kdot[2 * np + i] + kdot[3 * np + i]) / 6.0;
 			base[i] = base[i] + inc * a.dt;
 		}
@@ -249,6 +260,10 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 		if (tid == 0 && a.normalize) base[2 * P] = -(double)lnpsi_w[0];
 		__syncthreads();
 		for (int i = tid; i < np; i += blockDim.x) stage_params[i] = base[i];
+	} else if (a.mode == 3) {
+		// the predictor, or the next corrector's trial parameters
+		for (int i = tid; i < np; i += blockDim.x)
+			stage_params[i] = stage == 0 ? base[i] + kdot[i] * a.dt : base[i] + (kdot[i] + kdot[np + i]) * (a.dt / 2.0);
 	} else {
 		const double cdt = (stage < 2) ? a.dt / 2.0 : a.dt;
 		for (int i = tid; i < np; i += blockDim.x) stage_params[i] = base[i] + kd[i] * cdt;
@@ -260,7 +275,7 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 		for (int i = 0; i < np; i++)
 			if (!isfinite(stage_params[i])) st |= kStatusNonFinite;
 		dyn->status |= st;
-		dyn->stage = (a.mode == 1 && stage < 3) ? (uint32_t)(stage + 1) : 0u;
+		dyn->stage = ((a.mode == 1 && stage < 3) || (a.mode == 3 && stage < kPcCorrectors)) ? (uint32_t)(stage + 1) : 0u;
 		dyn->pass += 1u;
 	}
 }

@@ -474,6 +474,11 @@ int launch_cs_eval(tdvmc_ctx* ctx, bool adj) {
 // One RK stage on stored samples (CalculateNextParametersRK4ReuseSamples,
 // TDVMC.cpp:2037-2103, with the sample update of TDVMC.cpp:3654-3677 at the
 // first stage of a step).
+// Solvers on stored samples: RK4 (ODE_SOLVER_TYPE 3) and the predictor-corrector (5).
+inline bool cs_ode(int ode) { return ode == 3 || ode == 5; }
+// Stages per step of the time integrators (RK4 4, Euler 1, predictor + correctors).
+inline int stages_per_step(int ode) { return ode == 0 ? 1 : ode == 5 ? 1 + kPcCorrectors : 4; }
+
 template <typename T>
 int run_cs_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int kind, int64_t count) {
 	int rc;
@@ -496,8 +501,8 @@ int run_cs_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int kind, int64_t cou
 	}
 	if ((rc = launch_cs_eval<T>(ctx, adj))) return rc;
 	if ((rc = launch_reduce<T>(ctx, adj))) return rc;
-	return launch_solve<T>(ctx, o->imaginary_time, o->precondition, o->lin_solver, 1, o->normalize_wf, o->dt,
-	                       (o->use_adjoint == 2 && o->imaginary_time) ? 1 : 0);
+	return launch_solve<T>(ctx, o->imaginary_time, o->precondition, o->lin_solver, o->ode_solver == 5 ? 3 : 1,
+	                       o->normalize_wf, o->dt, (o->use_adjoint == 2 && o->imaginary_time) ? 1 : 0);
 }
 
 template <typename T>
@@ -540,8 +545,9 @@ int run_stage_any(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int kind = 0, int64_
 
 int check_opts(const tdvmc_step_opts* o) {
 	if (!o || !(o->dt == o->dt)) return TDVMC_ERR_ARG;
-	if (o->ode_solver != 0 && o->ode_solver != 2 && o->ode_solver != 3) return TDVMC_ERR_ARG;
-	if (o->ode_solver == 3 && (o->update_every < 0 || !(o->update_percent >= 0.0 && o->update_percent <= 100.0)))
+	if (o->ode_solver != 0 && o->ode_solver != 2 && !cs_ode(o->ode_solver)) return TDVMC_ERR_ARG;
+	if (cs_ode(o->ode_solver) &&
+	    (o->update_every < 0 || !(o->update_percent >= 0.0 && o->update_percent <= 100.0)))
 		return TDVMC_ERR_ARG;
 	if (o->lin_solver != 0 && o->lin_solver != 1) return TDVMC_ERR_ARG;
 	if (o->moves_per_stage < 0) return TDVMC_ERR_ARG;
@@ -606,11 +612,11 @@ void cs_plan(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int* kind, int64_t* count
 // Enqueues nsteps steps (graph replays) on the context's stream.
 int enqueue_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps) {
 	int rc;
-	if (o->ode_solver != 3) {
+	if (!cs_ode(o->ode_solver)) {
 		cudaGraphExec_t g;
 		int nk = 0;
 		if ((rc = get_graph(ctx, o, &g, &nk))) return rc;
-		const int nst = o->ode_solver == 0 ? 1 : 4;
+		const int nst = stages_per_step(o->ode_solver);
 		for (int s = 0; s < nsteps; s++)
 			for (int k = 0; k < nst; k++) {
 				CK(cudaGraphLaunch(g, ctx->st));
@@ -632,7 +638,7 @@ int enqueue_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps) {
 		if (kind != kCsReuse && (rc = get_graph(ctx, o, &g0, &nk0, kind, cnt))) return rc;
 		CK(cudaGraphLaunch(g0, ctx->st));
 		ctx->launches += nk0;
-		for (int k = 1; k < 4; k++) {
+		for (int k = 1; k < stages_per_step(o->ode_solver); k++) {
 			CK(cudaGraphLaunch(gr, ctx->st));
 			ctx->launches += nkr;
 		}
@@ -1322,7 +1328,7 @@ int tdvmc_run_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, td
 		CK(cudaStreamSynchronize(ctx->st));
 		fill_stats(ctx, m, o->moves_per_stage, stats);
 		// stored samples: the rate of the walkers the last refresh moved
-		if (o->ode_solver == 3 && ctx->cs_last_count > 0)
+		if (cs_ode(o->ode_solver) && ctx->cs_last_count > 0)
 			stats->accept_rate *= (double)ctx->nw / (double)ctx->cs_last_count;
 	}
 	if ((rc = read_status(ctx, &st))) return rc;
@@ -1346,7 +1352,7 @@ int tdvmc_time_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* o, int32_t nsteps, f
 	int rc = check_opts(o);
 	if (rc) return rc;
 	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
-	if (o->ode_solver == 3) {
+	if (cs_ode(o->ode_solver)) {
 		// build the graphs (and the store) outside the timed region
 		if ((rc = cs_alloc(ctx))) return rc;
 		cudaGraphExec_t g;
@@ -1392,7 +1398,7 @@ int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, float* ms, con
 	if ((rc = ensure_gbuf(ctx))) return rc;
 	ctx->prof = &ev;
 	ctx->prof_names = &nm;
-	if (o->ode_solver == 3) {
+	if (cs_ode(o->ode_solver)) {
 		// one first stage of the next stored-sample step (the store is not advanced)
 		int kind;
 		int64_t cnt;

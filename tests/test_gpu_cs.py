@@ -1,4 +1,4 @@
-"""GPU: correlated-sampling reuse (stored samples, ODE_SOLVER_TYPE 3).
+"""GPU: correlated-sampling reuse (stored samples, ODE_SOLVER_TYPE 3 and 5).
 
 Tolerances (stated per test):
   stored vs direct evaluation at the same walkers and parameters: FP64
@@ -6,7 +6,8 @@ Tolerances (stated per test):
       dE/d alpha (scaled by the largest magnitude of each quantity);
   RK4 on stored samples vs the FP64 oracle (sampling at the first stage,
       evaluation of the fixed samples at the three others, a rotating
-      refresh window on later steps): parameters relative 1e-9, walkers 1e-9.
+      refresh window on later steps): parameters relative 1e-9, walkers 1e-9;
+  the predictor-corrector on stored samples likewise (1e-9).
 """
 import os
 
@@ -103,6 +104,59 @@ def test_stored_sample_rk4_matches_oracle_fp64():
             if k < 3:
                 cur = base + kv * (dt / 2 if k < 2 else dt)
         base = orc.rk4_combine(base, ks, dt)
+        assert np.all(np.isfinite(base))
+        assert np.abs(after - Ro).max() < 1e-9, st
+        gR, gI, gpR, gpI = s.GetParameters()
+        assert relmax(np.concatenate([gR, gI, [gpR, gpI]]), base) < 1e-9, st
+
+
+def test_stored_sample_pc_matches_oracle_fp64():
+    """Three predictor-corrector steps on stored samples (ODE_SOLVER_TYPE 5,
+    CalculateNextParametersPCReuseSamples, TDVMC.cpp:1912-1967): Euler predictor,
+    then 6 passes u <- u + (u'(u) + u'(trial)) dt / 2, every pass evaluating the
+    stored samples; the first step samples every walker, the next two refresh
+    windows [0, nw/4) and [nw/4, nw/2).  Parameters and walkers to 1e-9."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "sample_d3_n27.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    nw, moves, step, dt, seed, pass0 = 64, 2 * n, 0.35, 1e-3, 23, 5
+    q = nw // 4
+    rng = np.random.default_rng(29)
+    R0 = np.repeat(z["R0"].T[None], nw, axis=0) + rng.normal(0, 0.05, size=(nw, dim, n))
+    R0 = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(R0)
+    uR, uI = np.asarray(z["uR"]), np.asarray(z["uI"])
+    sysp = tuple(z["sysp"])
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=sysp, potential="square", hbar2_2m=0.09, precision="fp64")
+    s.SetParameters(uR, uI, 0.0, 0.0)
+    s.SetWalkers(R0)
+    s.DoMetropolisSteps(0, step, seed, pass0)  # sets the Philox pass counter
+    td = T.TDVP(s, dt, moves, step, seed=seed, ode_solver=5, update_every=1, update_percent=25.0)
+
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_SQUARE, pot=sysp, hbar2_2m=0.09)
+    base = np.concatenate([uR, uI, [0.0, 0.0]])
+    Ro = R0.copy()
+
+    def rhs(cur):
+        out = o.stage(cur[:p], cur[p:2 * p], Ro, 0, step, seed, 0, threads=4, adjoint=False)
+        m = orc.centred(out["O"], out["eloc"])
+        dR, dI, pR, pI, _ = orc.solve_centred(m["O"], m["ER"], m["EI"], m["S"], m["cOER"], m["cOEI"])
+        return np.concatenate([dR, dI, [pR, pI]])
+
+    windows = [(0, nw), (0, q), (q, 2 * q)]
+    for st, (w0, w1) in enumerate(windows):
+        before = s.GetWalkers()
+        td.step()
+        after = s.GetWalkers()
+        moved = np.any(np.abs(after - before).reshape(nw, -1) > 0, axis=1)
+        assert not moved[:w0].any() and not moved[w1:].any()
+        pass_id = pass0 + 7 * st  # one pass per stage: predictor and 6 correctors
+        o.sample(base[:p], Ro, moves, step, seed, pass_id, w0=w0, nw=w1 - w0) if st else \
+            o.sample(base[:p], Ro, moves, step, seed, pass_id)
+        k0 = rhs(base)
+        trial = base + k0 * dt
+        for _ in range(6):
+            trial = base + (k0 + rhs(trial)) * (dt / 2)
+        base = trial
         assert np.all(np.isfinite(base))
         assert np.abs(after - Ro).max() < 1e-9, st
         gR, gI, gpR, gpI = s.GetParameters()
