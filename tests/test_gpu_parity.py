@@ -404,3 +404,45 @@ def test_maximum_size_matches_oracle(precision, tol):
         acc_o = o.sample(uR, Ro, 256, 0.1, seed=3, pass_id=2)
         assert acc == acc_o
         assert np.abs(s.GetWalkers() - Ro).max() < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("env", [{"TDVMC_HIST": "1"}, {"TDVMC_HIST": "2"}, {"TDVMC_EVAL_WALKERS_PER_BLOCK": "1"},
+                                 {"TDVMC_EVAL_WALKERS_PER_BLOCK": "4"}],
+                         ids=["hist1", "hist2", "wpb1", "wpb4"])
+def test_evaluation_variants_match_oracle(precision, env):
+    """The evaluation kernels' alternative histogram update modes (float4 slots,
+    shared-memory atomics) and forced walkers per block, selected through the
+    environment when the context is created: same results as the oracle at the
+    tolerances of the fixture cases."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "eval_d3_n343_p30.npz"))
+    cfgs = z["cfgs"]
+    nw = len(cfgs)
+    sysp = np.array([1.0, 1.0])
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        s = gpu_system(z, nw, precision, potential="lj", sysp=sysp, hbar2_2m=0.09)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    o = oracle_system(z, pot_kind=orc.POT_LJ, sysp=sysp, hbar2_2m=0.09)
+    s.SetParameters(z["uR"], z["uI"], float(z["phiR"]), float(z["phiI"]))
+    s.SetWalkers(soa(cfgs))
+    fwd = s.CalculateExpectationValues()
+    dE = s.CalculateLocalEnergyAdjoint()
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    for c, R in enumerate(cfgs):
+        if precision == "mixed" and min_pair_distance(R, float(z["L"])) < 0.7:
+            continue  # overlapping particles: see test_eval_and_adjoint_match_oracle
+        r = o.eval(z["uR"], z["uI"], R, adjoint=True)
+        assert relmax(fwd["O"][c], r["O"]) < tol
+        scaleE = max(np.abs(r["other"]).max(), 1.0)
+        assert np.abs(fwd["eloc"][c] - r["eloc"]).max() < tol * scaleE
+        assert np.abs(fwd["other"][c] - r["other"]).max() < tol * scaleE
+        scaled = max(np.abs(r["dE"]).max(), 1.0)
+        assert np.abs(dE[c] - r["dE"]).max() < (tol if precision == "fp64" else 3e-5) * scaled
