@@ -63,26 +63,42 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 	const T sr = in ? rinv : T(0);
 	const T* pc = piece + (size_t)j * kCsPiece;
 	const int s0 = j + 3;  // spline of piece q is s0 - q
+	// the 12 (spline, axis) slots of the pair are distinct: all loads first, then
+	// the stores, so the shared-memory round trips overlap
+	T b1[4], cur[4][3];
+	T* dq[4];
 #pragma unroll
 	for (int q = 0; q < 4; q++) {
-		const T b1 = fma(t, fma(t, pc[3 * q + 2], pc[3 * q + 1]), pc[3 * q]) * sr;  // B'(r) / r
-		T* dq = drow + (size_t)(s0 - q) * 3 * G + lane;
-		dq[0] = fma(b1, dx, dq[0]);
-		dq[G] = fma(b1, dy, dq[G]);
-		dq[2 * G] = fma(b1, dz, dq[2 * G]);
+		b1[q] = fma(t, fma(t, pc[3 * q + 2], pc[3 * q + 1]), pc[3 * q]);  // B'(r)
+		dq[q] = drow + (size_t)(s0 - q) * 3 * G + lane;
+		cur[q][0] = dq[q][0];
+		cur[q][1] = dq[q][G];
+		cur[q][2] = dq[q][2 * G];
+	}
+#pragma unroll
+	for (int q = 0; q < 4; q++) {
+		const T bs = b1[q] * sr;  // B'(r) / r
+		dq[q][0] = fma(bs, dx, cur[q][0]);
+		dq[q][G] = fma(bs, dy, cur[q][1]);
+		dq[q][2 * G] = fma(bs, dz, cur[q][2]);
 	}
 	if (STATS) {
 		const T on = in ? T(1) : T(0);
 		const T dm1 = (T)(sc.dim - 1);
+		T ov[4], dv[4];
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			ov[q] = oacc[(size_t)(s0 - q) * G + lane];
+			dv[q] = d2acc[(size_t)(s0 - q) * G + lane];
+		}
 #pragma unroll
 		for (int q = 0; q < 4; q++) {
 			const T* l = pc + 12 + 4 * q;
 			const T b = fma(t, fma(t, fma(t, l[3], l[2]), l[1]), l[0]) * on;
-			const T b1 = fma(t, fma(t, pc[3 * q + 2], pc[3 * q + 1]), pc[3 * q]);
 			const T b2 = fma(t, pc[28 + 2 * q + 1], pc[28 + 2 * q]);
-			const T lap = (b2 + dm1 * b1 * sr) * on;
-			oacc[(size_t)(s0 - q) * G + lane] += b;
-			d2acc[(size_t)(s0 - q) * G + lane] += T(2) * lap;  // both orderings of the pair
+			const T lap = (b2 + dm1 * b1[q] * sr) * on;
+			oacc[(size_t)(s0 - q) * G + lane] = ov[q] + b;
+			d2acc[(size_t)(s0 - q) * G + lane] = dv[q] + T(2) * lap;  // both orderings of the pair
 		}
 		vs.add(in ? pair_pot<T>(sc.pot_kind, r, rinv, pa, pb) : T(0));
 		nout += (ok && !(r <= (T)sc.rmax)) ? 1 : 0;
