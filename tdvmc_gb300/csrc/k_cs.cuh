@@ -108,7 +108,7 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 // Stores the correlated-sampling data of walkers (start + w) mod nw_total,
 // w < count (start from *wstart when given, else 0).
 template <typename T, int G>
-__global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* __restrict__ dyn,
+__global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const DynState* __restrict__ dyn,
                                                   const T* __restrict__ piece_g, const T* __restrict__ kb_g,
                                                   const T* __restrict__ hv_g, const int* __restrict__ lut_g,
                                                   const double* __restrict__ fold_g, const T* __restrict__ pos,
@@ -135,10 +135,11 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 	const unsigned wl = tid & 31;
 	const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
 	unsigned char* gbase = smem_raw + cs_cta_bytes<T>(nbin, sc.ncell) + (size_t)gib * cs_group_bytes<T>(n, ns, G);
-	Q4<T>* xs = reinterpret_cast<Q4<T>*>(gbase);
-	T* drow = reinterpret_cast<T*>(xs + n);
-	T* oacc = drow + (size_t)ns * 3 * G;
-	T* d2acc = oacc + (size_t)ns * G;
+	// disjoint regions: the compiler may move position loads across accumulator stores
+	Q4<T>* __restrict__ xs = reinterpret_cast<Q4<T>*>(gbase);
+	T* __restrict__ drow = reinterpret_cast<T*>(xs + n);
+	T* __restrict__ oacc = drow + (size_t)ns * 3 * G;
+	T* __restrict__ d2acc = oacc + (size_t)ns * G;
 	__syncthreads();
 
 	const T pa = (T)dyn->pa, pb = (T)dyn->pb;
@@ -173,6 +174,7 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 			const int base = s * G;
 			const int dend = (base + G < n) ? base + G : n;
 			// partners below the slot: every lane's pair is counted once (i < nrow)
+#pragma unroll 2
 			for (int i = 0; i < base; i++)
 				cs_pair<T, G, true>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			// the slot's own block: counted iff i < nrow
@@ -185,6 +187,7 @@ __global__ void __launch_bounds__(128) k_cs_store(SysConst sc, const DynState* _
 					                     pa, pb, vs, nout);
 			}
 			// partners above the slot: D only
+#pragma unroll 2
 			for (int i = dend; i < n; i++)
 				cs_pair<T, G, false>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			if (rowok)
