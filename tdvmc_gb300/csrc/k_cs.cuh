@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const DynState
 			const int base = s * G;
 			const int dend = (base + G < n) ? base + G : n;
 			// partners below the slot: every lane's pair is counted once (i < nrow)
-#pragma unroll 2
+#pragma unroll 4
 			for (int i = 0; i < base; i++)
 				cs_pair<T, G, true>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			// the slot's own block: counted iff i < nrow
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const DynState
 					                     pa, pb, vs, nout);
 			}
 			// partners above the slot: D only
-#pragma unroll 2
+#pragma unroll 4
 			for (int i = dend; i < n; i++)
 				cs_pair<T, G, false>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			if (rowok)
