@@ -5,11 +5,11 @@
 namespace tdvmc {
 int sample_slots_for(int n, int G) {
 	static const int l32[] = {1, 2, 4, 8, 11, 16, 32};
-	static const int l16[] = {1, 2, 4, 8};
+	static const int l16[] = {1, 2, 4, 8, 16, 22};
 	static const int l8[] = {1, 2, 4};
 	const int need = (n + G - 1) / G;
 	const int* l = G == 32 ? l32 : (G == 16 ? l16 : l8);
-	const int m = G == 32 ? 7 : (G == 16 ? 4 : 3);
+	const int m = G == 32 ? 7 : (G == 16 ? 6 : 3);
 	if (G != 32 && G != 16 && G != 8) return -1;
 	for (int i = 0; i < m; i++)
 		if (l[i] >= need) return l[i];
@@ -32,6 +32,8 @@ SampleFn<float> pick_sample_f32_packed(int G, int slots) {
 		case 2: return k_sample_f2<16, 2>;
 		case 4: return k_sample_f2<16, 4>;
 		case 8: return k_sample_f2<16, 8>;
+		case 16: return k_sample_f2<16, 16>;
+		case 22: return k_sample_f2<16, 22>;
 		}
 	} else if (G == 8) {
 		switch (slots) {

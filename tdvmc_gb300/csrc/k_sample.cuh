@@ -423,6 +423,8 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 							TDVMC_SET_SLOT(4) TDVMC_SET_SLOT(5) TDVMC_SET_SLOT(6) TDVMC_SET_SLOT(7)
 							TDVMC_SET_SLOT(8) TDVMC_SET_SLOT(9) TDVMC_SET_SLOT(10) TDVMC_SET_SLOT(11)
 							TDVMC_SET_SLOT(12) TDVMC_SET_SLOT(13) TDVMC_SET_SLOT(14) TDVMC_SET_SLOT(15)
+							TDVMC_SET_SLOT(16) TDVMC_SET_SLOT(17) TDVMC_SET_SLOT(18) TDVMC_SET_SLOT(19)
+							TDVMC_SET_SLOT(20) TDVMC_SET_SLOT(21)
 #undef TDVMC_SET_SLOT
 						}
 					}

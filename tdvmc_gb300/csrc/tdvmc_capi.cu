@@ -964,8 +964,14 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		tdvmc_destroy(ctx);
 		return TDVMC_ERR_ARG;
 	}
-	c.tiles.sgpb = 128 / c.tiles.sg;
 	c.tiles.eg = c.tiles.sg;
+	// FP32 sampler with uniform knots: where a full warp per walker needs 11 register
+	// slots, two walkers per warp (16 lanes, 22 slots) share each move's bookkeeping
+	// (1.5 % faster at N = 343); the evaluation keeps the full warp
+	if (c.prec == TDVMC_PREC_MIXED && c.sc.uniform && c.tiles.sg == 32 && slots_for(d->n, 32) == 11 &&
+	    slots_for(d->n, 16) == 22)
+		c.tiles.sg = 16;
+	c.tiles.sgpb = 128 / c.tiles.sg;
 	c.tiles.egpb = c.tiles.eg == 32 ? 0 : 32 / c.tiles.eg;
 	// TDVMC_EVAL_WALKERS_PER_BLOCK overrides the evaluation kernels' walkers per block
 	if (const char* e = std::getenv("TDVMC_EVAL_WALKERS_PER_BLOCK"))
