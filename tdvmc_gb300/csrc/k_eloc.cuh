@@ -522,7 +522,10 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 // it sits 17 lanes on).  kHalfSteps steps per iteration in two f32x2 streams;
 // the sum moves once per iteration, fed by one shuffle per step (p_j from
 // lane l + kHalfSteps - j), so its dependency chain is one shuffle long.  The
-// Laplacian enters the energy only as a total, twice the sum over pairs.
+// partners' rows of the next iteration are loaded one iteration ahead.  The
+// Laplacian enters the energy only as a total, twice the sum over pairs; the
+// pairs beyond r_max are not counted here (the caller takes all pairs less
+// the moment-0 total).
 constexpr int kHalfSteps = 4;
 
 // Potential of two pairs into vb (pair_pot; Lennard-Jones in f32x2 with the
