@@ -113,10 +113,11 @@ def test_native_driver_runs_a_reference_config(tmp_path):
     assert np.all(np.isfinite(pr))
 
 
-def test_native_driver_stored_samples_and_observables(tmp_path):
-    """ODE_SOLVER_TYPE 3 with a refresh window, and g(r) / S(k) every second step
-    from kVectors3D.json next to the config (written here from the fixture's
-    integer k vectors)."""
+@pytest.mark.parametrize("ode", [3, 5])
+def test_native_driver_stored_samples_and_observables(tmp_path, ode):
+    """ODE_SOLVER_TYPE 3 (RK4) or 5 (predictor-corrector) on stored samples with a
+    refresh window, and g(r) / S(k) every second step from kVectors3D.json next
+    to the config (written here from the fixture's integer k vectors)."""
     from tdvmc_gb300 import build as B
     B.build()
     z = np.load(os.path.join(ROOT, "tests", "golden", "obs_d3_n343.npz"))
@@ -128,7 +129,7 @@ def test_native_driver_stored_samples_and_observables(tmp_path):
     cfg = {
         "CONFIG_VERSION": "0.24", "SYSTEM_TYPE": "BosonsBulk", "N": 27, "LBOX": L, "DIM": 3, "N_PARAM": 10,
         "MC_STEP": 0.3, "MC_NSTEPS": 256, "MC_NTHERMSTEPS": 54, "MC_VERY_FIRST_NINITIALIZATIONSTEPS": 270,
-        "TIMESTEP": 0.001, "TOTALTIME": 0.0035, "IMAGINARY_TIME": 1, "ODE_SOLVER_TYPE": 3,
+        "TIMESTEP": 0.001, "TOTALTIME": 0.0035, "IMAGINARY_TIME": 1, "ODE_SOLVER_TYPE": ode,
         "UPDATE_SAMPLES_EVERY_NTH_STEP": 1, "UPDATE_SAMPLES_PERCENT": 25.0,
         "CALCULATE_ADDITIONAL_DATA_EVERY_NTH_STEP": 2, "MC_NADDITIONALTHERMSTEPS": 27, "GR_BIN_COUNT": 40,
         "LINEAR_EQUATION_SOLVER_TYPE": 0, "USE_PRECONDITIONING": 0, "USE_NORMALIZE_WF": 1,
