@@ -200,9 +200,10 @@ class BosonsBulk:
 
 
 class TDVP:
-    """One TDVP time step per call (ODE_SOLVER_TYPE 2 = RK4, 0 = Euler, 3 = RK4 on
-    stored samples with update_every / update_percent as UPDATE_SAMPLES_EVERY_NTH_STEP /
-    UPDATE_SAMPLES_PERCENT)."""
+    """One TDVP time step per call (ODE_SOLVER_TYPE 2 = RK4, 0 = Euler; on stored
+    samples 3 = RK4 (CalculateNextParametersRK4ReuseSamples) and 5 = predictor-corrector
+    (CalculateNextParametersPCReuseSamples), with update_every / update_percent as
+    UPDATE_SAMPLES_EVERY_NTH_STEP / UPDATE_SAMPLES_PERCENT)."""
 
     def __init__(self, system: BosonsBulk, dt, moves_per_stage, mc_step, seed=1, imaginary_time=0, ode_solver=2,
                  lin_solver=0, precondition=0, normalize_wf=0, use_adjoint=0, update_every=0, update_percent=100.0):
