@@ -314,7 +314,7 @@ void orc_eval(const orc_sys* s, const double* uR, const double* uI, const double
 	double* AR = (double*)calloc((size_t)ns, sizeof(double));
 	double* AI = (double*)calloc((size_t)ns, sizeof(double));
 	double nout, vint = 0.0, lapR = 0.0, lapI = 0.0;
-	double d[3], v[4], d1[4], d2[4];
+	double d[3], d1[4], d2[4];
 
 	spline_sums(s, R, S, &nout);
 	fold_apply(s, S, O);
