@@ -260,13 +260,14 @@ def test_ragged_sizes_match_oracle(nw, n, dim):
         assert np.abs(dE[w] - r["dE"]).max() < 1e-12 * max(np.abs(r["dE"]).max(), 1.0)
 
 
-@pytest.mark.parametrize("n", [65, 80, 96, 111, 337])
-def test_half_sweep_slot_edges_mixed(n):
+@pytest.mark.parametrize("dim,n", [(3, 65), (3, 80), (3, 96), (3, 111), (3, 337), (1, 70), (2, 70)])
+def test_half_sweep_slot_edges_mixed(dim, n):
     """FP32 32-lane evaluation (the half sweep of the forward kernel and the rotated
     own slot of the adjoint) at particle counts that leave the last slot of 32 rows
-    with 1, 16, 32, 15 and 17 rows; tolerances as in the fixture cases (1e-5, dE 3e-5)."""
+    with 1, 16, 32, 15, 17 and 6 rows, in 3D and at N = 70 in 1D and 2D; tolerances as
+    in the fixture cases (1e-5, dE 3e-5)."""
     import tdvmc_gb300 as T
-    dim, p, nw = 3, 12, 9
+    p, nw = 12, 9
     L = (n / 0.4) ** (1.0 / dim)
     rng = np.random.default_rng(n)
     R = rng.uniform(-L / 2, L / 2, size=(nw, dim, n))
