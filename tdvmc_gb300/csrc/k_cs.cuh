@@ -7,7 +7,9 @@
 //
 // Stored per walker, at spline level (s = 0..ns-1, before the boundary fold):
 //   D[s][a][n] = sum_{i != n, r <= r_max} B_s'(r_ni) (x_n - x_i)_a / r_ni
-//                (rows padded to npad = n rounded up to 4; the padding is zero)
+//                chunk-major: particle n at chunk n / 32, column n % 32, each chunk
+//                one contiguous block [3 s + a][32] (n padded to npad = n rounded
+//                up to 32; the padding is zero)
 //   D2[s]      = sum_n sum_{i != n, r <= r_max} (B_s''(r_ni) + (D-1)/r_ni B_s'(r_ni))
 //   O[k]       = BC-folded sum_{i < n, r <= r_max} B_s(r_ni)
 //   V          = pair potential over i < n, r <= r_max;  n_out = #pairs beyond r_max
@@ -26,15 +28,22 @@ namespace tdvmc {
 //   [12..27] l0, l1, l2, l3            (B in the local coordinate t)
 //   [28..35] 2h^2 l2, 6h^2 l3          (d2B/dr2 = c0 + t c1)
 constexpr int kCsPiece = 36;
+// Row stride of the piece table in shared memory: odd, so that lanes reading the
+// same entry of different intervals hit different banks (up to 32 intervals)
+constexpr int kCsPieceS = 37;
 
-__host__ __device__ inline int cs_npad(int n) { return (n + 3) & ~3; }
+__host__ __device__ inline int cs_npad(int n) { return (n + 31) & ~31; }
+// offset of D[e = 3 s + a][n] within one walker's block (ne = 3 ns rows)
+__host__ __device__ inline size_t cs_doff(int ne, int e, int n) {
+	return ((size_t)(n >> 5) * ne + e) * 32 + (n & 31);
+}
 
 // Shared memory of k_cs_store.
-//   CTA:   piece[nbin*36] | kb[nbin] | hv[nbin] | lut[ncell]
+//   CTA:   piece[nbin][37] (36 used) | kb[nbin] | hv[nbin] | lut[ncell]
 //   group: xs[n] | drow[ns*3*G] | oacc[ns*G] | d2acc[ns*G]   (lane-private columns)
 template <typename T>
 __host__ __device__ inline size_t cs_cta_bytes(int nbin, int ncell) {
-	size_t b = (size_t)nbin * kCsPiece * sizeof(T) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+	size_t b = (size_t)nbin * kCsPieceS * sizeof(T) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
 	return (b + 31) & ~(size_t)31;
 }
 template <typename T>
@@ -61,7 +70,7 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 	const int j = locate<T>(sc, r, kb, hv, lut, t);
 	t = in ? t : T(0);  // t is NaN for the self pair
 	const T sr = in ? rinv : T(0);
-	const T* pc = piece + (size_t)j * kCsPiece;
+	const T* pc = piece + (size_t)j * kCsPieceS;
 	const int s0 = j + 3;  // spline of piece q is s0 - q
 	// the 12 (spline, axis) slots of the pair are distinct: all loads first, then
 	// the stores, so the shared-memory round trips overlap
@@ -118,10 +127,11 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const DynState
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
 	T* piece = reinterpret_cast<T*>(smem_raw);
-	T* kb = piece + (size_t)nbin * kCsPiece;
+	T* kb = piece + (size_t)nbin * kCsPieceS;
 	T* hv = kb + nbin;
 	int* lut = reinterpret_cast<int*>(hv + nbin);
-	for (int i = threadIdx.x; i < nbin * kCsPiece; i += blockDim.x) piece[i] = piece_g[i];
+	for (int i = threadIdx.x; i < nbin * kCsPiece; i += blockDim.x)
+		piece[(i / kCsPiece) * kCsPieceS + i % kCsPiece] = piece_g[i];
 	for (int i = threadIdx.x; i < nbin; i += blockDim.x) {
 		kb[i] = kb_g[i];
 		hv[i] = hv_g[i];
@@ -191,7 +201,7 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const DynState
 			for (int i = dend; i < n; i++)
 				cs_pair<T, G, false>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			if (rowok)
-				for (int e = 0; e < ns * 3; e++) Dw[(size_t)e * npad + nrow] = drow[(size_t)e * G + lane];
+				for (int e = 0; e < ns * 3; e++) Dw[cs_doff(ns * 3, e, nrow)] = drow[(size_t)e * G + lane];
 		}
 		__syncwarp(gmask);
 		// lane-ordered sums of the lane-private accumulators
@@ -263,6 +273,72 @@ __host__ __device__ inline size_t cs_eval_smem_bytes(int n, int ns, int warps) {
 	return ((size_t)cs_ns2(ns) + (size_t)warps * ((size_t)2 * kCsPartRow * ns + cs_ns2(ns))) * sizeof(T);
 }
 
+// The end of one walker's stored-sample evaluation: the Laplacian sums from D2,
+// ln psi, O, E_loc, the kinetic sums and, with ADJ, dE/d alpha from
+// asum[2s + {0, 1}] = sum_n G_n . D[s][.][n] (complex).  One warp.
+template <typename T, bool ADJ>
+__device__ __forceinline__ void cs_finish_walker(const SysConst& sc, const double* __restrict__ params,
+                                 const double* __restrict__ fold_g, const T* __restrict__ D2,
+                                 const T* __restrict__ Os, const T* __restrict__ Vs,
+                                 const int32_t* __restrict__ nouts, int64_t w, const T* wR, const T* wI,
+                                 const T* asum, const KSum<T>& r1, const KSum<T>& i1, const KSum<T>& r1i1,
+                                 T* __restrict__ lnpsi_o, T* __restrict__ O_o, T* __restrict__ eloc_o,
+                                 T* __restrict__ other_o, T* __restrict__ dE_o) {
+	const int ns = sc.ns, P = sc.p;
+	const int lane = threadIdx.x & 31;
+	const double c = sc.hbar2_2m;
+	T l2r = T(0), l2i = T(0);
+	for (int s = lane; s < ns; s += 32) {
+		const T v = D2[(size_t)w * ns + s];
+		l2r = fma(wR[s], v, l2r);
+		l2i = fma(wI[s], v, l2i);
+	}
+	const T sR1 = group_sum<T, 32>(r1.value(), 0xffffffffu);
+	const T sI1 = group_sum<T, 32>(i1.value(), 0xffffffffu);
+	const T sR1I1 = group_sum<T, 32>(r1i1.value(), 0xffffffffu);
+	const T sR2 = group_sum<T, 32>(l2r, 0xffffffffu);
+	const T sI2 = group_sum<T, 32>(l2i, 0xffffffffu);
+	const T vint = Vs[w];
+	double lnp = 0.0;
+	for (int k = lane; k < P; k += 32) {
+		const T o = Os[(size_t)w * P + k];
+		O_o[(size_t)w * P + k] = o;
+		lnp += params[k] * (double)o;
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) lnp += __shfl_xor_sync(0xffffffffu, lnp, o);
+	if (lane == 0) {
+		lnp += params[P - 1] * (double)nouts[w];
+		const double kinR = -((double)sR1 - (double)sI1 + (double)sR2) * c;
+		const double kinI = -((double)sR1I1 + (double)sI2) * c;
+		lnpsi_o[w] = (T)lnp;
+		eloc_o[2 * w + 0] = (T)(kinR + (double)vint);
+		eloc_o[2 * w + 1] = (T)kinI;
+		T* ot = other_o + (size_t)w * 7;
+		ot[0] = (T)kinR;
+		ot[1] = vint;
+		ot[2] = sR1;
+		ot[3] = sI1;
+		ot[4] = sR2;
+		ot[5] = sI2;
+		ot[6] = sR1I1;
+	}
+	if (ADJ) {
+		__syncwarp();
+		for (int k = lane; k < P; k += 32) {
+			double dR = 0.0, dI = 0.0;
+			for (int s = 0; s < ns; s++) {
+				const double f = fold_g[(size_t)k * ns + s];
+				if (f == 0.0) continue;
+				dR += f * (2.0 * (double)asum[2 * s] + (double)D2[(size_t)w * ns + s]);
+				dI += f * (2.0 * (double)asum[2 * s + 1]);
+			}
+			dE_o[((size_t)w * P + k) * 2 + 0] = (T)(-c * dR);
+			dE_o[((size_t)w * P + k) * 2 + 1] = (T)(-c * dI);
+		}
+	}
+}
+
 template <typename T, bool ADJ>
 __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __restrict__ params,
                                                  const double* __restrict__ fold_g, const T* __restrict__ D,
@@ -293,7 +369,6 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 	__syncthreads();
 	T* part = gs_all + (size_t)warp * ((size_t)2 * kCsPartRow * ns + cs_ns2(ns));
 	T* asum = part + (size_t)2 * kCsPartRow * ns;
-	const double c = sc.hbar2_2m;
 
 	for (int64_t w = (int64_t)blockIdx.x * wpb + warp; w < nw; w += (int64_t)gridDim.x * wpb) {
 		const T* Dw = D + (size_t)w * ns * 3 * npad;
@@ -314,7 +389,7 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 #pragma unroll
 				for (int a = 0; a < 3; a++) {
 					T d[V];
-					Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + ((size_t)s * 3 + a) * npad + c0), d);
+					Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + cs_doff(3 * ns, 3 * s + a, c0)), d);
 #pragma unroll
 					for (int v = 0; v < V; v++) {
 						gr[a][v] = fma(a_, d[v], gr[a][v]);
@@ -337,7 +412,7 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 #pragma unroll
 					for (int a = 0; a < 3; a++) {
 						T d[V];
-						Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + ((size_t)s * 3 + a) * npad + c0), d);
+						Vec16<T>::get(*reinterpret_cast<const VT*>(Dw + cs_doff(3 * ns, 3 * s + a, c0)), d);
 #pragma unroll
 						for (int v = 0; v < V; v++) {
 							cr = fma(gr[a][v], d[v], cr);
@@ -349,42 +424,6 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 					pp[1] += ci;
 				}
 			}
-		}
-		T l2r = T(0), l2i = T(0);
-		for (int s = lane; s < ns; s += 32) {
-			const T v = D2[(size_t)w * ns + s];
-			l2r = fma(wR[s], v, l2r);
-			l2i = fma(wI[s], v, l2i);
-		}
-		const T sR1 = group_sum<T, 32>(r1.value(), 0xffffffffu);
-		const T sI1 = group_sum<T, 32>(i1.value(), 0xffffffffu);
-		const T sR1I1 = group_sum<T, 32>(r1i1.value(), 0xffffffffu);
-		const T sR2 = group_sum<T, 32>(l2r, 0xffffffffu);
-		const T sI2 = group_sum<T, 32>(l2i, 0xffffffffu);
-		const T vint = Vs[w];
-		double lnp = 0.0;
-		for (int k = lane; k < P; k += 32) {
-			const T o = Os[(size_t)w * P + k];
-			O_o[(size_t)w * P + k] = o;
-			lnp += params[k] * (double)o;
-		}
-#pragma unroll
-		for (int o = 16; o > 0; o >>= 1) lnp += __shfl_xor_sync(0xffffffffu, lnp, o);
-		if (lane == 0) {
-			lnp += params[P - 1] * (double)nouts[w];
-			const double kinR = -((double)sR1 - (double)sI1 + (double)sR2) * c;
-			const double kinI = -((double)sR1I1 + (double)sI2) * c;
-			lnpsi_o[w] = (T)lnp;
-			eloc_o[2 * w + 0] = (T)(kinR + (double)vint);
-			eloc_o[2 * w + 1] = (T)kinI;
-			T* ot = other_o + (size_t)w * 7;
-			ot[0] = (T)kinR;
-			ot[1] = vint;
-			ot[2] = sR1;
-			ot[3] = sI1;
-			ot[4] = sR2;
-			ot[5] = sI2;
-			ot[6] = sR1I1;
 		}
 		if (ADJ) {
 			__syncwarp();
@@ -399,19 +438,142 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 				asum[2 * s] = ar;
 				asum[2 * s + 1] = ai;
 			}
+		}
+		cs_finish_walker<T, ADJ>(sc, params, fold_g, D2, Os, Vs, nouts, w, wR, wI, asum, r1, i1, r1i1, lnpsi_o, O_o,
+		                         eloc_o, other_o, dE_o);
+		__syncwarp();
+	}
+}
+
+// Stored-sample evaluation in FP32 for ns <= 32: one warp per walker, the
+// walker's D streamed through shared memory one contiguous 32-particle chunk at
+// a time by 16-byte coalesced loads (each byte of D leaves HBM once), then one
+// particle per lane:
+// G_n from the chunk, and with ADJ the per-spline partial sums of G_n . D[s][.][n]
+// kept in registers.  At the walker's end the lanes' sums pass through the chunk
+// buffer (row of 2 ns + 1 floats per lane) and are added in lane order.
+constexpr int kCsStNs = 32;
+constexpr int kCsStBatch = 8;  // 16-byte loads in flight per lane while a chunk is staged
+__host__ __device__ inline int cs_st_warp_floats(int ns) {
+	const int chunk = ns * 3 * 32, tr = 32 * (2 * ns + 1);
+	return (((chunk > tr) ? chunk : tr) + 3) & ~3;
+}
+__host__ __device__ inline size_t cs_eval_st_smem_bytes(int ns, int warps) {
+	return ((size_t)cs_ns2(ns) + (size_t)warps * ((size_t)cs_st_warp_floats(ns) + cs_ns2(ns))) * sizeof(float);
+}
+
+template <bool ADJ>
+__global__ void __launch_bounds__(128, 4) k_cs_eval_st(SysConst sc, const double* __restrict__ params,
+                                                       const double* __restrict__ fold_g, const float* __restrict__ D,
+                                                       const float* __restrict__ D2, const float* __restrict__ Os,
+                                                       const float* __restrict__ Vs,
+                                                       const int32_t* __restrict__ nouts, int64_t nw,
+                                                       float* __restrict__ lnpsi_o, float* __restrict__ O_o,
+                                                       float* __restrict__ eloc_o, float* __restrict__ other_o,
+                                                       float* __restrict__ dE_o) {
+	extern __shared__ __align__(32) unsigned char smem_raw[];
+	const int n = sc.n, ns = sc.ns, P = sc.p;
+	const int npad = cs_npad(n), nrow = 3 * ns;
+	float* wR = reinterpret_cast<float*>(smem_raw);
+	float* wI = wR + ns;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int wpb = blockDim.x >> 5;
+	for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+		double r = 0.0, im = 0.0;
+		for (int k = 0; k < P; k++) {
+			const double f = fold_g[(size_t)k * ns + s];
+			r += params[k] * f;
+			im += params[P + k] * f;
+		}
+		wR[s] = (float)r;
+		wI[s] = (float)im;
+	}
+	__syncthreads();
+	const int wfl = cs_st_warp_floats(ns);
+	float* chunk = wR + cs_ns2(ns) + (size_t)warp * (wfl + cs_ns2(ns));  // [row = 3 s + a][32]
+	float* asum = chunk + wfl;
+
+	for (int64_t w = (int64_t)blockIdx.x * wpb + warp; w < nw; w += (int64_t)gridDim.x * wpb) {
+		const float* Dw = D + (size_t)w * nrow * npad;
+		KSum<float> r1, i1, r1i1;
+		float pr[kCsStNs], pi[kCsStNs];
+#pragma unroll
+		for (int s = 0; s < kCsStNs; s++) pr[s] = pi[s] = 0.f;
+		for (int c0 = 0; c0 < n; c0 += 32) {
+			// stage the chunk D[.][.][c0, c0 + 32): one contiguous block of 3 ns rows x 32
+			const float4* src = reinterpret_cast<const float4*>(Dw + (size_t)c0 * nrow);
+			float4* dst = reinterpret_cast<float4*>(chunk);
+			const int n4 = nrow * 8;
 			__syncwarp();
-			for (int k = lane; k < P; k += 32) {
-				double dR = 0.0, dI = 0.0;
-				for (int s = 0; s < ns; s++) {
-					const double f = fold_g[(size_t)k * ns + s];
-					if (f == 0.0) continue;
-					dR += f * (2.0 * (double)asum[2 * s] + (double)D2[(size_t)w * ns + s]);
-					dI += f * (2.0 * (double)asum[2 * s + 1]);
+			for (int q0 = 0; q0 < n4; q0 += 32 * kCsStBatch) {
+				float4 v[kCsStBatch];
+#pragma unroll
+				for (int b = 0; b < kCsStBatch; b++) {
+					const int q = q0 + 32 * b + lane;
+					v[b] = q < n4 ? __ldcs(src + q) : make_float4(0.f, 0.f, 0.f, 0.f);
 				}
-				dE_o[((size_t)w * P + k) * 2 + 0] = (T)(-c * dR);
-				dE_o[((size_t)w * P + k) * 2 + 1] = (T)(-c * dI);
+#pragma unroll
+				for (int b = 0; b < kCsStBatch; b++) {
+					const int q = q0 + 32 * b + lane;
+					if (q < n4) dst[q] = v[b];
+				}
+			}
+			__syncwarp();
+			float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f, gi0 = 0.f, gi1 = 0.f, gi2 = 0.f;
+#pragma unroll
+			for (int s = 0; s < kCsStNs; s++) {
+				if (s < ns) {
+					const float a_ = wR[s], b_ = wI[s];
+					const float d0 = chunk[(3 * s) * 32 + lane], d1 = chunk[(3 * s + 1) * 32 + lane],
+					            d2 = chunk[(3 * s + 2) * 32 + lane];
+					gr0 = fmaf(a_, d0, gr0);
+					gr1 = fmaf(a_, d1, gr1);
+					gr2 = fmaf(a_, d2, gr2);
+					gi0 = fmaf(b_, d0, gi0);
+					gi1 = fmaf(b_, d1, gi1);
+					gi2 = fmaf(b_, d2, gi2);
+				}
+			}
+			if (c0 + lane < n) {
+				r1.add(gr0 * gr0 + gr1 * gr1 + gr2 * gr2);
+				i1.add(gi0 * gi0 + gi1 * gi1 + gi2 * gi2);
+				r1i1.add(2.f * (gr0 * gi0 + gr1 * gi1 + gr2 * gi2));
+			}
+			if (ADJ) {
+#pragma unroll
+				for (int s = 0; s < kCsStNs; s++) {
+					if (s < ns) {
+						const float d0 = chunk[(3 * s) * 32 + lane], d1 = chunk[(3 * s + 1) * 32 + lane],
+						            d2 = chunk[(3 * s + 2) * 32 + lane];
+						pr[s] = fmaf(gr0, d0, fmaf(gr1, d1, fmaf(gr2, d2, pr[s])));
+						pi[s] = fmaf(gi0, d0, fmaf(gi1, d1, fmaf(gi2, d2, pi[s])));
+					}
+				}
 			}
 		}
+		if (ADJ) {
+			const int rl = 2 * ns + 1;
+			__syncwarp();
+#pragma unroll
+			for (int s = 0; s < kCsStNs; s++) {
+				if (s < ns) {
+					chunk[lane * rl + 2 * s] = pr[s];
+					chunk[lane * rl + 2 * s + 1] = pi[s];
+				}
+			}
+			__syncwarp();
+			for (int s = lane; s < ns; s += 32) {
+				float ar = 0.f, ai = 0.f;
+				for (int l = 0; l < 32; l++) {
+					ar += chunk[l * rl + 2 * s];
+					ai += chunk[l * rl + 2 * s + 1];
+				}
+				asum[2 * s] = ar;
+				asum[2 * s + 1] = ai;
+			}
+		}
+		cs_finish_walker<float, ADJ>(sc, params, fold_g, D2, Os, Vs, nouts, w, wR, wI, asum, r1, i1, r1i1, lnpsi_o,
+		                             O_o, eloc_o, other_o, dE_o);
 		__syncwarp();
 	}
 }

@@ -458,6 +458,22 @@ template <typename T>
 int launch_cs_eval(tdvmc_ctx* ctx, bool adj) {
 	const SysConst& s = ctx->sc;
 	const int threads = 128, wpb = threads / 32;
+	if constexpr (sizeof(T) == 4) {
+		if (s.ns <= kCsStNs) {
+			const size_t smem = cs_eval_st_smem_bytes(s.ns, wpb);
+			auto fn = adj ? k_cs_eval_st<true> : k_cs_eval_st<false>;
+			CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+			const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, wpb);
+			fn<<<grid, threads, smem, ctx->st>>>(s, ctx->stage, ctx->fold_d, (const float*)ctx->csD,
+			                                     (const float*)ctx->csD2, (const float*)ctx->csO, (const float*)ctx->csV,
+			                                     ctx->csN, ctx->nw, (float*)ctx->lnpsi, (float*)ctx->O, (float*)ctx->eloc,
+			                                     (float*)ctx->other7, (float*)ctx->dE);
+			ctx->launches++;
+			mark(ctx, adj ? "k_cs_eval_st_adjoint" : "k_cs_eval_st");
+			CK(cudaGetLastError());
+			return TDVMC_OK;
+		}
+	}
 	const size_t smem = cs_eval_smem_bytes<T>(s.n, s.ns, wpb);
 	auto fn = adj ? k_cs_eval<T, true> : k_cs_eval<T, false>;
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
