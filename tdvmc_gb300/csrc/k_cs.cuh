@@ -52,11 +52,19 @@ __host__ __device__ inline size_t cs_group_bytes(int n, int ns, int G) {
 	return (b + 31) & ~(size_t)31;
 }
 
+// With equal interval widths every interval has the same piece row (the
+// B-spline basis is translation invariant); it is passed as a kernel parameter,
+// so the polynomial evaluations take their coefficients from the constant bank.
+template <typename T> struct CsPieceRow {
+	T c[kCsPiece];
+};
+
 // One (row, partner) pair: the row's D columns always; with STATS also the
 // pair's O, D2, potential and outer count (unordered pairs, counted once).
-template <typename T, int G, bool STATS>
+// UNI: the piece row is pu for every interval, else row j of the shared table.
+template <typename T, int G, bool STATS, bool UNI>
 __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
-                                        const T* __restrict__ piece, const T* __restrict__ kb,
+                                        const CsPieceRow<T>& pu, const T* __restrict__ piece, const T* __restrict__ kb,
                                         const T* __restrict__ hv, const int* __restrict__ lut, T* __restrict__ drow,
                                         T* __restrict__ oacc, T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs,
                                         int& nout) {
@@ -70,7 +78,11 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 	const int j = locate<T>(sc, r, kb, hv, lut, t);
 	t = in ? t : T(0);  // t is NaN for the self pair
 	const T sr = in ? rinv : T(0);
-	const T* pc = piece + (size_t)j * kCsPieceS;
+	const T* pj = piece + (size_t)j * kCsPieceS;
+	auto pc = [&](int k) -> T {
+		if constexpr (UNI) return pu.c[k];
+		else return pj[k];
+	};
 	const int s0 = j + 3;  // spline of piece q is s0 - q
 	// the 12 (spline, axis) slots of the pair are distinct: all loads first, then
 	// the stores, so the shared-memory round trips overlap
@@ -78,7 +90,7 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 	T* dq[4];
 #pragma unroll
 	for (int q = 0; q < 4; q++) {
-		b1[q] = fma(t, fma(t, pc[3 * q + 2], pc[3 * q + 1]), pc[3 * q]);  // B'(r)
+		b1[q] = fma(t, fma(t, pc(3 * q + 2), pc(3 * q + 1)), pc(3 * q));  // B'(r)
 		dq[q] = drow + (size_t)(s0 - q) * 3 * G + lane;
 		cur[q][0] = dq[q][0];
 		cur[q][1] = dq[q][G];
@@ -102,9 +114,9 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 		}
 #pragma unroll
 		for (int q = 0; q < 4; q++) {
-			const T* l = pc + 12 + 4 * q;
-			const T b = fma(t, fma(t, fma(t, l[3], l[2]), l[1]), l[0]) * on;
-			const T b2 = fma(t, pc[28 + 2 * q + 1], pc[28 + 2 * q]);
+			const int l = 12 + 4 * q;
+			const T b = fma(t, fma(t, fma(t, pc(l + 3), pc(l + 2)), pc(l + 1)), pc(l)) * on;
+			const T b2 = fma(t, pc(28 + 2 * q + 1), pc(28 + 2 * q));
 			const T lap = (b2 + dm1 * b1[q] * sr) * on;
 			oacc[(size_t)(s0 - q) * G + lane] = ov[q] + b;
 			d2acc[(size_t)(s0 - q) * G + lane] = dv[q] + T(2) * lap;  // both orderings of the pair
@@ -116,8 +128,8 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 
 // Stores the correlated-sampling data of walkers (start + w) mod nw_total,
 // w < count (start from *wstart when given, else 0).
-template <typename T, int G>
-__global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const DynState* __restrict__ dyn,
+template <typename T, int G, bool UNI>
+__global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const CsPieceRow<T> pu, const DynState* __restrict__ dyn,
                                                   const T* __restrict__ piece_g, const T* __restrict__ kb_g,
                                                   const T* __restrict__ hv_g, const int* __restrict__ lut_g,
                                                   const double* __restrict__ fold_g, const T* __restrict__ pos,
@@ -186,20 +198,20 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const DynState
 			// partners below the slot: every lane's pair is counted once (i < nrow)
 #pragma unroll 4
 			for (int i = 0; i < base; i++)
-				cs_pair<T, G, true>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
+				cs_pair<T, G, true, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			// the slot's own block: counted iff i < nrow
 			for (int i = base; i < dend; i++) {
 				if (i < nrow)
-					cs_pair<T, G, true>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs,
+					cs_pair<T, G, true, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs,
 					                    nout);
 				else
-					cs_pair<T, G, false>(sc, xr, xs[i], rowok && i != nrow, piece, kb, hv, lut, drow, oacc, d2acc, lane,
+					cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok && i != nrow, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane,
 					                     pa, pb, vs, nout);
 			}
 			// partners above the slot: D only
 #pragma unroll 4
 			for (int i = dend; i < n; i++)
-				cs_pair<T, G, false>(sc, xr, xs[i], rowok, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
+				cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 			if (rowok)
 				for (int e = 0; e < ns * 3; e++) Dw[cs_doff(ns * 3, e, nrow)] = drow[(size_t)e * G + lane];
 		}
@@ -447,13 +459,13 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 
 // Stored-sample evaluation in FP32 for ns <= 32: one warp per walker, the
 // walker's D streamed through shared memory one contiguous 32-particle chunk at
-// a time by 16-byte coalesced loads (each byte of D leaves HBM once), then one
-// particle per lane:
-// G_n from the chunk, and with ADJ the per-spline partial sums of G_n . D[s][.][n]
-// kept in registers.  At the walker's end the lanes' sums pass through the chunk
-// buffer (row of 2 ns + 1 floats per lane) and are added in lane order.
+// a time by 16-byte cp.async copies (each byte of D leaves HBM once; one
+// buffer per warp keeps 16 warps on an SM, and the other warps' copies overlap
+// this warp's arithmetic), then one particle per lane: G_n from the chunk, and with ADJ the per-spline
+// partial sums of G_n . D[s][.][n] kept in registers.  At the walker's end the
+// lanes' sums pass through the buffer just used (row of 2 ns + 1 floats per
+// lane) and are added in lane order.
 constexpr int kCsStNs = 32;
-constexpr int kCsStBatch = 8;  // 16-byte loads in flight per lane while a chunk is staged
 __host__ __device__ inline int cs_st_warp_floats(int ns) {
 	const int chunk = ns * 3 * 32, tr = 32 * (2 * ns + 1);
 	return (((chunk > tr) ? chunk : tr) + 3) & ~3;
@@ -462,18 +474,27 @@ __host__ __device__ inline size_t cs_eval_st_smem_bytes(int ns, int warps) {
 	return ((size_t)cs_ns2(ns) + (size_t)warps * ((size_t)cs_st_warp_floats(ns) + cs_ns2(ns))) * sizeof(float);
 }
 
+// One lane's share of a chunk copy: n4 16-byte pieces, global -> shared, as one
+// cp.async group.
+__device__ __forceinline__ void cs_chunk_copy(float* dst, const float* src, int n4, int lane) {
+	const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+	for (int q = lane; q < n4; q += 32)
+		asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + 16u * (uint32_t)q),
+		             "l"(src + 4 * (size_t)q)
+		             : "memory");
+	asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cs_copy_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 template <bool ADJ>
-__global__ void __launch_bounds__(128, 4) k_cs_eval_st(SysConst sc, const double* __restrict__ params,
-                                                       const double* __restrict__ fold_g, const float* __restrict__ D,
-                                                       const float* __restrict__ D2, const float* __restrict__ Os,
-                                                       const float* __restrict__ Vs,
-                                                       const int32_t* __restrict__ nouts, int64_t nw,
-                                                       float* __restrict__ lnpsi_o, float* __restrict__ O_o,
-                                                       float* __restrict__ eloc_o, float* __restrict__ other_o,
-                                                       float* __restrict__ dE_o) {
+__global__ void __launch_bounds__(128, 4) k_cs_eval_st(
+    SysConst sc, const double* __restrict__ params, const double* __restrict__ fold_g, const float* __restrict__ D,
+    const float* __restrict__ D2, const float* __restrict__ Os, const float* __restrict__ Vs,
+    const int32_t* __restrict__ nouts, int64_t nw, float* __restrict__ lnpsi_o, float* __restrict__ O_o,
+    float* __restrict__ eloc_o, float* __restrict__ other_o, float* __restrict__ dE_o) {
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int n = sc.n, ns = sc.ns, P = sc.p;
-	const int npad = cs_npad(n), nrow = 3 * ns;
+	const int npad = cs_npad(n), nrow = 3 * ns, nch = npad / 32, n4 = nrow * 8;
 	float* wR = reinterpret_cast<float*>(smem_raw);
 	float* wI = wR + ns;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -492,33 +513,19 @@ __global__ void __launch_bounds__(128, 4) k_cs_eval_st(SysConst sc, const double
 	const int wfl = cs_st_warp_floats(ns);
 	float* chunk = wR + cs_ns2(ns) + (size_t)warp * (wfl + cs_ns2(ns));  // [row = 3 s + a][32]
 	float* asum = chunk + wfl;
+	const size_t wstride = (size_t)nrow * npad;
 
 	for (int64_t w = (int64_t)blockIdx.x * wpb + warp; w < nw; w += (int64_t)gridDim.x * wpb) {
-		const float* Dw = D + (size_t)w * nrow * npad;
+		const float* Dw = D + (size_t)w * wstride;
 		KSum<float> r1, i1, r1i1;
 		float pr[kCsStNs], pi[kCsStNs];
 #pragma unroll
 		for (int s = 0; s < kCsStNs; s++) pr[s] = pi[s] = 0.f;
-		for (int c0 = 0; c0 < n; c0 += 32) {
-			// stage the chunk D[.][.][c0, c0 + 32): one contiguous block of 3 ns rows x 32
-			const float4* src = reinterpret_cast<const float4*>(Dw + (size_t)c0 * nrow);
-			float4* dst = reinterpret_cast<float4*>(chunk);
-			const int n4 = nrow * 8;
+		for (int c = 0; c < nch; c++) {
+			cs_chunk_copy(chunk, Dw + (size_t)c * nrow * 32, n4, lane);
+			cs_copy_wait_all();
 			__syncwarp();
-			for (int q0 = 0; q0 < n4; q0 += 32 * kCsStBatch) {
-				float4 v[kCsStBatch];
-#pragma unroll
-				for (int b = 0; b < kCsStBatch; b++) {
-					const int q = q0 + 32 * b + lane;
-					v[b] = q < n4 ? __ldcs(src + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-				}
-#pragma unroll
-				for (int b = 0; b < kCsStBatch; b++) {
-					const int q = q0 + 32 * b + lane;
-					if (q < n4) dst[q] = v[b];
-				}
-			}
-			__syncwarp();
+			const int c0 = c * 32;
 			float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f, gi0 = 0.f, gi1 = 0.f, gi2 = 0.f;
 #pragma unroll
 			for (int s = 0; s < kCsStNs; s++) {
@@ -550,10 +557,10 @@ __global__ void __launch_bounds__(128, 4) k_cs_eval_st(SysConst sc, const double
 					}
 				}
 			}
+			__syncwarp();  // every lane is done with the chunk before the next copy
 		}
 		if (ADJ) {
 			const int rl = 2 * ns + 1;
-			__syncwarp();
 #pragma unroll
 			for (int s = 0; s < kCsStNs; s++) {
 				if (s < ns) {

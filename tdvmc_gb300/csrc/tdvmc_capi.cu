@@ -93,6 +93,8 @@ struct tdvmc_ctx {
 	std::map<GraphKey, int> graph_kernels;  // kernels launched by one replay
 	// stored samples (correlated-sampling reuse), allocated on first use
 	void *csD = nullptr, *csD2 = nullptr, *csO = nullptr, *csV = nullptr, *cs_piece = nullptr;
+	bool cs_uni = false;          // every interval has the same piece row (equal widths)
+	double cs_pu[kCsPiece] = {};  // that row
 	void* gbuf = nullptr;  // per-particle gradients [w][6][n] passed to the reverse (adjoint) kernel
 	// sampling / evaluation pipeline over walker chunks: the sampler runs on st,
 	// the evaluation of the previous chunk on st2 beside it.  Off by default:
@@ -442,10 +444,12 @@ int launch_cs_store(tdvmc_ctx* ctx, int64_t count, const int32_t* wstart) {
 	int gpb = 4;
 	while (gpb > 1 && cta + gpb * grp > 200 * 1024) gpb--;
 	const size_t smem = cta + gpb * grp;
-	auto fn = k_cs_store<T, G>;
+	auto fn = ctx->cs_uni ? k_cs_store<T, G, true> : k_cs_store<T, G, false>;
+	CsPieceRow<T> pu;
+	for (int k = 0; k < kCsPiece; k++) pu.c[k] = (T)ctx->cs_pu[k];
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const int grid = grid_for(ctx, (const void*)fn, G * gpb, smem, count, gpb);
-	fn<<<grid, G * gpb, smem, ctx->st>>>(s, ctx->dyn, (const T*)ctx->cs_piece, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut,
+	fn<<<grid, G * gpb, smem, ctx->st>>>(s, pu, ctx->dyn, (const T*)ctx->cs_piece, (const T*)ctx->kb, (const T*)ctx->hv, ctx->lut,
 	                               ctx->fold_d, (const T*)ctx->pos, count, ctx->nw, wstart, (T*)ctx->csD,
 	                               (T*)ctx->csD2, (T*)ctx->csO, (T*)ctx->csV, ctx->csN);
 	ctx->launches++;
@@ -940,6 +944,17 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 			pc[28 + 2 * q + 0] = 2.0 * h * h * l[2];
 			pc[28 + 2 * q + 1] = 6.0 * h * h * l[3];
 		}
+	{
+		// equal widths: one row for all intervals when the rows agree to rounding
+		double scale = 0.0;
+		for (int k = 0; k < kCsPiece; k++) scale = std::max(scale, std::fabs(piece[k]));
+		bool same = s.uniform != 0;
+		for (int j = 1; same && j < s.nbin; j++)
+			for (int k = 0; k < kCsPiece; k++)
+				if (std::fabs(piece[(size_t)j * kCsPiece + k] - piece[k]) > 1e-12 * scale) same = false;
+		c.cs_uni = same;
+		for (int k = 0; k < kCsPiece; k++) c.cs_pu[k] = piece[k];
+	}
 	std::vector<char> pieceT(piece.size() * ts);
 	for (size_t i = 0; i < piece.size(); i++) {
 		if (c.prec == TDVMC_PREC_FP64) ((double*)pieceT.data())[i] = piece[i];
