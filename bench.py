@@ -239,7 +239,13 @@ def run_ours(args):
                         precision="mixed")
     sysm.SetParameters(uR, uI)
     sysm.SetWalkers(R0)
-    td = T.TDVP(sysm, DT, MOVES, MC_STEP, seed=1, use_adjoint=1)
+    if args.stored and args.no_extras:
+        # profiling runs of the stored-sample path: RK4 (3) or the predictor-corrector (5)
+        # on stored samples, a rotating quarter of the walkers resampled per step
+        td = T.TDVP(sysm, DT, MOVES, MC_STEP, seed=1, use_adjoint=1, ode_solver=3 if args.stored == "rk4" else 5,
+                    update_every=1, update_percent=25.0)
+    else:
+        td = T.TDVP(sysm, DT, MOVES, MC_STEP, seed=1, use_adjoint=1)
     if args.autotune:
         sysm.Autotune(MOVES, MC_STEP)
     launches0 = sysm.LaunchCount()
@@ -395,6 +401,8 @@ def main():
     ap.add_argument("--walkers", type=int, default=NW, help="walkers (default: the 65,536 of the workload)")
     ap.add_argument("--no-extras", action="store_true",
                     help="time the steps only (no e2e, FP64, CPU or gate legs): for profiler runs on a small case")
+    ap.add_argument("--stored", choices=["rk4", "pc"], default=None,
+                    help="with --no-extras: time steps on stored samples (RK4 or the predictor-corrector)")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

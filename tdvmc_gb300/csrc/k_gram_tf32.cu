@@ -194,16 +194,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_gram_tf32(int p, int npad, int6
 	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
-// S[k][l] = (sum_b partial[b][k][l] + partial[b][l][k]) / (2 nw), FP64, fixed order
-__global__ void __launch_bounds__(256) k_gram_finalize(int p, int nblk, const float* __restrict__ partial, double inv_nw,
-                                                       double* __restrict__ S) {
-	for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
-		const int k = e / p, l = e % p;
-		double s = 0.0;
-		for (int b = 0; b < nblk; b++)
-			s += (double)partial[((size_t)b * p + k) * p + l] + (double)partial[((size_t)b * p + l) * p + k];
-		S[e] = 0.5 * s * inv_nw;
-	}
+// S[k][l] = (sum_b partial[b][k][l] + partial[b][l][k]) / (2 nw), FP64, fixed
+// order: one warp per entry, lane l adding blocks l, l + 32, ..., then a fixed
+// butterfly.
+constexpr int kGramFinThreads = 256;
+__global__ void __launch_bounds__(kGramFinThreads) k_gram_finalize(int p, int nblk, const float* __restrict__ partial,
+                                                                   double inv_nw, double* __restrict__ S) {
+	const int lane = threadIdx.x & 31;
+	const int e = blockIdx.x * (kGramFinThreads / 32) + (threadIdx.x >> 5);
+	if (e >= p * p) return;  // whole warps
+	const int k = e / p, l = e % p;
+	double s = 0.0;
+	for (int b = lane; b < nblk; b += 32)
+		s += (double)partial[((size_t)b * p + k) * p + l] + (double)partial[((size_t)b * p + l) * p + k];
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if (lane == 0) S[e] = 0.5 * s * inv_nw;
 }
 
 }  // namespace
@@ -224,7 +230,8 @@ int launch_gram_tf32(cudaStream_t st, int p, int64_t nw, const float* O, const d
 	const size_t smem = gram_smem_bytes();
 	if (cudaFuncSetAttribute(k_gram_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
 	k_gram_tf32<<<nblk, kThreads, smem, st>>>(p, npad, nw, O, means, partial);
-	k_gram_finalize<<<1, 256, 0, st>>>(p, nblk, partial, 1.0 / (double)nw, S);
+	k_gram_finalize<<<(p * p + kGramFinThreads / 32 - 1) / (kGramFinThreads / 32), kGramFinThreads, 0, st>>>(
+	    p, nblk, partial, 1.0 / (double)nw, S);
 	return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 

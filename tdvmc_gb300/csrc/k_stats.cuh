@@ -30,44 +30,83 @@ struct Cols1 {
 	__host__ __device__ int count() const { return 3 * p + 12; }
 };
 
+// Column col of walker w in the pass-1 layout (the wf column, exp(ln psi + phi^R),
+// comes from wfv: the block's exponentials, computed lane-parallel beforehand
+// because FP64 issue is scarce and exp is dozens of FP64 instructions).
+template <typename T>
+__device__ __forceinline__ T cols1_value(const Cols1& c, int col, int64_t w, const T* __restrict__ O,
+                                         const T* __restrict__ eloc, const T* __restrict__ other7,
+                                         const T* __restrict__ lnpsi, const int* __restrict__ acc,
+                                         const T* __restrict__ dE, int use_dE) {
+	const int p = c.p;
+	if (col < p) return O[(size_t)w * p + col];
+	if (col == c.ER()) return eloc[2 * w];
+	if (col == c.EI()) return eloc[2 * w + 1];
+	if (col < c.wf()) return other7[(size_t)w * 7 + (col - c.other())];
+	if (col == c.lnpsi()) return lnpsi[w];
+	if (col == c.acc()) return (T)acc[w];
+	return use_dE ? dE[(size_t)w * 2 * p + (col - c.dE())] : T(0);
+}
+
+// Pass 1: one thread per column over the block's walker range, four
+// independent FP64 running sums added in a fixed order (every walker's value
+// enters an FP64 sum directly, so FP32 inputs are added without FP32 rounding).
+constexpr int kReduce1MaxWalkers = 64;  // walkers per block (shared exponentials)
 template <typename T>
 __global__ void __launch_bounds__(256) k_reduce1(int p, int64_t nw, const T* __restrict__ O, const T* __restrict__ eloc,
                                                  const T* __restrict__ other7, const T* __restrict__ lnpsi,
                                                  const int* __restrict__ acc, const T* __restrict__ dE, int use_dE,
                                                  const double* __restrict__ params, double* __restrict__ partial) {
+	__shared__ double wfv[kReduce1MaxWalkers];
 	Cols1 c{p};
 	const int K = c.count();
 	const int64_t per = (nw + gridDim.x - 1) / gridDim.x;
 	const int64_t w0 = (int64_t)blockIdx.x * per;
 	const int64_t w1 = (w0 + per < nw) ? w0 + per : nw;
 	const double phiR = params[2 * p];
+	const int nloc = (int)(w1 > w0 ? w1 - w0 : 0);
+	for (int i = threadIdx.x; i < nloc; i += blockDim.x) wfv[i] = exp((double)lnpsi[w0 + i] + phiR);
+	__syncthreads();
 	for (int col = threadIdx.x; col < K; col += blockDim.x) {
-		double s = 0.0;
-		for (int64_t w = w0; w < w1; w++) {
-			double v;
-			if (col < p) v = (double)O[(size_t)w * p + col];
-			else if (col == c.ER()) v = (double)eloc[2 * w];
-			else if (col == c.EI()) v = (double)eloc[2 * w + 1];
-			else if (col < c.wf()) v = (double)other7[(size_t)w * 7 + (col - c.other())];
-			else if (col == c.wf()) v = exp((double)lnpsi[w] + phiR);
-			else if (col == c.lnpsi()) v = (double)lnpsi[w];
-			else if (col == c.acc()) v = (double)acc[w];
-			else v = use_dE ? (double)dE[(size_t)w * 2 * p + (col - c.dE())] : 0.0;
-			s += v;
+		double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+		if (col == c.wf()) {
+			int i = 0;
+			for (; i + 4 <= nloc; i += 4) {
+				s0 += wfv[i];
+				s1 += wfv[i + 1];
+				s2 += wfv[i + 2];
+				s3 += wfv[i + 3];
+			}
+			for (; i < nloc; i++) s0 += wfv[i];
+		} else {
+			int64_t w = w0;
+			for (; w + 4 <= w1; w += 4) {
+				s0 += (double)cols1_value(c, col, w, O, eloc, other7, lnpsi, acc, dE, use_dE);
+				s1 += (double)cols1_value(c, col, w + 1, O, eloc, other7, lnpsi, acc, dE, use_dE);
+				s2 += (double)cols1_value(c, col, w + 2, O, eloc, other7, lnpsi, acc, dE, use_dE);
+				s3 += (double)cols1_value(c, col, w + 3, O, eloc, other7, lnpsi, acc, dE, use_dE);
+			}
+			for (; w < w1; w++) s0 += (double)cols1_value(c, col, w, O, eloc, other7, lnpsi, acc, dE, use_dE);
 		}
-		partial[(size_t)blockIdx.x * K + col] = s;
+		partial[(size_t)blockIdx.x * K + col] = (s0 + s1) + (s2 + s3);
 	}
 }
 
-// Sum `nblk` partial rows of width K in fixed order and scale by `scale`.
-__global__ void __launch_bounds__(256) k_finalize(int K, int nblk, const double* __restrict__ partial, double scale,
-                                                  double* __restrict__ out) {
-	for (int col = threadIdx.x; col < K; col += blockDim.x) {
-		double s = 0.0;
-		for (int b = 0; b < nblk; b++) s += partial[(size_t)b * K + col];
-		out[col] = s * scale;
-	}
+// Sum `nblk` partial rows of width K in fixed order and scale by `scale`: one
+// warp per column, lane l adding rows l, l + 32, ..., then a fixed butterfly.
+constexpr int kFinalizeThreads = 256;
+__global__ void __launch_bounds__(kFinalizeThreads) k_finalize(int K, int nblk, const double* __restrict__ partial,
+                                                               double scale, double* __restrict__ out) {
+	const int lane = threadIdx.x & 31;
+	const int col = blockIdx.x * (kFinalizeThreads / 32) + (threadIdx.x >> 5);
+	if (col >= K) return;  // whole warps
+	double s = 0.0;
+	for (int b = lane; b < nblk; b += 32) s += partial[(size_t)b * K + col];
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if (lane == 0) out[col] = s * scale;
 }
+inline int finalize_blocks(int K) { return (K + kFinalizeThreads / 32 - 1) / (kFinalizeThreads / 32); }
 
 // Pass 2 (FP64): Y = [O - <O> | E^R - <E^R> | E^I - <E^I>] (p + 2 columns).
 // Block b stages walkers [b*chunk, (b+1)*chunk) of Y in shared memory and
@@ -92,12 +131,29 @@ __global__ void __launch_bounds__(256) k_reduce2(int p, int64_t nw, int chunk, c
 	}
 	__syncthreads();
 	const int npair = p * ncol;
-	for (int e = threadIdx.x; e < npair; e += blockDim.x) {
-		const int k = e / ncol, l = e % ncol;
-		double s = 0.0;
-		if (with_S || l >= p)
+	if (with_S) {
+		for (int e = threadIdx.x; e < npair; e += blockDim.x) {
+			const int k = e / ncol, l = e % ncol;
+			double s = 0.0;
 			for (int r = 0; r < nt; r++) s += ytile[r * ncol + k] * ytile[r * ncol + l];
-		partial[(size_t)blockIdx.x * npair + e] = s;
+			partial[(size_t)blockIdx.x * npair + e] = s;
+		}
+		return;
+	}
+	// only the energy columns l = p, p + 1; four lanes per entry (rows r = q mod 4),
+	// added in a fixed order; the S block of the row stays zero
+	for (int e = threadIdx.x; e < npair; e += blockDim.x)
+		if (e % ncol < p) partial[(size_t)blockIdx.x * npair + e] = 0.0;
+	for (int t = threadIdx.x; t < ((2 * p * 4 + 31) & ~31); t += blockDim.x) {
+		const int e2 = t >> 2, q = t & 3;
+		const bool on = e2 < 2 * p;
+		const int k = on ? e2 >> 1 : 0, l = p + (e2 & 1);
+		double s = 0.0;
+		if (on)
+			for (int r = q; r < nt; r += 4) s += ytile[r * ncol + k] * ytile[r * ncol + l];
+		s += __shfl_xor_sync(0xffffffffu, s, 1);
+		s += __shfl_xor_sync(0xffffffffu, s, 2);
+		if (on && q == 0) partial[(size_t)blockIdx.x * npair + k * ncol + l] = s;
 	}
 }
 

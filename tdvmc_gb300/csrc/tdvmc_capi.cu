@@ -354,7 +354,8 @@ int launch_reduce(tdvmc_ctx* ctx, bool adj) {
 	                                               (const T*)ctx->other7, (const T*)ctx->lnpsi, ctx->acc,
 	                                               (const T*)ctx->dE, adj ? 1 : 0, ctx->stage, ctx->part1);
 	mark(ctx, "k_reduce1");
-	k_finalize<<<1, 256, 0, ctx->st>>>(K1, ctx->nblk1, ctx->part1, 1.0 / (double)ctx->nw, ctx->means1);
+	k_finalize<<<finalize_blocks(K1), kFinalizeThreads, 0, ctx->st>>>(K1, ctx->nblk1, ctx->part1, 1.0 / (double)ctx->nw,
+	                                                                 ctx->means1);
 	mark(ctx, "k_finalize1");
 	ctx->launches += 2;
 	CK(cudaGetLastError());
@@ -364,7 +365,8 @@ int launch_reduce(tdvmc_ctx* ctx, bool adj) {
 	k_reduce2<T><<<ctx->nblk2, 256, sm2, ctx->st>>>(P, ctx->nw, ctx->chunk2, (const T*)ctx->O, (const T*)ctx->eloc,
 	                                                 ctx->means1, tc ? 0 : 1, ctx->part2);
 	mark(ctx, "k_reduce2");
-	k_finalize<<<1, 256, 0, ctx->st>>>(P * (P + 2), ctx->nblk2, ctx->part2, 1.0 / (double)ctx->nw, ctx->C2);
+	k_finalize<<<finalize_blocks(P * (P + 2)), kFinalizeThreads, 0, ctx->st>>>(P * (P + 2), ctx->nblk2, ctx->part2,
+	                                                                           1.0 / (double)ctx->nw, ctx->C2);
 	mark(ctx, "k_finalize2");
 	ctx->launches += 2;
 	CK(cudaGetLastError());
@@ -865,7 +867,9 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	const int np = 2 * P + 2;
 	Cols1 cols{P};
 	const int K1 = cols.count();
-	c.nblk1 = (int)std::min<int64_t>(std::max<int64_t>(1, (nw + 63) / 64), 4 * (int64_t)c.nsm);
+	// at most kReduce1MaxWalkers walkers per block: enough blocks for every walker
+	c.nblk1 = (int)std::max<int64_t>(std::min<int64_t>(std::max<int64_t>(1, (nw + 31) / 32), 8 * (int64_t)c.nsm),
+	                                 (nw + kReduce1MaxWalkers - 1) / kReduce1MaxWalkers);
 	c.chunk2 = (int)std::max<int64_t>(1, std::min<int64_t>(128, (96 * 1024) / ((P + 2) * 8)));
 	c.nblk2 = (int)((nw + c.chunk2 - 1) / c.chunk2);
 	c.nblkS = gram_blocks(nw, c.nsm);

@@ -61,6 +61,32 @@ def test_stored_eval_matches_direct_eval(precision, tol, golden, pot):
             assert relmax(got[key], ref[key]) < tol, (k, key, relmax(got[key], ref[key]))
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 2e-5)])
+def test_stored_eval_more_than_32_splines(precision, tol):
+    """P = 40 (42 splines, more than the FP32 evaluation keeps as register sums):
+    the stored evaluation with 16-byte loads over particles, N = 45 (two
+    32-particle chunks, the second mostly padding), equal-width knots."""
+    import tdvmc_gb300 as T
+    dim, n, p, L = 3, 45, 40, 4.2
+    nw = 96
+    rng = np.random.default_rng(5)
+    R = rng.uniform(0.0, L, size=(nw, dim, n))
+    s = T.BosonsBulk(dim, n, p, L, nw, system_params=(0.5, 2.0), potential="gauss", hbar2_2m=0.09,
+                     precision=precision)
+    uR = -0.3 * np.exp(-np.linspace(0.0, 3.0, p)) + 0.01 * rng.normal(size=p)
+    uI = 0.02 * rng.normal(size=p)
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R)
+    s.FillCorrelatedSamplingData()
+    for k, (a, b) in enumerate([(uR, uI), (1.2 * uR - 0.01, 0.7 * uI + 0.01)]):
+        s.SetParameters(a, b)
+        got = s.CalculateExpectationValuesForStoredSamples(adjoint=True)
+        ref = s.CalculateExpectationValues()
+        ref["dE"] = s.CalculateLocalEnergyAdjoint()
+        for key in ("lnpsi", "O", "eloc", "other", "dE"):
+            assert relmax(got[key], ref[key]) < tol, (k, key, relmax(got[key], ref[key]))
+
+
 def test_stored_sample_rk4_matches_oracle_fp64():
     """Three RK4 steps on stored samples: the first samples every walker, the
     next two refresh windows [0, nw/4) and [nw/4, nw/2) (UpdateSamplesConsecutive)."""
