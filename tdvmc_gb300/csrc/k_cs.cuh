@@ -59,25 +59,45 @@ template <typename T> struct CsPieceRow {
 	T c[kCsPiece];
 };
 
-// One (row, partner) pair: the row's D columns always; with STATS also the
-// pair's O, D2, potential and outer count (unordered pairs, counted once).
+// Geometry of one (row, partner) pair: minimum-image difference, distance,
+// interval and local coordinate (no shared-memory writes, so the geometry of
+// several partners can be computed before any of their accumulations).
+template <typename T> struct CsGeom {
+	T dx, dy, dz, r, rinv, t, sr;
+	int j;
+	bool in, out;  // within r_max (and not the self pair); beyond r_max
+};
+template <typename T>
+__device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
+                                             const T* __restrict__ kb, const T* __restrict__ hv,
+                                             const int* __restrict__ lut) {
+	CsGeom<T> g;
+	const T L = (T)sc.L, Lr = (T)sc.Lr;
+	g.dx = nic(xr.x - xi.x, L, Lr);
+	g.dy = nic(xr.y - xi.y, L, Lr);
+	g.dz = nic(xr.z - xi.z, L, Lr);
+	const T r2 = fma(g.dz, g.dz, fma(g.dy, g.dy, g.dx * g.dx));
+	g.rinv = rsqrt_(r2);
+	g.r = r2 * g.rinv;
+	g.in = ok && (g.r <= (T)sc.rmax);
+	g.out = ok && !(g.r <= (T)sc.rmax);
+	T t;
+	g.j = locate<T>(sc, g.r, kb, hv, lut, t);
+	g.t = g.in ? t : T(0);  // t is NaN for the self pair
+	g.sr = g.in ? g.rinv : T(0);
+	return g;
+}
+
+// The accumulations of one pair: the row's D columns always; with STATS also
+// the pair's O, D2, potential and outer count (unordered pairs, counted once).
 // UNI: the piece row is pu for every interval, else row j of the shared table.
 template <typename T, int G, bool STATS, bool UNI>
-__device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
-                                        const CsPieceRow<T>& pu, const T* __restrict__ piece, const T* __restrict__ kb,
-                                        const T* __restrict__ hv, const int* __restrict__ lut, T* __restrict__ drow,
-                                        T* __restrict__ oacc, T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs,
-                                        int& nout) {
-	const T L = (T)sc.L, Lr = (T)sc.Lr;
-	const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
-	const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-	const T rinv = rsqrt_(r2);
-	const T r = r2 * rinv;
-	const bool in = ok && (r <= (T)sc.rmax);
-	T t;
-	const int j = locate<T>(sc, r, kb, hv, lut, t);
-	t = in ? t : T(0);  // t is NaN for the self pair
-	const T sr = in ? rinv : T(0);
+__device__ __forceinline__ void cs_accum(const SysConst& sc, const CsGeom<T>& g, const CsPieceRow<T>& pu,
+                                         const T* __restrict__ piece, T* __restrict__ drow, T* __restrict__ oacc,
+                                         T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs, int& nout) {
+	const T dx = g.dx, dy = g.dy, dz = g.dz, r = g.r, rinv = g.rinv, t = g.t, sr = g.sr;
+	const bool in = g.in;
+	const int j = g.j;
 	const T* pj = piece + (size_t)j * kCsPieceS;
 	auto pc = [&](int k) -> T {
 		if constexpr (UNI) return pu.c[k];
@@ -122,8 +142,35 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
 			d2acc[(size_t)(s0 - q) * G + lane] = dv[q] + T(2) * lap;  // both orderings of the pair
 		}
 		vs.add(in ? pair_pot<T>(sc.pot_kind, r, rinv, pa, pb) : T(0));
-		nout += (ok && !(r <= (T)sc.rmax)) ? 1 : 0;
+		nout += g.out ? 1 : 0;
 	}
+}
+
+template <typename T, int G, bool STATS, bool UNI>
+__device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
+                                        const CsPieceRow<T>& pu, const T* __restrict__ piece, const T* __restrict__ kb,
+                                        const T* __restrict__ hv, const int* __restrict__ lut, T* __restrict__ drow,
+                                        T* __restrict__ oacc, T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs,
+                                        int& nout) {
+	cs_accum<T, G, STATS, UNI>(sc, cs_geom<T>(sc, xr, xi, ok, kb, hv, lut), pu, piece, drow, oacc, d2acc, lane, pa, pb,
+	                           vs, nout);
+}
+
+// kCsBatch partners [i, i + kCsBatch): all geometries first, then the accumulations
+// in partner order.
+constexpr int kCsBatch = 4;
+template <typename T, int G, bool STATS, bool UNI>
+__device__ __forceinline__ void cs_batch(const SysConst& sc, const Q4<T>& xr, const Q4<T>* __restrict__ xs, int i,
+                                         bool ok, const CsPieceRow<T>& pu, const T* __restrict__ piece,
+                                         const T* __restrict__ kb, const T* __restrict__ hv,
+                                         const int* __restrict__ lut, T* __restrict__ drow, T* __restrict__ oacc,
+                                         T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs, int& nout) {
+	CsGeom<T> g[kCsBatch];
+#pragma unroll
+	for (int u = 0; u < kCsBatch; u++) g[u] = cs_geom<T>(sc, xr, xs[i + u], ok, kb, hv, lut);
+#pragma unroll
+	for (int u = 0; u < kCsBatch; u++)
+		cs_accum<T, G, STATS, UNI>(sc, g[u], pu, piece, drow, oacc, d2acc, lane, pa, pb, vs, nout);
 }
 
 // Stores the correlated-sampling data of walkers (start + w) mod nw_total,
@@ -195,10 +242,11 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const CsPieceR
 			for (int e = lane; e < ns * 3 * G; e += G) drow[e] = T(0);
 			const int base = s * G;
 			const int dend = (base + G < n) ? base + G : n;
-			// partners below the slot: every lane's pair is counted once (i < nrow)
-#pragma unroll 4
-			for (int i = 0; i < base; i++)
-				cs_pair<T, G, true, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
+			// partners below the slot: every lane's pair is counted once (i < nrow);
+			// base is a multiple of G, so of kCsBatch
+			for (int i = 0; i < base; i += kCsBatch)
+				cs_batch<T, G, true, UNI>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
+				                          vs, nout);
 			// the slot's own block: counted iff i < nrow
 			for (int i = base; i < dend; i++) {
 				if (i < nrow)
@@ -209,9 +257,13 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const CsPieceR
 					                     pa, pb, vs, nout);
 			}
 			// partners above the slot: D only
-#pragma unroll 4
-			for (int i = dend; i < n; i++)
-				cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs, nout);
+			int i = dend;
+			for (; i + kCsBatch <= n; i += kCsBatch)
+				cs_batch<T, G, false, UNI>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
+				                           vs, nout);
+			for (; i < n; i++)
+				cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
+				                          vs, nout);
 			if (rowok)
 				for (int e = 0; e < ns * 3; e++) Dw[cs_doff(ns * 3, e, nrow)] = drow[(size_t)e * G + lane];
 		}
