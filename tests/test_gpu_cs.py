@@ -1,6 +1,8 @@
 """GPU: correlated-sampling reuse (stored samples, ODE_SOLVER_TYPE 3 and 5).
 
 Tolerances (stated per test):
+  RK4 / predictor-corrector on stored samples, mixed vs FP64 with fixed walkers:
+      parameter increments 2e-4 of their largest magnitude;
   stored vs direct evaluation at the same walkers and parameters: FP64
       relative 1e-11, mixed 2e-5 on ln psi, O_k, E_loc, the kinetic sums and
       dE/d alpha (scaled by the largest magnitude of each quantity);
@@ -187,6 +189,42 @@ def test_stored_sample_pc_matches_oracle_fp64():
         assert np.abs(after - Ro).max() < 1e-9, st
         gR, gI, gpR, gpI = s.GetParameters()
         assert relmax(np.concatenate([gR, gI, [gpR, gpI]]), base) < 1e-9, st
+
+
+@pytest.mark.parametrize("ode", [3, 5])
+def test_stored_sample_steps_mixed_track_fp64(ode):
+    """RK4 (3) and the predictor-corrector (5) on stored samples in mixed precision
+    against FP64, with no Metropolis moves, so both evaluate the same walkers:
+    N = 64, P = 30 (32 splines: the staged FP32 evaluation and the equal-width
+    store), Gaussian pair potential, real time, 256 walkers, three steps with
+    refresh windows of a quarter.  The parameter increments (about 1e-2) agree
+    to 2e-4 of their largest magnitude (FP32 pair sums and the 3xTF32 S through
+    the regularised solves; measured 1.7e-5); RK4 and the predictor-corrector
+    differ from each other by about 8e-3 on the same case."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "eval_d3_n64_p10.npz"))
+    dim, n, L = int(z["dim"]), int(z["n"]), float(z["L"])
+    p, nw = 30, 256
+    rng = np.random.default_rng(23)
+    cfgs = soa(z["cfgs"])
+    R = np.concatenate([cfgs] * (nw // len(cfgs) + 1))[:nw] + rng.normal(0, 0.02, size=(nw, dim, n))
+    uR = -0.4 * np.exp(-np.linspace(0.0, 4.0, p)) + 0.005 * rng.normal(size=p)
+    uI = 0.01 * rng.normal(size=p)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = T.BosonsBulk(dim, n, p, L, nw, system_params=(0.5, 2.0), potential="gauss", hbar2_2m=0.09,
+                         precision=prec)
+        s.SetParameters(uR, uI, 0.0, 0.0)
+        s.SetWalkers(R)
+        td = T.TDVP(s, 1e-3, 0, 0.3, seed=3, imaginary_time=0, use_adjoint=1, ode_solver=ode, update_every=1,
+                    update_percent=25.0)
+        st = td.step(3)
+        assert st["status"] == 0, st
+        gp = s.GetParameters()
+        out[prec] = np.concatenate([gp[0] - uR, gp[1] - uI])
+    d64, dmx = out["fp64"], out["mixed"]
+    assert np.abs(d64).max() > 0
+    assert np.abs(dmx - d64).max() < 2e-4 * np.abs(d64).max(), np.abs(dmx - d64).max() / np.abs(d64).max()
 
 
 def test_store_state_rules():
