@@ -511,9 +511,9 @@ __global__ void __launch_bounds__(128) k_cs_eval(SysConst sc, const double* __re
 
 // Stored-sample evaluation in FP32 for ns <= 32: one warp per walker, the
 // walker's D streamed through shared memory one contiguous 32-particle chunk at
-// a time by 16-byte cp.async copies (each byte of D leaves HBM once; one
-// buffer per warp keeps 16 warps on an SM, and the other warps' copies overlap
-// this warp's arithmetic), then one particle per lane: G_n from the chunk, and with ADJ the per-spline
+// a time by a TMA bulk copy (each byte of D leaves HBM once; one buffer per warp
+// keeps 16 warps on an SM, and the other warps' copies overlap this warp's
+// arithmetic), then one particle per lane: G_n from the chunk, and with ADJ the per-spline
 // partial sums of G_n . D[s][.][n] kept in registers.  At the walker's end the
 // lanes' sums pass through the buffer just used (row of 2 ns + 1 floats per
 // lane) and are added in lane order.
@@ -526,27 +526,45 @@ __host__ __device__ inline size_t cs_eval_st_smem_bytes(int ns, int warps) {
 	return ((size_t)cs_ns2(ns) + (size_t)warps * ((size_t)cs_st_warp_floats(ns) + cs_ns2(ns))) * sizeof(float);
 }
 
-// One lane's share of a chunk copy: n4 16-byte pieces, global -> shared, as one
-// cp.async group.
-__device__ __forceinline__ void cs_chunk_copy(float* dst, const float* src, int n4, int lane) {
-	const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-	for (int q = lane; q < n4; q += 32)
-		asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + 16u * (uint32_t)q),
-		             "l"(src + 4 * (size_t)q)
-		             : "memory");
-	asm volatile("cp.async.commit_group;\n" ::: "memory");
+// Each chunk is one TMA bulk copy (cp.async.bulk) issued by lane 0 and
+// completed on the warp's mbarrier.  Every wait is bounded: on time-out the
+// walker's E_loc is written as NaN (the statistics then report a non-finite
+// value), the warp waits once more, bounded, for its own copy and returns.
+constexpr unsigned kCsWaitLimit = 1u << 24;
+__device__ __forceinline__ bool cs_mbar_wait(uint32_t mbar, uint32_t parity) {
+	for (unsigned it = 0; it < kCsWaitLimit; it++) {
+		uint32_t done;
+		asm volatile(
+		    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		    "selp.u32 %0, 1, 0, p;\n\t}\n"
+		    : "=r"(done)
+		    : "r"(mbar), "r"(parity)
+		    : "memory");
+		if (done) return true;
+	}
+	return false;
 }
-__device__ __forceinline__ void cs_copy_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+// lane 0: order this warp's earlier generic accesses of dst before the async
+// write, arm the barrier with the byte count and start the copy
+__device__ __forceinline__ void cs_bulk_copy(uint32_t mbar, float* dst, const float* src, uint32_t bytes) {
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+	                 (uint32_t)__cvta_generic_to_shared(dst)),
+	             "l"(src), "r"(bytes), "r"(mbar)
+	             : "memory");
+}
 
+constexpr int kCsStWarps = 4;  // warps per block: 4 blocks (16 warps) per SM at 32 splines
 template <bool ADJ>
-__global__ void __launch_bounds__(128, 4) k_cs_eval_st(
+__global__ void __launch_bounds__(32 * kCsStWarps, 4) k_cs_eval_st(
     SysConst sc, const double* __restrict__ params, const double* __restrict__ fold_g, const float* __restrict__ D,
     const float* __restrict__ D2, const float* __restrict__ Os, const float* __restrict__ Vs,
     const int32_t* __restrict__ nouts, int64_t nw, float* __restrict__ lnpsi_o, float* __restrict__ O_o,
     float* __restrict__ eloc_o, float* __restrict__ other_o, float* __restrict__ dE_o) {
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int n = sc.n, ns = sc.ns, P = sc.p;
-	const int npad = cs_npad(n), nrow = 3 * ns, nch = npad / 32, n4 = nrow * 8;
+	const int npad = cs_npad(n), nrow = 3 * ns, nch = npad / 32;
 	float* wR = reinterpret_cast<float*>(smem_raw);
 	float* wI = wR + ns;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -566,6 +584,15 @@ __global__ void __launch_bounds__(128, 4) k_cs_eval_st(
 	float* chunk = wR + cs_ns2(ns) + (size_t)warp * (wfl + cs_ns2(ns));  // [row = 3 s + a][32]
 	float* asum = chunk + wfl;
 	const size_t wstride = (size_t)nrow * npad;
+	// one mbarrier per warp after the warps' regions
+	const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(smem_raw + cs_eval_st_smem_bytes(ns, wpb)) + 8u * warp;
+	const uint32_t cbytes = (uint32_t)nrow * 32u * 4u;
+	uint32_t phase = 0;
+	if (lane == 0) {
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncwarp();
 
 	for (int64_t w = (int64_t)blockIdx.x * wpb + warp; w < nw; w += (int64_t)gridDim.x * wpb) {
 		const float* Dw = D + (size_t)w * wstride;
@@ -574,8 +601,17 @@ __global__ void __launch_bounds__(128, 4) k_cs_eval_st(
 #pragma unroll
 		for (int s = 0; s < kCsStNs; s++) pr[s] = pi[s] = 0.f;
 		for (int c = 0; c < nch; c++) {
-			cs_chunk_copy(chunk, Dw + (size_t)c * nrow * 32, n4, lane);
-			cs_copy_wait_all();
+			if (lane == 0) cs_bulk_copy(mbar, chunk, Dw + (size_t)c * nrow * 32, cbytes);
+			const bool ok = cs_mbar_wait(mbar, phase);
+			phase ^= 1u;
+			if (!__all_sync(0xffffffffu, ok)) {
+				if (lane == 0) {
+					eloc_o[2 * w] = __int_as_float(0x7fc00000);
+					eloc_o[2 * w + 1] = __int_as_float(0x7fc00000);
+				}
+				cs_mbar_wait(mbar, phase ^ 1u);  // bounded: the copy still in flight
+				return;
+			}
 			__syncwarp();
 			const int c0 = c * 32;
 			float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f, gi0 = 0.f, gi1 = 0.f, gi2 = 0.f;

@@ -466,11 +466,12 @@ int launch_cs_eval(tdvmc_ctx* ctx, bool adj) {
 	const int threads = 128, wpb = threads / 32;
 	if constexpr (sizeof(T) == 4) {
 		if (s.ns <= kCsStNs) {
-			const size_t smem = cs_eval_st_smem_bytes(s.ns, wpb);
+			constexpr int wst = kCsStWarps;
+			const size_t smem = cs_eval_st_smem_bytes(s.ns, wst) + 8 * wst;
 			auto fn = adj ? k_cs_eval_st<true> : k_cs_eval_st<false>;
 			CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-			const int grid = grid_for(ctx, (const void*)fn, threads, smem, ctx->nw, wpb);
-			fn<<<grid, threads, smem, ctx->st>>>(s, ctx->stage, ctx->fold_d, (const float*)ctx->csD,
+			const int grid = grid_for(ctx, (const void*)fn, 32 * wst, smem, ctx->nw, wst);
+			fn<<<grid, 32 * wst, smem, ctx->st>>>(s, ctx->stage, ctx->fold_d, (const float*)ctx->csD,
 			                                     (const float*)ctx->csD2, (const float*)ctx->csO, (const float*)ctx->csV,
 			                                     ctx->csN, ctx->nw, (float*)ctx->lnpsi, (float*)ctx->O, (float*)ctx->eloc,
 			                                     (float*)ctx->other7, (float*)ctx->dE);
