@@ -63,6 +63,39 @@ def test_stored_eval_matches_direct_eval(precision, tol, golden, pot):
             assert relmax(got[key], ref[key]) < tol, (k, key, relmax(got[key], ref[key]))
 
 
+def test_stored_eval_n1000_tracks_direct():
+    """N = 1000 with 64 knots (66 splines, density 0.365): the stored evaluation
+    (larger store tiles, 16-byte loads over particles) equals the direct one to
+    1e-11 in FP64.  In mixed precision both carry the error of FP32 sums over
+    ~5e5 pairs per walker at this size (measured against FP64: O 5.5e-5, E_loc
+    1e-4, dE 3.2e-3 of the largest magnitude, the same for both), so the check is
+    that the stored evaluation's error against FP64 is at most twice the direct
+    evaluation's (measured ratio 1.00-1.01), plus 1e-6."""
+    import tdvmc_gb300 as T
+    dim, n, p, L, nw = 3, 1000, 64, 14.0, 96
+    rng = np.random.default_rng(5)
+    R = rng.uniform(0.0, L, size=(nw, dim, n))
+    uR = -0.3 * np.exp(-np.linspace(0.0, 3.0, p)) + 0.01 * rng.normal(size=p)
+    uI = 0.02 * rng.normal(size=p)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = T.BosonsBulk(dim, n, p, L, nw, system_params=(0.5, 2.0), potential="gauss", hbar2_2m=0.09,
+                         precision=prec)
+        s.SetParameters(uR, uI)
+        s.SetWalkers(R)
+        s.FillCorrelatedSamplingData()
+        got = s.CalculateExpectationValuesForStoredSamples(adjoint=True)
+        ref = s.CalculateExpectationValues()
+        ref["dE"] = s.CalculateLocalEnergyAdjoint()
+        out[prec] = (got, ref)
+    truth = out["fp64"][1]
+    for key in ("lnpsi", "O", "eloc", "other", "dE"):
+        assert relmax(out["fp64"][0][key], truth[key]) < 1e-11, key
+        e_st = relmax(out["mixed"][0][key], truth[key])
+        e_dir = relmax(out["mixed"][1][key], truth[key])
+        assert e_st <= 2.0 * e_dir + 1e-6, (key, e_st, e_dir)
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 2e-5)])
 def test_stored_eval_more_than_32_splines(precision, tol):
     """P = 40 (42 splines, more than the FP32 evaluation keeps as register sums):
