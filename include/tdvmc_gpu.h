@@ -154,8 +154,10 @@ int tdvmc_eval_local_adjoint(tdvmc_ctx* ctx, double* dE);
  * (InitCorrelatedSamplingData + FillCorrelatedSamplingData,
  * BosonsBulk.cpp:667-681; CSDataBulkSplines.h:9-16): per spline and particle
  * sum_i B'(r) rhat, the summed B'' + (D-1)/r B', O_k, V_int and the outer-pair
- * count.  About nw * (p+2) * 3 * n values of the working precision; the
- * store is allocated on first use (TDVMC_ERR_NOMEM if it does not fit).
+ * count.  nw * (p+2) * 3 * n32 values of the working precision, n32 = n
+ * rounded up to a multiple of 32 (8.9 GB in FP32 at nw = 65,536, n = 343,
+ * p = 30); the store is allocated on first use (TDVMC_ERR_NOMEM if it does
+ * not fit).
  * Moving the walkers (tdvmc_set_walkers, tdvmc_sample, a resampling step)
  * invalidates it. */
 int tdvmc_store_samples(tdvmc_ctx* ctx);
