@@ -30,6 +30,12 @@ struct SysConst {
 	double hinv;      // uniform: 1 / interval width
 	double cell_inv;  // non-uniform: 1 / lookup cell width
 	double hbar2_2m;
+	// FP32 evaluation: 1 / interval width as hf + hf_lo, so that the rounding of
+	// 1/h (a bias shared by every pair) stays out of the local coordinate t
+	float hf, hf_lo;
+	// FP32 distances in (rcut_lo, rcut_hi) lie within rounding of r_max: the
+	// cutoff of such a pair is decided again in FP64 from its FP32 coordinates
+	float rcut_lo, rcut_hi;
 };
 
 // Values that change between stages or steps live in device memory so a
@@ -101,11 +107,20 @@ __device__ __forceinline__ double pair_r(double r2) { return r2 * rsqrt_(r2); }
 template <typename T>
 __device__ __forceinline__ int locate(const SysConst& s, T r, const T* kb, const T* hv, const int* lut, T& t) {
 	if (s.uniform) {
-		const T x = r * (T)s.hinv;
-		T jf;
-		const int j = floor_clamp(x, s.nbin - 1, jf);
-		t = x - jf;
-		return j;
+		if constexpr (sizeof(T) == 4) {
+			// t = r / h - j with one rounding: r (hf + hf_lo) - j
+			const float x = r * s.hf;
+			float jf;
+			const int j = floor_clamp(x, s.nbin - 1, jf);
+			t = fmaf(r, s.hf_lo, fmaf(r, s.hf, -jf));
+			return j;
+		} else {
+			const T x = r * (T)s.hinv;
+			T jf;
+			const int j = floor_clamp(x, s.nbin - 1, jf);
+			t = x - jf;
+			return j;
+		}
 	}
 	int c = (int)(r * (T)s.cell_inv);
 	c = c < s.ncell - 1 ? c : s.ncell - 1;

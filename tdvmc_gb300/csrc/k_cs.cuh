@@ -79,8 +79,9 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
 	const T r2 = fma(g.dz, g.dz, fma(g.dy, g.dy, g.dx * g.dx));
 	g.rinv = rsqrt_(r2);
 	g.r = r2 * g.rinv;
-	g.in = ok && (g.r <= (T)sc.rmax);
-	g.out = ok && !(g.r <= (T)sc.rmax);
+	const bool cut = within_rmax<T>(sc, g.r, xr, xi);
+	g.in = ok && cut;
+	g.out = ok && !cut;
 	T t;
 	g.j = locate<T>(sc, g.r, kb, hv, lut, t);
 	g.t = g.in ? t : T(0);  // t is NaN for the self pair

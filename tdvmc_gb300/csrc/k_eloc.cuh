@@ -269,12 +269,45 @@ __device__ __forceinline__ T group_sum(T v, unsigned gmask) {
 	return v;
 }
 
+// Cutoff r <= r_max of one pair.  FP32: decided from the FP32 distance except
+// within rounding of r_max (rcut_lo < r < rcut_hi), where the distance of the
+// same FP32 coordinates is computed again in FP64, as the FP64 path computes
+// it.  A pair that crosses r_max moves a whole spline value between O_k and
+// the outer-pair count, so a rounding flip there would exceed every FP32
+// tolerance; at N = 1000 a few pairs per walker fall in the band.
+__device__ __forceinline__ bool cut_fp64(const SysConst& sc, const Q4<float>& a, const Q4<float>& b) {
+	const double dx = nic((double)a.x - (double)b.x, sc.L, sc.Lr);
+	const double dy = nic((double)a.y - (double)b.y, sc.L, sc.Lr);
+	const double dz = nic((double)a.z - (double)b.z, sc.L, sc.Lr);
+	return sqrt(fma(dz, dz, fma(dy, dy, dx * dx))) <= sc.rmax;
+}
+template <typename T>
+__device__ __forceinline__ bool within_rmax(const SysConst& sc, T r, const Q4<T>& a, const Q4<T>& b) {
+	if constexpr (sizeof(T) == 4) {
+		if (r > sc.rcut_lo && r < sc.rcut_hi) return cut_fp64(sc, a, b);
+	}
+	return r <= (T)sc.rmax;
+}
+// the same for the pairs (a, b0) and (a, b1) of one f32x2 stream
+__device__ __forceinline__ void within_rmax2(const SysConst& sc, float r0, float r1, const Q4<float>& a,
+                                             const Q4<float>& b0, const Q4<float>& b1, bool& in0, bool& in1) {
+	const float rmax = (float)sc.rmax;
+	in0 = r0 <= rmax;
+	in1 = r1 <= rmax;
+	const bool n0 = r0 > sc.rcut_lo && r0 < sc.rcut_hi, n1 = r1 > sc.rcut_lo && r1 < sc.rcut_hi;
+	if (n0 || n1) {
+		if (n0) in0 = cut_fp64(sc, a, b0);
+		if (n1) in1 = cut_fp64(sc, a, b1);
+	}
+}
+
 // Geometry and spline derivatives of one (row, partner) pair of the forward sweep.
 template <typename T> struct FwdPair {
 	T dx, dy, dz, r, rinv, t;
 	T gR, gI, lR, lI;
 	int j;
-	bool in;
+	bool in;   // counted: a valid pair within r_max
+	bool cut;  // within r_max
 };
 
 template <typename T>
@@ -289,7 +322,8 @@ __device__ __forceinline__ FwdPair<T> fwd_pair(const SysConst& sc, const Q4<T>& 
 	const T r2 = q.dx * q.dx + q.dy * q.dy + q.dz * q.dz;
 	q.rinv = rsqrt_(r2);
 	q.r = r2 * q.rinv;
-	q.in = ok && (q.r <= (T)sc.rmax);
+	q.cut = within_rmax<T>(sc, q.r, xr, xi);
+	q.in = ok && q.cut;
 	q.j = locate<T>(sc, q.r, kb, hv, lut, q.t);
 	const Q4<T> cR = coefC[3 * q.j];
 	const Q4<T> cI = coefC[3 * q.j + 1];
@@ -365,7 +399,7 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 				for (int h = 0; h < kNp; h++) {
 					const bool c = have[h] && ((ON == 1) ? true : (ii[h] < nrow));
 					fwd_stats<T, G, ADJ, HIST>(sc, q[h], q[h].in && c, hist, lane, pa, pb, vb);
-					nout += (rowok && ii[h] != nrow && c && !(q[h].r <= rmax)) ? 1 : 0;
+					nout += (rowok && ii[h] != nrow && c && !q[h].cut) ? 1 : 0;
 				}
 			}
 		}
@@ -393,7 +427,7 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
-	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mh2 = f2_make(-0.5f, -0.5f);
+	const f2_t H2 = f2_make(sc.hf, sc.hf), HL2 = f2_make(sc.hf_lo, sc.hf_lo), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
 	const float ymax = kRoundF + (float)(sc.nbin - 1);
@@ -426,7 +460,9 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 				float rA, rB;
 				f2_split(r, rA, rB);
 				const bool okA = haveA && rowok && ia != nrow, okB = haveB && rowok && ib != nrow;
-				const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
+				bool wA, wB;
+				within_rmax2(sc, rA, rB, xr, pA, pB, wA, wB);
+				const bool inA = okA && wA, inB = okB && wB;
 				float tA, tB;
 				int jA, jB;
 				if (sc.uniform) {
@@ -437,7 +473,8 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 					ya = fminf(ya, ymax);
 					yb = fminf(yb, ymax);
 					float xa, xb;
-					f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
+					// t = r / h - j with one rounding: r (hf + hf_lo) - j
+					f2_split(f2_fma(r, HL2, f2_fma(r, H2, f2_sub(R2, f2_make(ya, yb)))), xa, xb);
 					tA = xa;
 					tB = xb;
 					jA = __float_as_int(ya) - __float_as_int(kRoundF);
@@ -495,8 +532,8 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 						q.rinv = qb;
 						fwd_stats<float, G, ADJ, HIST>(sc, q, sB, hist, lane, pa, pb, vb);
 					}
-					nout += (okA && cA && !(rA <= rmax)) ? 1 : 0;
-					nout += (okB && cB && !(rB <= rmax)) ? 1 : 0;
+					nout += (okA && cA && !wA) ? 1 : 0;
+					nout += (okB && cB && !wB) ? 1 : 0;
 				}
 			}
 		}
@@ -556,7 +593,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
-	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mh2 = f2_make(-0.5f, -0.5f);
+	const f2_t H2 = f2_make(sc.hf, sc.hf), HL2 = f2_make(sc.hf_lo, sc.hf_lo), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
 	const float ymax = kRoundF + (float)(sc.nbin - 1);
@@ -605,7 +642,9 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			const f2_t r = f2_mul(r2, f2_make(qa, qb));
 			float rA, rB;
 			f2_split(r, rA, rB);
-			const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
+			bool wA, wB;
+			within_rmax2(sc, rA, rB, xr, pA, pB, wA, wB);
+			const bool inA = okA && wA, inB = okB && wB;
 			float tA, tB;
 			int jA, jB;
 			if (sc.uniform) {
@@ -615,7 +654,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 				ya = fminf(ya, ymax);
 				yb = fminf(yb, ymax);
 				float xa, xb;
-				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
+				f2_split(f2_fma(r, HL2, f2_fma(r, H2, f2_sub(R2, f2_make(ya, yb)))), xa, xb);
 				tA = xa;
 				tB = xb;
 				jA = __float_as_int(ya) - __float_as_int(kRoundF);
@@ -781,7 +820,7 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 			const T r2 = dx * dx + dy * dy + dz * dz;
 			const T rinv = rsqrt_(r2);
 			const T r = r2 * rinv;
-			const bool on = have && rowok && (r <= rmax) && (DIAG ? (ii < nrow) : true);
+			const bool on = have && rowok && within_rmax<T>(sc, r, xr, xi) && (DIAG ? (ii < nrow) : true);
 			T t;
 			jj[h] = locate<T>(sc, r, kb, hv, lut, t);
 			t = on ? t : T(0);  // t is NaN for the self pair
@@ -818,7 +857,7 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
-	const f2_t H2 = f2_make((float)sc.hinv, (float)sc.hinv), mh2 = f2_make(-0.5f, -0.5f);
+	const f2_t H2 = f2_make(sc.hf, sc.hf), HL2 = f2_make(sc.hf_lo, sc.hf_lo), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
 	const float ymax = kRoundF + (float)(sc.nbin - 1);
@@ -863,8 +902,10 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			const f2_t r = f2_mul(r2, f2_make(qa, qb));
 			float rA, rB;
 			f2_split(r, rA, rB);
-			const bool onA = haveA && rowok && (rA <= rmax) && ((DIAG && !ROT) ? (ia < nrow) : true);
-			const bool onB = haveB && rowok && (rB <= rmax) && ((DIAG && !ROT) ? (ib < nrow) : true);
+			bool wA, wB;
+			within_rmax2(sc, rA, rB, xr, pA, pB, wA, wB);
+			const bool onA = haveA && rowok && wA && ((DIAG && !ROT) ? (ia < nrow) : true);
+			const bool onB = haveB && rowok && wB && ((DIAG && !ROT) ? (ib < nrow) : true);
 			float tA, tB;
 			int jA, jB;
 			if (sc.uniform) {
@@ -874,7 +915,7 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 				ya = fminf(ya, ymax);
 				yb = fminf(yb, ymax);
 				float xa, xb;
-				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
+				f2_split(f2_fma(r, HL2, f2_fma(r, H2, f2_sub(R2, f2_make(ya, yb)))), xa, xb);
 				tA = xa;
 				tB = xb;
 				jA = __float_as_int(ya) - __float_as_int(kRoundF);
