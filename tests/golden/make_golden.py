@@ -157,15 +157,17 @@ def main():
     L2 = float(np.sqrt(64 / 0.3))
     g = np.linspace(0.0, 1.0, 20)
     knots2 = np.concatenate([[0.0], 0.7 + (L2 / 2 - 0.7) * (g[1:] - g[1]) ** 1.3 / (1 - g[1]) ** 1.3])
+    # (the parity set of the 2D Lennard-Jones configuration: 256 configurations on
+    # the 8x8 lattice with 0.05 jitter, seed 7)
     systems.append(dict(name="d2_n64_k20", dim=2, n=64, p=20, L=L2, knots=knots2, sysp=[1.0, 0.5], time=0.0,
-                        ncfg=16, seed=13))
+                        ncfg=256, seed=7, jitter=0.05))
     # 3D, N=64, L=4 (the fixture box of src/VMCSampler.h:18)
     systems.append(dict(name="d3_n64_p10", dim=3, n=64, p=10, L=4.0, knots=None, sysp=[0.6, 1.0], time=0.0,
                         ncfg=16, seed=14))
     # 3D, N=343, density 0.365, 30 parameters (the benchmark system)
     L3 = float((343 / 0.365) ** (1.0 / 3.0))
     systems.append(dict(name="d3_n343_p30", dim=3, n=343, p=30, L=L3, knots=None, sysp=[0.9, 1.0], time=0.0,
-                        ncfg=4, seed=15))
+                        ncfg=32, seed=15))
 
     for sysd in systems:
         rng = np.random.default_rng(sysd["seed"])
@@ -178,7 +180,7 @@ def main():
             if dim == 1:
                 R = rng.uniform(-L / 2, L / 2, size=(n, dim))
             else:
-                R = lattice(n, dim, L, rng, jitter=0.5) - L / 2
+                R = lattice(n, dim, L, rng, jitter=sysd.get("jitter", 0.5)) - L / 2
             cfgs.append(R)
         cfgs = np.array(cfgs)
         script = system_cmd(dim, n, p, L, sysd["knots"], sysd["sysp"], sysd["time"])
