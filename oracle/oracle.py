@@ -80,6 +80,13 @@ def lib():
         L.orc_solve_centred.restype = C.c_int
         L.orc_observables.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, C.c_void_p, _dp, _dp, _dp]
         L.orc_observables.restype = C.c_int
+        L.orc_drop_create.restype = C.c_void_p
+        L.orc_drop_create.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.orc_drop_free.argtypes = [C.c_void_p]
+        L.orc_drop_eval.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_void_p]
+        L.orc_drop_sample.argtypes = [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, C.c_int, C.c_double,
+                                      C.c_uint64, C.c_uint32]
+        L.orc_drop_sample.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -194,6 +201,44 @@ class OracleSystem:
         if adjoint:
             out["dE"] = dE
         return out
+
+
+class OracleDrop:
+    """One trapped drop (open boundaries, pair spline + one-body Gaussian) in FP64.
+    Parameter vectors have p + 1 entries (the pair spline, then alpha_p)."""
+
+    def __init__(self, n, p, rmax, v0=1.0, sigma=0.5, omega=1.0, hbar2_2m=0.5):
+        self.n, self.p = int(n), int(p)
+        h = lib().orc_drop_create(self.n, self.p, float(rmax), float(v0), float(sigma), float(omega),
+                                  float(hbar2_2m))
+        if not h:
+            raise ValueError("oracle rejected the drop")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_drop_free(self.h)
+            self.h = None
+
+    def eval(self, uR, uI, R, adjoint=False):
+        """R: (n, 3) particle-major."""
+        p1 = self.p + 1
+        uR = np.ascontiguousarray(uR, dtype=np.float64)
+        uI = np.ascontiguousarray(uI, dtype=np.float64)
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(-1)
+        lnpsi, O, eloc, other = np.zeros(1), np.zeros(p1), np.zeros(2), np.zeros(7)
+        dE = np.zeros(2 * p1) if adjoint else None
+        lib().orc_drop_eval(self.h, uR, uI, R, lnpsi, O, eloc, other, None if dE is None else dE.ctypes.data)
+        res = dict(lnpsi=lnpsi[0], O=O, eloc=eloc, other=other)
+        if adjoint:
+            res["dE"] = dE.reshape(p1, 2)
+        return res
+
+    def sample(self, uR, Rsoa, moves, step, seed, pass_id, walker0=0):
+        """In-place moves of walkers stored SoA (nw, 3, n); Philox walker index walker0 + w."""
+        assert Rsoa.dtype == np.float64 and Rsoa.flags["C_CONTIGUOUS"]
+        return lib().orc_drop_sample(self.h, np.ascontiguousarray(uR, dtype=np.float64), Rsoa, Rsoa.shape[0],
+                                     int(walker0), int(moves), float(step), int(seed), int(pass_id) & 0xFFFFFFFF)
 
 
 def solve(O, ER, EI, OO, OER, OEI, imag=0, precond=0, solver=0):

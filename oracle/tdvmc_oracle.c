@@ -955,3 +955,277 @@ int orc_observables(const orc_sys* s, const double* R, int gr_bins, int nshell, 
 	free(ss);
 	return count;
 }
+
+/* ------------------------------------------------------------------ */
+/* Trapped drops: open boundaries, pair spline + one-body Gaussian      */
+/* ------------------------------------------------------------------ */
+/* No reference system has this form.  The pair spline restates a1-a9 of
+ * BosonsBulk (knots, fold, outer-pair term uR[p-1] n_out, B-spline
+ * derivatives, BosonsBulk.cpp:61-87, 179-218, 220-336, 349-458, 522-545) with
+ * the plain displacement of the open-boundary cluster systems
+ * (BosonCluster.cpp:14 USE_NIC = false; VectorDisplacement in its pair loop,
+ * BosonCluster.cpp:296).  Added terms, parameter k = p:
+ *   ln psi += alpha_p sum_i |r_i|^2,  O_p = sum_i |r_i|^2,
+ *   V += kappa sum_i |r_i|^2 with kappa = omega^2 / (4 hbar2_2m) (the trap
+ *   (m/2) omega^2 r^2 with hbar = 1), and the Gaussian pair repulsion
+ *   v0 exp(-r^2 / (2 sigma^2)) over all pairs.
+ * Known answer: v0 = 0, uR[0..p-1] = uI = 0, alpha_p = -omega / (4 hbar2_2m)
+ * is the exact ground state, E_loc = (3/2) omega n for every configuration. */
+struct orc_drop {
+	orc_sys* s; /* pair spline on [0, rmax] (knots of a box of length 2 rmax) */
+	int n, p;
+	double v0, sigma, kappa;
+};
+
+orc_drop* orc_drop_create(int n, int p, double rmax, double v0, double sigma, double omega, double hbar2_2m)
+{
+	if (n < 2 || p < 4 || !(rmax > 0.0) || !(hbar2_2m > 0.0)) return NULL;
+	double none = 0.0;
+	orc_sys* s = orc_create(3, n, p, 2.0 * rmax, NULL, 0, ORC_POT_NONE, &none, 0, 0.0, hbar2_2m);
+	if (!s) return NULL;
+	orc_drop* d = (orc_drop*)calloc(1, sizeof(orc_drop));
+	d->s = s;
+	d->n = n;
+	d->p = p;
+	d->v0 = v0;
+	d->sigma = sigma;
+	d->kappa = omega * omega / (4.0 * hbar2_2m);
+	return d;
+}
+
+void orc_drop_free(orc_drop* d)
+{
+	if (!d) return;
+	orc_free(d->s);
+	free(d);
+}
+
+static double drop_disp(const double* a, const double* b, double* d)
+{
+	double r2 = 0.0;
+	for (int c = 0; c < 3; c++)
+	{
+		d[c] = a[c] - b[c];
+		r2 += d[c] * d[c];
+	}
+	return sqrt(r2);
+}
+
+/* pair function u(r) of the spline part (uR only) */
+static double drop_u(const orc_sys* s, const double* wR, double r, double uout)
+{
+	if (r > s->rmax) return uout;
+	int b = find_bin(s, r);
+	double v[4];
+	spline_eval(s, b, r, v, NULL, NULL);
+	double u = 0.0;
+	for (int q = 0; q < 4; q++) u += wR[b - q] * v[q];
+	return u;
+}
+
+void orc_drop_eval(const orc_drop* dp, const double* uR, const double* uI, const double* R, double* lnpsi,
+                   double* O, double* eloc, double* other7, double* dE)
+{
+	const orc_sys* s = dp->s;
+	const int n = dp->n, P = dp->p, ns = s->ns, D = 3;
+	double* S = (double*)calloc((size_t)ns, sizeof(double));
+	double* wR = (double*)calloc((size_t)ns, sizeof(double));
+	double* wI = (double*)calloc((size_t)ns, sizeof(double));
+	double* G = (double*)calloc((size_t)n * 6, sizeof(double));
+	double* Lsp = (double*)calloc((size_t)ns, sizeof(double));
+	double* AR = (double*)calloc((size_t)ns, sizeof(double));
+	double* AI = (double*)calloc((size_t)ns, sizeof(double));
+	double nout = 0.0, vint = 0.0, lapR = 0.0, lapI = 0.0, r2sum = 0.0;
+	double d[3], v[4], d1[4], d2[4];
+	/* spline sums, outer pairs, pair potential over i < a */
+	for (int a = 0; a < n; a++)
+		for (int i = 0; i < a; i++)
+		{
+			double r = drop_disp(R + a * D, R + i * D, d);
+			vint += dp->v0 * exp(-(r * r) / (2.0 * dp->sigma * dp->sigma));
+			if (r <= s->rmax)
+			{
+				int b = find_bin(s, r);
+				spline_eval(s, b, r, v, NULL, NULL);
+				for (int q = 0; q < 4; q++) S[b - q] += v[q];
+			}
+			else nout += 1.0;
+		}
+	fold_apply(s, S, O);
+	for (int a = 0; a < n; a++)
+		for (int c = 0; c < D; c++) r2sum += R[a * D + c] * R[a * D + c];
+	O[P] = r2sum;
+	double e = 0.0;
+	for (int k = 0; k < P; k++) e += uR[k] * O[k];
+	e += uR[P - 1] * nout + uR[P] * r2sum;
+	*lnpsi = e;
+	for (int k = 0; k < P; k++)
+		for (int j = 0; j < ns; j++)
+		{
+			wR[j] += uR[k] * s->fold[k * ns + j];
+			wI[j] += uI[k] * s->fold[k * ns + j];
+		}
+	/* ordered pairs within r_max: gradients and Laplacian of the pair part */
+	for (int a = 0; a < n; a++)
+		for (int i = 0; i < n; i++)
+		{
+			if (i == a) continue;
+			double r = drop_disp(R + a * D, R + i * D, d);
+			if (r > s->rmax) continue;
+			int b = find_bin(s, r);
+			spline_eval(s, b, r, NULL, d1, d2);
+			double u1R = 0, u1I = 0, u2R = 0, u2I = 0;
+			for (int q = 0; q < 4; q++)
+			{
+				int sp = b - q;
+				u1R += wR[sp] * d1[q];
+				u1I += wI[sp] * d1[q];
+				u2R += wR[sp] * d2[q];
+				u2I += wI[sp] * d2[q];
+				Lsp[sp] += d2[q] + (D - 1.0) / r * d1[q];
+			}
+			for (int c = 0; c < D; c++)
+			{
+				G[a * 6 + c] += u1R * d[c] / r;
+				G[a * 6 + 3 + c] += u1I * d[c] / r;
+			}
+			lapR += u2R + (D - 1.0) / r * u1R;
+			lapI += u2I + (D - 1.0) / r * u1I;
+		}
+	/* one-body term: gradient 2 alpha_p r, Laplacian 2 D alpha_p per particle */
+	for (int a = 0; a < n; a++)
+		for (int c = 0; c < D; c++)
+		{
+			G[a * 6 + c] += 2.0 * uR[P] * R[a * D + c];
+			G[a * 6 + 3 + c] += 2.0 * uI[P] * R[a * D + c];
+		}
+	lapR += 2.0 * D * uR[P] * n;
+	lapI += 2.0 * D * uI[P] * n;
+	double sR1 = 0, sI1 = 0, sR1I1 = 0, gr = 0, gi = 0;
+	for (int a = 0; a < n; a++)
+		for (int c = 0; c < D; c++)
+		{
+			const double x = G[a * 6 + c], y = G[a * 6 + 3 + c];
+			sR1 += x * x;
+			sI1 += y * y;
+			sR1I1 += 2.0 * x * y;
+			gr += x * R[a * D + c];
+			gi += y * R[a * D + c];
+		}
+	const double c = s->hbar2_2m;
+	const double vtot = vint + dp->kappa * r2sum;
+	double kinR = -(sR1 - sI1 + lapR) * c;
+	double kinI = -(sR1I1 + lapI) * c;
+	eloc[0] = kinR + vtot;
+	eloc[1] = kinI;
+	other7[0] = kinR;
+	other7[1] = vtot;
+	other7[2] = sR1;
+	other7[3] = sI1;
+	other7[4] = lapR;
+	other7[5] = lapI;
+	other7[6] = sR1I1;
+	if (dE)
+	{
+		/* A_s = sum over ordered pairs of B'_s(r) (G_a . rhat), G the full gradient */
+		for (int a = 0; a < n; a++)
+			for (int i = 0; i < n; i++)
+			{
+				if (i == a) continue;
+				double r = drop_disp(R + a * D, R + i * D, d);
+				if (r > s->rmax) continue;
+				int b = find_bin(s, r);
+				spline_eval(s, b, r, NULL, d1, NULL);
+				double g_r = 0, g_i = 0;
+				for (int cc = 0; cc < D; cc++)
+				{
+					g_r += G[a * 6 + cc] * d[cc] / r;
+					g_i += G[a * 6 + 3 + cc] * d[cc] / r;
+				}
+				for (int q = 0; q < 4; q++)
+				{
+					AR[b - q] += d1[q] * g_r;
+					AI[b - q] += d1[q] * g_i;
+				}
+			}
+		for (int k = 0; k < P; k++)
+		{
+			double re = 0, im = 0;
+			for (int j = 0; j < ns; j++)
+			{
+				double f = s->fold[k * ns + j];
+				if (f == 0.0) continue;
+				re += f * (2.0 * AR[j] + Lsp[j]);
+				im += f * (2.0 * AI[j]);
+			}
+			dE[2 * k] = -c * re;
+			dE[2 * k + 1] = -c * im;
+		}
+		/* d/d alpha_p of -c (lap + G.G): -c (2 D n + 4 sum_a G_a . r_a) */
+		dE[2 * P] = -c * (2.0 * D * n + 4.0 * gr);
+		dE[2 * P + 1] = -c * (4.0 * gi);
+	}
+	free(S);
+	free(wR);
+	free(wI);
+	free(G);
+	free(Lsp);
+	free(AR);
+	free(AI);
+}
+
+/* Metropolis moves of drop walkers stored walker-major SoA (R[w][d][i]):
+ * the move rule of DoMetropolisStep (TDVMC.cpp:858-916) with the direct
+ * exponent change sum_i u(r_new) - u(r_old) + alpha_p (|x_new|^2 - |x_old|^2)
+ * and no wrap (open boundaries).  Random numbers: Philox with counter
+ * {move, walker0 + w, pass, call}, as orc_sample.  Returns accepted moves. */
+int64_t orc_drop_sample(const orc_drop* dp, const double* uR, double* Rsoa, int64_t nw, int64_t walker0, int moves,
+                        double step, uint64_t seed, uint32_t pass)
+{
+	const orc_sys* s = dp->s;
+	const int n = dp->n, P = dp->p, ns = s->ns;
+	double* wR = (double*)calloc((size_t)ns, sizeof(double));
+	for (int k = 0; k < P; k++)
+		for (int j = 0; j < ns; j++) wR[j] += uR[k] * s->fold[k * ns + j];
+	double* R = (double*)malloc((size_t)n * 3 * sizeof(double));
+	int64_t acc = 0;
+	double d[3];
+	for (int64_t w = 0; w < nw; w++)
+	{
+		double* X = Rsoa + (size_t)w * 3 * n;
+		for (int a = 0; a < 3; a++)
+			for (int i = 0; i < n; i++) R[i * 3 + a] = X[a * n + i];
+		for (int m = 0; m < moves; m++)
+		{
+			int p;
+			double U, z[3], xn[3];
+			move_randoms(n, 3, (uint32_t)m, (uint32_t)(walker0 + w), pass, seed, &p, &U, z);
+			double* xo = R + p * 3;
+			double r2n = 0.0, r2o = 0.0;
+			for (int a = 0; a < 3; a++)
+			{
+				xn[a] = xo[a] + step * z[a];
+				r2n += xn[a] * xn[a];
+				r2o += xo[a] * xo[a];
+			}
+			double delta = uR[P] * (r2n - r2o);
+			for (int i = 0; i < n; i++)
+			{
+				if (i == p) continue;
+				const double rn = drop_disp(xn, R + i * 3, d);
+				const double ro = drop_disp(xo, R + i * 3, d);
+				delta += drop_u(s, wR, rn, uR[P - 1]) - drop_u(s, wR, ro, uR[P - 1]);
+			}
+			if (isfinite(delta) && 2.0 * delta >= log(U) && 2.0 * delta < 709.782712893384)
+			{
+				for (int a = 0; a < 3; a++) xo[a] = xn[a];
+				acc++;
+			}
+		}
+		for (int a = 0; a < 3; a++)
+			for (int i = 0; i < n; i++) X[a * n + i] = R[i * 3 + a];
+	}
+	free(R);
+	free(wR);
+	return acc;
+}

@@ -110,6 +110,20 @@ int orc_solve_centred(int p, int imag, int precond, int solver, const double* O,
 int orc_observables(const orc_sys* s, const double* R, int gr_bins, int nshell, const int* shell_off,
                     const double* kvec, double* gr, double* sk);
 
+/* Trapped drops (batched systems of uneven particle number): a 3D drop of n bosons
+ * with open boundaries, the BosonsBulk pair spline on [0, rmax] (p
+ * parameters) plus a one-body parameter alpha_p (ln psi += alpha_p sum |r_i|^2),
+ * harmonic trap kappa |r|^2 with kappa = omega^2 / (4 hbar2_2m) and the
+ * Gaussian pair repulsion v0 exp(-r^2 / (2 sigma^2)).  Parameter vectors have
+ * p + 1 entries; O[p+1], dE[2(p+1)].  R: n*3 particle-major. */
+typedef struct orc_drop orc_drop;
+orc_drop* orc_drop_create(int n, int p, double rmax, double v0, double sigma, double omega, double hbar2_2m);
+void orc_drop_free(orc_drop* d);
+void orc_drop_eval(const orc_drop* d, const double* uR, const double* uI, const double* R, double* lnpsi,
+                   double* O, double* eloc, double* other7, double* dE);
+int64_t orc_drop_sample(const orc_drop* d, const double* uR, double* Rsoa, int64_t nw, int64_t walker0, int moves,
+                        double step, uint64_t seed, uint32_t pass);
+
 #ifdef __cplusplus
 }
 #endif
