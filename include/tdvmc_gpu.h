@@ -262,7 +262,9 @@ int tdvmc_measure_fp32_peak(double* tflops);
  * allocates nothing.  The first call on a device looks up that array's
  * device address with the device current, so make the first call on each
  * device before any stream capture.  All calls share the array: calls whose
- * work overlaps on the GPU (other streams or host threads) race on it.
+ * work overlaps on the GPU (other streams or host threads) race on it.  A CUDA
+ * error already pending on the calling thread is left in place and returned
+ * as TDVMC_ERR_CUDA without launching anything.
  *
  * No counterpart in the reference (its averages live in host vectors,
  * TDVMC.cpp:1103-1109). */
@@ -271,6 +273,96 @@ int tdvmc_reduce_walkers_noalloc(const double* O, const double* eloc, int64_t nw
 
 /* Number of kernel launches issued by this context since creation. */
 int64_t tdvmc_launch_count(tdvmc_ctx* ctx);
+
+/* ------------------------------------------------------------------------
+ * Batched trapped drops: many independent 3D systems of uneven particle
+ * number, each with its own parameters, walkers, statistics and TDVP solve,
+ * every kernel one launch over all drops (persistent blocks taking work items
+ * of one drop from a device queue, drops with more particles first).
+ *
+ * A drop of n bosons (2..32) has open boundaries and
+ *   ln psi = sum_k alpha_k O_k + alpha_p sum_i |r_i|^2 + phi,
+ * where O_k (k < p) are the BC-folded pair-spline sums of BosonsBulk on
+ * uniform knots over [0, r_max] (with its outer-pair term alpha_{p-1} for
+ * pairs beyond r_max, BosonsBulk.cpp:61-87, 179-218, 522-545), evaluated with
+ * plain displacements as the open-boundary cluster systems do
+ * (BosonCluster.cpp:14 USE_NIC = false), and O_p = sum_i |r_i|^2 is the
+ * one-body Gaussian width.  Potential: the harmonic trap
+ * omega^2 / (4 hbar2_2m) |r|^2 ((m/2) omega^2 r^2 with hbar = 1) plus the
+ * Gaussian pair repulsion v0 exp(-r^2 / (2 sigma^2)) over all pairs.  No
+ * reference system has this form; the pair-spline part is the BosonsBulk
+ * algorithm (same fold, kinetic sums, adjoint) without the minimum image.
+ * With v0 = 0, alpha_k = 0 (k < p) and alpha_p = -omega / (4 hbar2_2m) the
+ * wave function is the exact ground state: E_loc = (3/2) omega n for every
+ * configuration.
+ *
+ * Per-drop arrays are drop-major: parameters [S][p+1], walker outputs
+ * [S][walkers][...], walkers x[s][w][d][i] concatenated over drops. */
+typedef struct tdvmc_drops tdvmc_drops;
+
+typedef struct tdvmc_drops_desc {
+	int32_t n_systems;         /* S >= 1 */
+	const int32_t* n;          /* particles per drop, S values in 2..32 */
+	int32_t p;                 /* pair-spline parameters per drop, 4..32 (uniform knots) */
+	const double* rmax;        /* per drop: range of the pair spline */
+	double omega;              /* trap frequency */
+	double v0, sigma;          /* Gaussian pair repulsion */
+	double hbar2_2m;
+	int32_t precision;         /* TDVMC_PREC_* */
+	int64_t walkers_per_system;
+} tdvmc_drops_desc;
+
+int tdvmc_drops_create(const tdvmc_drops_desc* desc, tdvmc_drops** out);
+int tdvmc_drops_destroy(tdvmc_drops* ctx);
+int tdvmc_drops_get_stream(tdvmc_drops* ctx, void** stream);
+/* uR, uI [S][p+1]; phiR, phiI [S] (either may be NULL: zeros).  Starts a new step. */
+int tdvmc_drops_set_params(tdvmc_drops* ctx, const double* uR, const double* uI, const double* phiR,
+                           const double* phiI);
+int tdvmc_drops_get_params(tdvmc_drops* ctx, double* uR, double* uI, double* phiR, double* phiI);
+/* x: S * walkers * 3 * n_s values, x[s][w][d][i]. */
+int tdvmc_drops_set_walkers(tdvmc_drops* ctx, const double* x);
+int tdvmc_drops_get_walkers(tdvmc_drops* ctx, double* x);
+/* moves_per_particle * n_s single-particle moves per walker (DoMetropolisStep,
+ * TDVMC.cpp:858-916) at the current parameters; Philox key `seed`, counter
+ * {move, s * walkers + w, pass, call}; *accepted: total accepted moves. */
+int tdvmc_drops_sample(tdvmc_drops* ctx, int32_t moves_per_particle, double mc_step, uint64_t seed, uint32_t pass,
+                       int64_t* accepted);
+/* Local quantities of every walker (CalculateWavefunction +
+ * CalculateExpectationValues for each drop): lnpsi [S][w], O [S][w][p+1],
+ * eloc [S][w][2], other7 [S][w][7] (as tdvmc_eval_local; V = trap + pair),
+ * and, when dE is not NULL, the adjoint dE [S][w][p+1][2] (dE_loc/d uR_k,
+ * no reference counterpart).  Any output may be NULL. */
+int tdvmc_drops_eval(tdvmc_drops* ctx, double* lnpsi, double* O, double* eloc, double* other7, double* dE);
+/* Per-drop walker means of the last evaluation (ParallelUpdateExpectationValues,
+ * TDVMC.cpp:1152-1220, per drop): O_mean [S][p+1], energy [S][2], centred S
+ * [S][p+1][p+1], cov_OER / cov_OEI [S][p+1], dE_mean [S][p+1][2] (zeros
+ * without the adjoint), accepted_mean [S] (accepted moves per walker of the
+ * last sampling pass).  Any output may be NULL. */
+int tdvmc_drops_reduce(tdvmc_drops* ctx, double* O_mean, double* energy, double* S, double* cov_OER,
+                       double* cov_OEI, double* dE_mean, double* accepted_mean);
+/* SolveForParametersDot (TDVMC.cpp:1713-1828) of every drop on its last
+ * reduction: uDotR/uDotI [S][p+1], phiDotR/phiDotI [S], status [S]
+ * (TDVMC_OK or TDVMC_ERR_NOT_PD / NONFINITE per drop; may be NULL).  Returns
+ * the worst status. */
+int tdvmc_drops_tdvp_rhs(tdvmc_drops* ctx, int32_t imaginary_time, int32_t precondition, int32_t lin_solver,
+                         double* uDotR, double* uDotI, double* phiDotR, double* phiDotI, int32_t* status);
+/* `nsteps` TDVP steps of every drop (ODE_SOLVER_TYPE 0 or 2): each stage is one
+ * CUDA-graph launch of prep -> sample -> evaluate (+adjoint) -> per-drop reduce
+ * -> per-drop solve.  opts->moves_per_stage is the number of moves PER
+ * PARTICLE (sweeps) of a sampling pass.  energy [S][2] (may be NULL): the
+ * first-stage energies of the last step; status [S] as tdvmc_drops_tdvp_rhs. */
+int tdvmc_drops_run_steps(tdvmc_drops* ctx, const tdvmc_step_opts* opts, int32_t nsteps, double* energy,
+                          int32_t* status);
+/* The same steps timed with CUDA events on the context stream (*ms). */
+int tdvmc_drops_time_steps(tdvmc_drops* ctx, const tdvmc_step_opts* opts, int32_t nsteps, float* ms);
+/* One stage eagerly with an event after every kernel (as tdvmc_profile_stage). */
+int tdvmc_drops_profile_stage(tdvmc_drops* ctx, const tdvmc_step_opts* opts, float* ms, const char** names,
+                              int32_t* count);
+/* Choose the walkers per block of the sampling and evaluation kernels from
+ * {32, 64, 128} by timing them on the current walkers (restored afterwards). */
+int tdvmc_drops_autotune(tdvmc_drops* ctx, int32_t moves_per_particle, double mc_step);
+int tdvmc_drops_get_tiles(tdvmc_drops* ctx, int32_t* sample_threads, int32_t* eval_threads);
+int64_t tdvmc_drops_launch_count(tdvmc_drops* ctx);
 
 #ifdef __cplusplus
 }

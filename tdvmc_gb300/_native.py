@@ -22,7 +22,12 @@ EXPORTS = ("tdvmc_status_string", "tdvmc_create", "tdvmc_destroy", "tdvmc_get_st
            "tdvmc_observables",
            "tdvmc_reduce_stats", "tdvmc_tdvp_rhs", "tdvmc_step",
            "tdvmc_get_step_operators", "tdvmc_run_steps", "tdvmc_time_steps", "tdvmc_profile_stage", "tdvmc_autotune", "tdvmc_get_tiles", "tdvmc_launch_count",
-           "tdvmc_measure_fp32_peak", "tdvmc_reduce_walkers_noalloc")
+           "tdvmc_measure_fp32_peak", "tdvmc_reduce_walkers_noalloc",
+           "tdvmc_drops_create", "tdvmc_drops_destroy", "tdvmc_drops_get_stream", "tdvmc_drops_set_params",
+           "tdvmc_drops_get_params", "tdvmc_drops_set_walkers", "tdvmc_drops_get_walkers", "tdvmc_drops_sample",
+           "tdvmc_drops_eval", "tdvmc_drops_reduce", "tdvmc_drops_tdvp_rhs", "tdvmc_drops_run_steps",
+           "tdvmc_drops_time_steps", "tdvmc_drops_profile_stage", "tdvmc_drops_autotune", "tdvmc_drops_get_tiles",
+           "tdvmc_drops_launch_count")
 
 
 class SystemDesc(C.Structure):
@@ -30,6 +35,12 @@ class SystemDesc(C.Structure):
                 ("user_knots", C.POINTER(C.c_double)), ("box_length", C.c_double), ("pot_kind", C.c_int32),
                 ("n_pot", C.c_int32), ("pot", C.c_double * 5), ("hbar2_2m", C.c_double), ("precision", C.c_int32),
                 ("n_walkers", C.c_int64)]
+
+
+class DropsDesc(C.Structure):
+    _fields_ = [("n_systems", C.c_int32), ("n", C.POINTER(C.c_int32)), ("p", C.c_int32),
+                ("rmax", C.POINTER(C.c_double)), ("omega", C.c_double), ("v0", C.c_double), ("sigma", C.c_double),
+                ("hbar2_2m", C.c_double), ("precision", C.c_int32), ("walkers_per_system", C.c_int64)]
 
 
 class Stats(C.Structure):
@@ -95,6 +106,25 @@ def load(build_if_missing: bool = True):
     L.tdvmc_measure_fp32_peak.argtypes = [P(C.c_double)]
     L.tdvmc_reduce_walkers_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    v = C.c_void_p
+    L.tdvmc_drops_create.argtypes = [P(DropsDesc), P(C.c_void_p)]
+    L.tdvmc_drops_destroy.argtypes = [v]
+    L.tdvmc_drops_get_stream.argtypes = [v, P(C.c_void_p)]
+    L.tdvmc_drops_set_params.argtypes = [v, d, d, d, d]
+    L.tdvmc_drops_get_params.argtypes = [v, d, d, d, d]
+    L.tdvmc_drops_set_walkers.argtypes = [v, d]
+    L.tdvmc_drops_get_walkers.argtypes = [v, d]
+    L.tdvmc_drops_sample.argtypes = [v, C.c_int32, C.c_double, C.c_uint64, C.c_uint32, P(C.c_int64)]
+    L.tdvmc_drops_eval.argtypes = [v, d, d, d, d, d]
+    L.tdvmc_drops_reduce.argtypes = [v, d, d, d, d, d, d, d]
+    L.tdvmc_drops_tdvp_rhs.argtypes = [v, C.c_int32, C.c_int32, C.c_int32, d, d, d, d, v]
+    L.tdvmc_drops_run_steps.argtypes = [v, P(StepOpts), C.c_int32, d, v]
+    L.tdvmc_drops_time_steps.argtypes = [v, P(StepOpts), C.c_int32, P(C.c_float)]
+    L.tdvmc_drops_profile_stage.argtypes = [v, P(StepOpts), P(C.c_float), P(C.c_char_p), P(C.c_int32)]
+    L.tdvmc_drops_autotune.argtypes = [v, C.c_int32, C.c_double]
+    L.tdvmc_drops_get_tiles.argtypes = [v, P(C.c_int32), P(C.c_int32)]
+    L.tdvmc_drops_launch_count.argtypes = [v]
+    L.tdvmc_drops_launch_count.restype = C.c_int64
     _lib = L
     return L
 

@@ -40,13 +40,15 @@ constexpr int kPcCorrectors = 6;
 constexpr int kStatusNotPD = 1;
 constexpr int kStatusNonFinite = 2;
 
+// The solve and stage update of one system by one CTA (dynamic shared memory:
+// solve_smem_bytes(p)).
 template <typename T>
-__global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict__ dyn, const double* __restrict__ means1,
-                                               const double* __restrict__ S, const double* __restrict__ cov,
-                                               const T* __restrict__ lnpsi_w, double* __restrict__ base,
-                                               double* __restrict__ stage_params, double* __restrict__ kdot,
-                                               double* __restrict__ rhs_out, double* __restrict__ means_step0,
-                                               int n_means) {
+__device__ __forceinline__ void solve_stage(SolveArgs a, DynState* __restrict__ dyn, const double* __restrict__ means1,
+                                            const double* __restrict__ S, const double* __restrict__ cov,
+                                            const T* __restrict__ lnpsi_w, double* __restrict__ base,
+                                            double* __restrict__ stage_params, double* __restrict__ kdot,
+                                            double* __restrict__ rhs_out, double* __restrict__ means_step0,
+                                            int n_means) {
 	extern __shared__ double sm[];
 	const int P = a.p;
 	const int np = 2 * P + 2;
@@ -279,6 +281,37 @@ __global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict
 		dyn->pass += 1u;
 	}
 }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_solve(SolveArgs a, DynState* __restrict__ dyn, const double* __restrict__ means1,
+                                               const double* __restrict__ S, const double* __restrict__ cov,
+                                               const T* __restrict__ lnpsi_w, double* __restrict__ base,
+                                               double* __restrict__ stage_params, double* __restrict__ kdot,
+                                               double* __restrict__ rhs_out, double* __restrict__ means_step0,
+                                               int n_means) {
+	solve_stage<T>(a, dyn, means1, S, cov, lnpsi_w, base, stage_params, kdot, rhs_out, means_step0, n_means);
+}
+
+// Independent systems, one CTA each (system b = blockIdx.x): its state, means
+// (n_means per system), S (p x p), covariances (p x 2), walkers (nws per
+// system, the first one normalises), parameter vectors (2p + 2 per system; the
+// RK slopes 4 x (2p + 2)).
+template <typename T>
+__global__ void __launch_bounds__(256) k_solve_systems(SolveArgs a, DynState* __restrict__ dyn,
+                                                       const double* __restrict__ means1, const double* __restrict__ S,
+                                                       const double* __restrict__ cov, const T* __restrict__ lnpsi_w,
+                                                       int64_t nws, double* __restrict__ base,
+                                                       double* __restrict__ stage_params, double* __restrict__ kdot,
+                                                       double* __restrict__ rhs_out, double* __restrict__ means_step0,
+                                                       int n_means) {
+	const size_t b = blockIdx.x;
+	const size_t np = 2 * (size_t)a.p + 2;
+	solve_stage<T>(a, dyn + b, means1 + b * n_means, S + b * a.p * a.p, cov + b * a.p * 2, lnpsi_w + b * nws,
+	               base + b * np, stage_params + b * np, kdot + b * 4 * np, rhs_out + b * np,
+	               means_step0 + b * n_means, n_means);
+}
+
+__host__ __device__ inline size_t solve_smem_bytes(int p) { return ((size_t)p * (p + 2) + 6 * (size_t)p + 8) * sizeof(double); }
 
 // Stage coefficient tables from the current stage parameters: per-spline
 // complex weights w_s = sum_k alpha_k fold[k][s], then per knot interval j the
