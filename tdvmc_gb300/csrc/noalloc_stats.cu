@@ -121,6 +121,9 @@ extern "C" int tdvmc_reduce_walkers_noalloc(const double* O, const double* eloc,
                                             double* cov_OEI, void* stream) {
 	if (!O || !eloc || !O_mean || !E_mean || !S || !cov_OER || !cov_OEI) return TDVMC_ERR_ARG;
 	if (p < 1 || p > kNaMaxP || nw < 1) return TDVMC_ERR_ARG;
+	// an error left by the caller's own earlier CUDA work is not this call's:
+	// report it without launching and without clearing it
+	if (cudaPeekAtLastError() != cudaSuccess) return TDVMC_ERR_CUDA;
 	int dev = 0;
 	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return TDVMC_ERR_CUDA;
 	double* scratch = nullptr;
