@@ -16,10 +16,34 @@
 // the k shells are the first 50 of kVectors{D}D.json next to the config file
 // (BosonsBulk.cpp:55, 124-139).
 //
+// Files as the reference: the config must carry CONFIG_VERSION "0.24"
+// (TDVMC.cpp:133, 3039-3043); walkers start from
+// <config dir>/coords/particleconfiguration_<N>_<DIM>D_<k>.csv when such files
+// exist (the last line, comma-separated x y z per particle;
+// LoadLastPositionsFromFile, TDVMC.cpp:640-670; walker w takes file w mod the
+// number of consecutive files k = 0, 1, ...), else from the jittered lattice;
+// at the end the driver writes AAFinish_particleconfiguration_<N>_<DIM>D.dat
+// (walker 0) and coords/particleconfiguration_<N>_<DIM>D_<k>.dat for the first
+// GPU_COORDS_FILES walkers (default 1) (TDVMC.cpp:4010-4018), and
+// AAFinish_tVMC.config: the input config with the final parameters
+// (WriteConfig, TDVMC.cpp:387-407, 4027-4034; numbers with 17 significant
+// digits where the reference prints 6).
+//
+// Parameter acceptance (USE_PARAMETER_ACCEPTANCE_CHECK = 1, TDVMC.cpp:3648-
+// 3800, AcceptNewParams 2585-2630): a step is tried at most twice, the second
+// time with twice the sampling effort; PARAMETER_ACCEPTANCE_CHECK_TYPE 0
+// rejects a non-positive-definite S, 1 also non-finite new parameters, 2 also a
+// relative change of any uR_k above 0.1 from the step's start.  A step that
+// needed its second trial sets the run back 5 steps (SetBackNSteps,
+// TDVMC.cpp:2746-2784, 3876-3880, 3909-3916): time, records and parameters of
+// the last 5 steps are dropped and the walkers restart from their initial
+// configuration with MC_VERY_FIRST_NINITIALIZATIONSTEPS moves.  Check types 3
+// and above are refused.
+//
 // Extra keys (all optional): GPU_WALKERS (default MC_NSTEPS), GPU_PRECISION
 // ("mixed" or "fp64"), POTENTIAL ("square" as BosonsBulk, "gauss", "lj"),
 // HBAR2_2M (default 1.0, the reference's constant), GPU_ADJOINT (0/1),
-// GPU_SEED.
+// GPU_SEED, GPU_COORDS_FILES.
 //
 // usage: tdvmc_run <config file> [output directory]
 #include "tdvmc_gpu.h"
@@ -225,6 +249,79 @@ bool read_k_shells(const std::string& path, int dim, double L, int nshell, std::
 	return true;
 }
 
+// JSON text of a value (numbers with 17 significant digits)
+std::string json_text(const Json& j) {
+	std::ostringstream o;
+	o.precision(17);
+	switch (j.kind) {
+	case Json::NUM:
+		o << j.num;
+		break;
+	case Json::STR:
+		o << '"' << j.str << '"';
+		break;
+	case Json::BOOL:
+		o << (j.b ? "true" : "false");
+		break;
+	case Json::ARR:
+		o << "\n\t[\n\t\t ";
+		for (size_t i = 0; i < j.arr.size(); i++) o << (i ? ", " : "") << json_text(j.arr[i]);
+		o << "\n\t]";
+		break;
+	case Json::OBJ: {
+		o << "{";
+		size_t i = 0;
+		for (auto& kv : j.obj) o << (i++ ? ", " : "") << '"' << kv.first << "\" : " << json_text(kv.second);
+		o << "}";
+		break;
+	}
+	default:
+		o << "null";
+	}
+	return o.str();
+}
+
+Json json_array(const std::vector<double>& v) {
+	Json j;
+	j.kind = Json::ARR;
+	for (double x : v) {
+		Json e;
+		e.kind = Json::NUM;
+		e.num = x;
+		j.arr.push_back(e);
+	}
+	return j;
+}
+
+// the last non-empty line of a coordinate file, numbers separated by commas
+// (LoadLastPositionsFromFile) or white space
+bool read_last_positions(const std::string& path, int n, int dim, std::vector<double>& xyz) {
+	std::ifstream f(path);
+	if (!f) return false;
+	std::string line, last;
+	while (std::getline(f, line))
+		if (line.find_first_not_of(" \t\r") != std::string::npos) last = line;
+	if (last.empty()) return false;
+	for (char& c : last)
+		if (c == ',') c = ' ';
+	std::istringstream in(last);
+	xyz.clear();
+	double v;
+	while (in >> v) xyz.push_back(v);
+	return (int)xyz.size() >= n * dim;
+}
+
+// one line of N x DIM coordinates, particle-major, in the data-file format
+// (WriteParticleInputFile: WriteDataToFile without a header)
+void write_positions(const std::string& path, const std::vector<double>& x, int64_t w, int n, int dim) {
+	std::ofstream f(path);
+	f.precision(15);
+	f << std::scientific;
+	for (int i = 0; i < n; i++)
+		for (int a = 0; a < dim; a++) f << std::setw(24) << x[((size_t)w * dim + a) * n + i];
+	f << "\n";
+}
+
 bool file_exists(const std::string& p) {
 	struct stat st;
 	return stat(p.c_str(), &st) == 0;
@@ -253,6 +350,13 @@ int main(int argc, char** argv) {
 	Config cfg;
 	Parser ps(text);
 	if (!ps.value(cfg.root) || cfg.root.kind != Json::OBJ) return 2;
+	// the reference refuses configs of another version (TDVMC.cpp:133, 3039-3043)
+	const std::string required_version = "0.24";
+	if (cfg.str("CONFIG_VERSION", "") != required_version) {
+		std::fprintf(stderr, "Config file is out of date.\nrequired: \"%s\"\nfound: \"%s\"\n",
+		             required_version.c_str(), cfg.str("CONFIG_VERSION", "").c_str());
+		return 1;
+	}
 	if (cfg.str("SYSTEM_TYPE", "BosonsBulk") != "BosonsBulk") {
 		std::fprintf(stderr, "only SYSTEM_TYPE BosonsBulk is implemented on the GPU\n");
 		return 2;
@@ -306,30 +410,56 @@ int main(int argc, char** argv) {
 	double phiR = cfg.num("PARAM_PHIR", 0.0), phiI = cfg.num("PARAM_PHII", 0.0);
 	if ((rc = tdvmc_set_params(ctx, uR.data(), uI.data(), phiR, phiI))) return die("tdvmc_set_params", rc);
 
-	// lattice start with 1/10 jitter per walker (TDVMC.cpp:713-760), one generator per walker
-	std::vector<double> x((size_t)walkers * DIM * N);
-	const int m = (int)std::lround(std::pow((double)N, 1.0 / DIM));
-	const double l = LBOX / m;
-	for (int64_t w = 0; w < walkers; w++) {
-		std::mt19937_64 gen((uint64_t)w + 1);
-		std::uniform_real_distribution<double> U(0.0, 1.0);
-		for (int i = 0; i < N; i++) {
-			int idx[3] = {0, 0, 0}, rem = i;
-			for (int a = DIM - 1; a >= 0; a--) {
-				idx[a] = rem % m;
-				rem /= m;
-			}
-			for (int a = 0; a < DIM; a++) {
-				double v = idx[a] * l + (U(gen) - 0.5) * l / 10.0;
-				if (DIM == 1) v -= LBOX / 2.0;
-				x[((size_t)w * DIM + a) * N + i] = v;
+	// initial walkers (InitCoordinateConfiguration, TDVMC.cpp:672-785): the last line of
+	// coords/particleconfiguration_<N>_<DIM>D_<k>.csv for k = 0, 1, ... (walker w takes
+	// file w mod K), else the lattice with 1/10 jitter, one generator per walker
+	std::vector<double> x0((size_t)walkers * DIM * N);
+	std::vector<std::vector<double>> files;
+	{
+		const std::string stem = cfg_dir + "coords/particleconfiguration_" + std::to_string(N) + "_" +
+		                         std::to_string(DIM) + "D_";
+		std::vector<double> xyz;
+		while (read_last_positions(stem + std::to_string(files.size()) + ".csv", N, DIM, xyz)) files.push_back(xyz);
+	}
+	if (!files.empty()) {
+		std::printf("init coordinates from %zu file(s) coords/particleconfiguration_%d_%dD_*.csv\n", files.size(), N,
+		            DIM);
+		for (int64_t w = 0; w < walkers; w++) {
+			const std::vector<double>& f = files[(size_t)(w % (int64_t)files.size())];
+			for (int i = 0; i < N; i++)
+				for (int a = 0; a < DIM; a++) x0[((size_t)w * DIM + a) * N + i] = f[(size_t)i * DIM + a];
+		}
+	} else {
+		const int m = (int)std::lround(std::pow((double)N, 1.0 / DIM));
+		const double l = LBOX / m;
+		for (int64_t w = 0; w < walkers; w++) {
+			std::mt19937_64 gen((uint64_t)w + 1);
+			std::uniform_real_distribution<double> U(0.0, 1.0);
+			for (int i = 0; i < N; i++) {
+				int idx[3] = {0, 0, 0}, rem = i;
+				for (int a = DIM - 1; a >= 0; a--) {
+					idx[a] = rem % m;
+					rem /= m;
+				}
+				for (int a = 0; a < DIM; a++) {
+					double v = idx[a] * l + (U(gen) - 0.5) * l / 10.0;
+					if (DIM == 1) v -= LBOX / 2.0;
+					x0[((size_t)w * DIM + a) * N + i] = v;
+				}
 			}
 		}
 	}
-	if ((rc = tdvmc_set_walkers(ctx, x.data(), walkers))) return die("tdvmc_set_walkers", rc);
 	int64_t acc = 0;
-	if (MC_VERY_FIRST > 0 && (rc = tdvmc_sample(ctx, MC_VERY_FIRST, MC_STEP, seed, 0xFFFFFFF0u, &acc)))
-		return die("tdvmc_sample", rc);
+	uint32_t restarts = 0;
+	// walkers from their initial configuration, thermalised (also after a set-back)
+	auto init_walkers = [&]() -> int {
+		int r = tdvmc_set_walkers(ctx, x0.data(), walkers);
+		if (r) return r;
+		if (MC_VERY_FIRST > 0) r = tdvmc_sample(ctx, MC_VERY_FIRST, MC_STEP, seed, 0xFFFFFFF0u - restarts, &acc);
+		restarts++;
+		return r;
+	};
+	if ((rc = init_walkers())) return die("initial walkers", rc);
 
 	tdvmc_step_opts o{};
 	o.dt = TIMESTEP;
@@ -352,6 +482,13 @@ int main(int argc, char** argv) {
 		return 2;
 	}
 	const bool acceptance_check = (int)cfg.num("USE_PARAMETER_ACCEPTANCE_CHECK", 0) == 1;
+	const int check_type = (int)cfg.num("PARAMETER_ACCEPTANCE_CHECK_TYPE", 0);
+	if (acceptance_check && (check_type < 0 || check_type > 2)) {
+		std::fprintf(stderr, "PARAMETER_ACCEPTANCE_CHECK_TYPE %d is not implemented on the GPU (0, 1 and 2 are)\n",
+		             check_type);
+		return 2;
+	}
+	const int coords_files = std::max(0, (int)cfg.num("GPU_COORDS_FILES", 1));
 
 	std::vector<std::vector<double>> allER, allEI, allO, allOther, allPR, allPI;
 	std::vector<double> times;
@@ -365,6 +502,9 @@ int main(int argc, char** argv) {
 			k_off.assign(1, 0);
 		}
 	}
+	// parameters at the start of the last steps (uRList etc., TDVMC.cpp:3437-3460)
+	std::vector<std::vector<double>> histR, histI;
+	std::vector<double> histPR, histPI;
 	int step = 0;
 	for (double t = 0.0; t <= TOTALTIME; t += TIMESTEP, step++) {
 		if ((rc = tdvmc_set_time(ctx, t))) return die("tdvmc_set_time", rc);
@@ -387,18 +527,50 @@ int main(int argc, char** argv) {
 		std::vector<double> pR(P), pI(P);
 		double p0R, p0I;
 		tdvmc_get_params(ctx, pR.data(), pI.data(), &p0R, &p0I);
+		histR.push_back(pR);
+		histI.push_back(pI);
+		histPR.push_back(p0R);
+		histPI.push_back(p0I);
+		if (histR.size() > 105) {
+			histR.erase(histR.begin());
+			histI.erase(histI.begin());
+			histPR.erase(histPR.begin());
+			histPI.erase(histPI.begin());
+		}
 		tdvmc_stats st{};
 		tdvmc_step_opts oo = o;
-		// a non-positive-definite S rejects the step (doNotAcceptStep, TDVMC.cpp:1583-1588,
-		// 2588-2591); retry once with twice the sampling effort (TDVMC.cpp:3648-3651)
-		for (int trial = 1; trial <= 2; trial++) {
+		// up to two trials, the second with twice the sampling effort (TDVMC.cpp:3648-3651);
+		// a trial is rejected by a non-positive-definite S (doNotAcceptStep,
+		// TDVMC.cpp:1583-1588) and, by check type, by non-finite or too large changes of
+		// the new parameters (AcceptNewParams, TDVMC.cpp:2585-2630)
+		int trial = 0;
+		bool accepted = false;
+		while (!accepted && trial < 2) {
+			trial++;
 			oo.moves_per_stage = o.moves_per_stage * trial;
 			rc = tdvmc_step(ctx, &oo, &st);
-			if (rc == TDVMC_OK || !acceptance_check || rc != TDVMC_ERR_NOT_PD) break;
-			std::fprintf(stderr, "PARAMETERS NOT ACCEPTED (t=%g), retrying\n", t);
-			tdvmc_set_params(ctx, pR.data(), pI.data(), p0R, p0I);
+			if (rc && rc != TDVMC_ERR_NOT_PD && rc != TDVMC_ERR_NONFINITE) return die("tdvmc_step", rc);
+			if (!acceptance_check) {
+				accepted = true;
+				break;
+			}
+			std::vector<double> nR(P), nI(P);
+			double nPR, nPI;
+			tdvmc_get_params(ctx, nR.data(), nI.data(), &nPR, &nPI);
+			accepted = rc != TDVMC_ERR_NOT_PD;
+			if (accepted && check_type >= 1 && histR.size() > 1)
+				for (int k = 0; k < P && accepted; k++) {
+					if (!std::isfinite(nR[k])) accepted = false;
+					else if (check_type == 2 && std::fabs(1.0 - nR[k] / pR[k]) > 0.1) accepted = false;
+				}
+			if (!accepted) {
+				std::fprintf(stderr, "PARAMETERS NOT ACCEPTED (t=%g, trial %d)\n", t, trial);
+				tdvmc_set_params(ctx, pR.data(), pI.data(), p0R, p0I);
+			}
 		}
-		if (rc && rc != TDVMC_ERR_NOT_PD) return die("tdvmc_step", rc);
+		// the reference's setback condition: a step that needed its second trial
+		// (TDVMC.cpp:3876-3880) rewinds 5 steps (SetBackNSteps, TDVMC.cpp:2746-2784)
+		const bool set_back = acceptance_check && trial == 2;
 		tdvmc_get_step_operators(ctx, O.data());
 		std::vector<double> other(st.other, st.other + 9);
 		std::vector<double> parR = pR, parI = pI;
@@ -430,6 +602,30 @@ int main(int argc, char** argv) {
 			std::fprintf(stderr, "Energy not finite\n");
 			break;
 		}
+		if (set_back) {
+			std::fprintf(stderr, "Parameters not accepted: SetBackNSteps(5) at t=%g\n", t);
+			for (int k = 0; k < 5 && !histR.empty() && !times.empty(); k++) {
+				t -= TIMESTEP;
+				step--;
+				times.pop_back();
+				allER.pop_back();
+				allEI.pop_back();
+				allO.pop_back();
+				allOther.pop_back();
+				allPR.pop_back();
+				allPI.pop_back();
+				pR = histR.back();
+				pI = histI.back();
+				p0R = histPR.back();
+				p0I = histPI.back();
+				histR.pop_back();
+				histI.pop_back();
+				histPR.pop_back();
+				histPI.pop_back();
+			}
+			if ((rc = tdvmc_set_params(ctx, pR.data(), pI.data(), p0R, p0I))) return die("tdvmc_set_params", rc);
+			if ((rc = init_walkers())) return die("walkers after the set-back", rc);
+		}
 	}
 	write_table("AllLocalEnergyR", "ER", allER);
 	write_table("AllLocalEnergyI", "EI", allEI);
@@ -440,6 +636,35 @@ int main(int argc, char** argv) {
 	std::vector<std::vector<double>> tt;
 	for (double t : times) tt.push_back({t});
 	write_table("Alltimes", "t", tt);
+
+	// files for successive runs (TDVMC.cpp:4010-4034)
+	std::vector<double> xf((size_t)walkers * DIM * N);
+	if ((rc = tdvmc_get_walkers(ctx, xf.data(), walkers))) return die("tdvmc_get_walkers", rc);
+	mkdir((g_out + "coords").c_str(), 0755);
+	for (int k = 0; k < coords_files && k < walkers; k++)
+		write_positions(g_out + "coords/particleconfiguration_" + std::to_string(N) + "_" + std::to_string(DIM) + "D_" +
+		                    std::to_string(k) + ".dat",
+		                xf, k, N, DIM);
+	write_positions(g_out + "AAFinish_particleconfiguration_" + std::to_string(N) + "_" + std::to_string(DIM) + "D.dat",
+	                xf, 0, N, DIM);
+	{
+		std::vector<double> fR(P), fI(P);
+		double fPR, fPI;
+		tdvmc_get_params(ctx, fR.data(), fI.data(), &fPR, &fPI);
+		Json fin = cfg.root;
+		fin.obj["PARAMS_REAL"] = json_array(fR);
+		fin.obj["PARAMS_IMAGINARY"] = json_array(fI);
+		fin.obj["PARAM_PHIR"].kind = Json::NUM;
+		fin.obj["PARAM_PHIR"].num = fPR;
+		fin.obj["PARAM_PHII"].kind = Json::NUM;
+		fin.obj["PARAM_PHII"].num = fPI;
+		std::ofstream f(g_out + "AAFinish_tVMC.config");
+		f << "{\n";
+		size_t i = 0;
+		for (auto& kv : fin.obj)
+			f << "\t\"" << kv.first << "\" : " << json_text(kv.second) << (++i < fin.obj.size() ? ",\n" : "\n");
+		f << "}";
+	}
 	tdvmc_destroy(ctx);
 	return 0;
 }

@@ -1,0 +1,124 @@
+"""CPU tests of the native host driver's control logic (tdvmc_run), linked
+against a CPU stand-in of the C ABI (tests/host/fake_capi.cpp): the
+CONFIG_VERSION check (TDVMC.cpp:3039-3043), the coordinate files read at the
+start and written at the end (TDVMC.cpp:640-670, 4010-4018), the final config
+(TDVMC.cpp:4027-4034), and the parameter-acceptance trials with the 5-step
+set-back (TDVMC.cpp:2585-2630, 2746-2784, 3648-3916)."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def driver(tmp_path_factory):
+    d = tmp_path_factory.mktemp("fakebuild")
+    exe = str(d / "tdvmc_run_fake")
+    subprocess.check_call(["g++", "-O1", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tdvmc_gb300", "csrc", "host", "tdvmc_run.cpp"),
+                           os.path.join(ROOT, "tests", "host", "fake_capi.cpp"), "-o", exe])
+    return exe
+
+
+def base_cfg(**kw):
+    c = {"CONFIG_VERSION": "0.24", "SYSTEM_TYPE": "BosonsBulk", "N": 8, "LBOX": 2.0, "DIM": 3, "N_PARAM": 4,
+         "MC_STEP": 0.3, "MC_NSTEPS": 4, "MC_NTHERMSTEPS": 16, "MC_VERY_FIRST_NINITIALIZATIONSTEPS": 5,
+         "TIMESTEP": 0.01, "TOTALTIME": 0.095, "IMAGINARY_TIME": 0, "ODE_SOLVER_TYPE": 2,
+         "WRITE_EVERY_NTH_STEP_TO_FILE": 1, "SYSTEM_PARAMS": [0.5, 1.0], "PARAMS_REAL": [1.0, 1.0, 1.0, 1.0],
+         "PARAMS_IMAGINARY": [0.0], "PARAM_PHIR": 0.0, "PARAM_PHII": 0.0}
+    c.update(kw)
+    return c
+
+
+def run(driver, tmp_path, cfg, env=None, coords=None):
+    cdir = tmp_path / "cfg"
+    cdir.mkdir(exist_ok=True)
+    if coords is not None:
+        (cdir / "coords").mkdir(exist_ok=True)
+        for k, line in enumerate(coords):
+            (cdir / "coords" / ("particleconfiguration_8_3D_%d.csv" % k)).write_text("junk\n" + line + "\n")
+    path = cdir / "run.config"
+    path.write_text(json.dumps(cfg))
+    out = tmp_path / "out"
+    log = tmp_path / "fake.log"
+    e = dict(os.environ, FAKE_LOG=str(log), **(env or {}))
+    r = subprocess.run([driver, str(path), str(out)], capture_output=True, text=True, env=e)
+    return r, out, (log.read_text().splitlines() if log.exists() else [])
+
+
+def table(path):
+    return np.loadtxt(path, skiprows=1, ndmin=2)
+
+
+def test_config_version_is_checked(driver, tmp_path):
+    r, _, _ = run(driver, tmp_path, base_cfg(CONFIG_VERSION="0.23"))
+    assert r.returncode == 1 and "out of date" in r.stderr
+
+
+def test_plain_run_and_end_files(driver, tmp_path):
+    r, out, log = run(driver, tmp_path, base_cfg())
+    assert r.returncode == 0, r.stderr
+    E = table(out / "AllLocalEnergyR.dat")[:, 0]
+    assert list(E) == list(range(1, 11))  # 10 steps, one trial each
+    assert sum(1 for l in log if l.startswith("step")) == 10
+    fin = json.loads((out / "AAFinish_tVMC.config").read_text())
+    uR = np.asarray(fin["PARAMS_REAL"])
+    assert np.allclose(uR, 1.0 + 0.01 * sum(range(1, 11)))
+    assert fin["CONFIG_VERSION"] == "0.24" and fin["N"] == 8
+    pos = np.loadtxt(out / "AAFinish_particleconfiguration_8_3D.dat")
+    assert pos.size == 24
+    assert (out / "coords" / "particleconfiguration_8_3D_0.dat").exists()
+
+
+def test_walkers_start_from_coordinate_files(driver, tmp_path):
+    lines = [",".join("%.17g" % (0.01 * (k + 1) * i) for i in range(24)) for k in range(2)]
+    r, out, log = run(driver, tmp_path, base_cfg(TOTALTIME=0.0), coords=lines)
+    assert r.returncode == 0, r.stderr
+    assert "from 2 file(s)" in r.stdout
+    # walker 0 takes file 0: its first coordinate (particle 0, x) is 0.0; the data
+    # written at the end is the walkers the (fake) library holds
+    pos = np.loadtxt(out / "AAFinish_particleconfiguration_8_3D.dat")
+    expect = np.array([0.01 * i for i in range(24)])
+    assert np.allclose(pos, expect)
+
+
+def test_rejected_step_retries_then_sets_back_five_steps(driver, tmp_path):
+    # call 7 (step 7) is not positive definite; its second trial (call 8) passes, and
+    # the reference then sets the run back 5 steps
+    cfg = base_cfg(USE_PARAMETER_ACCEPTANCE_CHECK=1, PARAMETER_ACCEPTANCE_CHECK_TYPE=0, TOTALTIME=0.095)
+    r, out, log = run(driver, tmp_path, cfg, env={"FAKE_NOT_PD": "7"})
+    assert r.returncode == 0, r.stderr
+    assert "SetBackNSteps(5)" in r.stderr
+    steps = [l for l in log if l.startswith("step")]
+    # the retried call used twice the moves
+    assert steps[6].endswith("moves 16") and steps[7].endswith("moves 32")
+    E = table(out / "AllLocalEnergyR.dat")[:, 0]
+    # steps 1-6 recorded, step 7 (trial 2, energy 8) recorded then 5 records dropped:
+    # 1, 2 remain, then the run continues from step 3 with calls 9, 10, ...
+    assert list(E[:3]) == [1, 2, 9]
+    assert len(E) == 10
+    # the walkers restarted from their initial configuration with the thermalisation moves
+    assert sum(1 for l in log if l.startswith("set_walkers")) == 2
+    assert sum(1 for l in log if l == "sample 5") == 2
+    # parameters restored to the start of the third step: 1 + 0.01 * (1 + 2)
+    sets = [float(l.split()[1]) for l in log if l.startswith("set_params")]
+    assert any(abs(v - (1.0 + 0.01 * 3)) < 1e-12 for v in sets)
+
+
+def test_check_type_2_rejects_large_changes(driver, tmp_path):
+    cfg = base_cfg(USE_PARAMETER_ACCEPTANCE_CHECK=1, PARAMETER_ACCEPTANCE_CHECK_TYPE=2, TOTALTIME=0.025)
+    r, out, log = run(driver, tmp_path, cfg, env={"FAKE_BIG": "2"})
+    assert r.returncode == 0, r.stderr
+    assert "PARAMETERS NOT ACCEPTED" in r.stderr
+    # type 0 accepts the same change
+    r0, _, _ = run(driver, tmp_path, dict(cfg, PARAMETER_ACCEPTANCE_CHECK_TYPE=0), env={"FAKE_BIG": "2"})
+    assert "PARAMETERS NOT ACCEPTED" not in r0.stderr
+
+
+def test_unimplemented_check_type_is_refused(driver, tmp_path):
+    r, _, _ = run(driver, tmp_path, base_cfg(USE_PARAMETER_ACCEPTANCE_CHECK=1, PARAMETER_ACCEPTANCE_CHECK_TYPE=3))
+    assert r.returncode == 2 and "PARAMETER_ACCEPTANCE_CHECK_TYPE 3" in r.stderr
