@@ -33,9 +33,9 @@ struct SysConst {
 	// FP32 evaluation: 1 / interval width as hf + hf_lo, so that the rounding of
 	// 1/h (a bias shared by every pair) stays out of the local coordinate t
 	float hf, hf_lo;
-	// FP32 distances in (rcut_lo, rcut_hi) lie within rounding of r_max: the
-	// cutoff of such a pair is decided again in FP64 from its FP32 coordinates
-	float rcut_lo, rcut_hi;
+	// FP32 distances with |r - r_max| < rcut_band lie within rounding of r_max:
+	// the cutoff of such a pair is decided again in FP64 from its FP32 coordinates
+	float rcut_band;
 };
 
 // Values that change between stages or steps live in device memory so a

@@ -345,9 +345,10 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 					const int sp = j + 3 - qq;
 					R(oS + sp) += lv[qq][0] + lv[qq][1] * t + lv[qq][2] * t2 + lv[qq][3] * t3;
 					if (ADJ) {
-						const T b1 = hj * (lv[qq][1] + T(2) * lv[qq][2] * t + T(3) * lv[qq][3] * t2);
+						// B'' of both orderings; the (D-1)/r B' part of the Laplacian of O_k
+						// enters through the reverse sweep's (D-1)/r term
 						const T b2 = hj * hj * (T(2) * lv[qq][2] + T(6) * lv[qq][3] * t);
-						R(oL + sp) += T(2) * (b2 + dm1 * b1 * rinv);  // both orderings of the pair
+						R(oL + sp) += T(2) * b2;
 					}
 				}
 			}

@@ -284,20 +284,26 @@ __device__ __forceinline__ bool cut_fp64(const SysConst& sc, const Q4<float>& a,
 template <typename T>
 __device__ __forceinline__ bool within_rmax(const SysConst& sc, T r, const Q4<T>& a, const Q4<T>& b) {
 	if constexpr (sizeof(T) == 4) {
-		if (r > sc.rcut_lo && r < sc.rcut_hi) return cut_fp64(sc, a, b);
+		if (fabsf(r - (float)sc.rmax) < sc.rcut_band) return cut_fp64(sc, a, b);
 	}
 	return r <= (T)sc.rmax;
 }
-// the same for the pairs (a, b0) and (a, b1) of one f32x2 stream
-__device__ __forceinline__ void within_rmax2(const SysConst& sc, float r0, float r1, const Q4<float>& a,
-                                             const Q4<float>& b0, const Q4<float>& b1, bool& in0, bool& in1) {
+// The same for the pairs (a, b0) and (a, b1) of one f32x2 stream, rows a, b0,
+// b1 of xs (indices below n when `valid`).  The coordinates are read again
+// from shared memory on the rare FP64 branch, so the hot path keeps no extra
+// registers alive for it.
+__device__ __forceinline__ void within_rmax2(const SysConst& sc, float r0, float r1, const Q4<float>* xs, int a,
+                                             int b0, int b1, bool valid, bool& in0, bool& in1) {
 	const float rmax = (float)sc.rmax;
 	in0 = r0 <= rmax;
 	in1 = r1 <= rmax;
-	const bool n0 = r0 > sc.rcut_lo && r0 < sc.rcut_hi, n1 = r1 > sc.rcut_lo && r1 < sc.rcut_hi;
-	if (n0 || n1) {
-		if (n0) in0 = cut_fp64(sc, a, b0);
-		if (n1) in1 = cut_fp64(sc, a, b1);
+	float d0, d1;
+	f2_split(f2_sub(f2_make(r0, r1), f2_make(rmax, rmax)), d0, d1);
+	const bool n0 = fabsf(d0) < sc.rcut_band, n1 = fabsf(d1) < sc.rcut_band;
+	if (valid && (n0 || n1)) {
+		const Q4<float> xa = xs[a];
+		if (n0) in0 = cut_fp64(sc, xa, xs[b0]);
+		if (n1) in1 = cut_fp64(sc, xa, xs[b1]);
 	}
 }
 
@@ -461,7 +467,7 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 				f2_split(r, rA, rB);
 				const bool okA = haveA && rowok && ia != nrow, okB = haveB && rowok && ib != nrow;
 				bool wA, wB;
-				within_rmax2(sc, rA, rB, xr, pA, pB, wA, wB);
+				within_rmax2(sc, rA, rB, xs, nrow, ia, ib, rowok, wA, wB);
 				const bool inA = okA && wA, inB = okB && wB;
 				float tA, tB;
 				int jA, jB;
@@ -584,7 +590,7 @@ __device__ __forceinline__ void pair_pot2(int kind, float rA, float rB, float qa
 	vb += inB ? vB : 0.f;
 }
 template <bool DIAG, bool ADJ, int HIST>
-__device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n, int lane, bool rowok,
+__device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n, int lane, int nrow, bool rowok,
                                                const Q4<float>& xr, const Q4<float>* __restrict__ xs,
                                                const Q4<float>* __restrict__ coefC, const float* __restrict__ kb,
                                                const float* __restrict__ hv, const int* __restrict__ lut,
@@ -643,7 +649,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			float rA, rB;
 			f2_split(r, rA, rB);
 			bool wA, wB;
-			within_rmax2(sc, rA, rB, xr, pA, pB, wA, wB);
+			within_rmax2(sc, rA, rB, xs, nrow, DIAG && ia >= n ? 0 : ia, DIAG && ib >= n ? 0 : ib, rowok, wA, wB);
 			const bool inA = okA && wA, inB = okB && wB;
 			float tA, tB;
 			int jA, jB;
@@ -783,14 +789,15 @@ __device__ __forceinline__ void half_block_s(const SysConst& sc, int sp, int n, 
 }
 
 template <typename T, bool DIAG, bool ADJ, int HIST>
-__device__ __forceinline__ void half_block(const SysConst& sc, int sp, int n, int lane, bool rowok, const Q4<T>& xr,
+__device__ __forceinline__ void half_block(const SysConst& sc, int sp, int n, int lane, int nrow, bool rowok,
+                                           const Q4<T>& xr,
                                            const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
                                            const T* __restrict__ kb, const T* __restrict__ hv,
                                            const int* __restrict__ lut, T* __restrict__ hist, T pa, T pb,
                                            KSum<T>* own, T* trav, KSum<T>& elR, KSum<T>& elI, KSum<T>& vsum) {
 	if constexpr (std::is_same<T, float>::value)
-		half_block_f32<DIAG, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own, trav,
-		                                elR, elI, vsum);
+		half_block_f32<DIAG, ADJ, HIST>(sc, sp, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
+		                                trav, elR, elI, vsum);
 	else
 		half_block_s<T, DIAG, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own, trav,
 		                                 elR, elI, vsum);
@@ -903,7 +910,7 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			float rA, rB;
 			f2_split(r, rA, rB);
 			bool wA, wB;
-			within_rmax2(sc, rA, rB, xr, pA, pB, wA, wB);
+			within_rmax2(sc, rA, rB, xs, nrow, ia, ib, rowok, wA, wB);
 			const bool onA = haveA && rowok && wA && ((DIAG && !ROT) ? (ia < nrow) : true);
 			const bool onB = haveB && rowok && wB && ((DIAG && !ROT) ? (ib < nrow) : true);
 			float tA, tB;
@@ -1049,16 +1056,16 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 #pragma unroll
 					for (int c = 0; c < 5; c++) pacc[c] = gacc[c * n + pr];
 					T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-					half_block<T, false, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
-					                                own, trav, e_lR, e_lI, e_v);
+					half_block<T, false, ADJ, HIST>(sc, sp, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa,
+					                                pb, own, trav, e_lR, e_lI, e_v);
 					// the partners' shares are home
 					xs[pr].w -= trav[0];
 #pragma unroll
 					for (int c = 0; c < 5; c++) gacc[c * n + pr] = pacc[c] - trav[c + 1];
 				}
 				T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-				half_block<T, true, ADJ, HIST>(sc, s, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
-				                               trav, e_lR, e_lI, e_v);
+				half_block<T, true, ADJ, HIST>(sc, s, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
+				                               own, trav, e_lR, e_lI, e_v);
 #pragma unroll
 				for (int c = 0; c < 6; c++) own[c].add(-__shfl_sync(0xffffffffu, trav[c], (lane + 15) & 31));
 				if (rowok) {  // later slots add their shares

@@ -823,8 +823,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	s.hf_lo = (float)(s.hinv - (double)s.hf);
 	// the FP32 distance of an FP32 pair is within a few 1e-7 (relative) of its FP64
 	// distance; 4e-6 leaves a margin of about ten
-	s.rcut_lo = (float)(s.rmax * (1.0 - 4e-6));
-	s.rcut_hi = (float)(s.rmax * (1.0 + 4e-6));
+	s.rcut_band = (float)(s.rmax * 4e-6);
 	std::vector<int> lut;
 	if (!s.uniform) {
 		const double span = s.rmax - kb[0];
