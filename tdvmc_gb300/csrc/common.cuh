@@ -30,8 +30,10 @@ struct SysConst {
 	double hinv;      // uniform: 1 / interval width
 	double cell_inv;  // non-uniform: 1 / lookup cell width
 	double hbar2_2m;
-	// FP32 evaluation: 1 / interval width as hf + hf_lo, so that the rounding of
-	// 1/h (a bias shared by every pair) stays out of the local coordinate t
+	// 1 / interval width as hf + hf_lo (FP32): hf is what the FP32 kernels use; the
+	// stored-sample store forms t = r (hf + hf_lo) - j with one rounding (its piece
+	// table is the plain one), the evaluation kernels use pieces composed with the
+	// map from their t to the true one
 	float hf, hf_lo;
 	// FP32 distances with |r - r_max| < rcut_band lie within rounding of r_max:
 	// the cutoff of such a pair is decided again in FP64 from its FP32 coordinates
@@ -107,20 +109,11 @@ __device__ __forceinline__ double pair_r(double r2) { return r2 * rsqrt_(r2); }
 template <typename T>
 __device__ __forceinline__ int locate(const SysConst& s, T r, const T* kb, const T* hv, const int* lut, T& t) {
 	if (s.uniform) {
-		if constexpr (sizeof(T) == 4) {
-			// t = r / h - j with one rounding: r (hf + hf_lo) - j
-			const float x = r * s.hf;
-			float jf;
-			const int j = floor_clamp(x, s.nbin - 1, jf);
-			t = fmaf(r, s.hf_lo, fmaf(r, s.hf, -jf));
-			return j;
-		} else {
-			const T x = r * (T)s.hinv;
-			T jf;
-			const int j = floor_clamp(x, s.nbin - 1, jf);
-			t = x - jf;
-			return j;
-		}
+		const T x = r * (T)s.hinv;
+		T jf;
+		const int j = floor_clamp(x, s.nbin - 1, jf);
+		t = x - jf;
+		return j;
 	}
 	int c = (int)(r * (T)s.cell_inv);
 	c = c < s.ncell - 1 ? c : s.ncell - 1;
@@ -191,6 +184,40 @@ __device__ __forceinline__ MoveRand<T> move_rand(uint32_t move, uint32_t walker,
 		m.z2 = c2;
 	}
 	return m;
+}
+
+// Bounded waits on an mbarrier phase (tensor-core commits, TMA bulk copies).
+// The bound is wall time from the %globaltimer nanosecond clock, read every 64
+// polls, so it does not depend on how long one try_wait suspends.  A kernel
+// waits for a completion first with its status limit; if that runs out it
+// records the failure and waits again, with the drain limit, for the same
+// completion, so no copy or MMA is left in flight when the block moves on or
+// exits.  A status limit of 0 gives up without polling (test of the failure
+// path).
+constexpr uint64_t kWaitStatusNs = 2000000000ull;  // 2 s
+constexpr uint64_t kWaitDrainNs = 4000000000ull;   // 4 s
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+	uint32_t done;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+	    "selp.u32 %0, 1, 0, p;\n\t}\n"
+	    : "=r"(done)
+	    : "r"(mbar), "r"(parity)
+	    : "memory");
+	return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_ns(uint32_t mbar, uint32_t parity, uint64_t limit_ns) {
+	if (limit_ns == 0) return false;
+	const uint64_t t0 = globaltimer_ns();
+	for (unsigned it = 1;; it++) {
+		if (mbar_try_wait(mbar, parity)) return true;
+		if ((it & 63u) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
+	}
 }
 
 // Kahan-compensated running sum.

@@ -83,7 +83,15 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
 	g.in = ok && cut;
 	g.out = ok && !cut;
 	T t;
-	g.j = locate<T>(sc, g.r, kb, hv, lut, t);
+	if (sizeof(T) == 4 && sc.uniform) {  // (dead code for T = double)
+		// t = r / h - j with one rounding, r (hf + hf_lo) - j: the store's piece table
+		// is the plain one (its rows are equal, so one row serves every interval)
+		float jf;
+		g.j = floor_clamp((float)g.r * sc.hf, sc.nbin - 1, jf);
+		t = (T)fmaf((float)g.r, sc.hf_lo, fmaf((float)g.r, sc.hf, -jf));
+	} else {
+		g.j = locate<T>(sc, g.r, kb, hv, lut, t);
+	}
 	g.t = g.in ? t : T(0);  // t is NaN for the self pair
 	g.sr = g.in ? g.rinv : T(0);
 	return g;
@@ -528,23 +536,10 @@ __host__ __device__ inline size_t cs_eval_st_smem_bytes(int ns, int warps) {
 }
 
 // Each chunk is one TMA bulk copy (cp.async.bulk) issued by lane 0 and
-// completed on the warp's mbarrier.  Every wait is bounded: on time-out the
-// walker's E_loc is written as NaN (the statistics then report a non-finite
-// value), the warp waits once more, bounded, for its own copy and returns.
-constexpr unsigned kCsWaitLimit = 1u << 24;
-__device__ __forceinline__ bool cs_mbar_wait(uint32_t mbar, uint32_t parity) {
-	for (unsigned it = 0; it < kCsWaitLimit; it++) {
-		uint32_t done;
-		asm volatile(
-		    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-		    "selp.u32 %0, 1, 0, p;\n\t}\n"
-		    : "=r"(done)
-		    : "r"(mbar), "r"(parity)
-		    : "memory");
-		if (done) return true;
-	}
-	return false;
-}
+// completed on the warp's mbarrier.  Every wait is bounded in time
+// (mbar_wait_ns): when the status limit runs out the walker's E_loc is written
+// as NaN (the statistics then report a non-finite value), the warp waits for
+// its own copy with the drain limit and returns.
 // lane 0: order this warp's earlier generic accesses of dst before the async
 // write, arm the barrier with the byte count and start the copy
 __device__ __forceinline__ void cs_bulk_copy(uint32_t mbar, float* dst, const float* src, uint32_t bytes) {
@@ -562,7 +557,7 @@ __global__ void __launch_bounds__(32 * kCsStWarps, 4) k_cs_eval_st(
     SysConst sc, const double* __restrict__ params, const double* __restrict__ fold_g, const float* __restrict__ D,
     const float* __restrict__ D2, const float* __restrict__ Os, const float* __restrict__ Vs,
     const int32_t* __restrict__ nouts, int64_t nw, float* __restrict__ lnpsi_o, float* __restrict__ O_o,
-    float* __restrict__ eloc_o, float* __restrict__ other_o, float* __restrict__ dE_o) {
+    float* __restrict__ eloc_o, float* __restrict__ other_o, float* __restrict__ dE_o, uint64_t wait_ns) {
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int n = sc.n, ns = sc.ns, P = sc.p;
 	const int npad = cs_npad(n), nrow = 3 * ns, nch = npad / 32;
@@ -603,14 +598,14 @@ __global__ void __launch_bounds__(32 * kCsStWarps, 4) k_cs_eval_st(
 		for (int s = 0; s < kCsStNs; s++) pr[s] = pi[s] = 0.f;
 		for (int c = 0; c < nch; c++) {
 			if (lane == 0) cs_bulk_copy(mbar, chunk, Dw + (size_t)c * nrow * 32, cbytes);
-			const bool ok = cs_mbar_wait(mbar, phase);
+			const bool ok = mbar_wait_ns(mbar, phase, wait_ns);
 			phase ^= 1u;
 			if (!__all_sync(0xffffffffu, ok)) {
 				if (lane == 0) {
 					eloc_o[2 * w] = __int_as_float(0x7fc00000);
 					eloc_o[2 * w + 1] = __int_as_float(0x7fc00000);
 				}
-				cs_mbar_wait(mbar, phase ^ 1u);  // bounded: the copy still in flight
+				mbar_wait_ns(mbar, phase ^ 1u, kWaitDrainNs);  // the copy still in flight
 				return;
 			}
 			__syncwarp();

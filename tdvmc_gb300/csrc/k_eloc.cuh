@@ -430,10 +430,10 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
                                               const float* __restrict__ hv, const int* __restrict__ lut,
                                               float* __restrict__ hist, int lane, float pa, float pb,
                                               KSum<float>* acc, KSum<float>& vsum, int& nout) {
-	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const float L = (float)sc.L, Lr = (float)sc.Lr;
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
-	const f2_t H2 = f2_make(sc.hf, sc.hf), HL2 = f2_make(sc.hf_lo, sc.hf_lo), mh2 = f2_make(-0.5f, -0.5f);
+	const f2_t H2 = f2_make(sc.hf, sc.hf), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
 	const float ymax = kRoundF + (float)(sc.nbin - 1);
@@ -479,8 +479,7 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 					ya = fminf(ya, ymax);
 					yb = fminf(yb, ymax);
 					float xa, xb;
-					// t = r / h - j with one rounding: r (hf + hf_lo) - j
-					f2_split(f2_fma(r, HL2, f2_fma(r, H2, f2_sub(R2, f2_make(ya, yb)))), xa, xb);
+					f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
 					tA = xa;
 					tB = xb;
 					jA = __float_as_int(ya) - __float_as_int(kRoundF);
@@ -595,11 +594,13 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
                                                const Q4<float>* __restrict__ coefC, const float* __restrict__ kb,
                                                const float* __restrict__ hv, const int* __restrict__ lut,
                                                float* __restrict__ hist, float pa, float pb, KSum<float>* own,
-                                               float* trav, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum) {
+                                               float* trav, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum,
+                                               float& nearmin) {
 	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const f2_t RM2 = f2_make(rmax, rmax);
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
-	const f2_t H2 = f2_make(sc.hf, sc.hf), HL2 = f2_make(sc.hf_lo, sc.hf_lo), mh2 = f2_make(-0.5f, -0.5f);
+	const f2_t H2 = f2_make(sc.hf, sc.hf), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
 	const float ymax = kRoundF + (float)(sc.nbin - 1);
@@ -648,9 +649,13 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			const f2_t r = f2_mul(r2, f2_make(qa, qb));
 			float rA, rB;
 			f2_split(r, rA, rB);
-			bool wA, wB;
-			within_rmax2(sc, rA, rB, xs, nrow, DIAG && ia >= n ? 0 : ia, DIAG && ib >= n ? 0 : ib, rowok, wA, wB);
-			const bool inA = okA && wA, inB = okB && wB;
+			const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
+			{
+				// distance to r_max: pairs within rounding of it are decided again after the block
+				float da, db;
+				f2_split(f2_sub(r, RM2), da, db);
+				nearmin = fminf(nearmin, fminf(fabsf(da), fabsf(db)));
+			}
 			float tA, tB;
 			int jA, jB;
 			if (sc.uniform) {
@@ -660,7 +665,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 				ya = fminf(ya, ymax);
 				yb = fminf(yb, ymax);
 				float xa, xb;
-				f2_split(f2_fma(r, HL2, f2_fma(r, H2, f2_sub(R2, f2_make(ya, yb)))), xa, xb);
+				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
 				tA = xa;
 				tB = xb;
 				jA = __float_as_int(ya) - __float_as_int(kRoundF);
@@ -790,17 +795,135 @@ __device__ __forceinline__ void half_block_s(const SysConst& sc, int sp, int n, 
 
 template <typename T, bool DIAG, bool ADJ, int HIST>
 __device__ __forceinline__ void half_block(const SysConst& sc, int sp, int n, int lane, int nrow, bool rowok,
-                                           const Q4<T>& xr,
+                                           float& nearmin, const Q4<T>& xr,
                                            const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
                                            const T* __restrict__ kb, const T* __restrict__ hv,
                                            const int* __restrict__ lut, T* __restrict__ hist, T pa, T pb,
                                            KSum<T>* own, T* trav, KSum<T>& elR, KSum<T>& elI, KSum<T>& vsum) {
 	if constexpr (std::is_same<T, float>::value)
 		half_block_f32<DIAG, ADJ, HIST>(sc, sp, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
-		                                trav, elR, elI, vsum);
+		                                trav, elR, elI, vsum, nearmin);
 	else
 		half_block_s<T, DIAG, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own, trav,
 		                                 elR, elI, vsum);
+}
+
+// The FP32 distance of a pair exactly as the f32x2 sweeps form it (each half of
+// an f32x2 operation rounds like the scalar one), so that a second look at a
+// pair sees the decision the sweep took.
+__device__ __forceinline__ float sweep_r(const SysConst& sc, const Q4<float>& a, const Q4<float>& b, float& q,
+                                         float& dx, float& dy, float& dz) {
+	const float L = (float)sc.L, Lr = (float)sc.Lr;
+	dx = nic(__fsub_rn(a.x, b.x), L, Lr);
+	dy = nic(__fsub_rn(a.y, b.y), L, Lr);
+	dz = nic(__fsub_rn(a.z, b.z), L, Lr);
+	const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+	q = rsqrt_(r2);
+	return __fmul_rn(r2, q);
+}
+// interval and local coordinate as the f32x2 sweeps form them (equal widths)
+__device__ __forceinline__ int sweep_t(const SysConst& sc, float r, const float* kb, const float* hv, const int* lut,
+                                       float& t) {
+	if (!sc.uniform) return locate<float>(sc, r, kb, hv, lut, t);
+	const float x = __fmul_rn(r, sc.hf);
+	const float y = fminf(__fadd_rn(__fadd_rn(x, -0.5f), kRoundF), kRoundF + (float)(sc.nbin - 1));
+	t = __fsub_rn(x, __fsub_rn(y, kRoundF));
+	return __float_as_int(y) - __float_as_int(kRoundF);
+}
+
+// Cutoff fix-up of one block of the FP32 half sweep (half_block_f32): the sweep
+// decides r <= r_max from the FP32 distance and records how close any pair
+// came to r_max; when a lane's block had a pair within rounding of it, the
+// group looks at the block's pairs again, decides those near r_max in FP64 from
+// the FP32 coordinates (as the FP64 path does) and, where that decision
+// differs, adds or removes the pair's terms.  Rare (a few pairs per walker at
+// N = 1000), and outside the sweep's inner loop.  Phase 1: the row's
+// gradient (own), the Laplacian, potential and moment terms; phase 2 (after
+// the rows' gradients are stored): the partner's gradient, atomically, since
+// several lanes may correct one partner.  ROWS: rows of the partners' gradients
+// (gRx in xs[].w, gRy..gIz in gacc[(c-1) n + i]).
+template <bool DIAG, int HIST>
+__device__ __forceinline__ void half_block_fix(const SysConst& sc, int sp, int n, int lane, int nrow, bool rowok,
+                                            Q4<float>* xs, float* gacc, const Q4<float>* coefC, const float* kb,
+                                            const float* hv, const int* lut, float* hist, float pa, float pb,
+                                            KSum<float>* own, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum,
+                                            int phase) {
+	if (!rowok) return;
+	const float rmax = (float)sc.rmax;
+	const float dm1 = (float)(sc.dim - 1);
+	const Q4<float> xr = xs[nrow];
+	constexpr int k0 = DIAG ? 1 : 0, k1 = DIAG ? 17 : 32;
+	for (int k = k0; k < k1; k++) {
+		const int i = sp * 32 + ((lane + k) & 31);
+		if (DIAG && !(i < n && (k < 16 || (k == 16 && lane < 16)))) continue;
+		const Q4<float> xi = xs[i];
+		float q, dx, dy, dz;
+		const float r = sweep_r(sc, xr, xi, q, dx, dy, dz);
+		if (!(fabsf(__fsub_rn(r, rmax)) < sc.rcut_band)) continue;
+		const bool in32 = r <= rmax;
+		if (cut_fp64(sc, xr, xi) == in32) continue;
+		const float sgn = in32 ? -1.f : 1.f;
+		float t;
+		const int j = sweep_t(sc, r, kb, hv, lut, t);
+		const Q4<float> cR = coefC[3 * j], cI = coefC[3 * j + 1], c2 = coefC[3 * j + 2];
+		const float gR = fmaf(t, fmaf(t, cR.z, cR.y), cR.x) * q;
+		const float gI = fmaf(t, fmaf(t, cI.z, cI.y), cI.x) * q;
+		const float g6[6] = {gR * dx, gR * dy, gR * dz, gI * dx, gI * dy, gI * dz};
+		if (phase == 1) {
+			const float lR = fmaf(dm1, gR, fmaf(t, c2.x, cR.w));
+			const float lI = fmaf(dm1, gI, fmaf(t, c2.y, cI.w));
+#pragma unroll
+			for (int c = 0; c < 6; c++) own[c].add(sgn * g6[c]);
+			elR.add(sgn * 2.f * lR);
+			elI.add(sgn * 2.f * lI);
+			vsum.add(sgn * pair_pot<float>(sc.pot_kind, r, q, pa, pb));
+			const float t2 = t * t;
+			const float v[8] = {sgn, sgn * t, sgn * t2, sgn * t2 * t, 0.f, 0.f, 0.f, 0.f};
+			hist_add8<HIST, HistSlots<HIST, false>::value, float, 32>(hist, j, lane, v, kFwdMoments);
+		} else {
+			atomicAdd(&xs[i].w, -sgn * g6[0]);
+#pragma unroll
+			for (int c = 1; c < 6; c++) atomicAdd(&gacc[(size_t)(c - 1) * n + i], -sgn * g6[c]);
+		}
+	}
+}
+
+// Cutoff fix-up of one region of the FP32 reverse sweep (rev_region_f2): the
+// pairs near r_max whose FP64 decision differs from the sweep's have their
+// moment terms added or removed (lane-private histogram records).
+template <int G, bool DIAG, int HIST, bool ROT>
+__device__ __forceinline__ void rev_region_fix(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const float* gn,
+                                            const Q4<float>* xs, const Q4<float>* g4, const float* gz,
+                                            const float* kb, const float* hv, const int* lut, float* hist, int lane) {
+	if (!rowok) return;
+	const float rmax = (float)sc.rmax;
+	const float dm1 = (float)(sc.dim - 1);
+	const Q4<float> xr = xs[nrow];
+	const int kend = ROT ? 17 : i1;
+	for (int k = ROT ? 1 : i0; k < kend; k++) {
+		int i = k;
+		if (ROT) {
+			i = i0 + ((lane + k) & 31);
+			if (!(i < i1 && (k < 16 || lane < 16))) continue;
+		} else if (DIAG && !(i < nrow)) {
+			continue;
+		}
+		const Q4<float> xi = xs[i];
+		float q, dx, dy, dz;
+		const float r = sweep_r(sc, xr, xi, q, dx, dy, dz);
+		if (!(fabsf(__fsub_rn(r, rmax)) < sc.rcut_band)) continue;
+		const bool in32 = r <= rmax;
+		if (cut_fp64(sc, xr, xi) == in32) continue;
+		const float sgn = in32 ? -1.f : 1.f;
+		float t;
+		const int j = sweep_t(sc, r, kb, hv, lut, t);
+		const Q4<float> gi = g4[i];
+		const float gR = ((gn[0] - xi.w) * dx + (gn[1] - gi.x) * dy + (gn[2] - gi.y) * dz + dm1) * q;
+		const float gI = ((gn[3] - gi.z) * dx + (gn[4] - gi.w) * dy + (gn[5] - gz[i]) * dz) * q;
+		const float t2 = t * t;
+		const float v[8] = {sgn * gR, sgn * gR * t, sgn * gR * t2, sgn * gI, sgn * gI * t, sgn * gI * t2, 0.f, 0.f};
+		hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, j, lane, v, kRevMoments);
+	}
 }
 
 // Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), kNp
@@ -860,11 +983,13 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
                                               const Q4<float>& xr, const float* gn, const Q4<float>* __restrict__ xs,
                                               const Q4<float>* __restrict__ g4, const float* __restrict__ gz,
                                               const float* __restrict__ kb, const float* __restrict__ hv,
-                                              const int* __restrict__ lut, float* __restrict__ hist, int lane) {
+                                              const int* __restrict__ lut, float* __restrict__ hist, int lane,
+                                              float& nearmin) {
 	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const f2_t RM2 = f2_make(rmax, rmax);
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
-	const f2_t H2 = f2_make(sc.hf, sc.hf), HL2 = f2_make(sc.hf_lo, sc.hf_lo), mh2 = f2_make(-0.5f, -0.5f);
+	const f2_t H2 = f2_make(sc.hf, sc.hf), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
 	const float ymax = kRoundF + (float)(sc.nbin - 1);
@@ -909,10 +1034,14 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			const f2_t r = f2_mul(r2, f2_make(qa, qb));
 			float rA, rB;
 			f2_split(r, rA, rB);
-			bool wA, wB;
-			within_rmax2(sc, rA, rB, xs, nrow, ia, ib, rowok, wA, wB);
-			const bool onA = haveA && rowok && wA && ((DIAG && !ROT) ? (ia < nrow) : true);
-			const bool onB = haveB && rowok && wB && ((DIAG && !ROT) ? (ib < nrow) : true);
+			const bool onA = haveA && rowok && (rA <= rmax) && ((DIAG && !ROT) ? (ia < nrow) : true);
+			const bool onB = haveB && rowok && (rB <= rmax) && ((DIAG && !ROT) ? (ib < nrow) : true);
+			{
+				// distance to r_max: pairs within rounding of it are decided again after the region
+				float da, db;
+				f2_split(f2_sub(r, RM2), da, db);
+				nearmin = fminf(nearmin, fminf(fabsf(da), fabsf(db)));
+			}
 			float tA, tB;
 			int jA, jB;
 			if (sc.uniform) {
@@ -922,7 +1051,7 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 				ya = fminf(ya, ymax);
 				yb = fminf(yb, ymax);
 				float xa, xb;
-				f2_split(f2_fma(r, HL2, f2_fma(r, H2, f2_sub(R2, f2_make(ya, yb)))), xa, xb);
+				f2_split(f2_sub(x, f2_sub(f2_make(ya, yb), R2)), xa, xb);
 				tA = xa;
 				tB = xb;
 				jA = __float_as_int(ya) - __float_as_int(kRoundF);
@@ -1056,22 +1185,49 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 #pragma unroll
 					for (int c = 0; c < 5; c++) pacc[c] = gacc[c * n + pr];
 					T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-					half_block<T, false, ADJ, HIST>(sc, sp, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa,
-					                                pb, own, trav, e_lR, e_lI, e_v);
+					float nearmin = 3.0e38f;
+					half_block<T, false, ADJ, HIST>(sc, sp, n, lane, nrow, rowok, nearmin, xr, xs, coefC, kb, hv, lut,
+					                                hist, pa, pb, own, trav, e_lR, e_lI, e_v);
 					// the partners' shares are home
 					xs[pr].w -= trav[0];
 #pragma unroll
 					for (int c = 0; c < 5; c++) gacc[c * n + pr] = pacc[c] - trav[c + 1];
+					if constexpr (std::is_same<T, float>::value) {
+						if (__any_sync(0xffffffffu, nearmin < sc.rcut_band)) {
+							__syncwarp();
+							half_block_fix<false, HIST>(sc, sp, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist,
+							                            pa, pb, own, e_lR, e_lI, e_v, 1);
+							half_block_fix<false, HIST>(sc, sp, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist,
+							                            pa, pb, own, e_lR, e_lI, e_v, 2);
+							__syncwarp();
+						}
+					}
 				}
 				T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-				half_block<T, true, ADJ, HIST>(sc, s, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb,
-				                               own, trav, e_lR, e_lI, e_v);
+				float nearmin = 3.0e38f;
+				half_block<T, true, ADJ, HIST>(sc, s, n, lane, nrow, rowok, nearmin, xr, xs, coefC, kb, hv, lut, hist,
+				                               pa, pb, own, trav, e_lR, e_lI, e_v);
 #pragma unroll
 				for (int c = 0; c < 6; c++) own[c].add(-__shfl_sync(0xffffffffu, trav[c], (lane + 15) & 31));
+				bool fix = false;
+				if constexpr (std::is_same<T, float>::value) {
+					fix = __any_sync(0xffffffffu, nearmin < sc.rcut_band);
+					if (fix)
+						half_block_fix<true, HIST>(sc, s, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist, pa,
+						                           pb, own, e_lR, e_lI, e_v, 1);
+				}
 				if (rowok) {  // later slots add their shares
 					xs[nrow].w = own[0].value();
 #pragma unroll
 					for (int c = 1; c < 6; c++) gacc[(c - 1) * n + nrow] = own[c].value();
+				}
+				if constexpr (std::is_same<T, float>::value) {
+					if (fix) {
+						__syncwarp();
+						half_block_fix<true, HIST>(sc, s, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist, pa,
+						                           pb, own, e_lR, e_lI, e_v, 2);
+						__syncwarp();
+					}
 				}
 			}
 			for (int r = lane; r < n; r += 32) {
@@ -1272,8 +1428,18 @@ __global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __res
 			const int base = s * G;
 			const int dend = (base + G < n) ? base + G : n;
 			if constexpr (std::is_same<T, float>::value) {
-				rev_region_f2<G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-				rev_region_f2<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				float nm0 = 3.0e38f, nm1 = 3.0e38f;
+				rev_region_f2<G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane,
+				                              nm0);
+				rev_region_f2<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist,
+				                                      lane, nm1);
+				// pairs within rounding of r_max, decided again in FP64 (rev_region_fix)
+				if (__any_sync(gmask, nm0 < sc.rcut_band))
+					rev_region_fix<G, false, HIST, false>(sc, 0, base, nrow, rowok, gn, xs, g4, gz, kb, hv, lut, hist,
+					                                      lane);
+				if (__any_sync(gmask, nm1 < sc.rcut_band))
+					rev_region_fix<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, gn, xs, g4, gz, kb, hv, lut,
+					                                       hist, lane);
 			} else {
 				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
 				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);

@@ -17,8 +17,12 @@
 // tcgen05.ld and written as the CTA's FP32 partial; a second kernel adds the
 // partials in FP64 in fixed order and symmetrises.
 //
-// Every mbarrier wait is bounded; on time-out the CTA writes NaN partials
-// (the solve then reports TDVMC_ERR_NONFINITE) instead of hanging.
+// Every mbarrier wait is bounded in time (mbar_wait_ns): a commit not seen
+// within the status limit marks the CTA failed and is then waited for with the
+// drain limit, so no MMA still reads a buffer that is restaged or writes the
+// accumulator that is read and freed; a failed CTA writes NaN partials (the
+// solve then reports TDVMC_ERR_NONFINITE) instead of hanging.
+#include "common.cuh"
 #include "k_gram_tf32.cuh"
 
 namespace tdvmc {
@@ -31,7 +35,6 @@ constexpr int kLBO = 128;                     // bytes between core matrices alo
 constexpr int kSBO = (kTileK / 4) * 128;      // bytes between 8-row groups
 constexpr int kTileBytes = (kM / 8) * kSBO;   // 16 KB per operand tile
 constexpr int kThreads = 128;
-constexpr unsigned kWaitLimit = 1u << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 	return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -71,18 +74,12 @@ __device__ __forceinline__ void commit(uint64_t* mbar) {
 	             : "memory");
 }
 
-__device__ __forceinline__ bool wait_parity(uint64_t* mbar, uint32_t parity) {
+// the commit of phase `parity`: status limit, then the drain limit on time-out;
+// false when the status limit ran out
+__device__ __forceinline__ bool wait_parity(uint64_t* mbar, uint32_t parity, uint64_t status_ns) {
 	const uint32_t a = smem_u32(mbar);
-	for (unsigned it = 0; it < kWaitLimit; it++) {
-		uint32_t done;
-		asm volatile(
-		    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-		    "selp.u32 %0, 1, 0, p;\n\t}\n"
-		    : "=r"(done)
-		    : "r"(a), "r"(parity)
-		    : "memory");
-		if (done) return true;
-	}
+	if (mbar_wait_ns(a, parity, status_ns)) return true;
+	mbar_wait_ns(a, parity, kWaitDrainNs);
 	return false;
 }
 
@@ -92,7 +89,8 @@ __device__ __forceinline__ uint32_t tile_off(int m, int kk) {
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_gram_tf32(int p, int npad, int64_t nw, const float* __restrict__ O,
-                                                           const double* __restrict__ means, float* __restrict__ partial) {
+                                                           const double* __restrict__ means, float* __restrict__ partial,
+                                                           uint64_t wait_ns) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
 	// 1024-byte aligned operand buffers: [buf][hi, lo]
 	unsigned char* base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
@@ -124,7 +122,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_gram_tf32(int p, int npad, int6
 	int it = 0;
 	for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
 		const int b = it & 1;
-		if (it >= 2 && !wait_parity(&mbar[b], (uint32_t)(((it - 2) >> 1) & 1))) failed = 1;
+		if (it >= 2 && !wait_parity(&mbar[b], (uint32_t)(((it - 2) >> 1) & 1), wait_ns)) failed = 1;
 		unsigned char* hi = base + b * 2 * kTileBytes;
 		unsigned char* lo = hi + kTileBytes;
 		// stage: thread tid owns parameter row m = tid, 32 walkers of the tile
@@ -162,8 +160,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_gram_tf32(int p, int npad, int6
 		}
 	}
 	// drain: the last commit of each buffer
-	if (it >= 1 && !wait_parity(&mbar[(it - 1) & 1], (uint32_t)(((it - 1) >> 1) & 1))) failed = 1;
-	if (it >= 2 && !wait_parity(&mbar[(it - 2) & 1], (uint32_t)(((it - 2) >> 1) & 1))) failed = 1;
+	if (it >= 1 && !wait_parity(&mbar[(it - 1) & 1], (uint32_t)(((it - 1) >> 1) & 1), wait_ns)) failed = 1;
+	if (it >= 2 && !wait_parity(&mbar[(it - 2) & 1], (uint32_t)(((it - 2) >> 1) & 1), wait_ns)) failed = 1;
 	asm volatile("tcgen05.fence::after_thread_sync;");
 	__syncthreads();
 
@@ -224,12 +222,12 @@ int gram_blocks(int64_t nw, int nsm) {
 size_t gram_smem_bytes() { return (size_t)4 * kTileBytes + 1024; }
 
 int launch_gram_tf32(cudaStream_t st, int p, int64_t nw, const float* O, const double* means, int nblk, float* partial,
-                     double* S, int) {
+                     double* S, int, uint64_t wait_ns) {
 	if (!gram_supported(p) || nblk < 1) return 1;
 	const int npad = (p + 15) / 16 * 16;
 	const size_t smem = gram_smem_bytes();
 	if (cudaFuncSetAttribute(k_gram_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
-	k_gram_tf32<<<nblk, kThreads, smem, st>>>(p, npad, nw, O, means, partial);
+	k_gram_tf32<<<nblk, kThreads, smem, st>>>(p, npad, nw, O, means, partial, wait_ns);
 	k_gram_finalize<<<(p * p + kGramFinThreads / 32 - 1) / (kGramFinThreads / 32), kGramFinThreads, 0, st>>>(
 	    p, nblk, partial, 1.0 / (double)nw, S);
 	return cudaGetLastError() == cudaSuccess ? 0 : 1;

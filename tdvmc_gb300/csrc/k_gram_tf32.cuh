@@ -12,8 +12,9 @@ namespace tdvmc {
 bool gram_supported(int p);
 // number of CTAs (walker chunks) the contraction uses for nw walkers
 int gram_blocks(int64_t nw, int nsm);
-// partial[nblk][p*p] (FP32) then S[p*p] = sum / nw (FP64); returns 0 on success
+// partial[nblk][p*p] (FP32) then S[p*p] = sum / nw (FP64); returns 0 on success.
+// wait_ns: status limit of the waits for the tensor-core commits (kWaitStatusNs)
 int launch_gram_tf32(cudaStream_t st, int p, int64_t nw, const float* O, const double* means, int nblk, float* partial,
-                     double* S, int nsm);
+                     double* S, int nsm, uint64_t wait_ns);
 
 }  // namespace tdvmc

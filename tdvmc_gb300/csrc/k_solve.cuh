@@ -348,7 +348,8 @@ __global__ void __launch_bounds__(128) k_prep(int p, int ns, int nbin, int ncoef
 		// evaluation table: du/dr = a0 + t (a1 + t a2), d2u/dr2 = b0 + t b1 with
 		// the interval's 1/h folded in; per interval three 4-vectors
 		// {a0R a1R a2R b0R} {a0I a1I a2I b0I} {b1R b1I 0 0}
-		const double hj = uniform ? hinv : (double)hv[j];
+		// 1/h as the kernels of type T see it (with the pieces in their coordinate)
+		const double hj = uniform ? (double)(T)hinv : (double)hv[j];
 		T* e = coefC + (size_t)j * 12;
 		e[0] = (T)(cr[1] * hj);
 		e[1] = (T)(2.0 * cr[2] * hj);

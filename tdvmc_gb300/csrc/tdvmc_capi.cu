@@ -66,6 +66,7 @@ struct tdvmc_ctx {
 	int nsm = 0;
 	cudaStream_t st = nullptr;
 	std::vector<double> knots, loc, fold, pot;
+	std::vector<double> locc;  // the pieces in the FP32 kernels' local coordinate (loc for FP64)
 	int npot = 0;
 	double time = 0.0;
 	Tiles tiles;
@@ -112,6 +113,10 @@ struct tdvmc_ctx {
 	int64_t cs_steps = 0;       // stored-sample steps since the last full store
 	int64_t cs_last_count = 0;  // walkers sampled by the last refresh
 	std::string err;
+	// status limit of the bounded hardware waits (k_gram_tf32, k_cs_eval_st);
+	// TDVMC_TEST_WAIT_NS at creation overrides it (0: give up at once, to test
+	// the failure path)
+	uint64_t wait_ns = kWaitStatusNs;
 	// eager profiling: events recorded after every kernel when set
 	std::vector<cudaEvent_t>* prof = nullptr;
 	std::vector<const char*>* prof_names = nullptr;
@@ -372,7 +377,7 @@ int launch_reduce(tdvmc_ctx* ctx, bool adj) {
 	CK(cudaGetLastError());
 	if (tc) {
 		int rc = launch_gram_tf32(ctx->st, P, ctx->nw, (const float*)ctx->O, ctx->means1, ctx->nblkS, ctx->partS,
-		                          ctx->Sg, ctx->nsm);
+		                          ctx->Sg, ctx->nsm, ctx->wait_ns);
 		ctx->launches += 2;
 		mark(ctx, "k_gram_tf32+finalize");
 		if (rc) {
@@ -474,7 +479,7 @@ int launch_cs_eval(tdvmc_ctx* ctx, bool adj) {
 			fn<<<grid, 32 * wst, smem, ctx->st>>>(s, ctx->stage, ctx->fold_d, (const float*)ctx->csD,
 			                                     (const float*)ctx->csD2, (const float*)ctx->csO, (const float*)ctx->csV,
 			                                     ctx->csN, ctx->nw, (float*)ctx->lnpsi, (float*)ctx->O, (float*)ctx->eloc,
-			                                     (float*)ctx->other7, (float*)ctx->dE);
+			                                     (float*)ctx->other7, (float*)ctx->dE, ctx->wait_ns);
 			ctx->launches++;
 			mark(ctx, adj ? "k_cs_eval_st_adjoint" : "k_cs_eval_st");
 			CK(cudaGetLastError());
@@ -925,6 +930,36 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		tdvmc_destroy(ctx);
 		return TDVMC_ERR_NOMEM;
 	}
+	// Local pieces as the FP32 kernels evaluate them.  Their local coordinate is
+	// t_f = r hf - j (equal widths, hf = 1/h rounded to FP32) or (r - kb_f) hv_f with
+	// the FP32-rounded interval tables; the true coordinate is the affine
+	// t = a_j t_f + b_j, a_j = hv / hv_f, b_j = j (a_j - 1) or (kb_f - kb) hv.  The
+	// pieces composed with that map (coefficients in t_f) keep the rounding of 1/h
+	// and of the knots, a bias shared by every pair of an interval, out of the
+	// spline values without an extra operation per pair; the derivatives in r are
+	// hv_f d/dt_f.  FP64 contexts use the pieces as they are.
+	c.locc = c.loc;
+	if (c.prec == TDVMC_PREC_MIXED)
+		for (int j = 0; j < s.nbin; j++) {
+			double a, b;
+			if (s.uniform) {
+				a = s.hinv / (double)s.hf;
+				b = (a - 1.0) * j;
+			} else {
+				a = hv[j] / (double)(float)hv[j];
+				b = ((double)(float)kb[j] - kb[j]) * hv[j];
+			}
+			const double binom[4][4] = {{1, 0, 0, 0}, {1, 1, 0, 0}, {1, 2, 1, 0}, {1, 3, 3, 1}};
+			for (int q = 0; q < 4; q++) {
+				const double* l = &c.loc[((size_t)j * 4 + q) * 4];
+				double* o = &c.locc[((size_t)j * 4 + q) * 4];
+				for (int k = 0; k < 4; k++) {
+					double v = 0.0;
+					for (int cc = k; cc < 4; cc++) v += l[cc] * binom[cc][k] * std::pow(a, k) * std::pow(b, cc - k);
+					o[k] = v;
+				}
+			}
+		}
 	// static tables
 	std::vector<char> kbT(s.nbin * ts), hvT(s.nbin * ts), locT(c.loc.size() * ts);
 	for (int j = 0; j < s.nbin; j++) {
@@ -938,7 +973,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	}
 	for (size_t i = 0; i < c.loc.size(); i++) {
 		if (c.prec == TDVMC_PREC_FP64) ((double*)locT.data())[i] = c.loc[i];
-		else ((float*)locT.data())[i] = (float)c.loc[i];
+		else ((float*)locT.data())[i] = (float)c.locc[i];
 	}
 	// stored-sample piece table: dB/dr, B and d2B/dr2 of the four pieces per interval
 	std::vector<double> piece((size_t)s.nbin * kCsPiece, 0.0);
@@ -983,7 +1018,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	          cudaMemcpy(c.hv, hvT.data(), hvT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.locT, locT.data(), locT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.cs_piece, pieceT.data(), pieceT.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-	          cudaMemcpy(c.loc_d, c.loc.data(), c.loc.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+	          cudaMemcpy(c.loc_d, c.locc.data(), c.locc.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.fold_d, c.fold.data(), c.fold.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.dyn, &dy, sizeof(dy), cudaMemcpyHostToDevice) == cudaSuccess &&
 	          cudaMemcpy(c.chunk_starts, starts.data(), starts.size() * sizeof(int32_t), cudaMemcpyHostToDevice) ==
@@ -1018,6 +1053,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	if (const char* e = std::getenv("TDVMC_EVAL_WALKERS_PER_BLOCK"))
 		c.tiles.egpb = std::max(1, std::min(128 / c.tiles.eg, std::atoi(e)));
 	if (const char* h = std::getenv("TDVMC_HIST")) c.tiles.hist = std::max(0, std::min(2, std::atoi(h)));
+	if (const char* wt = std::getenv("TDVMC_TEST_WAIT_NS")) c.wait_ns = (uint64_t)std::strtoull(wt, nullptr, 10);
 	// TDVMC_SAMPLER=scalar selects the scalar FP32 sampler
 	if (const char* sm = std::getenv("TDVMC_SAMPLER")) c.packed_sampler = std::strcmp(sm, "scalar") != 0;
 	*out = ctx;
@@ -1488,72 +1524,108 @@ int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, float* ms, con
 int tdvmc_autotune(tdvmc_ctx* ctx, int32_t moves, double mc_step) {
 	if (!ctx || moves < 1) return TDVMC_ERR_ARG;
 	if (!ctx->have_walkers) return TDVMC_ERR_STATE;
-	// candidates must not change the walkers: run on a copy and restore
+	// every candidate is timed twice (the second time counts) on the current walkers,
+	// which are restored after each sampling candidate; on any error the context keeps
+	// its starting tiles, and the copy and the events are released on every path
 	const size_t bytes = (size_t)ctx->nw * ctx->sc.dim * ctx->sc.n * tsize(ctx->prec);
-	void* save = nullptr;
-	CK(cudaMalloc(&save, bytes));
-	CK(cudaMemcpyAsync(save, ctx->pos, bytes, cudaMemcpyDeviceToDevice, ctx->st));
-	cudaEvent_t e0, e1;
-	CK(cudaEventCreate(&e0));
-	CK(cudaEventCreate(&e1));
-	Tiles best = ctx->tiles;
+	const Tiles start = ctx->tiles;
+	Tiles best = start;
 	float best_s = 1e30f, best_e = 1e30f;
-	const int n = ctx->sc.n;
-	const int gs[3] = {8, 16, 32};
+	void* save = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
 	int rc = TDVMC_OK;
-	for (int gi = 0; gi < 3 && rc == TDVMC_OK; gi++) {
-		const int G = gs[gi];
-		if (slots_for(n, G) < 0 || (G > 8 && n < G / 2)) continue;
-		for (int gpb : {1, 2, 4, 8}) {
-			if (G * gpb > 128) continue;
-			ctx->tiles.sg = G;
-			ctx->tiles.sgpb = gpb;
-			rc = ctx->prec == TDVMC_PREC_FP64 ? launch_prep<double>(ctx) : launch_prep<float>(ctx);
-			if (rc) break;
-			CK(cudaEventRecord(e0, ctx->st));
-			rc = ctx->prec == TDVMC_PREC_FP64 ? launch_sample<double>(ctx, moves, mc_step, 7)
-			                                  : launch_sample<float>(ctx, moves, mc_step, 7);
-			CK(cudaEventRecord(e1, ctx->st));
-			CK(cudaEventSynchronize(e1));
-			float ms = 0;
-			cudaEventElapsedTime(&ms, e0, e1);
-			if (rc == TDVMC_OK && ms < best_s) {
-				best_s = ms;
-				best.sg = G;
-				best.sgpb = gpb;
-			}
-			rc = TDVMC_OK;
-			CK(cudaMemcpyAsync(ctx->pos, save, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+	auto timed = [&](auto&& launch, float& ms) -> int {
+		if (cudaEventRecord(e0, ctx->st) != cudaSuccess) return TDVMC_ERR_CUDA;
+		const int r = launch();
+		if (cudaEventRecord(e1, ctx->st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+			return TDVMC_ERR_CUDA;
+		if (r) return r;
+		return cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess ? TDVMC_OK : TDVMC_ERR_CUDA;
+	};
+	do {
+		if (cudaMalloc(&save, bytes) != cudaSuccess) {
+			save = nullptr;
+			cudaGetLastError();
+			rc = TDVMC_ERR_NOMEM;
+			break;
+		}
+		if (cudaMemcpyAsync(save, ctx->pos, bytes, cudaMemcpyDeviceToDevice, ctx->st) != cudaSuccess ||
+		    cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+			rc = TDVMC_ERR_CUDA;
+			break;
 		}
 		if ((rc = ensure_gbuf(ctx))) break;
-		for (int gpb : {0, 1, 2, 4}) {
-			if (G * gpb > 128) continue;
-			const size_t smem = ctx->prec == TDVMC_PREC_FP64 ? eloc_smem<double>(ctx, G, gpb, true)
-			                                                 : eloc_smem<float>(ctx, G, gpb, true);
-			if (smem > 220 * 1024) continue;
-			ctx->tiles.eg = G;
-			ctx->tiles.egpb = gpb;
-			CK(cudaEventRecord(e0, ctx->st));
-			rc = ctx->prec == TDVMC_PREC_FP64 ? launch_eloc<double>(ctx, true) : launch_eloc<float>(ctx, true);
-			CK(cudaEventRecord(e1, ctx->st));
-			CK(cudaEventSynchronize(e1));
-			float ms = 0;
-			cudaEventElapsedTime(&ms, e0, e1);
-			if (rc == TDVMC_OK && ms < best_e) {
-				best_e = ms;
-				best.eg = G;
-				best.egpb = gpb;
+		const int n = ctx->sc.n;
+		for (int G : {8, 16, 32}) {
+			if (slots_for(n, G) < 0 || (G > 8 && n < G / 2)) continue;
+			for (int gpb : {1, 2, 4, 8}) {
+				if (G * gpb > 128) continue;
+				ctx->tiles.sg = G;
+				ctx->tiles.sgpb = gpb;
+				if ((rc = ctx->prec == TDVMC_PREC_FP64 ? launch_prep<double>(ctx) : launch_prep<float>(ctx))) break;
+				float ms = 0.f;
+				for (int rep = 0; rep < 2 && !rc; rep++) {
+					rc = timed([&] {
+						return ctx->prec == TDVMC_PREC_FP64 ? launch_sample<double>(ctx, moves, mc_step, 7)
+						                                    : launch_sample<float>(ctx, moves, mc_step, 7);
+					}, ms);
+					if (!rc && cudaMemcpyAsync(ctx->pos, save, bytes, cudaMemcpyDeviceToDevice, ctx->st) != cudaSuccess)
+						rc = TDVMC_ERR_CUDA;
+				}
+				if (rc == TDVMC_ERR_ARG) {  // no kernel for this tile: not a candidate
+					rc = TDVMC_OK;
+					continue;
+				}
+				if (rc) break;
+				if (ms < best_s) {
+					best_s = ms;
+					best.sg = G;
+					best.sgpb = gpb;
+				}
 			}
-			rc = TDVMC_OK;
+			if (rc) break;
+			for (int gpb : {0, 1, 2, 4})
+				for (int hist : {0, 1, 2}) {
+					if (G * gpb > 128 || (G != 32 && hist != 0) || rc) continue;
+					ctx->tiles.eg = G;
+					ctx->tiles.egpb = gpb;
+					ctx->tiles.hist = hist;
+					const size_t smem = ctx->prec == TDVMC_PREC_FP64 ? eloc_smem<double>(ctx, G, gpb, true)
+					                                                 : eloc_smem<float>(ctx, G, gpb, true);
+					if (smem > 220 * 1024) continue;
+					float ms = 0.f;
+					for (int rep = 0; rep < 2 && !rc; rep++)
+						rc = timed([&] {
+							return ctx->prec == TDVMC_PREC_FP64 ? launch_eloc<double>(ctx, true)
+							                                    : launch_eloc<float>(ctx, true);
+						}, ms);
+					if (rc == TDVMC_ERR_ARG) {
+						rc = TDVMC_OK;
+						continue;
+					}
+					if (!rc && ms < best_e) {
+						best_e = ms;
+						best.eg = G;
+						best.egpb = gpb;
+						best.hist = hist;
+					}
+				}
+			if (rc) break;
 		}
+	} while (false);
+	if (save) {
+		cudaMemcpyAsync(ctx->pos, save, bytes, cudaMemcpyDeviceToDevice, ctx->st);
+		cudaStreamSynchronize(ctx->st);
+		cudaFree(save);
 	}
-	ctx->tiles = best;
+	if (e0) cudaEventDestroy(e0);
+	if (e1) cudaEventDestroy(e1);
+	ctx->tiles = rc ? start : best;
 	for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
 	ctx->graphs.clear();
-	cudaEventDestroy(e0);
-	cudaEventDestroy(e1);
-	cudaFree(save);
-	CK(cudaStreamSynchronize(ctx->st));
+	ctx->graph_kernels.clear();
+	ctx->have_eval = false;
+	if (!rc && cudaStreamSynchronize(ctx->st) != cudaSuccess) rc = TDVMC_ERR_CUDA;
 	return rc;
 }
 

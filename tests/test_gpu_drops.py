@@ -10,7 +10,8 @@ Tolerances (stated per test):
   FP64 sampler chain vs the oracle chain (same Philox stream): positions
       1e-9, identical acceptance counts;
   per-drop reduction and solve vs numpy / the oracle solve: 1e-10;
-  one RK4 step of every drop vs the oracle step: parameters 1e-9.
+  one RK4 step of every drop vs the oracle step: parameters 1e-9;
+  an adjoint-driven imaginary-time Euler step vs the oracle: parameters 1e-9.
 """
 import numpy as np
 import pytest
@@ -178,31 +179,36 @@ def test_drops_rk4_step_matches_oracle():
     del res
 
 
-def test_drops_imaginary_time_approaches_ground_state():
-    """Imaginary-time steps of non-interacting drops from a too-narrow Gaussian
-    move the one-body parameter toward the exact -omega / (4 hbar2_2m) and the
-    energy toward (3/2) omega n, every drop independently (mixed precision)."""
+def test_drops_adjoint_imaginary_time_step_matches_oracle():
+    """An imaginary-time Euler step of every drop driven by the adjoint
+    (F_k = -(cov(O_k, E^R) + <dE_loc/d uR_k> / 2)), FP64 against the oracle run
+    the same way: parameters relative 1e-9."""
     import tdvmc_gb300 as T
-    rng = np.random.default_rng(12)
+    rng = np.random.default_rng(19)
     ns = [3, 6, 10, 20]
-    nw = 2048
-    d = T.TrappedDrops(ns, P, RMAX, nw, omega=1.0, v0=0.0, sigma=0.5, hbar2_2m=0.5, precision="mixed")
-    uR = np.zeros((4, P + 1))
-    uR[:, P] = -0.8
-    d.SetParameters(uR, np.zeros((4, P + 1)))
-    d.SetWalkers(walkers(rng, ns, nw, True))
-    d.DoMetropolisSteps(20, 0.5, seed=1, pass_id=100)
-    td = T.DropsTDVP(d, 0.05, 2, 0.5, seed=2, imaginary_time=1, use_adjoint=1)
-    e0 = None
-    for _ in range(30):
-        out = td.step(1)
-        if e0 is None:
-            e0 = out["energy"][:, 0].copy()
-    aP = d.GetParameters()[0][:, P]
-    e = out["energy"][:, 0]
-    exact = 1.5 * np.array(ns)
-    assert (np.abs(aP + 0.5) < np.abs(-0.8 + 0.5) / 3).all(), aP
-    assert (np.abs(e - exact) < 0.5 * np.abs(e0 - exact)).all(), (e0, e)
+    nw, dt, sweeps, step, seed = 128, 5e-3, 2, 0.5, 23
+    d = T.TrappedDrops(ns, P, RMAX, nw, v0=1.0, sigma=0.5, precision="fp64")
+    uR, uI = params(rng, len(ns))
+    uI[:] = 0.0
+    W = walkers(rng, ns, nw, False)
+    d.SetParameters(uR, uI)
+    d.SetWalkers(W)
+    out = T.DropsTDVP(d, dt, sweeps, step, seed=seed, imaginary_time=1, ode_solver=0, use_adjoint=2).step(1)
+    assert (out["status"] == 0).all()
+    gR, gI, gpR, gpI = d.GetParameters()
+    p1 = P + 1
+    for s, n in enumerate(ns):
+        o = orc.OracleDrop(n, P, RMAX, v0=1.0, sigma=0.5)
+        R = np.ascontiguousarray(W[s])
+        o.sample(uR[s], R, sweeps * n, step, seed=seed, pass_id=0, walker0=s * nw)
+        ev = [o.eval(uR[s], uI[s], R[w].T, adjoint=True) for w in range(nw)]
+        c = orc.centred(np.array([e["O"] for e in ev]), np.array([e["eloc"] for e in ev]))
+        dER = np.array([e["dE"][:, 0] for e in ev]).mean(0)
+        r = orc.solve_centred(c["O"], c["ER"], c["EI"], c["S"], c["cOER"] + 0.5 * dER, c["cOEI"], imag=1)
+        new = np.concatenate([uR[s], uI[s], [0.0, 0.0]]) + np.concatenate([r[0], r[1], [r[2], r[3]]]) * dt
+        assert rel(gR[s], new[:p1]) < 1e-9, n
+        assert rel(gI[s], new[p1:2 * p1]) < 1e-9 or np.abs(new[p1:2 * p1]).max() < 1e-300
+        assert abs(gpR[s] - new[2 * p1]) < 1e-9 * max(abs(new[2 * p1]), 1.0)
 
 
 def test_drops_autotune_keeps_walkers_and_results():

@@ -51,7 +51,13 @@ def test_noalloc_statistics_match_reduce_stats(nw, p):
         return lib.tdvmc_reduce_walkers_noalloc(C.c_void_p(O.data_ptr()), C.c_void_p(E.data_ptr()), nw, p,
                                                 *[C.c_void_p(t.data_ptr()) for t in outs], stream)
 
-    assert call() == N.OK  # warm-up: the first call on a device looks up the static array
+    # warm-up of everything the checks below run: the first call on a device looks up
+    # the static array, and torch's own kernels are loaded on their first use
+    for t in outs:
+        t.fill_(float("nan"))
+    assert call() == N.OK
+    torch.cuda.synchronize()
+    [t.cpu() for t in outs]
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
     for k in range(2):
