@@ -837,18 +837,23 @@ __device__ __forceinline__ int sweep_t(const SysConst& sc, float r, const float*
 // group looks at the block's pairs again, decides those near r_max in FP64 from
 // the FP32 coordinates (as the FP64 path does) and, where that decision
 // differs, adds or removes the pair's terms.  Rare (a few pairs per walker at
-// N = 1000), and outside the sweep's inner loop.  Phase 1: the row's
-// gradient (own), the Laplacian, potential and moment terms; phase 2 (after
-// the rows' gradients are stored): the partner's gradient, atomically, since
-// several lanes may correct one partner.  ROWS: rows of the partners' gradients
-// (gRx in xs[].w, gRy..gIz in gacc[(c-1) n + i]).
+// N = 1000), and a separate function: the sweep's code and registers do not
+// carry it.  Phase 1 returns the row's gradient, Laplacian and potential terms
+// and updates the moments (lane-private records); phase 2 (after the rows'
+// gradients are stored) corrects the partner's gradient, atomically, since
+// several lanes may correct one partner (gRx in xs[].w, gRy..gIz in
+// gacc[(c-1) n + i]).
+struct FixTerms {
+	float g[6];
+	float lR, lI, v;
+};
 template <bool DIAG, int HIST>
-__device__ __forceinline__ void half_block_fix(const SysConst& sc, int sp, int n, int lane, int nrow, bool rowok,
-                                            Q4<float>* xs, float* gacc, const Q4<float>* coefC, const float* kb,
-                                            const float* hv, const int* lut, float* hist, float pa, float pb,
-                                            KSum<float>* own, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum,
-                                            int phase) {
-	if (!rowok) return;
+__device__ __noinline__ FixTerms half_block_fix(SysConst sc, int sp, int n, int lane, int nrow, bool rowok,
+                                                Q4<float>* xs, float* gacc, const Q4<float>* coefC, const float* kb,
+                                                const float* hv, const int* lut, float* hist, float pa, float pb,
+                                                int phase) {
+	FixTerms out = {{0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, 0.f, 0.f, 0.f};
+	if (!rowok) return out;
 	const float rmax = (float)sc.rmax;
 	const float dm1 = (float)(sc.dim - 1);
 	const Q4<float> xr = xs[nrow];
@@ -870,13 +875,11 @@ __device__ __forceinline__ void half_block_fix(const SysConst& sc, int sp, int n
 		const float gI = fmaf(t, fmaf(t, cI.z, cI.y), cI.x) * q;
 		const float g6[6] = {gR * dx, gR * dy, gR * dz, gI * dx, gI * dy, gI * dz};
 		if (phase == 1) {
-			const float lR = fmaf(dm1, gR, fmaf(t, c2.x, cR.w));
-			const float lI = fmaf(dm1, gI, fmaf(t, c2.y, cI.w));
 #pragma unroll
-			for (int c = 0; c < 6; c++) own[c].add(sgn * g6[c]);
-			elR.add(sgn * 2.f * lR);
-			elI.add(sgn * 2.f * lI);
-			vsum.add(sgn * pair_pot<float>(sc.pot_kind, r, q, pa, pb));
+			for (int c = 0; c < 6; c++) out.g[c] += sgn * g6[c];
+			out.lR += sgn * 2.f * fmaf(dm1, gR, fmaf(t, c2.x, cR.w));
+			out.lI += sgn * 2.f * fmaf(dm1, gI, fmaf(t, c2.y, cI.w));
+			out.v += sgn * pair_pot<float>(sc.pot_kind, r, q, pa, pb);
 			const float t2 = t * t;
 			const float v[8] = {sgn, sgn * t, sgn * t2, sgn * t2 * t, 0.f, 0.f, 0.f, 0.f};
 			hist_add8<HIST, HistSlots<HIST, false>::value, float, 32>(hist, j, lane, v, kFwdMoments);
@@ -886,13 +889,17 @@ __device__ __forceinline__ void half_block_fix(const SysConst& sc, int sp, int n
 			for (int c = 1; c < 6; c++) atomicAdd(&gacc[(size_t)(c - 1) * n + i], -sgn * g6[c]);
 		}
 	}
+	return out;
 }
 
 // Cutoff fix-up of one region of the FP32 reverse sweep (rev_region_f2): the
 // pairs near r_max whose FP64 decision differs from the sweep's have their
 // moment terms added or removed (lane-private histogram records).
+struct Grad6 {
+	float v[6];
+};
 template <int G, bool DIAG, int HIST, bool ROT>
-__device__ __forceinline__ void rev_region_fix(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const float* gn,
+__device__ __noinline__ void rev_region_fix(SysConst sc, int i0, int i1, int nrow, bool rowok, Grad6 gn,
                                             const Q4<float>* xs, const Q4<float>* g4, const float* gz,
                                             const float* kb, const float* hv, const int* lut, float* hist, int lane) {
 	if (!rowok) return;
@@ -918,8 +925,8 @@ __device__ __forceinline__ void rev_region_fix(const SysConst& sc, int i0, int i
 		float t;
 		const int j = sweep_t(sc, r, kb, hv, lut, t);
 		const Q4<float> gi = g4[i];
-		const float gR = ((gn[0] - xi.w) * dx + (gn[1] - gi.x) * dy + (gn[2] - gi.y) * dz + dm1) * q;
-		const float gI = ((gn[3] - gi.z) * dx + (gn[4] - gi.w) * dy + (gn[5] - gz[i]) * dz) * q;
+		const float gR = ((gn.v[0] - xi.w) * dx + (gn.v[1] - gi.x) * dy + (gn.v[2] - gi.y) * dz + dm1) * q;
+		const float gI = ((gn.v[3] - gi.z) * dx + (gn.v[4] - gi.w) * dy + (gn.v[5] - gz[i]) * dz) * q;
 		const float t2 = t * t;
 		const float v[8] = {sgn * gR, sgn * gR * t, sgn * gR * t2, sgn * gI, sgn * gI * t, sgn * gI * t2, 0.f, 0.f};
 		hist_add8<HIST, HistSlots<HIST, true>::value, float, G>(hist, j, lane, v, kRevMoments);
@@ -1195,10 +1202,15 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 					if constexpr (std::is_same<T, float>::value) {
 						if (__any_sync(0xffffffffu, nearmin < sc.rcut_band)) {
 							__syncwarp();
+							const FixTerms f = half_block_fix<false, HIST>(sc, sp, n, lane, nrow, rowok, xs, gacc, coefC,
+							                                              kb, hv, lut, hist, pa, pb, 1);
+#pragma unroll
+							for (int c = 0; c < 6; c++) own[c].add(f.g[c]);
+							e_lR.add(f.lR);
+							e_lI.add(f.lI);
+							e_v.add(f.v);
 							half_block_fix<false, HIST>(sc, sp, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist,
-							                            pa, pb, own, e_lR, e_lI, e_v, 1);
-							half_block_fix<false, HIST>(sc, sp, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist,
-							                            pa, pb, own, e_lR, e_lI, e_v, 2);
+							                            pa, pb, 2);
 							__syncwarp();
 						}
 					}
@@ -1212,9 +1224,15 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 				bool fix = false;
 				if constexpr (std::is_same<T, float>::value) {
 					fix = __any_sync(0xffffffffu, nearmin < sc.rcut_band);
-					if (fix)
-						half_block_fix<true, HIST>(sc, s, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist, pa,
-						                           pb, own, e_lR, e_lI, e_v, 1);
+					if (fix) {
+						const FixTerms f = half_block_fix<true, HIST>(sc, s, n, lane, nrow, rowok, xs, gacc, coefC, kb,
+						                                             hv, lut, hist, pa, pb, 1);
+#pragma unroll
+						for (int c = 0; c < 6; c++) own[c].add(f.g[c]);
+						e_lR.add(f.lR);
+						e_lI.add(f.lI);
+						e_v.add(f.v);
+					}
 				}
 				if (rowok) {  // later slots add their shares
 					xs[nrow].w = own[0].value();
@@ -1225,7 +1243,7 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 					if (fix) {
 						__syncwarp();
 						half_block_fix<true, HIST>(sc, s, n, lane, nrow, rowok, xs, gacc, coefC, kb, hv, lut, hist, pa,
-						                           pb, own, e_lR, e_lI, e_v, 2);
+						                           pb, 2);
 						__syncwarp();
 					}
 				}
@@ -1434,12 +1452,15 @@ __global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __res
 				rev_region_f2<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist,
 				                                      lane, nm1);
 				// pairs within rounding of r_max, decided again in FP64 (rev_region_fix)
-				if (__any_sync(gmask, nm0 < sc.rcut_band))
-					rev_region_fix<G, false, HIST, false>(sc, 0, base, nrow, rowok, gn, xs, g4, gz, kb, hv, lut, hist,
-					                                      lane);
-				if (__any_sync(gmask, nm1 < sc.rcut_band))
-					rev_region_fix<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, gn, xs, g4, gz, kb, hv, lut,
-					                                       hist, lane);
+				if (__any_sync(gmask, nm0 < sc.rcut_band || nm1 < sc.rcut_band)) {
+					const Grad6 g6 = {{gn[0], gn[1], gn[2], gn[3], gn[4], gn[5]}};
+					if (__any_sync(gmask, nm0 < sc.rcut_band))
+						rev_region_fix<G, false, HIST, false>(sc, 0, base, nrow, rowok, g6, xs, g4, gz, kb, hv, lut, hist,
+						                                      lane);
+					if (__any_sync(gmask, nm1 < sc.rcut_band))
+						rev_region_fix<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, g6, xs, g4, gz, kb, hv, lut,
+						                                       hist, lane);
+				}
 			} else {
 				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
 				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);

@@ -826,9 +826,11 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	s.hinv = hv[0];
 	s.hf = (float)s.hinv;
 	s.hf_lo = (float)(s.hinv - (double)s.hf);
-	// the FP32 distance of an FP32 pair is within a few 1e-7 (relative) of its FP64
-	// distance; 4e-6 leaves a margin of about ten
-	s.rcut_band = (float)(s.rmax * 4e-6);
+	// the FP32 distance of an FP32 pair is within about 3.5e-7 (relative) of its FP64
+	// distance (the rounding of the differences, of r^2, of r^2 times the hardware
+	// reciprocal square root, whose relative error is below 2^-22.9); the band of
+	// 1e-6 keeps a margin of about three
+	s.rcut_band = (float)(s.rmax * 1e-6);
 	std::vector<int> lut;
 	if (!s.uniform) {
 		const double span = s.rmax - kb[0];

@@ -346,7 +346,7 @@ def test_packed_sampler_follows_scalar_chain_mixed():
     z = np.load(os.path.join(GOLD, "eval_d3_n343_p30.npz"))
     nw, n = 512, int(z["n"])
     rng = np.random.default_rng(11)
-    R0 = np.concatenate([soa(z["cfgs"])] * (nw // 4)) + rng.normal(0, 0.02, size=(nw, 3, n))
+    R0 = np.concatenate([soa(z["cfgs"])] * (nw // len(z["cfgs"]))) + rng.normal(0, 0.02, size=(nw, 3, n))
     uR = np.asarray(z["uR"])
     out = {}
     for mode in ("packed", "scalar"):
