@@ -166,12 +166,15 @@ def cpu_port_rate(threads, walkers_per_thread=1, seed=11):
 def run_reference(args):
     threads = os.cpu_count() or 1
     rates = []
+    t_probe = 1.0
     for _ in range(args.warmup):
-        cpu_port_rate(threads, 1)
+        _, t_probe, _ = cpu_port_rate(threads, 1)
+    # about 10 s of CPU work per measured step (one RK stage of wpt walkers per thread)
+    wpt = int(min(2048, max(1, np.ceil(10.0 / max(t_probe, 1e-3)))))
     t_all = 0.0
     nws = 0
     for k in range(args.steps):
-        r, t, nws = cpu_port_rate(threads, 8, seed=100 + k)
+        r, t, nws = cpu_port_rate(threads, wpt, seed=100 + k)
         rates.append(r)
         t_all += t
     v = float(np.mean(rates))
@@ -183,9 +186,160 @@ def run_reference(args):
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
                              "sample": "per step: one RK stage (686 moves + E_loc + adjoint) of %d walkers "
-                                       "on %d threads, extrapolated x4 stages x65536 walkers" % (nws, threads)},
+                                       "on %d threads (%.1f s of CPU work per step on average), extrapolated "
+                                       "x4 stages x65536 walkers" % (nws, threads, t_all / max(args.steps, 1))},
             "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+# batched trapped drops: 512 drops in 3D harmonic traps (omega = 1), Gaussian pair
+# repulsion v0 = 1, sigma = 0.5, particle numbers drawn uniformly from {3, 6, 10, 20}
+# (seed 4), a 12-knot pair spline plus a one-body Gaussian width each, 4,096 walkers
+# per drop, units hbar = m = omega = 1 (hbar^2 / 2m = 0.5)
+DROPS, DROP_WALKERS, DROP_P, DROP_RMAX = 512, 4096, 12, 4.0
+DROP_NS = (3, 6, 10, 20)
+DROP_DT, DROP_SWEEPS, DROP_STEP = 1e-3, 2, 0.6
+
+
+def drops_workload(precision="mixed", walkers=DROP_WALKERS):
+    import tdvmc_gb300 as T
+    rng = np.random.default_rng(4)
+    ns = rng.choice(DROP_NS, size=DROPS)
+    d = T.TrappedDrops(ns, DROP_P, DROP_RMAX, walkers, omega=1.0, v0=1.0, sigma=0.5, hbar2_2m=0.5,
+                       precision=precision)
+    r = np.linspace(0.0, DROP_RMAX, DROP_P)
+    uR = np.tile(np.concatenate([0.3 * np.exp(-r / 0.7), [-0.45]]), (DROPS, 1))
+    d.SetParameters(uR, np.zeros_like(uR))
+    wr = np.random.default_rng(5)
+    d.SetWalkers([wr.normal(scale=0.7, size=(walkers, 3, n)) for n in ns])
+    return d, ns
+
+
+def run_drops(sync, steps, warmup):
+    """The batched-drops workload: RK4 steps of all 512 drops, each stage one graph
+    replay (prep, sample, evaluate + adjoint, per-drop reduce, per-drop solve), tiles
+    chosen by the autotuner."""
+    import tdvmc_gb300 as T
+    d, ns = drops_workload()
+    d.DoMetropolisSteps(10, DROP_STEP, seed=9, pass_id=0xFFFFFF00)  # thermalise
+    tiles = d.Autotune(DROP_SWEEPS, DROP_STEP)
+    td = T.DropsTDVP(d, DROP_DT, DROP_SWEEPS, DROP_STEP, seed=3, use_adjoint=1)
+    td.time_steps(warmup)
+    sync()
+    l0 = d.LaunchCount()
+    ms = td.time_steps(steps)
+    launches = d.LaunchCount() - l0
+    prof = td.profile_stage()
+    out = td.step(1)
+    e = out["energy"][:, 0]
+    d.close()
+    return {"value": steps / (ms / 1000.0), "unit": "steps/s", "drops": DROPS, "walkers_per_drop": DROP_WALKERS,
+            "particles": {str(n): int((ns == n).sum()) for n in DROP_NS}, "spline_params": DROP_P,
+            "dt": DROP_DT, "sweeps_per_stage": DROP_SWEEPS, "ms_per_step": ms / steps,
+            "kernels_ms_per_stage": {k: v for k, v in prof}, "tiles": tiles,
+            "gpu_launches_per_step": launches // steps, "status_ok": bool((out["status"] == 0).all()),
+            "energy_per_particle_mean": float(np.mean(e / ns))}
+
+
+# large bulk: N = 1,000 on a 10x10x10 start, LJ at density 0.365, 64 knots,
+# 262,144 walkers; imaginary-time preparation driven by the adjoint dE_loc/d alpha,
+# then a density quench (0.365 -> 0.40, box and walkers rescaled, parameters kept
+# per knot) and real-time RK4 steps dt = 2.5e-4, with an FP64 evaluation of the same
+# walkers every 10 steps
+C5_N, C5_P, C5_RHO, C5_RHO_Q, C5_NW = 1000, 64, 0.365, 0.40, 262144
+C5_DT_IMAG, C5_DT = 1e-3, 2.5e-4
+C5_STEP = 0.17
+C5_CHECK_WALKERS = 8192
+
+
+def c5_walkers(nw, L, seed=5):
+    m = 10
+    l = L / m
+    idx = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 3)
+    rng = np.random.default_rng(seed)
+    R = np.empty((nw, 3, C5_N))
+    for w0 in range(0, nw, 8192):
+        w1 = min(nw, w0 + 8192)
+        x = idx[None] * l + (rng.uniform(size=(w1 - w0, C5_N, 3)) - 0.5) * l / 10.0 - L / 2
+        R[w0:w1] = np.transpose(x, (0, 2, 1))
+    return R
+
+
+def c5_gate(sysm, L, nsub):
+    """|dE/N| between the mixed evaluation and an FP64 evaluation of the same
+    (FP32-held) walkers, first nsub walkers."""
+    import tdvmc_gb300 as T
+    Rm = sysm.GetWalkers()[:nsub]
+    fm = sysm.CalculateExpectationValues()
+    gp = sysm.GetParameters()
+    s64 = T.BosonsBulk(3, C5_N, C5_P, L, nsub, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
+                       precision="fp64")
+    s64.SetParameters(*gp)
+    s64.SetWalkers(Rm)
+    f64 = s64.CalculateExpectationValues()
+    s64.close()
+    return abs(fm["eloc"][:nsub, 0].mean() - f64["eloc"][:, 0].mean()) / C5_N
+
+
+def run_c5(sync, imag_steps, real_steps, timed_steps, check_every=10, nw=C5_NW, log=None):
+    """Imaginary-time preparation (use_adjoint = 2), density quench, real-time RK4
+    steps; returns the timed real-time steps/s and the FP64 gate at every check."""
+    import tdvmc_gb300 as T
+    L0 = (C5_N / C5_RHO) ** (1.0 / 3.0)
+    L1 = (C5_N / C5_RHO_Q) ** (1.0 / 3.0)
+    r = np.linspace(0.0, L0 / 2, C5_P)
+    uR = -0.5 * (1.1 / np.maximum(r, 0.5)) ** 5
+    uR -= uR[-1]
+    R = c5_walkers(nw, L0)
+    s0 = T.BosonsBulk(3, C5_N, C5_P, L0, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
+                      precision="mixed")
+    s0.SetParameters(uR, np.zeros(C5_P))
+    s0.SetWalkers(R)
+    del R
+    gates = []
+    t0 = time.perf_counter()
+    ti = T.TDVP(s0, C5_DT_IMAG, 2 * C5_N, C5_STEP, seed=5, imaginary_time=1, use_adjoint=2)
+    e_imag = []
+    for k in range(imag_steps):
+        out = ti.step(1)
+        e_imag.append(out["energy"][0] / C5_N)
+        if log:
+            log("imag step %d E/N %.6f acc %.3f status %d" % (k, e_imag[-1], out["accept_rate"], out["status"]))
+    gp = s0.GetParameters()
+    Rq = s0.GetWalkers() * (L1 / L0)
+    s0.close()
+    s1 = T.BosonsBulk(3, C5_N, C5_P, L1, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
+                      precision="mixed")
+    s1.SetParameters(*gp)
+    s1.SetWalkers(Rq)
+    del Rq
+    tr = T.TDVP(s1, C5_DT, 2 * C5_N, C5_STEP, seed=6, use_adjoint=1)
+    e_real = []
+    for k in range(real_steps - timed_steps):
+        out = tr.step(1)
+        e_real.append(out["energy"][0] / C5_N)
+        if check_every and (k + 1) % check_every == 0:
+            g = c5_gate(s1, L1, min(C5_CHECK_WALKERS, nw))
+            gates.append({"step": k + 1, "dE_per_N": g})
+            if log:
+                log("real step %d E/N %.6f acc %.3f status %d gate %.2e"
+                    % (k + 1, e_real[-1], out["accept_rate"], out["status"], g))
+    ms_timed = None
+    if timed_steps > 0:
+        sync()
+        ms_timed = tr.time_steps(timed_steps)  # CUDA events on the library's stream
+    res = {"imag_steps": imag_steps, "real_steps": real_steps, "walkers": nw, "particles": C5_N, "params": C5_P,
+           "rho": [C5_RHO, C5_RHO_Q], "dt_imag": C5_DT_IMAG, "dt": C5_DT, "moves_per_stage": 2 * C5_N,
+           "energy_per_particle_imag": e_imag[-3:], "energy_per_particle_real": e_real[-3:],
+           "gates": gates, "gate_pass": bool(all(g["dE_per_N"] < 1e-5 for g in gates)),
+           "wall_s": time.perf_counter() - t0}
+    if ms_timed is not None:
+        res["value"] = timed_steps / (ms_timed / 1000.0)
+        res["unit"] = "steps/s"
+        res["ms_per_step"] = ms_timed / timed_steps
+        res["gate_after_timed"] = c5_gate(s1, L1, min(C5_CHECK_WALKERS, nw))
+    s1.close()
+    return res
 
 
 class Ranks:
@@ -292,25 +446,27 @@ def run_ours(args):
     h2d = (2 * P + 2) * 8 * 2 + 4
     d2h = (3 * P + 12) * 8 + 24 + (2 * P + 2) * 8
 
-    # |dE/N| gate: FP64 evaluation of the same walkers (subset) vs the mixed path
-    nsub = 4096
-    Rm = sysm.GetWalkers()[:nsub]
+    # |dE/N| gate: FP64 evaluation of all the walkers the mixed path holds (its FP32
+    # coordinates) against the mixed evaluation
+    Rm = sysm.GetWalkers()
     fm = sysm.CalculateExpectationValues()
     gp = sysm.GetParameters()
-    s64 = T.BosonsBulk(DIM, N, P, L, nsub, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
+    s64 = T.BosonsBulk(DIM, N, P, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=HBAR2_2M,
                        precision="fp64")
     s64.SetParameters(gp[0], gp[1], gp[2], gp[3])
     s64.SetWalkers(Rm)
     f64 = s64.CalculateExpectationValues()
-    dE_per_N = abs(fm["eloc"][:nsub, 0].mean() - f64["eloc"][:, 0].mean()) / N
+    dE_per_N = abs(fm["eloc"][:, 0].mean() - f64["eloc"][:, 0].mean()) / N
+    del Rm
 
-    # plain FP64 GPU path, same kernels in double, on nsub walkers, scaled
-    s64.SetWalkers(R0[:nsub])
+    # plain FP64 GPU path, same kernels in double, at the full walker count
+    s64.SetWalkers(R0)
     s64.SetParameters(uR, uI)
     td64 = T.TDVP(s64, DT, MOVES, MC_STEP, seed=1, use_adjoint=1)
     td64.time_steps(1)
     ms64 = td64.time_steps(1)
-    fp64_steps_s = (1000.0 / ms64) * nsub / NW
+    fp64_steps_s = 1000.0 / ms64
+    s64.close()
 
     # RK4 on stored samples (ODE_SOLVER_TYPE 3, correlated-sampling reuse): the
     # first stage of every step resamples a rotating quarter of the walkers, the
@@ -326,6 +482,15 @@ def run_ours(args):
                  update_percent=25.0)
     td5.time_steps(1)
     ms5 = td5.time_steps(args.steps)
+
+    # batched trapped drops (512 drops of 3-20 particles, 4,096 walkers each)
+    drops = run_drops(sync, args.steps, args.warmup) if args.extras_drops else None
+    # large bulk (N = 1,000, 262,144 walkers): one imaginary-time step driven by the
+    # adjoint, the density quench, one real-time step, then two timed real-time steps
+    c5 = run_c5(sync, 1, 3, 2, check_every=0) if args.extras_c5 else None
+    if c5:
+        c5["workload"] = ("3D N=1000 LJ bosons rho=0.365 -> 0.40 quench, P=64, 262144 walkers, "
+                          "RK4 dt=2.5e-4, 2 sweeps/stage")
 
     # FP32 pipe ceiling and roofline of the dominant kernel
     import ctypes as C
@@ -372,9 +537,12 @@ def run_ours(args):
                      "peak_source": "measured FP32 FMA loop (tdvmc_measure_fp32_peak)",
                      "traffic": traffic, "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "kernels_ms_per_stage": kt,
-        "fp64_gpu": {"value": fp64_steps_s, "unit": "steps/s", "walkers_timed": nsub, "scaled_to": NW,
+        "fp64_gpu": {"value": fp64_steps_s, "unit": "steps/s", "walkers_timed": nw, "steps_timed": 1,
                      "speedup_mixed_over_fp64": value / world / fp64_steps_s},
-        "gate": {"dE_per_N": dE_per_N, "pass": bool(dE_per_N < 1e-5), "walkers": nsub},
+        "gate": {"dE_per_N": dE_per_N, "pass": bool(dE_per_N < 1e-5), "walkers": nw,
+                 "against": "FP64 GPU evaluation of the same FP32-held walkers"},
+        "batched_drops": drops,
+        "large_bulk": c5,
         "stored_sample_rk4": {"value": args.steps / (ms3 / 1000.0), "unit": "steps/s", "update_every": 1,
                               "update_percent": 25.0, "kernels_ms_refresh_stage": prof3},
         "stored_sample_pc": {"value": args.steps / (ms5 / 1000.0), "unit": "steps/s", "update_every": 1,
@@ -391,6 +559,24 @@ def run_ours(args):
         print(json.dumps(line))
 
 
+def run_workload(args):
+    """One of the other workloads alone, one JSON line (not the headline metric)."""
+    import torch
+    torch.cuda.set_device(0)
+    sync = torch.cuda.synchronize
+    if args.workload == "drops":
+        out = run_drops(sync, args.steps, args.warmup)
+        out["workload"] = ("512 trapped 3D drops, N in {3,6,10,20}, 12-knot spline + one-body width, "
+                           "4096 walkers/drop, RK4 dt=1e-3, 2 sweeps/stage, adjoint, autotuned tiles")
+    else:
+        def log(msg):
+            print(msg, file=sys.stderr, flush=True)
+        out = run_c5(sync, 50, 200, 0, check_every=10, log=log)
+        out["workload"] = ("3D N=1000 LJ bosons rho=0.365, P=64, 262144 walkers: 50 imaginary-time steps "
+                           "(adjoint force), quench to rho=0.40, 200 real-time RK4 steps dt=2.5e-4")
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -403,7 +589,15 @@ def main():
                     help="time the steps only (no e2e, FP64, CPU or gate legs): for profiler runs on a small case")
     ap.add_argument("--stored", choices=["rk4", "pc"], default=None,
                     help="with --no-extras: time steps on stored samples (RK4 or the predictor-corrector)")
+    ap.add_argument("--extras-drops", type=int, default=1, help="time the batched-drops workload as an extra")
+    ap.add_argument("--extras-c5", type=int, default=1, help="time the large-bulk workload as an extra")
+    ap.add_argument("--workload", choices=["bulk", "drops", "c5"], default="bulk",
+                    help="drops: the batched-drops workload alone; c5: the full large-bulk run (50 imaginary-"
+                         "time steps, quench, 200 real-time steps, FP64 check every 10 steps)")
     args = ap.parse_args()
+    if args.workload != "bulk":
+        run_workload(args)
+        return
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
