@@ -215,12 +215,12 @@ def drops_workload(precision="mixed", walkers=DROP_WALKERS):
     return d, ns
 
 
-def run_drops(sync, steps, warmup):
+def run_drops(sync, steps, warmup, walkers=DROP_WALKERS):
     """The batched-drops workload: RK4 steps of all 512 drops, each stage one graph
     replay (prep, sample, evaluate + adjoint, per-drop reduce, per-drop solve), tiles
     chosen by the autotuner."""
     import tdvmc_gb300 as T
-    d, ns = drops_workload()
+    d, ns = drops_workload(walkers=walkers)
     d.DoMetropolisSteps(10, DROP_STEP, seed=9, pass_id=0xFFFFFF00)  # thermalise
     tiles = d.Autotune(DROP_SWEEPS, DROP_STEP)
     td = T.DropsTDVP(d, DROP_DT, DROP_SWEEPS, DROP_STEP, seed=3, use_adjoint=1)
@@ -233,7 +233,7 @@ def run_drops(sync, steps, warmup):
     out = td.step(1)
     e = out["energy"][:, 0]
     d.close()
-    return {"value": steps / (ms / 1000.0), "unit": "steps/s", "drops": DROPS, "walkers_per_drop": DROP_WALKERS,
+    return {"value": steps / (ms / 1000.0), "unit": "steps/s", "drops": DROPS, "walkers_per_drop": walkers,
             "particles": {str(n): int((ns == n).sum()) for n in DROP_NS}, "spline_params": DROP_P,
             "dt": DROP_DT, "sweeps_per_stage": DROP_SWEEPS, "ms_per_step": ms / steps,
             "kernels_ms_per_stage": {k: v for k, v in prof}, "tiles": tiles,
@@ -565,7 +565,7 @@ def run_workload(args):
     torch.cuda.set_device(0)
     sync = torch.cuda.synchronize
     if args.workload == "drops":
-        out = run_drops(sync, args.steps, args.warmup)
+        out = run_drops(sync, args.steps, args.warmup, walkers=args.drop_walkers)
         out["workload"] = ("512 trapped 3D drops, N in {3,6,10,20}, 12-knot spline + one-body width, "
                            "4096 walkers/drop, RK4 dt=1e-3, 2 sweeps/stage, adjoint, autotuned tiles")
     else:
@@ -591,6 +591,8 @@ def main():
                     help="with --no-extras: time steps on stored samples (RK4 or the predictor-corrector)")
     ap.add_argument("--extras-drops", type=int, default=1, help="time the batched-drops workload as an extra")
     ap.add_argument("--extras-c5", type=int, default=1, help="time the large-bulk workload as an extra")
+    ap.add_argument("--drop-walkers", type=int, default=DROP_WALKERS,
+                    help="with --workload drops: walkers per drop (smaller for profiler runs)")
     ap.add_argument("--workload", choices=["bulk", "drops", "c5"], default="bulk",
                     help="drops: the batched-drops workload alone; c5: the full large-bulk run (50 imaginary-"
                          "time steps, quench, 200 real-time steps, FP64 check every 10 steps)")
