@@ -38,6 +38,9 @@ struct SysConst {
 	// FP32 distances with |r - r_max| < rcut_band lie within rounding of r_max:
 	// the cutoff of such a pair is decided again in FP64 from its FP32 coordinates
 	float rcut_band;
+	// -2 (L - Lf), Lf the FP32 box length: the first-order share of the FP32 box
+	// length's remainder in the r^2 of a wrapped pair (see pair_r2_f32)
+	float lc;
 };
 
 // Values that change between stages or steps live in device memory so a
@@ -67,6 +70,34 @@ __device__ __forceinline__ float nic(float d, float L, float Lr) {
 __device__ __forceinline__ double nic(double d, double L, double Lr) {
 	const double k = __dadd_rn(__fma_rn(d, Lr, kRoundD), -kRoundD);
 	return __fma_rn(-k, L, d);
+}
+
+// FP32 squared pair distance from the raw differences d of two FP32 positions.
+// Minimum image d - k Lf, k = rint(d / L), with the FP32 box length Lf.  The
+// remainder L - Lf is not subtracted from d: a shifted difference d - k Lf is
+// exact on the FP32 grid, so rounding d - k L back to FP32 would move every
+// wrapped pair by the same fraction of an ulp, a bias that the splines next to
+// r_max = L/2 sum coherently over a dense shell of pairs.  It enters r^2 at
+// first order instead, as -2 (L - Lf) sum_a k_a d_a, where the rounding of r^2
+// is unbiased.  dx, dy, dz return the shifted differences (the pair direction).
+__device__ __forceinline__ float pair_r2_f32(float lc, float L, float Lr, float& dx, float& dy, float& dz) {
+	const float kx = __fadd_rn(__fmaf_rn(dx, Lr, kRoundF), -kRoundF);
+	const float ky = __fadd_rn(__fmaf_rn(dy, Lr, kRoundF), -kRoundF);
+	const float kz = __fadd_rn(__fmaf_rn(dz, Lr, kRoundF), -kRoundF);
+	dx = __fmaf_rn(-kx, L, dx);
+	dy = __fmaf_rn(-ky, L, dy);
+	dz = __fmaf_rn(-kz, L, dz);
+	const float kd = __fmaf_rn(kz, dz, __fmaf_rn(ky, dy, __fmul_rn(kx, dx)));
+	return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, __fmul_rn(kd, lc))));
+}
+// FP32 distance from r^2 and q ~ 1/r (hardware rsqrt): r^2 q and one Newton step
+// r + (r^2 - r r) q / 2.  The relative error of rsqrt.approx (below 2^-22.9) is
+// correlated over a narrow range of r, so without the step it too would enter
+// the sums over a shell of pairs coherently; after it r is within about one
+// rounding of sqrt(r^2).
+__device__ __forceinline__ float pair_r_newton(float r2, float q) {
+	const float r = __fmul_rn(r2, q);
+	return __fmaf_rn(__fmaf_rn(-r, r, r2), __fmul_rn(0.5f, q), r);
 }
 
 // floor(x) for 0 <= x < 2^22 clamped to jmax, as (integer, float), without

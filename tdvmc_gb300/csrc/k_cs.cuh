@@ -73,12 +73,23 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
                                              const int* __restrict__ lut) {
 	CsGeom<T> g;
 	const T L = (T)sc.L, Lr = (T)sc.Lr;
-	g.dx = nic(xr.x - xi.x, L, Lr);
-	g.dy = nic(xr.y - xi.y, L, Lr);
-	g.dz = nic(xr.z - xi.z, L, Lr);
-	const T r2 = fma(g.dz, g.dz, fma(g.dy, g.dy, g.dx * g.dx));
-	g.rinv = rsqrt_(r2);
-	g.r = r2 * g.rinv;
+	if constexpr (sizeof(T) == 4) {
+		// FP32: the evaluation kernels' distance (box remainder in r^2, one Newton step)
+		float dx = xr.x - xi.x, dy = xr.y - xi.y, dz = xr.z - xi.z;
+		const float r2 = pair_r2_f32(sc.lc, L, Lr, dx, dy, dz);
+		g.dx = dx;
+		g.dy = dy;
+		g.dz = dz;
+		g.rinv = rsqrt_(r2);
+		g.r = pair_r_newton(r2, g.rinv);
+	} else {
+		g.dx = nic(xr.x - xi.x, L, Lr);
+		g.dy = nic(xr.y - xi.y, L, Lr);
+		g.dz = nic(xr.z - xi.z, L, Lr);
+		const T r2 = fma(g.dz, g.dz, fma(g.dy, g.dy, g.dx * g.dx));
+		g.rinv = rsqrt_(r2);
+		g.r = r2 * g.rinv;
+	}
 	const bool cut = within_rmax<T>(sc, g.r, xr, xi);
 	g.in = ok && cut;
 	g.out = ok && !cut;

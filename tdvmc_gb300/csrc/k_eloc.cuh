@@ -422,6 +422,44 @@ __device__ __forceinline__ void fwd_region(const SysConst& sc, int i0, int i1, i
 // the pairs are independent chains for the scheduler.  The table-dependent
 // derivative polynomials stay scalar.  The local coordinate of a pair outside
 // the support (NaN for the self pair) is zeroed before the masks multiply.
+// FP32 distances of two pairs in one f32x2 stream (each half of an f32x2
+// operation rounds as the scalar one does, so sweep_r reproduces r).  FWD, the
+// forward sweeps: pair_r2_f32 (the box length's remainder in r^2) and
+// pair_r_newton; the O_k moments, E_loc and the gradients that the adjoint reads
+// all come from these.  The adjoint sweeps keep the plain minimum image with Lf
+// and r^2 q: at N = 1000, P = 64 on a lattice with a shell of pairs at r_max,
+// dE/d alpha agrees with FP64 to 4e-6 relative either way, and the plain form
+// costs 8 % less adjoint time (measured).
+struct F2Box {
+	f2_t Lr, mL, R, lc;
+};
+__device__ __forceinline__ F2Box f2_box(const SysConst& sc) {
+	const float L = (float)sc.L, Lr = (float)sc.Lr;
+	return F2Box{f2_make(Lr, Lr), f2_make(-L, -L), f2_make(kRoundF, kRoundF), f2_make(sc.lc, sc.lc)};
+}
+template <bool FWD>
+__device__ __forceinline__ f2_t pair_r_f2(const F2Box& b, f2_t& dx, f2_t& dy, f2_t& dz, float& qa, float& qb) {
+	const f2_t kx = f2_sub(f2_fma(dx, b.Lr, b.R), b.R);
+	const f2_t ky = f2_sub(f2_fma(dy, b.Lr, b.R), b.R);
+	const f2_t kz = f2_sub(f2_fma(dz, b.Lr, b.R), b.R);
+	dx = f2_fma(kx, b.mL, dx);
+	dy = f2_fma(ky, b.mL, dy);
+	dz = f2_fma(kz, b.mL, dz);
+	f2_t r2;
+	if (FWD) {
+		const f2_t kd = f2_fma(kz, dz, f2_fma(ky, dy, f2_mul(kx, dx)));
+		r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, f2_mul(kd, b.lc))));
+	} else {
+		r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+	}
+	float ra, rb;
+	f2_split(r2, ra, rb);
+	qa = rsqrt_(ra);
+	qb = rsqrt_(rb);
+	if (!FWD) return f2_mul(r2, f2_make(qa, qb));
+	return f2_make(pair_r_newton(ra, qa), pair_r_newton(rb, qb));
+}
+
 constexpr int kF2 = 2;
 template <int G, int ON, bool ADJ, int HIST>
 __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1, int nrow, bool rowok,
@@ -430,9 +468,9 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
                                               const float* __restrict__ hv, const int* __restrict__ lut,
                                               float* __restrict__ hist, int lane, float pa, float pb,
                                               KSum<float>* acc, KSum<float>& vsum, int& nout) {
-	const float L = (float)sc.L, Lr = (float)sc.Lr;
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
-	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
+	const f2_t R2 = f2_make(kRoundF, kRoundF);
+	const F2Box box = f2_box(sc);
 	const f2_t H2 = f2_make(sc.hf, sc.hf), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
@@ -454,15 +492,8 @@ __device__ __forceinline__ void fwd_region_f2(const SysConst& sc, int i0, int i1
 				f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
 				f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 				f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
-				// minimum image: d - L rint(d / L) (see nic)
-				dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
-				dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
-				dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
-				const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-				float ra, rb;
-				f2_split(r2, ra, rb);
-				const float qa = rsqrt_(ra), qb = rsqrt_(rb);
-				const f2_t r = f2_mul(r2, f2_make(qa, qb));
+				float qa, qb;
+				const f2_t r = pair_r_f2<true>(box, dx, dy, dz, qa, qb);
 				float rA, rB;
 				f2_split(r, rA, rB);
 				const bool okA = haveA && rowok && ia != nrow, okB = haveB && rowok && ib != nrow;
@@ -596,10 +627,11 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
                                                float* __restrict__ hist, float pa, float pb, KSum<float>* own,
                                                float* trav, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum,
                                                float& nearmin) {
-	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const float rmax = (float)sc.rmax;
 	const f2_t RM2 = f2_make(rmax, rmax);
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
-	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
+	const f2_t R2 = f2_make(kRoundF, kRoundF);
+	const F2Box box = f2_box(sc);
 	const f2_t H2 = f2_make(sc.hf, sc.hf), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
@@ -639,14 +671,8 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
 			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
-			dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
-			dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
-			dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
-			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-			float ra, rb;
-			f2_split(r2, ra, rb);
-			const float qa = rsqrt_(ra), qb = rsqrt_(rb);
-			const f2_t r = f2_mul(r2, f2_make(qa, qb));
+			float qa, qb;
+			const f2_t r = pair_r_f2<true>(box, dx, dy, dz, qa, qb);
 			float rA, rB;
 			f2_split(r, rA, rB);
 			const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
@@ -810,16 +836,24 @@ __device__ __forceinline__ void half_block(const SysConst& sc, int sp, int n, in
 
 // The FP32 distance of a pair exactly as the f32x2 sweeps form it (each half of
 // an f32x2 operation rounds like the scalar one), so that a second look at a
-// pair sees the decision the sweep took.
+// pair sees the decision the sweep took; fwd as in pair_r_f2.
 __device__ __forceinline__ float sweep_r(const SysConst& sc, const Q4<float>& a, const Q4<float>& b, float& q,
-                                         float& dx, float& dy, float& dz) {
+                                         float& dx, float& dy, float& dz, bool fwd) {
 	const float L = (float)sc.L, Lr = (float)sc.Lr;
-	dx = nic(__fsub_rn(a.x, b.x), L, Lr);
-	dy = nic(__fsub_rn(a.y, b.y), L, Lr);
-	dz = nic(__fsub_rn(a.z, b.z), L, Lr);
-	const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+	if (!fwd) {
+		dx = nic(__fsub_rn(a.x, b.x), L, Lr);
+		dy = nic(__fsub_rn(a.y, b.y), L, Lr);
+		dz = nic(__fsub_rn(a.z, b.z), L, Lr);
+		const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+		q = rsqrt_(r2);
+		return __fmul_rn(r2, q);
+	}
+	dx = __fsub_rn(a.x, b.x);
+	dy = __fsub_rn(a.y, b.y);
+	dz = __fsub_rn(a.z, b.z);
+	const float r2 = pair_r2_f32(sc.lc, L, Lr, dx, dy, dz);
 	q = rsqrt_(r2);
-	return __fmul_rn(r2, q);
+	return pair_r_newton(r2, q);
 }
 // interval and local coordinate as the f32x2 sweeps form them (equal widths)
 __device__ __forceinline__ int sweep_t(const SysConst& sc, float r, const float* kb, const float* hv, const int* lut,
@@ -863,7 +897,7 @@ __device__ __noinline__ FixTerms half_block_fix(SysConst sc, int sp, int n, int 
 		if (DIAG && !(i < n && (k < 16 || (k == 16 && lane < 16)))) continue;
 		const Q4<float> xi = xs[i];
 		float q, dx, dy, dz;
-		const float r = sweep_r(sc, xr, xi, q, dx, dy, dz);
+		const float r = sweep_r(sc, xr, xi, q, dx, dy, dz, true);
 		if (!(fabsf(__fsub_rn(r, rmax)) < sc.rcut_band)) continue;
 		const bool in32 = r <= rmax;
 		if (cut_fp64(sc, xr, xi) == in32) continue;
@@ -917,7 +951,7 @@ __device__ __noinline__ void rev_region_fix(SysConst sc, int i0, int i1, int nro
 		}
 		const Q4<float> xi = xs[i];
 		float q, dx, dy, dz;
-		const float r = sweep_r(sc, xr, xi, q, dx, dy, dz);
+		const float r = sweep_r(sc, xr, xi, q, dx, dy, dz, false);
 		if (!(fabsf(__fsub_rn(r, rmax)) < sc.rcut_band)) continue;
 		const bool in32 = r <= rmax;
 		if (cut_fp64(sc, xr, xi) == in32) continue;
@@ -992,10 +1026,11 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
                                               const float* __restrict__ kb, const float* __restrict__ hv,
                                               const int* __restrict__ lut, float* __restrict__ hist, int lane,
                                               float& nearmin) {
-	const float rmax = (float)sc.rmax, L = (float)sc.L, Lr = (float)sc.Lr;
+	const float rmax = (float)sc.rmax;
 	const f2_t RM2 = f2_make(rmax, rmax);
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
-	const f2_t Lr2 = f2_make(Lr, Lr), mL2 = f2_make(-L, -L), R2 = f2_make(kRoundF, kRoundF);
+	const f2_t R2 = f2_make(kRoundF, kRoundF);
+	const F2Box box = f2_box(sc);
 	const f2_t H2 = f2_make(sc.hf, sc.hf), mh2 = f2_make(-0.5f, -0.5f);
 	const float dm1 = (float)(sc.dim - 1);
 	const f2_t dm12 = f2_make(dm1, dm1);
@@ -1031,14 +1066,8 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			f2_t dx = f2_sub(X2, f2_make(pA.x, pB.x));
 			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
-			dx = f2_fma(f2_sub(f2_fma(dx, Lr2, R2), R2), mL2, dx);
-			dy = f2_fma(f2_sub(f2_fma(dy, Lr2, R2), R2), mL2, dy);
-			dz = f2_fma(f2_sub(f2_fma(dz, Lr2, R2), R2), mL2, dz);
-			const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-			float ra, rb;
-			f2_split(r2, ra, rb);
-			const float qa = rsqrt_(ra), qb = rsqrt_(rb);
-			const f2_t r = f2_mul(r2, f2_make(qa, qb));
+			float qa, qb;
+			const f2_t r = pair_r_f2<false>(box, dx, dy, dz, qa, qb);
 			float rA, rB;
 			f2_split(r, rA, rB);
 			const bool onA = haveA && rowok && (rA <= rmax) && ((DIAG && !ROT) ? (ia < nrow) : true);

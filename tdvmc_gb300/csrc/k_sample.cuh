@@ -55,6 +55,16 @@ __device__ __forceinline__ T pair_u(const SysConst& sc, T r2, const Q4<T>* __res
 	return c.x + tau * (c.y + tau * (c.z + tau * c.w));
 }
 
+// The samplers hold the particles of a walker in register slots of G lanes
+// (particle s*G + lane in slot s), compiled for a few slot counts, so the
+// slots past n (a partial slot, and whole slots where the count was rounded
+// up) hold no particle.  They hold a phantom three box lengths away on every
+// axis instead: per axis min(|d|, L - |d|) is then below -1.5 L, so its
+// distance to any position in the box exceeds r_max (at most L/2), both of its
+// pair terms in a move read the constant outer-pair entry, and they cancel
+// exactly in the move's difference (u - u with finite tau).
+constexpr float kPhantomBoxes = 3.0f;
+
 // squared minimum-image distance of two positions inside [-L/2, L/2]:
 // per axis min(|d|, L - |d|), exact for |d| <= L (Sterbenz)
 template <typename T>
@@ -117,12 +127,13 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 #pragma unroll
 		for (int s = 0; s < SLOTS; s++) {
 			int i = s * G + lane;
-			x[s] = y[s] = z[s] = T(0);
+			// slots past n hold the phantom (see kPhantomBoxes)
+			x[s] = y[s] = z[s] = (T)kPhantomBoxes * L;
 			if (i < n) {
 				// positions into [-L/2, L/2] (AlignCoordinates, TDVMC.cpp:2569-2582)
 				x[s] = nic(pw[i], L, Lr);
-				if (sc.dim > 1) y[s] = nic(pw[n + i], L, Lr);
-				if (sc.dim > 2) z[s] = nic(pw[2 * n + i], L, Lr);
+				y[s] = sc.dim > 1 ? nic(pw[n + i], L, Lr) : T(0);
+				z[s] = sc.dim > 2 ? nic(pw[2 * n + i], L, Lr) : T(0);
 				xs[i] = Q4<T>{x[s], y[s], z[s], T(0)};
 			}
 		}
@@ -312,15 +323,16 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 		bool inside = true;
 #pragma unroll
 		for (int k = 0; k < NP; k++) {
-			float x[2] = {0.f, 0.f}, y[2] = {0.f, 0.f}, z[2] = {0.f, 0.f};
+			const float ph = kPhantomBoxes * L;  // slots past n hold the phantom (see kPhantomBoxes)
+			float x[2] = {ph, ph}, y[2] = {ph, ph}, z[2] = {ph, ph};
 #pragma unroll
 			for (int h = 0; h < 2; h++) {
 				const int i = (2 * k + h) * G + lane;
 				if (2 * k + h < SLOTS && i < n) {
 					// positions into [-L/2, L/2] (AlignCoordinates, TDVMC.cpp:2569-2582)
 					x[h] = nic(pw[i], L, Lr);
-					if (sc.dim > 1) y[h] = nic(pw[n + i], L, Lr);
-					if (sc.dim > 2) z[h] = nic(pw[2 * n + i], L, Lr);
+					y[h] = sc.dim > 1 ? nic(pw[n + i], L, Lr) : 0.f;
+					z[h] = sc.dim > 2 ? nic(pw[2 * n + i], L, Lr) : 0.f;
 					inside = inside && fabsf(x[h]) <= half && fabsf(y[h]) <= half && fabsf(z[h]) <= half;
 					xs[i] = Q4<float>{x[h], y[h], z[h], 0.f};
 				}

@@ -795,7 +795,8 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	s.Lr = 1.0 / d->box_length;
 	s.hbar2_2m = d->hbar2_2m;
 	s.pot_kind = d->pot_kind;
-	if (s.ns - 2 != P || s.nbin > kMaxBins) {
+	// r_max below 1.5 L: the samplers' phantom slots (kPhantomBoxes) lie beyond it
+	if (s.ns - 2 != P || s.nbin > kMaxBins || !(s.rmax < 1.5 * s.L)) {
 		delete ctx;
 		return TDVMC_ERR_ARG;
 	}
@@ -826,11 +827,12 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	s.hinv = hv[0];
 	s.hf = (float)s.hinv;
 	s.hf_lo = (float)(s.hinv - (double)s.hf);
-	// the FP32 distance of an FP32 pair is within about 3.5e-7 (relative) of its FP64
-	// distance (the rounding of the differences, of r^2, of r^2 times the hardware
-	// reciprocal square root, whose relative error is below 2^-22.9); the band of
-	// 1e-6 keeps a margin of about three
+	// the FP32 distance of an FP32 pair is within about 2.5e-7 (relative) of its FP64
+	// distance (the rounding of the differences and of r^2, the first-order box
+	// remainder, the Newton-refined square root); the band of 1e-6 keeps a margin of
+	// about four
 	s.rcut_band = (float)(s.rmax * 1e-6);
+	s.lc = (float)(-2.0 * (s.L - (double)(float)s.L));
 	std::vector<int> lut;
 	if (!s.uniform) {
 		const double span = s.rmax - kb[0];

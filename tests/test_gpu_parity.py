@@ -337,6 +337,49 @@ def test_adjoint_driven_imaginary_time_step_matches_oracle_fp64():
     assert relmax(dR0, dR) > 1e-9
 
 
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed-scalar"])
+@pytest.mark.parametrize("dim,n", [(1, 20), (2, 40), (3, 150), (3, 300)])
+def test_sampler_padded_slots_follow_oracle_chain(dim, n, mode):
+    """Particle counts whose register slots run past n (the slot count is rounded
+    up to a compiled one: N = 20 on 8 lanes in 4 slots, 40 on 16 lanes in 4, 150
+    on 32 lanes in 8, 300 on 32 lanes in 11) in 1D, 2D and 3D.  FP64: the chain
+    equals the oracle's (same Philox stream; positions 1e-9, identical
+    acceptance).  FP32, packed and scalar samplers: the same moves on at least
+    90 % of the walkers (a decision within FP32 rounding of its threshold may
+    send a walker its own way), positions within 1e-4, acceptance within 1 %."""
+    import tdvmc_gb300 as T
+    precision = "fp64" if mode == "fp64" else "mixed"
+    L = (n / 0.5) ** (1.0 / dim)
+    nw, p, moves, step = 32, 10, 2 * n, 0.5
+    rng = np.random.default_rng(100 * dim + n)
+    uR, uI = 0.3 * rng.normal(size=p), 0.1 * rng.normal(size=p)
+    R0 = rng.uniform(-L / 2, L / 2, size=(nw, dim, n))
+    if precision == "mixed":
+        R0 = R0.astype(np.float32).astype(np.float64)
+    if mode == "mixed-scalar":
+        os.environ["TDVMC_SAMPLER"] = "scalar"
+    try:
+        s = T.BosonsBulk(dim, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", precision=precision)
+    finally:
+        os.environ.pop("TDVMC_SAMPLER", None)
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R0)
+    acc = s.DoMetropolisSteps(moves, step, seed=21, pass_id=4)
+    Rg = s.GetWalkers()
+    s.close()
+    o = orc.OracleSystem(dim, n, p, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0))
+    Ro = np.ascontiguousarray(R0.copy())
+    acc_o = o.sample(uR, Ro, moves, step, seed=21, pass_id=4)
+    assert 0.1 < acc_o / (moves * nw) < 0.95
+    if precision == "fp64":
+        assert acc == acc_o
+        assert np.abs(Rg - Ro).max() < 1e-9
+    else:
+        d = np.abs(Rg - Ro).reshape(nw, -1).max(1)
+        assert (d < 1e-4).mean() >= 0.9, d
+        assert abs(acc - acc_o) <= 0.01 * acc_o, (acc, acc_o)
+
+
 def test_packed_sampler_follows_scalar_chain_mixed():
     """The f32x2 FP32 sampler (uniform knots) walks the scalar FP32 sampler's
     chain bit for bit: same Philox stream and update arithmetic, and every pair
