@@ -300,11 +300,15 @@ def run_c5(sync, imag_steps, real_steps, timed_steps, check_every=10, nw=C5_NW, 
     t0 = time.perf_counter()
     ti = T.TDVP(s0, C5_DT_IMAG, 2 * C5_N, C5_STEP, seed=5, imaginary_time=1, use_adjoint=2)
     e_imag = []
+    sync()
+    t_imag = time.perf_counter()
     for k in range(imag_steps):
         out = ti.step(1)
         e_imag.append(out["energy"][0] / C5_N)
         if log:
             log("imag step %d E/N %.6f acc %.3f status %d" % (k, e_imag[-1], out["accept_rate"], out["status"]))
+    sync()
+    t_imag = time.perf_counter() - t_imag
     gp = s0.GetParameters()
     Rq = s0.GetWalkers() * (L1 / L0)
     s0.close()
@@ -315,15 +319,20 @@ def run_c5(sync, imag_steps, real_steps, timed_steps, check_every=10, nw=C5_NW, 
     del Rq
     tr = T.TDVP(s1, C5_DT, 2 * C5_N, C5_STEP, seed=6, use_adjoint=1)
     e_real = []
+    t_real, t_gate = time.perf_counter(), 0.0
     for k in range(real_steps - timed_steps):
         out = tr.step(1)
         e_real.append(out["energy"][0] / C5_N)
         if check_every and (k + 1) % check_every == 0:
+            t_g = time.perf_counter()
             g = c5_gate(s1, L1, min(C5_CHECK_WALKERS, nw))
+            t_gate += time.perf_counter() - t_g
             gates.append({"step": k + 1, "dE_per_N": g})
             if log:
                 log("real step %d E/N %.6f acc %.3f status %d gate %.2e"
                     % (k + 1, e_real[-1], out["accept_rate"], out["status"], g))
+    sync()
+    t_real = time.perf_counter() - t_real - t_gate
     ms_timed = None
     if timed_steps > 0:
         sync()
@@ -332,6 +341,9 @@ def run_c5(sync, imag_steps, real_steps, timed_steps, check_every=10, nw=C5_NW, 
            "rho": [C5_RHO, C5_RHO_Q], "dt_imag": C5_DT_IMAG, "dt": C5_DT, "moves_per_stage": 2 * C5_N,
            "energy_per_particle_imag": e_imag[-3:], "energy_per_particle_real": e_real[-3:],
            "gates": gates, "gate_pass": bool(all(g["dE_per_N"] < 1e-5 for g in gates)),
+           "gate_walkers": min(C5_CHECK_WALKERS, nw),
+           "imag_steps_per_s_wall": imag_steps / t_imag if imag_steps else None,
+           "real_steps_per_s_wall": (real_steps - timed_steps) / t_real if real_steps > timed_steps else None,
            "wall_s": time.perf_counter() - t0}
     if ms_timed is not None:
         res["value"] = timed_steps / (ms_timed / 1000.0)
@@ -571,7 +583,7 @@ def run_workload(args):
     else:
         def log(msg):
             print(msg, file=sys.stderr, flush=True)
-        out = run_c5(sync, 50, 200, 0, check_every=10, log=log)
+        out = run_c5(sync, 50, 200, 10, check_every=10, log=log)
         out["workload"] = ("3D N=1000 LJ bosons rho=0.365, P=64, 262144 walkers: 50 imaginary-time steps "
                            "(adjoint force), quench to rho=0.40, 200 real-time RK4 steps dt=2.5e-4")
     print(json.dumps(out))
