@@ -4,7 +4,7 @@ Tolerances (stated per test):
   RK4 / predictor-corrector on stored samples, mixed vs FP64 with fixed walkers:
       parameter increments 2e-4 of their largest magnitude;
   stored vs direct evaluation at the same walkers and parameters: FP64
-      relative 1e-11, mixed 2e-5 on ln psi, O_k, E_loc, the kinetic sums and
+      relative 1e-11, mixed 1e-5 on ln psi, O_k, E_loc, the kinetic sums and
       dE/d alpha (scaled by the largest magnitude of each quantity);
   RK4 on stored samples vs the FP64 oracle (sampling at the first stage,
       evaluation of the fixed samples at the three others, a rotating
@@ -34,7 +34,7 @@ def soa(cfgs):
     return np.ascontiguousarray(np.transpose(np.asarray(cfgs), (0, 2, 1)))
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 2e-5)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
 @pytest.mark.parametrize("golden,pot", [("eval_d3_n343_p30", "square"), ("eval_d2_n64_k20", "lj"),
                                         ("eval_d1_n20_p10", "gauss")])
 def test_stored_eval_matches_direct_eval(precision, tol, golden, pot):
@@ -101,7 +101,7 @@ def test_stored_eval_n1000_tracks_direct():
         assert relmax(out["mixed"][1][key], truth[key]) < 1e-5, (key, relmax(out["mixed"][1][key], truth[key]))
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 2e-5)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
 def test_stored_eval_more_than_32_splines(precision, tol):
     """P = 40 (42 splines, more than the FP32 evaluation keeps as register sums):
     the stored evaluation with 16-byte loads over particles, N = 45 (two
