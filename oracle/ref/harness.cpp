@@ -323,8 +323,18 @@ static void cmd_additional()
 	}
 }
 
+// the reference's own entry point (src/TDVMC.cpp main, renamed by build_ref.sh)
+int tdvmc_reference_main(int argc, char** argv);
+
 int main(int argc, char** argv)
 {
+	// "--run <config file>": the reference's full program on that config (its time
+	// loop and output files), as main(argc = 2) runs it (TDVMC.cpp:4307 ff.)
+	if (argc > 2 && string(argv[1]) == "--run")
+	{
+		char* args[2] = {argv[0], argv[2]};
+		return tdvmc_reference_main(2, args);
+	}
 	configDirectory = argc > 1 ? string(argv[1]) : string("./");
 	OUT_DIR = "./";
 	string cmd;

@@ -6,7 +6,11 @@ reference C++ sources of mathiasgartner/TDVMC linked with
 outputs as ``.npz`` files.  Needs the reference checkout (default
 ``/root/reference``); the fixtures are committed so the tests never need it.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference] [obs | driver]
+
+The driver fixture (``driver_d3_n27/``) holds the output files of the
+reference's full program on a small config, for the host driver's file
+format and values.
 """
 from __future__ import annotations
 
@@ -120,13 +124,63 @@ def observables(ref_root):
         print("observables", c["name"], np.array(gr).shape, np.array(sk).shape)
 
 
+# The reference's full program on a small 3D config (imaginary-time RK4, three
+# written steps): its output files, as the host driver's files are compared with.
+DRIVER_CONFIG = {
+    "CONFIG_VERSION": "0.24", "SYSTEM_TYPE": "BosonsBulk", "OUT_DIR_SUFFIX": "", "N": 27, "LBOX": 3.6, "DIM": 3,
+    "N_PARAM": 10, "RHO": 1.0, "RC": 0.0, "MC_STEP": 0.3, "MC_STEP_OFFSET": 0.0, "MC_NSTEPS": 8192,
+    "MC_NTHERMSTEPS": 54, "MC_NINITIALIZATIONSTEPS": 0, "MC_VERY_FIRST_NINITIALIZATIONSTEPS": 270,
+    "MC_NADDITIONALSTEPS": 0, "MC_NADDITIONALTHERMSTEPS": 0, "MC_NADDITIONALINITIALIZATIONSTEPS": 0,
+    "TIMESTEP": 0.001, "TOTALTIME": 0.0025, "IMAGINARY_TIME": 1, "ODE_SOLVER_TYPE": 2,
+    "LINEAR_EQUATION_SOLVER_TYPE": 0, "USE_PRECONDITIONING": 0, "USE_PARAMETER_ACCEPTANCE_CHECK": 0,
+    "PARAMETER_ACCEPTANCE_CHECK_TYPE": 0, "WRITE_EVERY_NTH_STEP_TO_FILE": 1,
+    "CALCULATE_ADDITIONAL_DATA_EVERY_NTH_STEP": 1000000, "WRITE_SINGLE_FILES": 0,
+    "MC_NSTEP_MULTIPLICATION_FACTOR_FOR_WRITE_DATA": 1, "USE_MEAN_FOR_FINAL_PARAMETERS": 0, "USE_NORMALIZE_WF": 1,
+    "USE_ADJUST_PARAMETERS": 0, "UPDATE_SAMPLES_EVERY_NTH_STEP": 0, "UPDATE_SAMPLES_PERCENT": 100.0,
+    "GR_BIN_COUNT": 50, "USE_NURBS": 0, "NURBS_GRID": [0.0], "PARTICLE_TYPES": [0], "SYSTEM_PARAMS": [0.6, 1.0],
+    "PARAMS_REAL": [-2.0, -2.0, -1.0, -0.5, -0.2, -0.1, -0.05, 0.0, 0.0, 0.0], "PARAMS_IMAGINARY": [0.0] * 10,
+    "PARAM_PHIR": 0.0, "PARAM_PHII": 0.0,
+}
+DRIVER_FILES = ("LocalEnergyR", "LocalEnergyI", "ParametersR", "ParametersI", "OtherExpectationValues",
+                "LocalOperators", "timesSystem")
+
+
+def driver_run(ref_root):
+    """Runs the reference program (``ref_harness --run``) on DRIVER_CONFIG in a
+    scratch directory that also holds the k-vector tables it reads from the
+    config's directory, and keeps the config and the output files above."""
+    import json
+    import shutil
+    import tempfile
+    dst = os.path.join(HERE, "driver_d3_n27")
+    os.makedirs(dst, exist_ok=True)
+    with open(os.path.join(dst, "run.config"), "w") as f:
+        json.dump(DRIVER_CONFIG, f, indent=1)
+    with tempfile.TemporaryDirectory() as tmp:
+        for name in ("kVectors3D.json", "kNorm3D.csv"):
+            os.symlink(os.path.join(ref_root, "config", name), os.path.join(tmp, name))
+        cfg = dict(DRIVER_CONFIG, OUTPUT_DIRECTORY=tmp + "/out/")
+        os.makedirs(cfg["OUTPUT_DIRECTORY"])
+        with open(os.path.join(tmp, "run.config"), "w") as f:
+            json.dump(cfg, f, indent=1)
+        subprocess.run([HARNESS, "--run", os.path.join(tmp, "run.config")], check=True, capture_output=True)
+        (sub,) = os.listdir(cfg["OUTPUT_DIRECTORY"])
+        for name in DRIVER_FILES:
+            shutil.copy(os.path.join(cfg["OUTPUT_DIRECTORY"], sub, name + ".dat"), os.path.join(dst, name + ".dat"))
+    print("driver run", sub)
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != "obs" else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] not in ("obs", "driver") else "/root/reference"
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root])
     if "obs" in sys.argv[1:]:
         observables(ref_root)
         return
+    if "driver" in sys.argv[1:]:
+        driver_run(ref_root)
+        return
+    driver_run(ref_root)
     observables(ref_root)
 
     # ---- NIC known answers (the reference's own unit test vectors) ----
