@@ -212,13 +212,21 @@ void append_line(const std::string& name, const std::vector<double>& v) {
 	f << "\n";
 }
 
-void write_table(const std::string& name, const std::string& header, const std::vector<std::vector<double>>& rows) {
+// A file of one header line and rows (every nth row from the nth on): a single
+// header as its own line, several as 24-wide columns (Utils.cpp:809-858).
+void write_table(const std::string& name, const std::vector<std::string>& header,
+                 const std::vector<std::vector<double>>& rows, int nth = 1) {
 	std::ofstream f(g_out + name + ".dat");
 	f.precision(15);
 	f << std::scientific;
-	f << std::setw(24) << header << "\n";
-	for (auto& r : rows) {
-		for (double x : r) f << std::setw(24) << x;
+	if (header.size() == 1) {
+		f << header[0];
+	} else {
+		for (auto& h : header) f << std::setw(24) << h;
+	}
+	f << "\n";
+	for (size_t i = (size_t)nth - 1; i < rows.size(); i += (size_t)nth) {
+		for (double x : rows[i]) f << std::setw(24) << x;
 		f << "\n";
 	}
 }
@@ -409,6 +417,25 @@ int main(int argc, char** argv) {
 	uI.resize(P, 0.0);
 	double phiR = cfg.num("PARAM_PHIR", 0.0), phiI = cfg.num("PARAM_PHII", 0.0);
 	if ((rc = tdvmc_set_params(ctx, uR.data(), uI.data(), phiR, phiI))) return die("tdvmc_set_params", rc);
+	{
+		// start parameters, one per line, and the per-step files with their headers
+		// (TDVMC.cpp:3117-3128)
+		std::vector<std::vector<double>> cR, cI;
+		for (int k = 0; k < P; k++) {
+			cR.push_back({uR[k]});
+			cI.push_back({uI[k]});
+		}
+		write_table("ParametersR0", {"uR_k..."}, cR);
+		write_table("ParametersI0", {"uI_k..."}, cI);
+		const std::vector<std::vector<double>> none;
+		write_table("LocalEnergyR", {"E^R"}, none);
+		write_table("LocalEnergyI", {"E^I"}, none);
+		write_table("LocalOperators", {"<O_k>..."}, none);
+		write_table("OtherExpectationValues", {"kinetic, potential, wf, g(r)"}, none);
+		write_table("ParametersR", {"uR_k..."}, none);
+		write_table("ParametersI", {"uI_k..."}, none);
+		write_table("times", {"t"}, none);
+	}
 
 	// initial walkers (InitCoordinateConfiguration, TDVMC.cpp:672-785): the last line of
 	// coords/particleconfiguration_<N>_<DIM>D_<k>.csv for k = 0, 1, ... (walker w takes
@@ -449,6 +476,8 @@ int main(int argc, char** argv) {
 			}
 		}
 	}
+	// the start configuration (of walker 0), as the reference writes its chain's (TDVMC.cpp:3095-3098)
+	write_positions(g_out + "particleconfiguration.dat", x0, 0, N, DIM);
 	int64_t acc = 0;
 	uint32_t restarts = 0;
 	// walkers from their initial configuration, thermalised (also after a set-back)
@@ -627,15 +656,19 @@ int main(int argc, char** argv) {
 			if ((rc = init_walkers())) return die("walkers after the set-back", rc);
 		}
 	}
-	write_table("AllLocalEnergyR", "ER", allER);
-	write_table("AllLocalEnergyI", "EI", allEI);
-	write_table("AllLocalOperators", "<O_k>", allO);
-	write_table("AllOtherExpectationValues", "kinetic", allOther);
-	write_table("AllParametersR", "uR_k", allPR);
-	write_table("AllParametersI", "uI_k", allPI);
+	// the run's series (TDVMC.cpp:3939-3953)
+	for (int nth : {1, 100}) {
+		const std::string sfx = nth == 1 ? "" : "_every100th";
+		write_table("AllLocalEnergyR" + sfx, {"ER"}, allER, nth);
+		write_table("AllLocalEnergyI" + sfx, {"EI"}, allEI, nth);
+		write_table("AllLocalOperators" + sfx, {"<O_k>", "..."}, allO, nth);
+		write_table("AllOtherExpectationValues" + sfx, {"kinetic", "potential", "wf", "g(r)"}, allOther, nth);
+		write_table("AllParametersR" + sfx, {"uR_k", "..."}, allPR, nth);
+		write_table("AllParametersI" + sfx, {"uI_k", "..."}, allPI, nth);
+	}
 	std::vector<std::vector<double>> tt;
 	for (double t : times) tt.push_back({t});
-	write_table("Alltimes", "t", tt);
+	write_table("Alltimes", {"t"}, tt);
 
 	// files for successive runs (TDVMC.cpp:4010-4034)
 	std::vector<double> xf((size_t)walkers * DIM * N);

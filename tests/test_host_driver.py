@@ -122,3 +122,35 @@ def test_check_type_2_rejects_large_changes(driver, tmp_path):
 def test_unimplemented_check_type_is_refused(driver, tmp_path):
     r, _, _ = run(driver, tmp_path, base_cfg(USE_PARAMETER_ACCEPTANCE_CHECK=1, PARAMETER_ACCEPTANCE_CHECK_TYPE=3))
     assert r.returncode == 2 and "PARAMETER_ACCEPTANCE_CHECK_TYPE 3" in r.stderr
+
+
+def test_output_files_have_the_reference_layout(driver, tmp_path):
+    """The driver on the config of tests/golden/driver_d3_n27 (the reference's
+    own program run on it, tests/golden/make_golden.py): every file the fixture
+    holds comes out with the same header line, the same number of rows and
+    columns, and every number in the reference's 24-wide %.15e layout
+    (Utils.cpp:809-858); the start-parameter files equal the reference's."""
+    import re
+    gold = os.path.join(ROOT, "tests", "golden", "driver_d3_n27")
+    cfg = json.load(open(os.path.join(gold, "run.config")))
+    r, out, _ = run(driver, tmp_path, cfg)
+    assert r.returncode == 0, r.stderr
+    num = re.compile(r"^( {2,3}-?\d\.\d{15}e[+-]\d{2})+$")
+    for name in sorted(os.listdir(gold)):
+        if not name.endswith(".dat"):
+            continue
+        ref = open(os.path.join(gold, name)).read().splitlines()
+        got = open(out / name).read().splitlines()
+        assert len(got) == len(ref), name
+        has_header = name != "timesSystem.dat"
+        if has_header:
+            assert got[0] == ref[0], (name, got[0], ref[0])
+        for a, b in zip(got[int(has_header):], ref[int(has_header):]):
+            assert num.match(a) and len(a) == len(b), (name, a, b)
+    for name in ("ParametersR0.dat", "ParametersI0.dat", "times.dat"):
+        assert (out / name).exists(), name
+    assert open(out / "ParametersR0.dat").read().splitlines()[0] == "uR_k..."
+    p0 = np.loadtxt(out / "ParametersR0.dat", skiprows=1)
+    assert np.array_equal(p0, np.asarray(cfg["PARAMS_REAL"]))
+    assert open(out / "AllParametersR.dat").read().splitlines()[0] == "%24s%24s" % ("uR_k", "...")
+    assert open(out / "AllLocalEnergyR.dat").read().splitlines()[0] == "ER"
