@@ -105,26 +105,41 @@ def test_stored_eval_n1000_tracks_direct():
 def test_stored_eval_more_than_32_splines(precision, tol):
     """P = 40 (42 splines, more than the FP32 evaluation keeps as register sums):
     the stored evaluation with 16-byte loads over particles, N = 45 (two
-    32-particle chunks, the second mostly padding), equal-width knots."""
+    32-particle chunks, the second mostly padding), equal-width knots.  FP64:
+    stored equals direct at 1e-11.  Mixed, on FP32-representable walkers: the
+    stored and the direct evaluation each match the FP64 evaluation at 1e-5."""
     import tdvmc_gb300 as T
     dim, n, p, L = 3, 45, 40, 4.2
     nw = 96
     rng = np.random.default_rng(5)
-    R = rng.uniform(0.0, L, size=(nw, dim, n))
-    s = T.BosonsBulk(dim, n, p, L, nw, system_params=(0.5, 2.0), potential="gauss", hbar2_2m=0.09,
-                     precision=precision)
+    R = rng.uniform(0.0, L, size=(nw, dim, n)).astype(np.float32).astype(np.float64)
     uR = -0.3 * np.exp(-np.linspace(0.0, 3.0, p)) + 0.01 * rng.normal(size=p)
     uI = 0.02 * rng.normal(size=p)
-    s.SetParameters(uR, uI)
-    s.SetWalkers(R)
-    s.FillCorrelatedSamplingData()
-    for k, (a, b) in enumerate([(uR, uI), (1.2 * uR - 0.01, 0.7 * uI + 0.01)]):
-        s.SetParameters(a, b)
-        got = s.CalculateExpectationValuesForStoredSamples(adjoint=True)
-        ref = s.CalculateExpectationValues()
-        ref["dE"] = s.CalculateLocalEnergyAdjoint()
+    pars = [(uR, uI), (1.2 * uR - 0.01, 0.7 * uI + 0.01)]
+    out = {}
+    for prec in sorted({precision, "fp64"}):
+        s = T.BosonsBulk(dim, n, p, L, nw, system_params=(0.5, 2.0), potential="gauss", hbar2_2m=0.09,
+                         precision=prec)
+        s.SetParameters(uR, uI)
+        s.SetWalkers(R)
+        s.FillCorrelatedSamplingData()
+        out[prec] = []
+        for a, b in pars:
+            s.SetParameters(a, b)
+            got = s.CalculateExpectationValuesForStoredSamples(adjoint=True)
+            ref = s.CalculateExpectationValues()
+            ref["dE"] = s.CalculateLocalEnergyAdjoint()
+            out[prec].append((got, ref))
+        s.close()
+    for k in range(len(pars)):
+        got, ref = out[precision][k]
+        truth = out["fp64"][k][1]
         for key in ("lnpsi", "O", "eloc", "other", "dE"):
-            assert relmax(got[key], ref[key]) < tol, (k, key, relmax(got[key], ref[key]))
+            if precision == "fp64":
+                assert relmax(got[key], ref[key]) < tol, (k, key, relmax(got[key], ref[key]))
+            else:
+                assert relmax(got[key], truth[key]) < tol, (k, key, relmax(got[key], truth[key]))
+                assert relmax(ref[key], truth[key]) < tol, (k, key, relmax(ref[key], truth[key]))
 
 
 def test_stored_sample_rk4_matches_oracle_fp64():
