@@ -23,6 +23,8 @@ int sample_slots_for(int n, int lanes);
 SampleFn<float> pick_sample_f32(int lanes, int slots);
 // FP32, uniform knots: packed f32x2 pair arithmetic (null where not instantiated)
 SampleFn<float> pick_sample_f32_packed(int lanes, int slots);
+// the same with the lane's coordinates in shared memory (null where not instantiated)
+SampleFn<float> pick_sample_f32_packed_shared(int lanes, int slots);
 SampleFn<double> pick_sample_f64(int lanes, int slots);
 ElocFn<float> pick_eloc_f32(int lanes, bool adj, int hist);
 ElocFn<double> pick_eloc_f64(int lanes, bool adj, int hist);

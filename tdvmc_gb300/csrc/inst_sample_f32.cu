@@ -16,6 +16,23 @@ int sample_slots_for(int n, int G) {
 	return -1;
 }
 
+SampleFn<float> pick_sample_f32_packed_shared(int G, int slots) {
+	if (G == 32) {
+		switch (slots) {
+		case 8: return k_sample_f2<32, 8, true>;
+		case 11: return k_sample_f2<32, 11, true>;
+		case 16: return k_sample_f2<32, 16, true>;
+		case 32: return k_sample_f2<32, 32, true>;
+		}
+	} else if (G == 16) {
+		switch (slots) {
+		case 16: return k_sample_f2<16, 16, true>;
+		case 22: return k_sample_f2<16, 22, true>;
+		}
+	}
+	return nullptr;
+}
+
 SampleFn<float> pick_sample_f32_packed(int G, int slots) {
 	if (G == 32) {
 		switch (slots) {
@@ -25,6 +42,7 @@ SampleFn<float> pick_sample_f32_packed(int G, int slots) {
 		case 8: return k_sample_f2<32, 8>;
 		case 11: return k_sample_f2<32, 11>;
 		case 16: return k_sample_f2<32, 16>;
+		case 32: return k_sample_f2<32, 32, true>;
 		}
 	} else if (G == 16) {
 		switch (slots) {

@@ -272,8 +272,13 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 // with a coordinate outside [-L/2, L/2] after wrapping (non-finite or too large
 // to wrap exactly) makes no moves, as in the scalar sampler where every
 // quotient of such a walker is rejected, and a proposal outside is rejected.
-template <int G, int SLOTS>
-__global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
+//
+// CS (coordinates in shared memory): the lane's own coordinates are read from
+// the shared mirror at each move (two 16-byte loads per slot pair) instead of
+// being held in registers, for slot counts whose coordinates would not fit in
+// registers (32 slots: 96 registers); same arithmetic, same chain.
+template <int G, int SLOTS, bool CS = false>
+__global__ void __launch_bounds__(128, CS ? (SLOTS > 16 ? 3 : 4) : (SLOTS <= 11 ? 5 : 3)) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
                                                    const float* __restrict__ uout_g, const float* __restrict__ kb_g,
                                                    const float* __restrict__ hv_g, const int* __restrict__ lut_g,
                                                    float* __restrict__ pos, int64_t nw, int64_t nw_total,
@@ -319,11 +324,22 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 		// own particles in slot pairs (slot s: pair s / 2, half s % 2), so the
 		// differences of two slots to a moving particle are one f32x2 subtraction
 		constexpr int NP = (SLOTS + 1) / 2;
-		f2_t PX[NP], PY[NP], PZ[NP];
+		constexpr int NR = CS ? 1 : NP;  // register slot pairs
+		f2_t PX[NR], PY[NR], PZ[NR];
 		bool inside = true;
+		const float ph = kPhantomBoxes * L;
+		if (CS) {
+			for (int i = lane; i < n; i += G) {
+				const float x = nic(pw[i], L, Lr);
+				const float y = sc.dim > 1 ? nic(pw[n + i], L, Lr) : 0.f;
+				const float z = sc.dim > 2 ? nic(pw[2 * n + i], L, Lr) : 0.f;
+				inside = inside && fabsf(x) <= half && fabsf(y) <= half && fabsf(z) <= half;
+				xs[i] = Q4<float>{x, y, z, 0.f};
+			}
+		}
 #pragma unroll
-		for (int k = 0; k < NP; k++) {
-			const float ph = kPhantomBoxes * L;  // slots past n hold the phantom (see kPhantomBoxes)
+		for (int k = 0; k < (CS ? 0 : NP); k++) {
+			// slots past n hold the phantom (see kPhantomBoxes)
 			float x[2] = {ph, ph}, y[2] = {ph, ph}, z[2] = {ph, ph};
 #pragma unroll
 			for (int h = 0; h < 2; h++) {
@@ -337,9 +353,9 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 					xs[i] = Q4<float>{x[h], y[h], z[h], 0.f};
 				}
 			}
-			PX[k] = f2_make(x[0], x[1]);
-			PY[k] = f2_make(y[0], y[1]);
-			PZ[k] = f2_make(z[0], z[1]);
+			PX[CS ? 0 : k] = f2_make(x[0], x[1]);
+			PY[CS ? 0 : k] = f2_make(y[0], y[1]);
+			PZ[CS ? 0 : k] = f2_make(z[0], z[1]);
 		}
 		const bool walker_ok = __all_sync(gmask, inside);
 		__syncwarp(gmask);
@@ -368,22 +384,33 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 				float dsum = 0.f;
 				const f2_t N0 = f2_make(xn0, xn0), N1 = f2_make(xn1, xn1), N2 = f2_make(xn2, xn2);
 				const f2_t O0 = f2_make(xo.x, xo.x), O1 = f2_make(xo.y, xo.y), O2 = f2_make(xo.z, xo.z);
+				f2_t CX, CY, CZ;  // CS: the slot pair's coordinates, loaded at its first slot
 #pragma unroll
 				for (int s = 0; s < SLOTS; s++) {
+					if (CS && (s & 1) == 0) {
+						const int i0 = s * G + lane, i1 = i0 + G;
+						const Q4<float> c0 = xs[i0 < n ? i0 : 0];
+						const Q4<float> c1 = xs[i1 < n ? i1 : 0];
+						CX = f2_make(i0 < n ? c0.x : ph, i1 < n ? c1.x : ph);
+						CY = f2_make(i0 < n ? c0.y : ph, i1 < n ? c1.y : ph);
+						CZ = f2_make(i0 < n ? c0.z : ph, i1 < n ? c1.z : ph);
+					}
+					const f2_t SX = CS ? CX : PX[CS ? 0 : s / 2], SY = CS ? CY : PY[CS ? 0 : s / 2];
+					const f2_t SZ = CS ? CZ : PZ[CS ? 0 : s / 2];
 					float an, ao, bn, bo, cn, co;
 					{
 						float d[2];
-						f2_split(f2_sub(PX[s / 2], N0), d[0], d[1]);
+						f2_split(f2_sub(SX, N0), d[0], d[1]);
 						an = d[s & 1];
-						f2_split(f2_sub(PX[s / 2], O0), d[0], d[1]);
+						f2_split(f2_sub(SX, O0), d[0], d[1]);
 						ao = d[s & 1];
-						f2_split(f2_sub(PY[s / 2], N1), d[0], d[1]);
+						f2_split(f2_sub(SY, N1), d[0], d[1]);
 						bn = d[s & 1];
-						f2_split(f2_sub(PY[s / 2], O1), d[0], d[1]);
+						f2_split(f2_sub(SY, O1), d[0], d[1]);
 						bo = d[s & 1];
-						f2_split(f2_sub(PZ[s / 2], N2), d[0], d[1]);
+						f2_split(f2_sub(SZ, N2), d[0], d[1]);
 						cn = d[s & 1];
-						f2_split(f2_sub(PZ[s / 2], O2), d[0], d[1]);
+						f2_split(f2_sub(SZ, O2), d[0], d[1]);
 						co = d[s & 1];
 					}
 					const f2_t mx = f2_make(fminf(fabsf(an), L - fabsf(an)), fminf(fabsf(ao), L - fabsf(ao)));
@@ -414,7 +441,9 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 				const float two = 2.f * dsum;
 				const bool accept = isfinite(two) && (two >= lum) && (two < (float)kLogDblMax);
 				if (accept) {
-					if (lane == (p & (G - 1))) {
+					if constexpr (CS) {
+						if (lane == (p & (G - 1))) xs[p] = Q4<float>{xn0, xn1, xn2, 0.f};
+					} else if (lane == (p & (G - 1))) {
 						xs[p] = Q4<float>{xn0, xn1, xn2, 0.f};
 						const float nx = xn0, ny = xn1, nz = xn2;
 						switch (p / G) {
@@ -445,8 +474,17 @@ __global__ void __launch_bounds__(128, SLOTS <= 11 ? 5 : 3) k_sample_f2(SysConst
 				__syncwarp(gmask);
 			}
 		}
+		if (CS && walker_ok) {
+			__syncwarp(gmask);
+			for (int i = lane; i < n; i += G) {
+				const Q4<float> c = xs[i];
+				pw[i] = c.x;
+				if (sc.dim > 1) pw[n + i] = c.y;
+				if (sc.dim > 2) pw[2 * n + i] = c.z;
+			}
+		}
 #pragma unroll
-		for (int s = 0; s < SLOTS && walker_ok; s++) {
+		for (int s = 0; s < SLOTS && walker_ok && !CS; s++) {
 			const int i = s * G + lane;
 			if (i < n) {
 				float d[2];

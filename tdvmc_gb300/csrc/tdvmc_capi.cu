@@ -90,6 +90,7 @@ struct tdvmc_ctx {
 	int nblk1 = 0, nblk2 = 0, chunk2 = 0, nblkS = 0;
 	bool gram_tc = false;  // S on the tensor cores (mixed precision only)
 	bool packed_sampler = true;  // FP32 uniform-knot sampler with f32x2 pair arithmetic
+	bool shared_coords = false;  // its variant with the lane's coordinates in shared memory
 	std::map<GraphKey, cudaGraphExec_t> graphs;
 	std::map<GraphKey, int> graph_kernels;  // kernels launched by one replay
 	// stored samples (correlated-sampling reuse), allocated on first use
@@ -228,7 +229,10 @@ int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed, int64_t
 	const int slots = slots_for(ctx->sc.n, G);
 	SampleFn<T> fn = nullptr;
 	if constexpr (std::is_same<T, float>::value)
-		if (ctx->packed_sampler && ctx->sc.uniform) fn = pick_sample_f32_packed(G, slots);
+		if (ctx->packed_sampler && ctx->sc.uniform) {
+			if (ctx->shared_coords) fn = pick_sample_f32_packed_shared(G, slots);
+			if (!fn) fn = pick_sample_f32_packed(G, slots);
+		}
 	if (!fn) fn = pick_sample<T>(G, slots);
 	if (!fn) return TDVMC_ERR_ARG;
 	const int threads = G * gpb;
@@ -1051,6 +1055,11 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	if (c.prec == TDVMC_PREC_MIXED && c.sc.uniform && c.tiles.sg == 32 && slots_for(d->n, 32) == 11 &&
 	    slots_for(d->n, 16) == 22)
 		c.tiles.sg = 16;
+	// TDVMC_SAMPLE_LANES overrides the sampler's lanes per walker (8, 16 or 32)
+	if (const char* sl = std::getenv("TDVMC_SAMPLE_LANES")) {
+		const int g = std::atoi(sl);
+		if ((g == 8 || g == 16 || g == 32) && slots_for(d->n, g) > 0) c.tiles.sg = g;
+	}
 	c.tiles.sgpb = 128 / c.tiles.sg;
 	c.tiles.egpb = c.tiles.eg == 32 ? 0 : 32 / c.tiles.eg;
 	// TDVMC_EVAL_WALKERS_PER_BLOCK overrides the evaluation kernels' walkers per block
@@ -1059,7 +1068,10 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	if (const char* h = std::getenv("TDVMC_HIST")) c.tiles.hist = std::max(0, std::min(2, std::atoi(h)));
 	if (const char* wt = std::getenv("TDVMC_TEST_WAIT_NS")) c.wait_ns = (uint64_t)std::strtoull(wt, nullptr, 10);
 	// TDVMC_SAMPLER=scalar selects the scalar FP32 sampler
-	if (const char* sm = std::getenv("TDVMC_SAMPLER")) c.packed_sampler = std::strcmp(sm, "scalar") != 0;
+	if (const char* sm = std::getenv("TDVMC_SAMPLER")) {
+		c.packed_sampler = std::strcmp(sm, "scalar") != 0;
+		c.shared_coords = std::strcmp(sm, "shared") == 0;
+	}
 	*out = ctx;
 	return TDVMC_OK;
 }

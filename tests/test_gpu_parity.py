@@ -338,11 +338,12 @@ def test_adjoint_driven_imaginary_time_step_matches_oracle_fp64():
 
 
 @pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed-scalar"])
-@pytest.mark.parametrize("dim,n", [(1, 20), (2, 40), (3, 150), (3, 300)])
+@pytest.mark.parametrize("dim,n", [(1, 20), (2, 40), (3, 150), (3, 300), (3, 600)])
 def test_sampler_padded_slots_follow_oracle_chain(dim, n, mode):
     """Particle counts whose register slots run past n (the slot count is rounded
     up to a compiled one: N = 20 on 8 lanes in 4 slots, 40 on 16 lanes in 4, 150
-    on 32 lanes in 8, 300 on 32 lanes in 11) in 1D, 2D and 3D.  FP64: the chain
+    on 32 lanes in 8, 300 on 32 lanes in 11, 600 on 32 lanes in 32, whose packed
+    FP32 sampler reads the lane's coordinates from shared memory) in 1D, 2D and 3D.  FP64: the chain
     equals the oracle's (same Philox stream; positions 1e-9, identical
     acceptance).  FP32, packed and scalar samplers: the same moves on at least
     90 % of the walkers (a decision within FP32 rounding of its threshold may
@@ -378,6 +379,42 @@ def test_sampler_padded_slots_follow_oracle_chain(dim, n, mode):
         d = np.abs(Rg - Ro).reshape(nw, -1).max(1)
         assert (d < 1e-4).mean() >= 0.9, d
         assert abs(acc - acc_o) <= 0.01 * acc_o, (acc, acc_o)
+
+
+def test_packed_sampler_with_shared_coordinates_follows_scalar_chain():
+    """N = 600 (32 slots of 32 lanes: the packed sampler that reads the lane's
+    own coordinates from shared memory at each move) walks the scalar FP32
+    sampler's chain bit for bit: identical walkers and acceptance counts."""
+    import tdvmc_gb300 as T
+    n, p, nw = 600, 20, 256
+    L = (n / 0.365) ** (1.0 / 3.0)
+    rng = np.random.default_rng(17)
+    m = 9
+    idx = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    R0 = idx[None] * (L / m) + (rng.uniform(size=(nw, n, 3)) - 0.5) * (L / m) * 0.3 - L / 2
+    R0 = np.ascontiguousarray(np.transpose(R0, (0, 2, 1))).astype(np.float32).astype(np.float64)
+    r = np.linspace(0.0, L / 2, p)
+    uR = -0.5 * (1.1 / np.maximum(r, 0.5)) ** 5
+    uR -= uR[-1]
+    out = {}
+    for mode in ("packed", "scalar"):
+        if mode == "scalar":
+            os.environ["TDVMC_SAMPLER"] = "scalar"
+        try:
+            s = T.BosonsBulk(3, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=0.09,
+                             precision="mixed")
+        finally:
+            os.environ.pop("TDVMC_SAMPLER", None)
+        assert s.Tiles()["sample_lanes"] == 32
+        s.SetParameters(uR, np.zeros(p))
+        s.SetWalkers(R0)
+        acc = s.DoMetropolisSteps(2 * n, 0.17, seed=5, pass_id=9)
+        out[mode] = (acc, s.GetWalkers())
+        s.close()
+    (a_p, R_p), (a_s, R_s) = out["packed"], out["scalar"]
+    assert a_p == a_s
+    assert np.array_equal(R_p, R_s)
+    assert 0.2 < a_p / (2 * n * nw) < 0.9
 
 
 def test_packed_sampler_follows_scalar_chain_mixed():
@@ -458,14 +495,14 @@ def test_maximum_size_matches_oracle(precision, tol):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("env", [{"TDVMC_HIST": "1"}, {"TDVMC_HIST": "2"}, {"TDVMC_EVAL_WALKERS_PER_BLOCK": "1"},
-                                 {"TDVMC_EVAL_WALKERS_PER_BLOCK": "4"}],
-                         ids=["hist1", "hist2", "wpb1", "wpb4"])
+@pytest.mark.parametrize("env", [{"TDVMC_HIST": "0"}, {"TDVMC_HIST": "1"}, {"TDVMC_HIST": "2"},
+                                 {"TDVMC_EVAL_WALKERS_PER_BLOCK": "1"}, {"TDVMC_EVAL_WALKERS_PER_BLOCK": "4"}],
+                         ids=["hist0", "hist1", "hist2", "wpb1", "wpb4"])
 def test_evaluation_variants_match_oracle(precision, env):
-    """The evaluation kernels' alternative histogram update modes (float4 slots,
-    shared-memory atomics) and forced walkers per block, selected through the
-    environment when the context is created: same results as the oracle at the
-    tolerances of the fixture cases."""
+    """The evaluation kernels' histogram update modes (lane-private records,
+    float4 slots, shared-memory atomics) and forced walkers per block, selected
+    through the environment when the context is created: same results as the
+    oracle at the tolerances of the fixture cases."""
     import tdvmc_gb300 as T
     z = np.load(os.path.join(GOLD, "eval_d3_n343_p30.npz"))
     cfgs = z["cfgs"]
