@@ -350,6 +350,8 @@ def run_c5(sync, imag_steps, real_steps, timed_steps, check_every=10, nw=C5_NW, 
         res["unit"] = "steps/s"
         res["ms_per_step"] = ms_timed / timed_steps
         res["gate_after_timed"] = c5_gate(s1, L1, min(C5_CHECK_WALKERS, nw))
+        res["kernels_ms_per_stage"] = {k: v for k, v in tr.profile_stage()}
+        res["tiles"] = s1.Tiles()
     s1.close()
     return res
 
