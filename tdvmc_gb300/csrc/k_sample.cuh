@@ -74,10 +74,11 @@ __device__ __forceinline__ T mi_r2(T dx, T dy, T dz, T L) {
 	return fma(mz, mz, fma(my, my, mx * mx));
 }
 
-// Shared memory: coef[ncoef] | kb[nbin] | hv[nbin] | lut[ncell] | mirror[groups][n]
+// Shared memory: coef[ncoef][copies] | kb[nbin] | hv[nbin] | lut[ncell] | mirror[groups][n]
+// (copies: 1 for k_sample, kCoefCopies for k_sample_f2)
 template <typename T>
-__host__ __device__ inline size_t sample_smem_bytes(int ncoef, int nbin, int ncell, int n, int groups) {
-	size_t b = (size_t)ncoef * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
+__host__ __device__ inline size_t sample_smem_bytes(int ncoef, int nbin, int ncell, int n, int groups, int copies = 1) {
+	size_t b = (size_t)ncoef * copies * sizeof(Q4<T>) + 2 * (size_t)nbin * sizeof(T) + (size_t)ncell * sizeof(int);
 	b = (b + 31) & ~(size_t)31;
 	return b + (size_t)groups * n * sizeof(Q4<T>);
 }
@@ -250,6 +251,12 @@ __device__ __forceinline__ Q4<float> lds_q4(uint32_t addr) {
 	return c;
 }
 
+// The packed sampler holds its pair-function table in kCoefCopies interleaved
+// copies (entry j of copy c at [j][c]) and lane l reads copy l mod kCoefCopies:
+// the 8 lanes of each quarter-warp 16-byte load then hit 8 different bank
+// groups whatever entries they read, so the table loads have no bank conflicts.
+constexpr int kCoefCopies = 8;
+
 // FP32 sampler for uniform knots with packed pair arithmetic.  It walks the
 // same chain as k_sample<float>, bit for bit: same random numbers, moves and
 // acceptance rule, and every pair term and partial sum rounded the same way.
@@ -286,22 +293,24 @@ __global__ void __launch_bounds__(128, CS ? (SLOTS > 16 ? 3 : 4) : (SLOTS <= 11 
                                                    const uint32_t* __restrict__ pass_ptr, int* __restrict__ acc_out) {
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	Q4<float>* coef = reinterpret_cast<Q4<float>*>(smem_raw);
-	size_t off = (size_t)sc.ncoef * sizeof(Q4<float>) + 2 * (size_t)sc.nbin * sizeof(float) + (size_t)sc.ncell * sizeof(int);
+	size_t off = (size_t)sc.ncoef * kCoefCopies * sizeof(Q4<float>) + 2 * (size_t)sc.nbin * sizeof(float) +
+	             (size_t)sc.ncell * sizeof(int);
 	off = (off + 31) & ~(size_t)31;
 	Q4<float>* mirror_all = reinterpret_cast<Q4<float>*>(smem_raw + off);
-	for (int i = threadIdx.x; i < sc.ncoef; i += blockDim.x) coef[i] = coef_g[i];
+	for (int i = threadIdx.x; i < sc.ncoef * kCoefCopies; i += blockDim.x) coef[i] = coef_g[i / kCoefCopies];
 	__syncthreads();
 	(void)uout_g;
 	(void)kb_g;
 	(void)hv_g;
 	(void)lut_g;
 
-	// byte address of entry j is coef_a + (bits(y) << 4) with y = kRoundF + j
-	const uint32_t coef_a =
-	    (uint32_t)__cvta_generic_to_shared(coef) - ((uint32_t)__float_as_uint(kRoundF) << 4);
 	const int n = sc.n;
 	const int tid = threadIdx.x;
 	const int lane = tid & (G - 1);
+	// byte address of entry j of this lane's copy is coef_a + (bits(y) << 7), y = kRoundF + j
+	// (128 bytes per entry: the kCoefCopies copies of 16 bytes)
+	const uint32_t coef_a = (uint32_t)__cvta_generic_to_shared(coef) + ((uint32_t)(tid & (kCoefCopies - 1)) << 4) -
+	                        ((uint32_t)__float_as_uint(kRoundF) << 7);
 	const int gib = tid / G;
 	const int gpb = blockDim.x / G;
 	const unsigned wl = tid & 31;
@@ -427,8 +436,8 @@ __global__ void __launch_bounds__(128, CS ? (SLOTS > 16 ? 3 : 4) : (SLOTS <= 11 
 					float ya, yb, ta, tb;
 					f2_split(yv, ya, yb);
 					f2_split(tau, ta, tb);
-					const Q4<float> ca = lds_q4(coef_a + (min(__float_as_uint(ya), ymax) << 4));
-					const Q4<float> cb = lds_q4(coef_a + (min(__float_as_uint(yb), ymax) << 4));
+					const Q4<float> ca = lds_q4(coef_a + (min(__float_as_uint(ya), ymax) << 7));
+					const Q4<float> cb = lds_q4(coef_a + (min(__float_as_uint(yb), ymax) << 7));
 					const float un = fmaf(ta, fmaf(ta, fmaf(ta, ca.w, ca.z), ca.y), ca.x);
 					const float uo = fmaf(tb, fmaf(tb, fmaf(tb, cb.w, cb.z), cb.y), cb.x);
 					const bool ok = (s == SLOTS - 1) ? (last_ok && s != self_slot) : (s != self_slot);

@@ -233,10 +233,12 @@ int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed, int64_t
 			if (ctx->shared_coords) fn = pick_sample_f32_packed_shared(G, slots);
 			if (!fn) fn = pick_sample_f32_packed(G, slots);
 		}
+	const bool packed = fn != nullptr;
 	if (!fn) fn = pick_sample<T>(G, slots);
 	if (!fn) return TDVMC_ERR_ARG;
 	const int threads = G * gpb;
-	const size_t smem = sample_smem_bytes<T>(ctx->sc.ncoef, ctx->sc.nbin, ctx->sc.ncell, ctx->sc.n, gpb);
+	const size_t smem =
+	    sample_smem_bytes<T>(ctx->sc.ncoef, ctx->sc.nbin, ctx->sc.ncell, ctx->sc.n, gpb, packed ? kCoefCopies : 1);
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const int grid = grid_for(ctx, (const void*)fn, threads, smem, count, gpb);
 	uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
