@@ -67,10 +67,13 @@ template <typename T> struct CsGeom {
 	int j;
 	bool in, out;  // within r_max (and not the self pair); beyond r_max
 };
+// FP32: r <= r_max from the FP32 distance; nearmin collects |r - r_max|, and the
+// pairs within rounding of r_max are decided again in FP64 after the slot
+// (cs_fix_slot).  force: the pair as within r_max whatever r is (the fix-up).
 template <typename T>
 __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
                                              const T* __restrict__ kb, const T* __restrict__ hv,
-                                             const int* __restrict__ lut) {
+                                             const int* __restrict__ lut, T& nearmin, bool force = false) {
 	CsGeom<T> g;
 	const T L = (T)sc.L, Lr = (T)sc.Lr;
 	if constexpr (sizeof(T) == 4) {
@@ -90,7 +93,8 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
 		g.rinv = rsqrt_(r2);
 		g.r = r2 * g.rinv;
 	}
-	const bool cut = within_rmax<T>(sc, g.r, xr, xi);
+	const bool cut = force || g.r <= (T)sc.rmax;
+	if constexpr (sizeof(T) == 4) nearmin = fminf(nearmin, fabsf(g.r - (T)sc.rmax));
 	g.in = ok && cut;
 	g.out = ok && !cut;
 	T t;
@@ -171,8 +175,8 @@ __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, con
                                         const CsPieceRow<T>& pu, const T* __restrict__ piece, const T* __restrict__ kb,
                                         const T* __restrict__ hv, const int* __restrict__ lut, T* __restrict__ drow,
                                         T* __restrict__ oacc, T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs,
-                                        int& nout) {
-	cs_accum<T, G, STATS, UNI>(sc, cs_geom<T>(sc, xr, xi, ok, kb, hv, lut), pu, piece, drow, oacc, d2acc, lane, pa, pb,
+                                        int& nout, T& nearmin) {
+	cs_accum<T, G, STATS, UNI>(sc, cs_geom<T>(sc, xr, xi, ok, kb, hv, lut, nearmin), pu, piece, drow, oacc, d2acc, lane, pa, pb,
 	                           vs, nout);
 }
 
@@ -184,13 +188,70 @@ __device__ __forceinline__ void cs_batch(const SysConst& sc, const Q4<T>& xr, co
                                          bool ok, const CsPieceRow<T>& pu, const T* __restrict__ piece,
                                          const T* __restrict__ kb, const T* __restrict__ hv,
                                          const int* __restrict__ lut, T* __restrict__ drow, T* __restrict__ oacc,
-                                         T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs, int& nout) {
+                                         T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs, int& nout,
+                                         T& nearmin) {
 	CsGeom<T> g[kCsBatch];
 #pragma unroll
-	for (int u = 0; u < kCsBatch; u++) g[u] = cs_geom<T>(sc, xr, xs[i + u], ok, kb, hv, lut);
+	for (int u = 0; u < kCsBatch; u++) g[u] = cs_geom<T>(sc, xr, xs[i + u], ok, kb, hv, lut, nearmin);
 #pragma unroll
 	for (int u = 0; u < kCsBatch; u++)
 		cs_accum<T, G, STATS, UNI>(sc, g[u], pu, piece, drow, oacc, d2acc, lane, pa, pb, vs, nout);
+}
+
+// Cutoff fix-up of one row (FP32, the row's lane alone): the pairs whose FP32
+// distance lies within rounding of r_max (sc.rcut_band) are decided again in
+// FP64 from the FP32 coordinates, as the evaluation kernels decide them; where
+// that differs from the sweep's decision the pair's terms are added (FP64 in)
+// or removed (FP64 out): the row's D columns, and for counted pairs (i < nrow)
+// O, D2, the potential and the outer count.  Rare; a separate function so the
+// sweep's code and registers do not carry it.
+struct CsFix {
+	float v;
+	int nout;
+};
+template <int G, bool UNI>
+__device__ __noinline__ CsFix cs_fix_slot(SysConst sc, CsPieceRow<float> pu, const float* piece, const float* kb,
+                                          const float* hv, const int* lut, const Q4<float>* xs, float* drow,
+                                          float* oacc, float* d2acc, int n, int nrow, int lane, float pa, float pb) {
+	CsFix f = {0.f, 0};
+	const Q4<float> xr = xs[nrow];
+	const float rmax = (float)sc.rmax, dm1 = (float)(sc.dim - 1);
+	for (int i = 0; i < n; i++) {
+		if (i == nrow) continue;
+		float nm = 3.0e38f;
+		const CsGeom<float> g = cs_geom<float>(sc, xr, xs[i], true, kb, hv, lut, nm, true);
+		if (!(fabsf(g.r - rmax) < sc.rcut_band)) continue;
+		const bool in32 = g.r <= rmax, in64 = cut_fp64(sc, xr, xs[i]);
+		if (in64 == in32) continue;
+		const float sgn = in64 ? 1.f : -1.f;
+		const float* pj = piece + (size_t)g.j * kCsPieceS;
+		auto pc = [&](int k) -> float {
+			if constexpr (UNI) return pu.c[k];
+			else return pj[k];
+		};
+		const int s0 = g.j + 3;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const float b1 = fmaf(g.t, fmaf(g.t, pc(3 * q + 2), pc(3 * q + 1)), pc(3 * q));
+			const float bs = sgn * b1 * g.sr;
+			float* dq = drow + (size_t)(s0 - q) * 3 * G + lane;
+			dq[0] = fmaf(bs, g.dx, dq[0]);
+			dq[G] = fmaf(bs, g.dy, dq[G]);
+			dq[2 * G] = fmaf(bs, g.dz, dq[2 * G]);
+			if (i < nrow) {
+				const int l = 12 + 4 * q;
+				const float b = fmaf(g.t, fmaf(g.t, fmaf(g.t, pc(l + 3), pc(l + 2)), pc(l + 1)), pc(l));
+				const float b2 = fmaf(g.t, pc(28 + 2 * q + 1), pc(28 + 2 * q));
+				oacc[(size_t)(s0 - q) * G + lane] += sgn * b;
+				d2acc[(size_t)(s0 - q) * G + lane] += sgn * 2.f * (b2 + dm1 * b1 * g.sr);
+			}
+		}
+		if (i < nrow) {
+			f.v += sgn * pair_pot<float>(sc.pot_kind, g.r, g.rinv, pa, pb);
+			f.nout -= in64 ? 1 : -1;
+		}
+	}
+	return f;
 }
 
 // Stores the correlated-sampling data of walkers (start + w) mod nw_total,
@@ -260,30 +321,39 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const CsPieceR
 			const bool rowok = nrow < n;
 			const Q4<T> xr = rowok ? xs[nrow] : Q4<T>{T(0), T(0), T(0), T(0)};
 			for (int e = lane; e < ns * 3 * G; e += G) drow[e] = T(0);
+			T nearmin = T(3.0e38);
 			const int base = s * G;
 			const int dend = (base + G < n) ? base + G : n;
 			// partners below the slot: every lane's pair is counted once (i < nrow);
 			// base is a multiple of G, so of kCsBatch
 			for (int i = 0; i < base; i += kCsBatch)
 				cs_batch<T, G, true, UNI>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
-				                          vs, nout);
+				                          vs, nout, nearmin);
 			// the slot's own block: counted iff i < nrow
 			for (int i = base; i < dend; i++) {
 				if (i < nrow)
 					cs_pair<T, G, true, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs,
-					                    nout);
+					                    nout, nearmin);
 				else
 					cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok && i != nrow, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane,
-					                     pa, pb, vs, nout);
+					                     pa, pb, vs, nout, nearmin);
 			}
 			// partners above the slot: D only
 			int i = dend;
 			for (; i + kCsBatch <= n; i += kCsBatch)
 				cs_batch<T, G, false, UNI>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
-				                           vs, nout);
+				                           vs, nout, nearmin);
 			for (; i < n; i++)
 				cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
-				                          vs, nout);
+				                          vs, nout, nearmin);
+			if constexpr (sizeof(T) == 4) {
+				if (rowok && nearmin < sc.rcut_band) {
+					const CsFix f = cs_fix_slot<G, UNI>(sc, pu, piece, kb, hv, lut, xs, drow, oacc, d2acc, n, nrow, lane,
+					                                    pa, pb);
+					vs.add(f.v);
+					nout += f.nout;
+				}
+			}
 			if (rowok)
 				for (int e = 0; e < ns * 3; e++) Dw[cs_doff(ns * 3, e, nrow)] = drow[(size_t)e * G + lane];
 		}
