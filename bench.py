@@ -585,9 +585,15 @@ def run_workload(args):
     else:
         def log(msg):
             print(msg, file=sys.stderr, flush=True)
-        out = run_c5(sync, 50, 200, 10, check_every=10, log=log)
-        out["workload"] = ("3D N=1000 LJ bosons rho=0.365, P=64, 262144 walkers: 50 imaginary-time steps "
-                           "(adjoint force), quench to rho=0.40, 200 real-time RK4 steps dt=2.5e-4")
+        if args.walkers != NW:
+            # a short run at another walker count (profiler runs): one imaginary-time and one
+            # real-time step, no FP64 checks
+            out = run_c5(sync, 1, 1, 0, check_every=0, nw=args.walkers, log=log)
+        else:
+            out = run_c5(sync, 50, 200, 10, check_every=10, log=log)
+        out["workload"] = ("3D N=1000 LJ bosons rho=0.365, P=64, %d walkers: %d imaginary-time steps "
+                           "(adjoint force), quench to rho=0.40, %d real-time RK4 steps dt=2.5e-4"
+                           % (out["walkers"], out["imag_steps"], out["real_steps"]))
     print(json.dumps(out))
 
 
@@ -598,7 +604,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--autotune", type=int, default=0)
-    ap.add_argument("--walkers", type=int, default=NW, help="walkers (default: the 65,536 of the workload)")
+    ap.add_argument("--walkers", type=int, default=NW,
+                    help="walkers (default: the 65,536 of the workload; with --workload c5 another count runs "
+                         "one imaginary-time and one real-time step, for profiler runs)")
     ap.add_argument("--no-extras", action="store_true",
                     help="time the steps only (no e2e, FP64, CPU or gate legs): for profiler runs on a small case")
     ap.add_argument("--stored", choices=["rk4", "pc"], default=None,
