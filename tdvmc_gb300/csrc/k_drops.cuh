@@ -461,75 +461,110 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 // pass 1 the means of the DropCols columns (FP64 sums in a fixed order), pass 2
 // S_kl = <(O_k - <O_k>)(O_l - <O_l>)> and cov(O_k, E^R), cov(O_k, E^I).  The
 // centred products are formed in T and summed in T over runs of 32 walkers,
-// each run added in FP64 (FP64 issue is scarce on this GPU).
+// each run added in FP64 (FP64 issue is scarce on this GPU).  Both passes stage
+// the drop's walkers in chunks of 32 through shared memory with coalesced loads
+// (the walker rows are contiguous), so the sums read shared memory instead of
+// waiting on a strided global load per walker; the order of every sum is that
+// of a walker-by-walker loop.
 constexpr int kDropReduceThreads = 256;
+constexpr int kDropRedChunk = 32;                     // walkers per staged chunk = the pass-2 run
+constexpr int kDropCols = 3 * (kDropMaxP + 1) + 10;   // DropCols count at the largest p
+constexpr int kDropEntries = (kDropMaxP + 1) * (kDropMaxP + 2) / 2 + 2 * (kDropMaxP + 1);
+constexpr int kDropEntriesPerThread = (kDropEntries + kDropReduceThreads - 1) / kDropReduceThreads;
 template <typename T>
 __global__ void __launch_bounds__(kDropReduceThreads) k_drop_reduce(
     DropConst dc, const T* __restrict__ O, const T* __restrict__ eloc, const T* __restrict__ other7,
     const int* __restrict__ acc, const T* __restrict__ dE, int use_dE, double* __restrict__ means,
     double* __restrict__ S, double* __restrict__ cov) {
-	__shared__ double m_s[3 * (kDropMaxP + 1) + 10];
+	__shared__ double m_s[kDropCols];
+	__shared__ T ch[kDropRedChunk * kDropCols];
 	const int s = blockIdx.x, tid = threadIdx.x;
 	const int p1 = dc.p1;
 	const DropCols cl{p1};
 	const int K = cl.count();
 	const int64_t g0 = (int64_t)s * dc.nws, nw = dc.nws;
-	// pass 1: thread per column, four interleaved FP64 sums
-	for (int col = tid; col < K; col += blockDim.x) {
-		double a[4] = {0, 0, 0, 0};
-		for (int64_t w = 0; w < nw; w++) {
-			const int64_t g = g0 + w;
-			double v;
-			if (col < p1) v = (double)O[(size_t)g * p1 + col];
-			else if (col == cl.ER()) v = (double)eloc[2 * g];
-			else if (col == cl.EI()) v = (double)eloc[2 * g + 1];
-			else if (col < cl.acc()) v = (double)other7[(size_t)g * 7 + (col - cl.other())];
-			else if (col == cl.acc()) v = (double)acc[g];
-			else v = use_dE ? (double)dE[(size_t)g * 2 * p1 + (col - cl.dE())] : 0.0;
-			a[w & 3] += v;
+	// pass 1: thread per column (K <= kDropCols < blockDim), four interleaved FP64 sums
+	double a[4] = {0, 0, 0, 0};
+	for (int64_t w0 = 0; w0 < nw; w0 += kDropRedChunk) {
+		const int cw = (int)(nw - w0 < kDropRedChunk ? nw - w0 : kDropRedChunk);
+		__syncthreads();
+		for (int e = tid; e < cw * K; e += blockDim.x) {
+			const int w = e / K, col = e - w * K;
+			const int64_t g = g0 + w0 + w;
+			T v;
+			if (col < p1) v = O[(size_t)g * p1 + col];
+			else if (col == cl.ER()) v = eloc[2 * g];
+			else if (col == cl.EI()) v = eloc[2 * g + 1];
+			else if (col < cl.acc()) v = other7[(size_t)g * 7 + (col - cl.other())];
+			else if (col == cl.acc()) v = (T)acc[g];
+			else v = use_dE ? dE[(size_t)g * 2 * p1 + (col - cl.dE())] : T(0);
+			ch[w * K + col] = v;
 		}
+		__syncthreads();
+		if (tid < K)
+			for (int w = 0; w < cw; w++) a[(w0 + w) & 3] += (double)ch[w * K + tid];
+	}
+	if (tid < K) {
 		const double mval = ((a[0] + a[1]) + (a[2] + a[3])) / (double)nw;
-		m_s[col] = mval;
-		means[(size_t)s * K + col] = mval;
+		m_s[tid] = mval;
+		means[(size_t)s * K + tid] = mval;
 	}
 	__syncthreads();
-	// pass 2: thread per entry of the upper triangle of S and the two covariance columns
-	const int nS = p1 * (p1 + 1) / 2;
-	for (int e = tid; e < nS + 2 * p1; e += blockDim.x) {
-		int i, j;
+	// pass 2: thread per entry of the upper triangle of S and the two covariance
+	// columns; the chunk holds the centred O_k and E^R, E^I of its walkers
+	const int nS = p1 * (p1 + 1) / 2, nE = nS + 2 * p1, R = p1 + 2;
+	int ei[kDropEntriesPerThread], ej[kDropEntriesPerThread];
+	double acc64[kDropEntriesPerThread];
+#pragma unroll
+	for (int q = 0; q < kDropEntriesPerThread; q++) {
+		const int e = tid + q * kDropReduceThreads;
+		int i = 0, j = 0;
 		if (e < nS) {
 			// row-major upper triangle: e -> (i, j), j >= i
-			i = 0;
 			int rem = e;
 			while (rem >= p1 - i) {
 				rem -= p1 - i;
 				i++;
 			}
 			j = i + rem;
-		} else {
+		} else if (e < nE) {
 			i = (e - nS) >> 1;
-			j = -1 - ((e - nS) & 1);  // -1: E^R, -2: E^I
+			j = p1 + ((e - nS) & 1);  // column p1: E^R, p1 + 1: E^I
 		}
-		const T mi = (T)m_s[i];
-		const T mj = j >= 0 ? (T)m_s[j] : (T)m_s[j == -1 ? cl.ER() : cl.EI()];
-		double acc64 = 0.0;
-		for (int64_t w0 = 0; w0 < nw; w0 += 32) {
+		ei[q] = i;
+		ej[q] = j;
+		acc64[q] = 0.0;
+	}
+	for (int64_t w0 = 0; w0 < nw; w0 += kDropRedChunk) {
+		const int cw = (int)(nw - w0 < kDropRedChunk ? nw - w0 : kDropRedChunk);
+		__syncthreads();
+		for (int e = tid; e < cw * R; e += blockDim.x) {
+			const int w = e / R, col = e - w * R;
+			const int64_t g = g0 + w0 + w;
+			T v;
+			if (col < p1) v = O[(size_t)g * p1 + col] - (T)m_s[col];
+			else v = eloc[2 * g + (col - p1)] - (T)m_s[col == p1 ? cl.ER() : cl.EI()];
+			ch[w * R + col] = v;
+		}
+		__syncthreads();
+#pragma unroll
+		for (int q = 0; q < kDropEntriesPerThread; q++) {
+			if (tid + q * kDropReduceThreads >= nE) break;
 			T run = T(0);
-			const int64_t w1 = w0 + 32 < nw ? w0 + 32 : nw;
-			for (int64_t w = w0; w < w1; w++) {
-				const int64_t g = g0 + w;
-				const T oi = O[(size_t)g * p1 + i] - mi;
-				const T oj = (j >= 0 ? O[(size_t)g * p1 + j] : eloc[2 * g + (j == -1 ? 0 : 1)]) - mj;
-				run = fma(oi, oj, run);
-			}
-			acc64 += (double)run;
+			for (int w = 0; w < cw; w++) run = fma(ch[w * R + ei[q]], ch[w * R + ej[q]], run);
+			acc64[q] += (double)run;
 		}
-		const double v = acc64 / (double)nw;
+	}
+#pragma unroll
+	for (int q = 0; q < kDropEntriesPerThread; q++) {
+		const int e = tid + q * kDropReduceThreads;
+		if (e >= nE) break;
+		const double v = acc64[q] / (double)nw;
 		if (e < nS) {
-			S[(size_t)s * p1 * p1 + (size_t)i * p1 + j] = v;
-			S[(size_t)s * p1 * p1 + (size_t)j * p1 + i] = v;
+			S[(size_t)s * p1 * p1 + (size_t)ei[q] * p1 + ej[q]] = v;
+			S[(size_t)s * p1 * p1 + (size_t)ej[q] * p1 + ei[q]] = v;
 		} else {
-			cov[((size_t)s * p1 + i) * 2 + (j == -1 ? 0 : 1)] = v;
+			cov[((size_t)s * p1 + ei[q]) * 2 + (ej[q] - p1)] = v;
 		}
 	}
 }
