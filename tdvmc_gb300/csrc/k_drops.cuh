@@ -285,6 +285,49 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 #pragma unroll
 		for (int c = 0; c < 4; c++) lv[q][c] = (T)loc[q * 4 + c];
 	const T dm1 = T(2);
+	// the fold's nonzero entries, row by row (a few per row: the boundary rows and
+	// one per interior parameter), so each walker's O_k and dE_k sums skip the zeros
+	// of the dense [P][ns] matrix; the order of every sum is that of the dense loop
+	constexpr int kNnzMax = 4 * (kDropMaxP + 2);
+	__shared__ int fk_start[kDropMaxP + 1], fk_sp[kNnzMax];
+	__shared__ double fk_f[kNnzMax];
+	__shared__ int fk_dense;
+	if (tid == 0) {
+		int e = 0;
+		fk_dense = 0;
+		for (int k = 0; k < P; k++) {
+			fk_start[k] = e;
+			for (int sp = 0; sp < ns; sp++) {
+				const double f = fold[(size_t)k * ns + sp];
+				if (f == 0.0) continue;
+				if (e < kNnzMax) {
+					fk_sp[e] = sp;
+					fk_f[e] = f;
+				}
+				e++;
+			}
+		}
+		fk_start[P] = e;
+		fk_dense = e > kNnzMax;
+	}
+	__syncthreads();
+	auto fold_row = [&](int k, int oRow, double scale, int oAdd) -> double {
+		// sum over sp of fold[k][sp] * (scale * R(oRow + sp) + R(oAdd + sp)) (oAdd < 0: none)
+		double v = 0.0;
+		if (!fk_dense) {
+			for (int e = fk_start[k]; e < fk_start[k + 1]; e++) {
+				const int sp = fk_sp[e];
+				v += fk_f[e] * (scale * (double)R(oRow + sp) + (oAdd >= 0 ? (double)R(oAdd + sp) : 0.0));
+			}
+		} else {
+			for (int sp = 0; sp < ns; sp++) {
+				const double f = fold[(size_t)k * ns + sp];
+				if (f == 0.0) continue;
+				v += f * (scale * (double)R(oRow + sp) + (oAdd >= 0 ? (double)R(oAdd + sp) : 0.0));
+			}
+		}
+		return v;
+	};
 	for (;;) {
 		const int it = next_item(counter);
 		if (it >= nitems) break;
@@ -391,11 +434,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 		// O_k: fold of the spline sums (FP64), O_p; ln psi in FP64
 		double lnp = prm[P - 1] * (double)nout + prm[P] * r2sum;
 		for (int k = 0; k < P; k++) {
-			double ok = 0.0;
-			for (int sp = 0; sp < ns; sp++) {
-				const double f = fold[(size_t)k * ns + sp];
-				if (f != 0.0) ok += f * (double)R(oS + sp);
-			}
+			const double ok = fold_row(k, oS, 1.0, -1);
 			O_o[(size_t)g * p1 + k] = (T)ok;
 			lnp += prm[k] * ok;
 		}
@@ -441,13 +480,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 				}
 			}
 			for (int k = 0; k < P; k++) {
-				double re = 0.0, im = 0.0;
-				for (int sp = 0; sp < ns; sp++) {
-					const double f = fold[(size_t)k * ns + sp];
-					if (f == 0.0) continue;
-					re += f * (2.0 * (double)R(oA + sp) + (double)R(oL + sp));
-					im += f * (2.0 * (double)R(oB + sp));
-				}
+				const double re = fold_row(k, oA, 2.0, oL), im = fold_row(k, oB, 2.0, -1);
 				dE_o[((size_t)g * p1 + k) * 2 + 0] = (T)(-c * re);
 				dE_o[((size_t)g * p1 + k) * 2 + 1] = (T)(-c * im);
 			}
