@@ -166,11 +166,12 @@ def cpu_port_rate(threads, walkers_per_thread=1, seed=11):
 def run_reference(args):
     threads = os.cpu_count() or 1
     rates = []
-    t_probe = 1.0
+    t_probe = 2.0
     for _ in range(args.warmup):
-        _, t_probe, _ = cpu_port_rate(threads, 1)
-    # about 10 s of CPU work per measured step (one RK stage of wpt walkers per thread)
-    wpt = int(min(2048, max(1, np.ceil(10.0 / max(t_probe, 1e-3)))))
+        _, t_probe, _ = cpu_port_rate(threads, 2)
+    # about 10 s of CPU work per measured step (one RK stage of wpt walkers per thread);
+    # the probe runs two walkers per thread, so its fixed start-up cost counts half
+    wpt = int(min(2048, max(1, np.ceil(10.0 / max(t_probe / 2.0, 1e-3)))))
     t_all = 0.0
     nws = 0
     for k in range(args.steps):
