@@ -169,9 +169,10 @@ def run_reference(args):
     t_probe = 2.0
     for _ in range(args.warmup):
         _, t_probe, _ = cpu_port_rate(threads, 2)
-    # about 10 s of CPU work per measured step (one RK stage of wpt walkers per thread);
-    # the probe runs two walkers per thread, so its fixed start-up cost counts half
-    wpt = int(min(2048, max(1, np.ceil(10.0 / max(t_probe / 2.0, 1e-3)))))
+    # at least about 10 s of CPU work per measured step (one RK stage of wpt walkers per
+    # thread); the probe's time per walker still carries part of a fixed start-up cost
+    # (with one walker per thread the steps came out at about half the target), hence 15 s
+    wpt = int(min(2048, max(1, np.ceil(15.0 / max(t_probe / 2.0, 1e-3)))))
     t_all = 0.0
     nws = 0
     for k in range(args.steps):
