@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "libtdvmc_oracle.so")
 SRC = os.path.join(HERE, "tdvmc_oracle.c")
 
 POT_NONE, POT_SQUARE, POT_GAUSS, POT_LJ = 0, 1, 2, 3
+SYS_BOSONS_BULK, SYS_NU_PB = 0, 1  # BosonsBulk, NUBosonsBulkPB (tdvmc_oracle.h)
 
 _lib = None
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -52,6 +53,7 @@ def lib():
         L.orc_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_int,
                                  C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double]
         L.orc_free.argtypes = [C.c_void_p]
+        L.orc_set_variant.argtypes = [C.c_void_p, C.c_int]
         L.orc_num_knots.argtypes = [C.c_void_p]
         L.orc_num_splines.argtypes = [C.c_void_p]
         L.orc_rmax.argtypes = [C.c_void_p]
@@ -111,7 +113,7 @@ class OracleSystem:
     """One periodic pair-spline Bose system (BosonsBulk semantics) in FP64."""
 
     def __init__(self, dim, n, p, L, user_knots=None, pot_kind=POT_SQUARE, pot=(0.5, 2.0),
-                 time=0.0, hbar2_2m=1.0):
+                 time=0.0, hbar2_2m=1.0, variant=SYS_BOSONS_BULK):
         self.dim, self.n, self.p, self.L = int(dim), int(n), int(p), float(L)
         uk = None if user_knots is None else np.ascontiguousarray(user_knots, dtype=np.float64)
         pv = np.ascontiguousarray(pot, dtype=np.float64)
@@ -122,6 +124,8 @@ class OracleSystem:
         if not h:
             raise ValueError("oracle rejected the system (parameter count or sizes)")
         self.h = h
+        if variant != SYS_BOSONS_BULK:
+            lib().orc_set_variant(h, int(variant))
         self.nk = lib().orc_num_knots(h)
         self.ns = lib().orc_num_splines(h)
         self.rmax = lib().orc_rmax(h)

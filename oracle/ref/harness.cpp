@@ -10,6 +10,7 @@
 //
 // Commands (whitespace-separated text on stdin):
 //   SYSTEM dim n p L nuser [user knots..] nsp [system params..] time
+//   SYSTEMPB (same arguments)   -> the same with PhysicalSystems::NUBosonsBulkPB
 //   PARAMS uR[p] uI[p] phiR phiI
 //   WEIGHTS                      -> knot vector and SplineFactory weights
 //   EVAL ncfg [cfg: n*dim]...    -> lnpsi, wf, O[p], E_R, E_I, other[9], LJ sum
@@ -25,6 +26,7 @@
 #include "SplineFactory.h"
 #include "Utils.h"
 #include "PhysicalSystems/BosonsBulk.h"
+#include "PhysicalSystems/NUBosonsBulkPB.h"
 #include "Potentials/LJ.h"
 #include "Observables/ObservableVsOnGrid.h"
 
@@ -79,7 +81,7 @@ static vector<vector<double> > read_cfg()
 	return R;
 }
 
-static void cmd_system()
+static void cmd_system(bool pb)
 {
 	int nuser, nsp;
 	double t;
@@ -103,10 +105,20 @@ static void cmd_system()
 	isRootRank = true;
 
 	if (sys) delete sys;
-	auto* b = new PhysicalSystems::BosonsBulk(sp, configDirectory);
-	if (nuser > 0) b->SetNodes(user);
-	b->SetPairDistributionBinCount(GR_BIN_COUNT);
-	sys = b;
+	if (pb)
+	{
+		auto* b = new PhysicalSystems::NUBosonsBulkPB(sp, configDirectory);
+		if (nuser > 0) b->SetNodes(user);
+		b->SetGrBinCount(GR_BIN_COUNT);
+		sys = b;
+	}
+	else
+	{
+		auto* b = new PhysicalSystems::BosonsBulk(sp, configDirectory);
+		if (nuser > 0) b->SetNodes(user);
+		b->SetPairDistributionBinCount(GR_BIN_COUNT);
+		sys = b;
+	}
 	Init();
 	sys->InitSystem();
 	PostSystemInit();
@@ -340,7 +352,8 @@ int main(int argc, char** argv)
 	string cmd;
 	while (cin >> cmd)
 	{
-		if (cmd == "SYSTEM") cmd_system();
+		if (cmd == "SYSTEM") cmd_system(false);
+		else if (cmd == "SYSTEMPB") cmd_system(true);
 		else if (cmd == "PARAMS") cmd_params();
 		else if (cmd == "WEIGHTS") cmd_weights();
 		else if (cmd == "EVAL") cmd_eval();

@@ -23,6 +23,7 @@ struct orc_sys {
 	int np1, np2, np3;
 	double L, Lr, L2, rmax, hbar2_2m, time;
 	int pot_kind, npot;
+	int variant;
 	double pot[5];
 	double knots[ORC_MAX_KNOTS];
 	/* fold[k][s]: parameter k <- spline s (boundary-condition combination) */
@@ -176,6 +177,36 @@ orc_sys* orc_create(int dim, int n, int p, double L, const double* user_knots, i
 	return s;
 }
 
+/* NUBosonsBulkPB::RefreshLocalOperators (NUBosonsBulkPB.cpp:216-226) over the
+ * p + 2 splines of the knot vector (the system declares p + 3; the last is never
+ * filled) */
+void orc_set_variant(orc_sys* s, int variant)
+{
+	s->variant = variant;
+	if (variant != ORC_SYS_NU_PB) return;
+	int P = s->p, ns = s->ns;
+	memset(s->fold, 0, (size_t)P * ns * sizeof(double));
+	for (int k = 0; k < P; k++) s->fold[k * ns + k + 1] = 1.0;
+	s->fold[1 * ns + 0] += 1.0;
+	s->fold[(P - 1) * ns + ns - 1] += 1.0;
+}
+
+/* The distance a pair enters the spline sums with, and whether it does.
+ * BosonsBulk: r, inside r <= r_max (r < r_max for a moved particle's new
+ * position, strict).  NUBosonsBulkPB: r' = 2 r_max - r beyond r_max, inside
+ * r' < r_max (NUBosonsBulkPB.cpp:240-247, 321-326, 629-660). */
+static int pair_inside(const orc_sys* s, double r, int strict, double* reff)
+{
+	if (s->variant == ORC_SYS_NU_PB)
+	{
+		double rr = (r < s->rmax) ? r : 2.0 * s->rmax - r;
+		*reff = rr;
+		return rr < s->rmax;
+	}
+	*reff = r;
+	return strict ? (r < s->rmax) : (r <= s->rmax);
+}
+
 void orc_free(orc_sys* s)
 {
 	if (!s) return;
@@ -279,11 +310,11 @@ static void spline_sums(const orc_sys* s, const double* R, double* S, double* no
 	for (int a = 0; a < n; a++)
 		for (int i = 0; i < a; i++)
 		{
-			double r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
-			if (r <= s->rmax)
+			double re, r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
+			if (pair_inside(s, r, 0, &re))
 			{
-				int b = find_bin(s, r);
-				spline_eval(s, b, r, v, NULL, NULL);
+				int b = find_bin(s, re);
+				spline_eval(s, b, re, v, NULL, NULL);
 				for (int q = 0; q < 4; q++) S[b - q] += v[q];
 			}
 			else *nout += 1.0;
@@ -338,7 +369,7 @@ void orc_eval(const orc_sys* s, const double* uR, const double* uI, const double
 		{
 			if (i == a) continue;
 			double r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
-			if (r > s->rmax) continue;
+			if (!pair_inside(s, r, 0, &r)) continue; /* r: the distance the pair enters with */
 			if (i < a) vint += pair_potential(s, r);
 			int b = find_bin(s, r);
 			spline_eval(s, b, r, NULL, d1, d2);
@@ -397,7 +428,7 @@ void orc_eval(const orc_sys* s, const double* uR, const double* uI, const double
 			{
 				if (i == a) continue;
 				double r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
-				if (r > s->rmax) continue;
+				if (!pair_inside(s, r, 0, &r)) continue;
 				int b = find_bin(s, r);
 				spline_eval(s, b, r, NULL, d1, NULL);
 				double gR = 0, gI = 0;
@@ -457,7 +488,7 @@ static void move_sums(const orc_sys* s, const double* R, int p, const double* x,
 	{
 		if (i == p) continue;
 		double r = orc_nic_disp(R + i * D, x, D, s->L, d);
-		int inside = strict ? (r < s->rmax) : (r <= s->rmax);
+		int inside = pair_inside(s, r, strict, &r);
 		if (inside)
 		{
 			int b = find_bin(s, r);

@@ -32,6 +32,18 @@ enum { ORC_POT_NONE = 0, ORC_POT_SQUARE = 1, ORC_POT_GAUSS = 2, ORC_POT_LJ = 3 }
 
 typedef struct orc_sys orc_sys;
 
+/* System variants.  BOSONS_BULK: PhysicalSystems::BosonsBulk.  NU_PB:
+ * PhysicalSystems::NUBosonsBulkPB (NUBosonsBulkPB.cpp), the same pair spline with
+ * a pair beyond r_max entering at the mirrored distance r' = 2 r_max - r
+ * (counted outside only at r' = r_max, :240-247, 321-326), its own fold of the
+ * p + 2 splines into the p parameters (O_k = S_{k+1}, O_1 += S_0,
+ * O_{p-1} += S_{p+1}, :216-226), the gradient, the Laplacian's (D-1)/r and the
+ * square-well potential all taken at r' (:321-393: the unit vector is the
+ * displacement over r', and the sign flip of the mirrored pairs' derivative is
+ * commented out), and r < r_max (strict) for the old and the new position of a
+ * move (:622-660). */
+enum { ORC_SYS_BOSONS_BULK = 0, ORC_SYS_NU_PB = 1 };
+
 /* Build a system.  user_knots == NULL (nuser = 0) gives the uniform grid of
  * BosonsBulk.cpp:61-67; otherwise the grid is mirrored as in
  * BosonsBulk.cpp:35-44.  Returns NULL on a parameter-count mismatch
@@ -39,6 +51,8 @@ typedef struct orc_sys orc_sys;
 orc_sys* orc_create(int dim, int n, int p, double L, const double* user_knots, int nuser,
                     int pot_kind, const double* pot, int npot, double time, double hbar2_2m);
 void orc_free(orc_sys* s);
+/* Switch an existing system to a variant (rebuilds the fold). */
+void orc_set_variant(orc_sys* s, int variant);
 int orc_num_knots(const orc_sys* s);
 int orc_num_splines(const orc_sys* s);
 double orc_rmax(const orc_sys* s);

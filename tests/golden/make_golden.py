@@ -6,7 +6,7 @@ reference C++ sources of mathiasgartner/TDVMC linked with
 outputs as ``.npz`` files.  Needs the reference checkout (default
 ``/root/reference``); the fixtures are committed so the tests never need it.
 
-    python tests/golden/make_golden.py [/path/to/reference] [obs | driver]
+    python tests/golden/make_golden.py [/path/to/reference] [obs | driver | pb]
 
 The driver fixture (``driver_d3_n27/``) holds the output files of the
 reference's full program on a small config, for the host driver's file
@@ -170,8 +170,65 @@ def driver_run(ref_root):
     print("driver run", sub)
 
 
+def pb_systems(ref_root):
+    """The mirrored-distance variant (PhysicalSystems::NUBosonsBulkPB) on fixed
+    configurations and single-particle moves: pb_eval_<name>.npz, the layout of
+    the eval_ fixtures.  The system reads its r_max from the knot vector before
+    it builds default knots, so it is always given knots (NURBS_GRID)."""
+    L2 = float(np.sqrt(64 / 0.3))
+    g = np.linspace(0.0, 1.0, 20)
+    knots2 = np.concatenate([[0.0], 0.7 + (L2 / 2 - 0.7) * (g[1:] - g[1]) ** 1.3 / (1 - g[1]) ** 1.3])
+    systems = [
+        dict(name="d3_n64_p10", dim=3, n=64, p=10, L=4.4, knots=np.linspace(0.0, 2.2, 10), sysp=[0.9, 1.0],
+             ncfg=16, seed=31, jitter=0.5),
+        dict(name="d2_n64_k20", dim=2, n=64, p=20, L=L2, knots=knots2, sysp=[1.0, 0.5], ncfg=16, seed=32,
+             jitter=0.3),
+        dict(name="d1_n20_p10", dim=1, n=20, p=10, L=20.0, knots=np.linspace(0.0, 10.0, 10), sysp=[0.5, 2.0],
+             ncfg=16, seed=33),
+    ]
+    for sysd in systems:
+        rng = np.random.default_rng(sysd["seed"])
+        dim, n, p, L = sysd["dim"], sysd["n"], sysd["p"], sysd["L"]
+        uR = rng.normal(0.0, 0.3, size=p)
+        uI = rng.normal(0.0, 0.1, size=p)
+        phiR, phiI = 0.1, -0.2
+        cfgs = []
+        for c in range(sysd["ncfg"]):
+            if dim == 1:
+                R = rng.uniform(-L / 2, L / 2, size=(n, dim))
+            else:
+                R = lattice(n, dim, L, rng, jitter=sysd["jitter"]) - L / 2
+            cfgs.append(R)
+        cfgs = np.array(cfgs)
+        script = system_cmd(dim, n, p, L, sysd["knots"], sysd["sysp"], 0.0).replace("SYSTEM", "SYSTEMPB", 1)
+        script += "PARAMS %s %s %.17g %.17g\n" % (fmt(uR), fmt(uI), phiR, phiI)
+        script += "EVAL %d\n" % len(cfgs)
+        for R in cfgs:
+            script += fmt(R) + "\n"
+        moves = []
+        for c in range(16):
+            R = cfgs[c % len(cfgs)]
+            part = int(rng.integers(n))
+            newpos = R[part] + rng.normal(0.0, 0.4, size=dim)
+            moves.append((R, part, newpos))
+        script += "MOVE %d\n" % len(moves)
+        for R, part, newpos in moves:
+            script += "%s %d %s\n" % (fmt(R), part, fmt(newpos))
+        rows = run(ref_root, script)
+        ev = np.array(rows["EVAL"])
+        mv = np.array(rows["MOVE"])
+        np.savez(os.path.join(HERE, "pb_eval_%s.npz" % sysd["name"]),
+                 dim=dim, n=n, p=p, L=L, knots=np.asarray(sysd["knots"]), sysp=np.array(sysd["sysp"]), time=0.0,
+                 uR=uR, uI=uI, phiR=phiR, phiI=phiI, cfgs=cfgs,
+                 ref_lnpsi=ev[:, 0], ref_wf=ev[:, 1], ref_O=ev[:, 2:2 + p], ref_ER=ev[:, 2 + p],
+                 ref_EI=ev[:, 3 + p], ref_other=ev[:, 4 + p:13 + p],
+                 move_cfg=np.array([m[0] for m in moves]), move_part=np.array([m[1] for m in moves]),
+                 move_new=np.array([m[2] for m in moves]), ref_move=mv)
+        print("pb eval", sysd["name"], ev.shape, mv.shape)
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] not in ("obs", "driver") else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] not in ("obs", "driver", "pb") else "/root/reference"
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root])
     if "obs" in sys.argv[1:]:
@@ -180,7 +237,11 @@ def main():
     if "driver" in sys.argv[1:]:
         driver_run(ref_root)
         return
+    if "pb" in sys.argv[1:]:
+        pb_systems(ref_root)
+        return
     driver_run(ref_root)
+    pb_systems(ref_root)
     observables(ref_root)
 
     # ---- NIC known answers (the reference's own unit test vectors) ----

@@ -172,3 +172,58 @@ def test_oracle_observables_match_reference(name):
     # the k grid of the structure factor is the shell norm
     kn = np.sqrt((z["kvec"][z["shell_off"][:-1]] ** 2).sum(1))
     assert np.allclose(kn, z["ref_kgrid"], rtol=1e-14)
+
+
+PB_FILES = sorted(glob.glob(os.path.join(GOLD, "pb_eval_*.npz")))
+
+
+def load_pb(z):
+    return orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), user_knots=z["knots"],
+                            pot_kind=orc.POT_SQUARE, pot=z["sysp"], time=float(z["time"]), variant=orc.SYS_NU_PB)
+
+
+@pytest.mark.parametrize("path", PB_FILES, ids=[os.path.basename(p)[8:-4] for p in PB_FILES])
+def test_pb_eval_matches_reference(path):
+    """The mirrored-distance system (NUBosonsBulkPB.cpp): ln psi, O_k, E_loc,
+    the potential and the kinetic partial sums on fixed configurations, against
+    the reference's own evaluation at the tolerance of its spline weights."""
+    z = np.load(path)
+    s = load_pb(z)
+    for c, R in enumerate(z["cfgs"]):
+        r = s.eval(z["uR"], z["uI"], R)
+        assert relmax(r["lnpsi"], z["ref_lnpsi"][c]) < RTOL_REF
+        assert relmax(r["O"], z["ref_O"][c]) < RTOL_REF
+        scaleE = max(abs(z["ref_other"][c][0]), abs(z["ref_other"][c][1]), 1.0)
+        assert abs(r["eloc"][0] - z["ref_ER"][c]) < RTOL_REF * scaleE
+        assert abs(r["eloc"][1] - z["ref_EI"][c]) < RTOL_REF * scaleE
+        assert abs(r["other"][0] - z["ref_other"][c][0]) < RTOL_REF * scaleE
+        assert r["other"][1] == z["ref_other"][c][1]
+        assert relmax(r["other"][2:7], z["ref_other"][c][4:9]) < RTOL_REF
+
+
+def test_pb_fixtures_exercise_the_mirror():
+    """The 3D fixture holds pairs beyond r_max (entering at 2 r_max - r) and pairs
+    whose mirrored distance lies inside the square well (a potential the
+    BosonsBulk convention would not count)."""
+    z = np.load(os.path.join(GOLD, "pb_eval_d3_n64_p10.npz"))
+    L, rmax, a = float(z["L"]), float(z["knots"][-1]), float(z["sysp"][0])
+    beyond = well = 0
+    for R in z["cfgs"]:
+        for i in range(len(R)):
+            for j in range(i):
+                r, _ = orc.nic_disp(R[i], R[j], L)
+                beyond += r >= rmax
+                well += r >= rmax and 2 * rmax - r < a
+    assert beyond > 1000 and well > 0
+    assert any(v > 0 for v in z["ref_other"][:, 1])
+
+
+@pytest.mark.parametrize("path", PB_FILES, ids=[os.path.basename(p)[8:-4] for p in PB_FILES])
+def test_pb_move_matches_reference(path):
+    """Exponent change of a single-particle move of the mirrored-distance system
+    (NUBosonsBulkPB.cpp:612-690: r < r_max for the old and the new position)."""
+    z = np.load(path)
+    s = load_pb(z)
+    for R, part, new, ref in zip(z["move_cfg"], z["move_part"], z["move_new"], z["ref_move"]):
+        d = s.move_delta(z["uR"], R, int(part), new)
+        assert abs(d - (ref[1] - ref[0])) < RTOL_REF * max(abs(ref[0]), 1.0)
