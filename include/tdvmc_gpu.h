@@ -51,6 +51,19 @@ extern "C" {
 #define TDVMC_POT_GAUSS 2  /* b exp(-(r/a)^2 / 2)  (BosonsBulk.cpp:263-265)  */
 #define TDVMC_POT_LJ 3     /* 4 b ((a/r)^12 - (a/r)^6) (Potentials/LJ.cpp:16-22) */
 
+/* physical systems: the reference's SYSTEM_TYPE (src/TDVMC.cpp:2843-2850, 2953-2960) */
+#define TDVMC_SYS_BOSONS_BULK 0 /* PhysicalSystems::BosonsBulk */
+/* PhysicalSystems::NUBosonsBulkPB: a pair at r >= r_max enters every sum at the
+ * mirrored distance r' = 2 r_max - r and counts iff r' < r_max; gradient terms
+ * d / r' with the sign of d (NUBosonsBulkPB.cpp:333-336, 381-392); Laplacian
+ * (D-1)/r' (398); square-well potential b [r' < a] (347-350); boundary fold
+ * O_k = S_{k+1}, O_1 += S_0, O_{p-1} += S_{p+1} (219-228).  Requires the knots
+ * (n_user_knots = p: the reference reads them before it builds any default),
+ * pot_kind TDVMC_POT_SQUARE, and 2 r_max >= sqrt(dim) L / 2 so that every
+ * mirrored distance is non-negative (below that the reference indexes its
+ * spline tables out of range). */
+#define TDVMC_SYS_NU_BOSONS_BULK_PB 1
+
 typedef struct tdvmc_ctx tdvmc_ctx;
 
 /* System description: the reference's globals N, DIM, N_PARAM, LBOX
@@ -68,6 +81,7 @@ typedef struct tdvmc_system_desc {
 	double pot[5];
 	double hbar2_2m;           /* HBAR2_2M; 1.0 in the reference */
 	int32_t precision;         /* TDVMC_PREC_* */
+	int32_t system_type;       /* TDVMC_SYS_*; 0 (zero-initialised) is BosonsBulk */
 	int64_t n_walkers;         /* independent Markov chains, >= 1 */
 } tdvmc_system_desc;
 
@@ -177,7 +191,8 @@ int tdvmc_eval_stored(tdvmc_ctx* ctx, double* lnpsi, double* O, double* eloc, do
  * CalculateAdditionalSystemProperties, TDVMC.cpp:1332-1388).
  * g(r): the grid [0, r_max) with spacing r_max / gr_bins (GR_BIN_COUNT,
  * BosonsBulk.cpp:145); gr[] receives *gr_count (<= gr_bins) values: pairs
- * i < j with r < r_max, each adding D/(N-1) / (volume of its shell).
+ * i < j with r < r_max, each adding D/(N-1) / (volume of its shell)
+ * (NUBosonsBulkPB: 1 / (volume of its shell), NUBosonsBulkPB.cpp:602-612).
  * S(k): kvec[nvec*dim] are the k vectors already scaled by 2 pi / L (the
  * integer vectors of kVectors{D}D.json), shell s owns rows
  * shell_off[s] .. shell_off[s+1]-1 (shell_off[0] = 0, nvec <= 4096);

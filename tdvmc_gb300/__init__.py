@@ -6,4 +6,4 @@ interface (``system`` for the periodic bulk system, ``drops`` for batched
 trapped drops of uneven particle number) and builds it (``build``).
 """
 from .drops import DropsTDVP, TrappedDrops  # noqa: F401
-from .system import BosonsBulk, TDVP  # noqa: F401
+from .system import BosonsBulk, NUBosonsBulkPB, TDVP  # noqa: F401

@@ -14,6 +14,7 @@ from . import build as _build
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_NOT_PD, ERR_NONFINITE = range(7)
 PREC_FP64, PREC_MIXED = 0, 1
 POT_NONE, POT_SQUARE, POT_GAUSS, POT_LJ = 0, 1, 2, 3
+SYS_BOSONS_BULK, SYS_NU_BOSONS_BULK_PB = 0, 1
 
 # every entry point of include/tdvmc_gpu.h
 EXPORTS = ("tdvmc_status_string", "tdvmc_create", "tdvmc_destroy", "tdvmc_get_stream", "tdvmc_set_time",
@@ -34,7 +35,7 @@ class SystemDesc(C.Structure):
     _fields_ = [("dim", C.c_int32), ("n", C.c_int32), ("p", C.c_int32), ("n_user_knots", C.c_int32),
                 ("user_knots", C.POINTER(C.c_double)), ("box_length", C.c_double), ("pot_kind", C.c_int32),
                 ("n_pot", C.c_int32), ("pot", C.c_double * 5), ("hbar2_2m", C.c_double), ("precision", C.c_int32),
-                ("n_walkers", C.c_int64)]
+                ("system_type", C.c_int32), ("n_walkers", C.c_int64)]
 
 
 class DropsDesc(C.Structure):

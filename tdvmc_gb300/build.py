@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # translation units compiled in parallel; the kernel instantiations are
 # spread over them by the TDVMC_TU_* macros in tdvmc_capi.cu
-UNITS = ["tdvmc_capi.cu", "inst_sample_f32.cu", "inst_sample_f64.cu", "inst_eloc_f32.cu", "inst_eloc_f64.cu",
+UNITS = ["tdvmc_capi.cu", "inst_sample_f32.cu", "inst_sample_f64.cu", "inst_eloc_f32.cu", "inst_eloc_f64.cu", "inst_pb.cu",
          "k_gram_tf32.cu", "k_peak.cu", "noalloc_stats.cu", "drops_capi.cu"]
 
 

@@ -41,6 +41,8 @@ struct SysConst {
 	// -2 (L - Lf), Lf the FP32 box length: the first-order share of the FP32 box
 	// length's remainder in the r^2 of a wrapped pair (see pair_r2_f32)
 	float lc;
+	// 1: NUBosonsBulkPB, a pair at r >= r_max enters at r' = 2 r_max - r (mirror_r)
+	int mirror;
 };
 
 // Values that change between stages or steps live in device memory so a
@@ -133,6 +135,25 @@ __device__ __forceinline__ float pair_r(float r2) {
 	return r;
 }
 __device__ __forceinline__ double pair_r(double r2) { return r2 * rsqrt_(r2); }
+
+// NUBosonsBulkPB (NUBosonsBulkPB.cpp:249-253, 333-336, 690-693): a pair at r >= r_max enters at
+// the mirrored distance r' = 2 r_max - r (m2 = 2 r_max), and q ~ 1/r becomes
+// 1/r' (correctly rounded).  The pair's direction keeps the sign of d: the
+// reference's first-derivative factor stays 1 (outsideL2 is never set).
+__device__ __forceinline__ void mirror_r(float m2, float& r, float& q) {
+	const float rm = __fsub_rn(m2, r);
+	if (rm < r) {
+		r = rm;
+		q = __frcp_rn(rm);
+	}
+}
+__device__ __forceinline__ void mirror_r(double m2, double& r, double& q) {
+	const double rm = __dsub_rn(m2, r);
+	if (rm < r) {
+		r = rm;
+		q = __drcp_rn(rm);
+	}
+}
 
 // Interval lookup over [0, r_max]: returns j (interval index; knot k_{j+3})
 // and the local coordinate t in [0, 1].  kb[j] = left knot, hv[j] = 1/width,

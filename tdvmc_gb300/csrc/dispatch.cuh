@@ -31,6 +31,18 @@ ElocFn<double> pick_eloc_f64(int lanes, bool adj, int hist);
 RevFn<float> pick_eloc_rev_f32(int lanes, int hist);
 RevFn<double> pick_eloc_rev_f64(int lanes, int hist);
 
+// NUBosonsBulkPB (mirrored distances): 32 lanes, histogram mode 0, the scalar
+// sampler; null for any other tile
+template <typename T> SampleFn<T> pick_sample_pb(int lanes, int slots);
+template <typename T> ElocFn<T> pick_eloc_pb(int lanes, bool adj, int hist);
+template <typename T> RevFn<T> pick_eloc_rev_pb(int lanes, int hist);
+template <> SampleFn<float> pick_sample_pb<float>(int lanes, int slots);
+template <> SampleFn<double> pick_sample_pb<double>(int lanes, int slots);
+template <> ElocFn<float> pick_eloc_pb<float>(int lanes, bool adj, int hist);
+template <> ElocFn<double> pick_eloc_pb<double>(int lanes, bool adj, int hist);
+template <> RevFn<float> pick_eloc_rev_pb<float>(int lanes, int hist);
+template <> RevFn<double> pick_eloc_rev_pb<double>(int lanes, int hist);
+
 template <typename T> SampleFn<T> pick_sample(int lanes, int slots);
 template <> inline SampleFn<float> pick_sample<float>(int g, int s) { return pick_sample_f32(g, s); }
 template <> inline SampleFn<double> pick_sample<double>(int g, int s) { return pick_sample_f64(g, s); }

@@ -70,6 +70,7 @@ template <typename T> struct CsGeom {
 // FP32: r <= r_max from the FP32 distance; nearmin collects |r - r_max|, and the
 // pairs within rounding of r_max are decided again in FP64 after the slot
 // (cs_fix_slot).  force: the pair as within r_max whatever r is (the fix-up).
+// sc.mirror: the distances of NUBosonsBulkPB (mirror_r).
 template <typename T>
 __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
                                              const T* __restrict__ kb, const T* __restrict__ hv,
@@ -93,8 +94,15 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
 		g.rinv = rsqrt_(r2);
 		g.r = r2 * g.rinv;
 	}
-	const bool cut = force || g.r <= (T)sc.rmax;
-	if constexpr (sizeof(T) == 4) nearmin = fminf(nearmin, fabsf(g.r - (T)sc.rmax));
+	bool cut;
+	if (sc.mirror) {
+		// NUBosonsBulkPB: the mirrored distance, counted iff r' < r_max (no second look)
+		mirror_r((T)(2.0 * sc.rmax), g.r, g.rinv);
+		cut = g.r < (T)sc.rmax;
+	} else {
+		cut = force || g.r <= (T)sc.rmax;
+		if constexpr (sizeof(T) == 4) nearmin = fminf(nearmin, fabsf(g.r - (T)sc.rmax));
+	}
 	g.in = ok && cut;
 	g.out = ok && !cut;
 	T t;

@@ -316,7 +316,8 @@ template <typename T> struct FwdPair {
 	bool cut;  // within r_max
 };
 
-template <typename T>
+// MIR: the mirrored distance of NUBosonsBulkPB (mirror_r), counted iff r' < r_max.
+template <typename T, bool MIR = false>
 __device__ __forceinline__ FwdPair<T> fwd_pair(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
                                                const Q4<T>* __restrict__ coefC, const T* __restrict__ kb,
                                                const T* __restrict__ hv, const int* __restrict__ lut) {
@@ -328,7 +329,12 @@ __device__ __forceinline__ FwdPair<T> fwd_pair(const SysConst& sc, const Q4<T>& 
 	const T r2 = q.dx * q.dx + q.dy * q.dy + q.dz * q.dz;
 	q.rinv = rsqrt_(r2);
 	q.r = r2 * q.rinv;
-	q.cut = within_rmax<T>(sc, q.r, xr, xi);
+	if constexpr (MIR) {
+		mirror_r((T)(2.0 * sc.rmax), q.r, q.rinv);
+		q.cut = q.r < (T)sc.rmax;
+	} else {
+		q.cut = within_rmax<T>(sc, q.r, xr, xi);
+	}
 	q.in = ok && q.cut;
 	q.j = locate<T>(sc, q.r, kb, hv, lut, q.t);
 	const Q4<T> cR = coefC[3 * q.j];
@@ -619,7 +625,7 @@ __device__ __forceinline__ void pair_pot2(int kind, float rA, float rB, float qa
 	vb += inA ? vA : 0.f;
 	vb += inB ? vB : 0.f;
 }
-template <bool DIAG, bool ADJ, int HIST>
+template <bool DIAG, bool ADJ, int HIST, bool MIR = false>
 __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n, int lane, int nrow, bool rowok,
                                                const Q4<float>& xr, const Q4<float>* __restrict__ xs,
                                                const Q4<float>* __restrict__ coefC, const float* __restrict__ kb,
@@ -627,7 +633,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
                                                float* __restrict__ hist, float pa, float pb, KSum<float>* own,
                                                float* trav, KSum<float>& elR, KSum<float>& elI, KSum<float>& vsum,
                                                float& nearmin) {
-	const float rmax = (float)sc.rmax;
+	const float rmax = (float)sc.rmax, m2 = (float)(2.0 * sc.rmax);
 	const f2_t RM2 = f2_make(rmax, rmax);
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t R2 = f2_make(kRoundF, kRoundF);
@@ -672,11 +678,20 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
 			float qa, qb;
-			const f2_t r = pair_r_f2<true>(box, dx, dy, dz, qa, qb);
+			f2_t r = pair_r_f2<true>(box, dx, dy, dz, qa, qb);
 			float rA, rB;
 			f2_split(r, rA, rB);
-			const bool inA = okA && (rA <= rmax), inB = okB && (rB <= rmax);
-			{
+			bool inA, inB;
+			if constexpr (MIR) {
+				// mirrored distances: r' = r_max is a set of measure zero, no second look
+				mirror_r(m2, rA, qa);
+				mirror_r(m2, rB, qb);
+				r = f2_make(rA, rB);
+				inA = okA && (rA < rmax);
+				inB = okB && (rB < rmax);
+			} else {
+				inA = okA && (rA <= rmax);
+				inB = okB && (rB <= rmax);
 				// distance to r_max: pairs within rounding of it are decided again after the block
 				float da, db;
 				f2_split(f2_sub(r, RM2), da, db);
@@ -768,7 +783,7 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 // The half sweep of half_block_f32 in scalar arithmetic (FP64): the same
 // rotation schedule, travelling partner sums and statistics, two steps per
 // iteration as independent pairs.
-template <typename T, bool DIAG, bool ADJ, int HIST>
+template <typename T, bool DIAG, bool ADJ, int HIST, bool MIR = false>
 __device__ __forceinline__ void half_block_s(const SysConst& sc, int sp, int n, int lane, bool rowok,
                                              const Q4<T>& xr, const Q4<T>* __restrict__ xs,
                                              const Q4<T>* __restrict__ coefC, const T* __restrict__ kb,
@@ -787,7 +802,7 @@ __device__ __forceinline__ void half_block_s(const SysConst& sc, int sp, int n, 
 			const int kk = k + h;
 			const int i = sp * 32 + ((lane + kk) & 31);
 			const bool ok = DIAG ? (rowok && i < n && (kk < 16 || (kk == 16 && lane < 16))) : rowok;
-			q[h] = fwd_pair<T>(sc, xr, xs[DIAG && i >= n ? 0 : i], ok, coefC, kb, hv, lut);
+			q[h] = fwd_pair<T, MIR>(sc, xr, xs[DIAG && i >= n ? 0 : i], ok, coefC, kb, hv, lut);
 		}
 #pragma unroll
 		for (int h = 0; h < S; h++) {
@@ -819,7 +834,7 @@ __device__ __forceinline__ void half_block_s(const SysConst& sc, int sp, int n, 
 	vsum.add(vb);
 }
 
-template <typename T, bool DIAG, bool ADJ, int HIST>
+template <typename T, bool DIAG, bool ADJ, int HIST, bool MIR = false>
 __device__ __forceinline__ void half_block(const SysConst& sc, int sp, int n, int lane, int nrow, bool rowok,
                                            float& nearmin, const Q4<T>& xr,
                                            const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ coefC,
@@ -827,10 +842,10 @@ __device__ __forceinline__ void half_block(const SysConst& sc, int sp, int n, in
                                            const int* __restrict__ lut, T* __restrict__ hist, T pa, T pb,
                                            KSum<T>* own, T* trav, KSum<T>& elR, KSum<T>& elI, KSum<T>& vsum) {
 	if constexpr (std::is_same<T, float>::value)
-		half_block_f32<DIAG, ADJ, HIST>(sc, sp, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
+		half_block_f32<DIAG, ADJ, HIST, MIR>(sc, sp, n, lane, nrow, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own,
 		                                trav, elR, elI, vsum, nearmin);
 	else
-		half_block_s<T, DIAG, ADJ, HIST>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own, trav,
+		half_block_s<T, DIAG, ADJ, HIST, MIR>(sc, sp, n, lane, rowok, xr, xs, coefC, kb, hv, lut, hist, pa, pb, own, trav,
 		                                 elR, elI, vsum);
 }
 
@@ -969,7 +984,7 @@ __device__ __noinline__ void rev_region_fix(SysConst sc, int i0, int i1, int nro
 
 // Reverse sweep over unordered pairs (i < nrow) for partners [i0, i1), kNp
 // partners per iteration.
-template <typename T, int G, bool DIAG, int HIST>
+template <typename T, int G, bool DIAG, int HIST, bool MIR = false>
 __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, int nrow, bool rowok, const Q4<T>& xr,
                                            const T* gn, const Q4<T>* __restrict__ xs, const Q4<T>* __restrict__ g4,
                                            const T* __restrict__ gz, const T* __restrict__ kb,
@@ -989,9 +1004,16 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 			const T giz = gz[ii];
 			const T dx = nic(xr.x - xi.x, L, Lr), dy = nic(xr.y - xi.y, L, Lr), dz = nic(xr.z - xi.z, L, Lr);
 			const T r2 = dx * dx + dy * dy + dz * dz;
-			const T rinv = rsqrt_(r2);
-			const T r = r2 * rinv;
-			const bool on = have && rowok && within_rmax<T>(sc, r, xr, xi) && (DIAG ? (ii < nrow) : true);
+			T rinv = rsqrt_(r2);
+			T r = r2 * rinv;
+			bool cut;
+			if constexpr (MIR) {
+				mirror_r((T)(2.0 * sc.rmax), r, rinv);
+				cut = r < rmax;
+			} else {
+				cut = within_rmax<T>(sc, r, xr, xi);
+			}
+			const bool on = have && rowok && cut && (DIAG ? (ii < nrow) : true);
 			T t;
 			jj[h] = locate<T>(sc, r, kb, hv, lut, t);
 			t = on ? t : T(0);  // t is NaN for the self pair
@@ -1019,14 +1041,14 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 // slot [i0, i1), lane l meets row i0 + (l + k) mod 32 at steps k = 1..16
 // (step 16 for lanes below 16 only), every unordered pair of the slot once
 // with no idle lanes; the pair terms do not depend on which row is first.
-template <int G, bool DIAG, int HIST, bool ROT = false>
+template <int G, bool DIAG, int HIST, bool ROT = false, bool MIR = false>
 __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1, int nrow, bool rowok,
                                               const Q4<float>& xr, const float* gn, const Q4<float>* __restrict__ xs,
                                               const Q4<float>* __restrict__ g4, const float* __restrict__ gz,
                                               const float* __restrict__ kb, const float* __restrict__ hv,
                                               const int* __restrict__ lut, float* __restrict__ hist, int lane,
                                               float& nearmin) {
-	const float rmax = (float)sc.rmax;
+	const float rmax = (float)sc.rmax, m2 = (float)(2.0 * sc.rmax);
 	const f2_t RM2 = f2_make(rmax, rmax);
 	const f2_t X2 = f2_make(xr.x, xr.x), Y2 = f2_make(xr.y, xr.y), Z2 = f2_make(xr.z, xr.z);
 	const f2_t R2 = f2_make(kRoundF, kRoundF);
@@ -1067,17 +1089,27 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
 			float qa, qb;
-			const f2_t r = pair_r_f2<false>(box, dx, dy, dz, qa, qb);
+			f2_t r = MIR ? pair_r_f2<true>(box, dx, dy, dz, qa, qb) : pair_r_f2<false>(box, dx, dy, dz, qa, qb);
 			float rA, rB;
 			f2_split(r, rA, rB);
-			const bool onA = haveA && rowok && (rA <= rmax) && ((DIAG && !ROT) ? (ia < nrow) : true);
-			const bool onB = haveB && rowok && (rB <= rmax) && ((DIAG && !ROT) ? (ib < nrow) : true);
-			{
+			bool cA, cB;
+			if constexpr (MIR) {
+				// mirrored distances, formed as the forward sweep forms them (no second look)
+				mirror_r(m2, rA, qa);
+				mirror_r(m2, rB, qb);
+				r = f2_make(rA, rB);
+				cA = rA < rmax;
+				cB = rB < rmax;
+			} else {
+				cA = rA <= rmax;
+				cB = rB <= rmax;
 				// distance to r_max: pairs within rounding of it are decided again after the region
 				float da, db;
 				f2_split(f2_sub(r, RM2), da, db);
 				nearmin = fminf(nearmin, fminf(fabsf(da), fabsf(db)));
 			}
+			const bool onA = haveA && rowok && cA && ((DIAG && !ROT) ? (ia < nrow) : true);
+			const bool onB = haveB && rowok && cB && ((DIAG && !ROT) ? (ib < nrow) : true);
 			float tA, tB;
 			int jA, jB;
 			if (sc.uniform) {
@@ -1143,7 +1175,8 @@ __device__ __forceinline__ void hist_reduce(T* hist, T* red, int nbin, int nm, i
 // dE_loc/d alpha to dE_o, which k_eloc_rev completes.
 // FP32 32-lane groups: at most 2 walkers (64 threads) per block and 5 blocks
 // per SM, so that registers (<= 204) and shared memory both allow 10 resident walkers.
-template <typename T, int G, bool ADJ, int HIST>
+// MIR: NUBosonsBulkPB (mirrored distances; 32-lane groups only).
+template <typename T, int G, bool ADJ, int HIST, bool MIR = false>
 __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 32 && sizeof(T) == 4) ? 5 : 1)
     k_eloc(SysConst sc, const DynState* __restrict__ dyn, const Q4<T>* __restrict__ coefC_g,
                                               const T* __restrict__ kb_g, const T* __restrict__ hv_g,
@@ -1152,6 +1185,7 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
                                               const T* __restrict__ pos, int64_t nw, T* __restrict__ lnpsi_o,
                                               T* __restrict__ O_o, T* __restrict__ eloc_o, T* __restrict__ other_o,
                                               T* __restrict__ dE_o, T* __restrict__ gout) {
+	static_assert(!MIR || G == 32, "mirrored distances: 32-lane groups");
 	constexpr int NM = kFwdMoments;
 	constexpr int NMH = HistSlots<HIST, false>::value;
 	extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -1222,7 +1256,7 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 					for (int c = 0; c < 5; c++) pacc[c] = gacc[c * n + pr];
 					T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
 					float nearmin = 3.0e38f;
-					half_block<T, false, ADJ, HIST>(sc, sp, n, lane, nrow, rowok, nearmin, xr, xs, coefC, kb, hv, lut,
+					half_block<T, false, ADJ, HIST, MIR>(sc, sp, n, lane, nrow, rowok, nearmin, xr, xs, coefC, kb, hv, lut,
 					                                hist, pa, pb, own, trav, e_lR, e_lI, e_v);
 					// the partners' shares are home
 					xs[pr].w -= trav[0];
@@ -1246,7 +1280,7 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 				}
 				T trav[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
 				float nearmin = 3.0e38f;
-				half_block<T, true, ADJ, HIST>(sc, s, n, lane, nrow, rowok, nearmin, xr, xs, coefC, kb, hv, lut, hist,
+				half_block<T, true, ADJ, HIST, MIR>(sc, s, n, lane, nrow, rowok, nearmin, xr, xs, coefC, kb, hv, lut, hist,
 				                               pa, pb, own, trav, e_lR, e_lI, e_v);
 #pragma unroll
 				for (int c = 0; c < 6; c++) own[c].add(-__shfl_sync(0xffffffffu, trav[c], (lane + 15) & 31));
@@ -1407,11 +1441,12 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 // of k_eloc, accumulating sum t^c ((G_n - G_i) . rhat_ni + (D-1)/r) per
 // interval, then adds 2 sum_n G_n . sD_k + the (D-1)/r B' part of the
 // Laplacian of O_k to the dE_o that k_eloc started.
-template <typename T, int G, int HIST>
+template <typename T, int G, int HIST, bool MIR = false>
 __global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __restrict__ kb_g, const T* __restrict__ hv_g,
                                                   const int* __restrict__ lut_g, const T* __restrict__ loc_g,
                                                   const double* __restrict__ fold_g, const T* __restrict__ pos,
                                                   const T* __restrict__ gin, int64_t nw, T* __restrict__ dE_o) {
+	static_assert(!MIR || G == 32, "mirrored distances: 32-lane groups");
 	constexpr int NMH = HistSlots<HIST, true>::value;
 	extern __shared__ __align__(32) unsigned char smem_raw[];
 	const int nbin = sc.nbin, n = sc.n, ns = sc.ns, P = sc.p;
@@ -1476,10 +1511,10 @@ __global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __res
 			const int dend = (base + G < n) ? base + G : n;
 			if constexpr (std::is_same<T, float>::value) {
 				float nm0 = 3.0e38f, nm1 = 3.0e38f;
-				rev_region_f2<G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane,
-				                              nm0);
-				rev_region_f2<G, true, HIST, G == 32>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist,
-				                                      lane, nm1);
+				rev_region_f2<G, false, HIST, false, MIR>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist,
+				                                          lane, nm0);
+				rev_region_f2<G, true, HIST, G == 32, MIR>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut,
+				                                           hist, lane, nm1);
 				// pairs within rounding of r_max, decided again in FP64 (rev_region_fix)
 				if (__any_sync(gmask, nm0 < sc.rcut_band || nm1 < sc.rcut_band)) {
 					const Grad6 g6 = {{gn[0], gn[1], gn[2], gn[3], gn[4], gn[5]}};
@@ -1491,8 +1526,8 @@ __global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __res
 						                                       hist, lane);
 				}
 			} else {
-				rev_region<T, G, false, HIST>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
-				rev_region<T, G, true, HIST>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				rev_region<T, G, false, HIST, MIR>(sc, 0, base, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
+				rev_region<T, G, true, HIST, MIR>(sc, base, dend, nrow, rowok, xr, gn, xs, g4, gz, kb, hv, lut, hist, lane);
 			}
 		}
 		hist_reduce<T, G, HIST, NMH>(hist, redr, nbin, kRevMoments, lane, gmask);

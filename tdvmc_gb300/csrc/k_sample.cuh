@@ -28,11 +28,15 @@ template <typename T> struct alignas(4 * sizeof(T)) Q4 {
 // centred local coordinate tau = t - 1/2 (better conditioned and one
 // operation shorter); entries nbin .. ncoef-1 are the constant outer-pair
 // value uR[p-1] (coefficients (u, 0, 0, 0)), selected for r >= r_max.
-template <typename T>
+// MIR (NUBosonsBulkPB): r enters as r' = min(r, 2 r_max - r) (mirror_r), held
+// at 0 and above for the phantom slots, whose two terms of a move then read
+// the same entry and still cancel exactly.
+template <typename T, bool MIR = false>
 __device__ __forceinline__ T pair_u(const SysConst& sc, T r2, const Q4<T>* __restrict__ coef,
                                     const T* __restrict__ kb, const T* __restrict__ hv,
                                     const int* __restrict__ lut) {
-	const T r = pair_r(r2);
+	T r = pair_r(r2);
+	if constexpr (MIR) r = fmax(fmin(r, (T)(2.0 * sc.rmax) - r), T(0));
 	T tau;
 	int j;
 	if (sc.uniform) {
@@ -83,7 +87,7 @@ __host__ __device__ inline size_t sample_smem_bytes(int ncoef, int nbin, int nce
 	return b + (size_t)groups * n * sizeof(Q4<T>);
 }
 
-template <typename T, int G, int SLOTS>
+template <typename T, int G, int SLOTS, bool MIR = false>
 __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __restrict__ coef_g, const T* __restrict__ uout_g,
                                                 const T* __restrict__ kb_g, const T* __restrict__ hv_g,
                                                 const int* __restrict__ lut_g, T* __restrict__ pos, int64_t nw,
@@ -169,8 +173,8 @@ __global__ void __launch_bounds__(128) k_sample(SysConst sc, const Q4<T>* __rest
 					if (s == SLOTS - 1) valid = valid && (s * G + lane < n);
 					const T r2n = mi_r2(x[s] - xn0, y[s] - xn1, z[s] - xn2, L);
 					const T r2o = mi_r2(x[s] - xo.x, y[s] - xo.y, z[s] - xo.z, L);
-					const T un = pair_u<T>(sc, r2n, coef, kb, hv, lut);
-					const T uo = pair_u<T>(sc, r2o, coef, kb, hv, lut);
+					const T un = pair_u<T, MIR>(sc, r2n, coef, kb, hv, lut);
+					const T uo = pair_u<T, MIR>(sc, r2o, coef, kb, hv, lut);
 					dsum += valid ? (un - uo) : T(0);
 				}
 #pragma unroll

@@ -229,12 +229,12 @@ int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed, int64_t
 	const int slots = slots_for(ctx->sc.n, G);
 	SampleFn<T> fn = nullptr;
 	if constexpr (std::is_same<T, float>::value)
-		if (ctx->packed_sampler && ctx->sc.uniform) {
+		if (ctx->packed_sampler && ctx->sc.uniform && !ctx->sc.mirror) {
 			if (ctx->shared_coords) fn = pick_sample_f32_packed_shared(G, slots);
 			if (!fn) fn = pick_sample_f32_packed(G, slots);
 		}
 	const bool packed = fn != nullptr;
-	if (!fn) fn = pick_sample<T>(G, slots);
+	if (!fn) fn = ctx->sc.mirror ? pick_sample_pb<T>(G, slots) : pick_sample<T>(G, slots);
 	if (!fn) return TDVMC_ERR_ARG;
 	const int threads = G * gpb;
 	const size_t smem =
@@ -319,8 +319,9 @@ int launch_eloc(tdvmc_ctx* ctx, bool adj, int64_t w0 = 0, int64_t count = -1, cu
 	if (!st) st = ctx->st;
 	const int G = ctx->tiles.eg;
 	const int hist = G == 32 ? ctx->tiles.hist : 0;
-	ElocFn<T> fn = pick_eloc<T>(G, adj, hist);
-	RevFn<T> fr = adj ? pick_eloc_rev<T>(G, hist) : nullptr;
+	const bool pb = ctx->sc.mirror != 0;
+	ElocFn<T> fn = pb ? pick_eloc_pb<T>(G, adj, hist) : pick_eloc<T>(G, adj, hist);
+	RevFn<T> fr = !adj ? nullptr : pb ? pick_eloc_rev_pb<T>(G, hist) : pick_eloc_rev<T>(G, hist);
 	if (!fn || (adj && !fr)) return TDVMC_ERR_ARG;
 	const SysConst& s = ctx->sc;
 	// the gradient scratch: the adjoint's input, and the 32-lane forward's partner sums
@@ -767,6 +768,11 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		return TDVMC_ERR_ARG;
 	if (d->n_user_knots > 0 && (d->user_knots == nullptr || d->n_user_knots != d->p)) return TDVMC_ERR_ARG;
 	if (d->n_pot < 0 || d->n_pot > 5) return TDVMC_ERR_ARG;
+	if (d->system_type != TDVMC_SYS_BOSONS_BULK && d->system_type != TDVMC_SYS_NU_BOSONS_BULK_PB) return TDVMC_ERR_ARG;
+	const bool pb = d->system_type == TDVMC_SYS_NU_BOSONS_BULK_PB;
+	// NUBosonsBulkPB reads r_max from its knot vector before it builds default knots
+	// (NUBosonsBulkPB.cpp:76, 91-97), and its potential is the square well (347-350)
+	if (pb && (d->n_user_knots == 0 || d->pot_kind != TDVMC_POT_SQUARE)) return TDVMC_ERR_ARG;
 	ctx = new tdvmc_ctx();
 	tdvmc_ctx& c = *ctx;
 	c.prec = d->precision;
@@ -801,8 +807,12 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	s.Lr = 1.0 / d->box_length;
 	s.hbar2_2m = d->hbar2_2m;
 	s.pot_kind = d->pot_kind;
-	// r_max below 1.5 L: the samplers' phantom slots (kPhantomBoxes) lie beyond it
-	if (s.ns - 2 != P || s.nbin > kMaxBins || !(s.rmax < 1.5 * s.L)) {
+	s.mirror = pb ? 1 : 0;
+	// r_max below 1.5 L: the samplers' phantom slots (kPhantomBoxes) lie beyond it.
+	// Mirrored distances 2 r_max - r stay non-negative for every pair (the largest
+	// minimum-image distance is sqrt(dim) L / 2; a margin of 1e-5 covers rounding).
+	if (s.ns - 2 != P || s.nbin > kMaxBins || !(s.rmax < 1.5 * s.L) ||
+	    (pb && !(2.0 * s.rmax >= std::sqrt((double)s.dim) * s.L / 2.0 * (1.0 + 1e-5)))) {
 		delete ctx;
 		return TDVMC_ERR_ARG;
 	}
@@ -819,6 +829,15 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	for (int i = 2, sp = 3; i < P - 2; i++, sp++) c.fold[(size_t)i * s.ns + sp] = 1.0;
 	for (int i = P - 2, idx = 0; i < P; i++, idx++)
 		for (int j = 0; j < 3; j++) c.fold[(size_t)i * s.ns + s.ns - 3 + j] = bce[idx][j];
+	if (pb) {
+		// NUBosonsBulkPB::RefreshLocalOperators (NUBosonsBulkPB.cpp:219-228):
+		// O_k = S_{k+1}, O_1 += S_0, O_{p-1} += S_{p+1} (the system declares a further
+		// spline S_{p+2} that no pair ever fills)
+		std::fill(c.fold.begin(), c.fold.end(), 0.0);
+		for (int k = 0; k < P; k++) c.fold[(size_t)k * s.ns + k + 1] = 1.0;
+		c.fold[(size_t)1 * s.ns + 0] += 1.0;
+		c.fold[(size_t)(P - 1) * s.ns + s.ns - 1] += 1.0;
+	}
 	// interval geometry
 	std::vector<double> kb(s.nbin), hv(s.nbin);
 	double hmin = 1e300, hmaxw = 0.0;
@@ -1057,8 +1076,10 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	if (c.prec == TDVMC_PREC_MIXED && c.sc.uniform && c.tiles.sg == 32 && slots_for(d->n, 32) == 11 &&
 	    slots_for(d->n, 16) == 22)
 		c.tiles.sg = 16;
+	// NUBosonsBulkPB: its kernels are built for a full warp per walker
+	if (pb) c.tiles.sg = c.tiles.eg = 32;
 	// TDVMC_SAMPLE_LANES overrides the sampler's lanes per walker (8, 16 or 32)
-	if (const char* sl = std::getenv("TDVMC_SAMPLE_LANES")) {
+	if (const char* sl = std::getenv("TDVMC_SAMPLE_LANES"); sl && !pb) {
 		const int g = std::atoi(sl);
 		if ((g == 8 || g == 16 || g == 32) && slots_for(d->n, g) > 0) c.tiles.sg = g;
 	}
@@ -1067,7 +1088,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	// TDVMC_EVAL_WALKERS_PER_BLOCK overrides the evaluation kernels' walkers per block
 	if (const char* e = std::getenv("TDVMC_EVAL_WALKERS_PER_BLOCK"))
 		c.tiles.egpb = std::max(1, std::min(128 / c.tiles.eg, std::atoi(e)));
-	if (const char* h = std::getenv("TDVMC_HIST")) c.tiles.hist = std::max(0, std::min(2, std::atoi(h)));
+	if (const char* h = std::getenv("TDVMC_HIST"); h && !pb) c.tiles.hist = std::max(0, std::min(2, std::atoi(h)));
 	if (const char* wt = std::getenv("TDVMC_TEST_WAIT_NS")) c.wait_ns = (uint64_t)std::strtoull(wt, nullptr, 10);
 	// TDVMC_SAMPLER=scalar selects the scalar FP32 sampler
 	if (const char* sm = std::getenv("TDVMC_SAMPLER")) {
@@ -1272,7 +1293,8 @@ int tdvmc_observables(tdvmc_ctx* ctx, int32_t gr_bins, int32_t nshell, const int
 	}
 	if (D > 1)
 		for (int i = count - 1; i > 0; i--) scale[i] = scale[i] - scale[i - 1];
-	const double weight = 1.0 / ((double)(N - 1)) * D;
+	// NUBosonsBulkPB adds 1.0 per pair (NUBosonsBulkPB.cpp:602-612)
+	const double weight = s.mirror ? 1.0 : 1.0 / ((double)(N - 1)) * D;
 	// k vectors padded to 3 components, in the working precision
 	const bool f64 = ctx->prec == TDVMC_PREC_FP64;
 	const size_t ts = tsize(ctx->prec);

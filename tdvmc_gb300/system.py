@@ -40,6 +40,8 @@ class BosonsBulk:
     (NURBS_GRID with USE_NURBS=1), ``hbar2_2m`` (HBAR2_2M).
     """
 
+    SYSTEM_TYPE = N.SYS_BOSONS_BULK
+
     def __init__(self, dim, n, n_param, box_length, n_walkers, system_params=(0.5, 2.0), potential="square",
                  user_knots=None, hbar2_2m=1.0, precision="fp64"):
         self.lib = N.load()
@@ -59,6 +61,7 @@ class BosonsBulk:
         d.hbar2_2m = float(hbar2_2m)
         d.precision = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
         d.n_walkers = self.nw
+        d.system_type = self.SYSTEM_TYPE
         self.precision = precision
         h = C.c_void_p()
         N.check(self.lib.tdvmc_create(C.byref(d), C.byref(h)), "tdvmc_create")
@@ -197,6 +200,23 @@ class BosonsBulk:
         s = C.c_void_p()
         N.check(self.lib.tdvmc_get_stream(self.h, C.byref(s)), "tdvmc_get_stream")
         return s.value
+
+
+class NUBosonsBulkPB(BosonsBulk):
+    """``PhysicalSystems::NUBosonsBulkPB`` (src/PhysicalSystems/NUBosonsBulkPB.cpp),
+    batched over walkers: the BosonsBulk methods with every pair at r >= r_max
+    entering at the mirrored distance 2 r_max - r (counted iff it lies below
+    r_max), gradient terms d / r' with the sign of d, the square-well potential
+    and the fold O_k = S_{k+1}, O_1 += S_0, O_{p-1} += S_{p+1}.  ``user_knots``
+    (NURBS_GRID) is required: the reference reads r_max from them before it
+    would build default knots (NUBosonsBulkPB.cpp:76, 91-97)."""
+
+    SYSTEM_TYPE = N.SYS_NU_BOSONS_BULK_PB
+
+    def __init__(self, dim, n, n_param, box_length, n_walkers, user_knots, system_params=(0.5, 2.0),
+                 hbar2_2m=1.0, precision="fp64"):
+        super().__init__(dim, n, n_param, box_length, n_walkers, system_params=system_params, potential="square",
+                         user_knots=user_knots, hbar2_2m=hbar2_2m, precision=precision)
 
 
 class TDVP:

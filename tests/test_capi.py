@@ -68,3 +68,38 @@ def test_no_gpu_create_reports_cuda_error():
     with pytest.raises(N.TdvmcError) as e:
         T.BosonsBulk(3, 8, 10, 4.0, 4)
     assert e.value.code == N.ERR_CUDA
+
+
+def test_mirrored_system_descriptor_checks():
+    """NUBosonsBulkPB descriptors that the reference could not run are refused
+    before any device call: no knots (it reads r_max from them), a potential other
+    than its square well, knots so short that a mirrored distance 2 r_max - r
+    could turn negative, and an unknown system type."""
+    import ctypes as C
+    import numpy as np
+    from tdvmc_gb300 import _native as N
+    lib = N.load()
+
+    def create(system_type=N.SYS_NU_BOSONS_BULK_PB, knots=(0.0, 0.5, 1.0, 1.5, 2.0), pot=N.POT_SQUARE, L=4.0,
+               dim=3):
+        d = N.SystemDesc()
+        d.dim, d.n, d.p = dim, 8, 5
+        kn = None if knots is None else np.ascontiguousarray(knots, dtype=np.float64)
+        d.n_user_knots = 0 if kn is None else kn.size
+        d.user_knots = C.POINTER(C.c_double)() if kn is None else kn.ctypes.data_as(C.POINTER(C.c_double))
+        d.box_length, d.pot_kind, d.n_pot = L, pot, 2
+        d.pot[0], d.pot[1] = 0.5, 1.0
+        d.hbar2_2m, d.precision, d.system_type, d.n_walkers = 1.0, N.PREC_FP64, system_type, 4
+        h = C.c_void_p()
+        rc = lib.tdvmc_create(C.byref(d), C.byref(h))
+        if rc == 0:
+            lib.tdvmc_destroy(h)
+        return rc
+
+    assert create(knots=None) == N.ERR_ARG
+    assert create(pot=N.POT_LJ) == N.ERR_ARG
+    # 3D, L = 4: the largest minimum-image distance is 2 sqrt(3) = 3.46, so r_max must reach 1.73
+    assert create(knots=(0.0, 0.4, 0.8, 1.2, 1.6)) == N.ERR_ARG
+    assert create(system_type=7) == N.ERR_ARG
+    # 1D: r_max = L / 4 + 0.4 is enough
+    assert create(knots=(0.0, 0.35, 0.7, 1.05, 1.4), dim=1) != N.ERR_ARG

@@ -1,0 +1,211 @@
+"""GPU parity of the mirrored-distance system (PhysicalSystems::NUBosonsBulkPB)
+through the C ABI, against the FP64 oracle's NUBosonsBulkPB variant and the
+reference's own values in the pb_eval_* fixtures.
+
+Tolerances (stated per test):
+  FP64 path   relative 1e-12 against the oracle (ln psi, O_k, E_loc, the kinetic
+              sums, dE_loc/d alpha), and the fixtures' tolerance 5e-9 against the
+              reference's own numbers;
+  mixed path  relative 1e-5 per walker on FP32-representable coordinates;
+  sampler     FP64: the oracle's chain (positions 1e-9, identical acceptance);
+              FP32: the same moves on at least 90 % of the walkers;
+  steps       FP64 RK4 step (direct and on stored samples): parameters 1e-9.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+PB_FILES = sorted(glob.glob(os.path.join(GOLD, "pb_eval_*.npz")))
+RTOL_REF = 5e-9
+
+pytestmark = pytest.mark.gpu
+
+
+def relmax(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def soa(cfgs):
+    return np.ascontiguousarray(np.transpose(np.asarray(cfgs), (0, 2, 1)))
+
+
+def gpu_pb(z, nw, precision, hbar2_2m=1.0):
+    import tdvmc_gb300 as T
+    s = T.NUBosonsBulkPB(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), nw, user_knots=z["knots"],
+                         system_params=z["sysp"], hbar2_2m=hbar2_2m, precision=precision)
+    s.SetTime(float(z["time"]))
+    return s
+
+
+def oracle_pb(z, hbar2_2m=1.0):
+    return orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), user_knots=z["knots"],
+                            pot_kind=orc.POT_SQUARE, pot=z["sysp"], time=float(z["time"]), hbar2_2m=hbar2_2m,
+                            variant=orc.SYS_NU_PB)
+
+
+CASES = [(f, prec) for f in PB_FILES for prec in ("fp64", "mixed")]
+
+
+@pytest.mark.parametrize("path,precision", CASES,
+                         ids=["%s-%s" % (os.path.basename(c[0])[8:-4], c[1]) for c in CASES])
+def test_pb_eval_and_adjoint_match_oracle(path, precision):
+    z = np.load(path)
+    cfgs = z["cfgs"]
+    if precision == "mixed":
+        cfgs = cfgs.astype(np.float32).astype(np.float64)
+    nw = len(cfgs)
+    s = gpu_pb(z, nw, precision)
+    o = oracle_pb(z)
+    s.SetParameters(z["uR"], z["uI"], float(z["phiR"]), float(z["phiI"]))
+    s.SetWalkers(soa(cfgs))
+    fwd = s.CalculateExpectationValues()
+    dE = s.CalculateLocalEnergyAdjoint()
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    for c, R in enumerate(cfgs):
+        r = o.eval(z["uR"], z["uI"], R, adjoint=True)
+        scale_lnpsi = max(abs(r["lnpsi"]), np.abs(z["uR"]).max() * len(R))
+        assert abs(fwd["lnpsi"][c] - r["lnpsi"]) < tol * scale_lnpsi
+        assert relmax(fwd["O"][c], r["O"]) < tol
+        scaleE = max(np.abs(r["other"]).max(), 1.0)
+        assert np.abs(fwd["eloc"][c] - r["eloc"]).max() < tol * scaleE
+        assert np.abs(fwd["other"][c] - r["other"]).max() < tol * scaleE
+        scaled = max(np.abs(r["dE"]).max(), 1.0)
+        assert np.abs(dE[c] - r["dE"]).max() < tol * scaled
+        if precision == "fp64":
+            # the reference's own evaluation of the same configuration
+            assert relmax(fwd["lnpsi"][c], z["ref_lnpsi"][c]) < RTOL_REF
+            assert relmax(fwd["O"][c], z["ref_O"][c]) < RTOL_REF
+            sE = max(abs(z["ref_other"][c][0]), abs(z["ref_other"][c][1]), 1.0)
+            assert abs(fwd["eloc"][c][0] - z["ref_ER"][c]) < RTOL_REF * sE
+            assert abs(fwd["eloc"][c][1] - z["ref_EI"][c]) < RTOL_REF * sE
+            assert fwd["other"][c][1] == z["ref_other"][c][1]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["d1_n20_p10", "d2_n64_k20", "d3_n64_p10"])
+def test_pb_sampler_follows_oracle_chain(name, precision):
+    """Metropolis moves with mirrored distances (NUBosonsBulkPB.cpp:684-740) on
+    32 lanes per walker, whose padded register slots hold phantoms: FP64 the
+    oracle's chain; FP32 the same moves on at least 90 % of the walkers,
+    acceptance within 1 %."""
+    z = np.load(os.path.join(GOLD, "pb_eval_%s.npz" % name))
+    dim, n, L = int(z["dim"]), int(z["n"]), float(z["L"])
+    nw, moves, step = 32, 2 * n, 0.4 if dim > 1 else 1.0
+    rng = np.random.default_rng(7 + dim)
+    R0 = np.concatenate([soa(z["cfgs"])] * (nw // len(z["cfgs"]) + 1))[:nw]
+    R0 = R0 + rng.normal(0, 0.02, size=R0.shape)
+    R0 = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(R0)
+    if precision == "mixed":
+        R0 = R0.astype(np.float32).astype(np.float64)
+    uR = 0.5 * np.asarray(z["uR"])
+    s = gpu_pb(z, nw, precision)
+    s.SetParameters(uR, z["uI"])
+    s.SetWalkers(R0)
+    acc = s.DoMetropolisSteps(moves, step, seed=55, pass_id=9)
+    Rg = s.GetWalkers()
+    s.close()
+    o = oracle_pb(z)
+    Ro = np.ascontiguousarray(R0.copy())
+    acc_o = o.sample(uR, Ro, moves, step, seed=55, pass_id=9)
+    assert 0.05 < acc_o / (moves * nw) < 0.98
+    if precision == "fp64":
+        assert acc == acc_o
+        assert np.abs(Rg - Ro).max() < 1e-9
+    else:
+        d = np.abs(Rg - Ro).reshape(nw, -1).max(1)
+        assert (d < 1e-4).mean() >= 0.9, d
+        assert abs(acc - acc_o) <= 0.01 * acc_o, (acc, acc_o)
+
+
+@pytest.mark.parametrize("ode", [2, 3])
+def test_pb_tdvp_step_matches_oracle_fp64(ode):
+    """One RK4 step of the mirrored-distance system, direct (ODE_SOLVER_TYPE 2)
+    and on stored samples (3): sampling, evaluation, reduction, solve, update."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "pb_eval_d3_n64_p10.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    nw, moves, step, dt, seed, pass0 = 64, n, 0.3, 1e-3, 13, 2
+    rng = np.random.default_rng(4)
+    R0 = np.concatenate([soa(z["cfgs"])] * 4)[:nw] + rng.normal(0, 0.02, size=(nw, dim, n))
+    R0 = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(R0)
+    uR, uI = 0.5 * np.asarray(z["uR"]), np.asarray(z["uI"])
+    s = gpu_pb(z, nw, "fp64", hbar2_2m=0.09)
+    s.SetParameters(uR, uI, 0.0, 0.0)
+    s.SetWalkers(R0)
+    s.DoMetropolisSteps(0, step, seed, pass0)  # sets the Philox pass counter
+    kw = dict(update_every=1, update_percent=25.0) if ode == 3 else {}
+    td = T.TDVP(s, dt, moves, step, seed=seed, ode_solver=ode, **kw)
+    td.step()
+    gR, gI, gpR, gpI = s.GetParameters()
+
+    o = oracle_pb(z, hbar2_2m=0.09)
+    base = np.concatenate([uR, uI, [0.0, 0.0]])
+    cur = base.copy()
+    Ro = R0.copy()
+    if ode == 3:
+        o.sample(uR, Ro, moves, step, seed, pass0)
+    ks = []
+    for k in range(4):
+        if ode == 3:
+            out = o.stage(cur[:p], cur[p:2 * p], Ro, 0, step, seed, 0, threads=4, adjoint=False)
+        else:
+            out = o.stage(cur[:p], cur[p:2 * p], Ro, moves, step, seed, pass0 + k, threads=4, adjoint=False)
+        m = orc.centred(out["O"], out["eloc"])
+        dR, dI, pR, pI, _ = orc.solve_centred(m["O"], m["ER"], m["EI"], m["S"], m["cOER"], m["cOEI"])
+        kv = np.concatenate([dR, dI, [pR, pI]])
+        ks.append(kv)
+        if k < 3:
+            cur = base + kv * (dt / 2 if k < 2 else dt)
+    new = orc.rk4_combine(base, ks, dt)
+    assert np.abs(s.GetWalkers() - Ro).max() < 1e-9
+    assert relmax(np.concatenate([gR, gI, [gpR, gpI]]), new) < 1e-9
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
+def test_pb_stored_eval_matches_direct_eval(precision, tol):
+    """The stored-sample columns (k_cs_store) of the mirrored distances give the
+    direct evaluation at the stored parameters and at others."""
+    z = np.load(os.path.join(GOLD, "pb_eval_d2_n64_k20.npz"))
+    cfgs = soa(z["cfgs"])
+    nw = 2 * len(cfgs)
+    rng = np.random.default_rng(12)
+    R = np.concatenate([cfgs] * 2) + rng.normal(0, 0.01, size=(nw,) + cfgs.shape[1:])
+    s = gpu_pb(z, nw, precision, hbar2_2m=0.09)
+    uR, uI = np.asarray(z["uR"]), np.asarray(z["uI"])
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R)
+    s.FillCorrelatedSamplingData()
+    for k, (a, b) in enumerate([(uR, uI), (1.1 * uR + 0.01, 0.5 * uI - 0.02)]):
+        s.SetParameters(a, b)
+        got = s.CalculateExpectationValuesForStoredSamples(adjoint=True)
+        ref = s.CalculateExpectationValues()
+        ref["dE"] = s.CalculateLocalEnergyAdjoint()
+        for key in ("lnpsi", "O", "eloc", "other", "dE"):
+            assert relmax(got[key], ref[key]) < tol, (k, key, relmax(got[key], ref[key]))
+
+
+def test_pb_pair_distribution_weight():
+    """g(r) of NUBosonsBulkPB adds 1 per pair (NUBosonsBulkPB.cpp:602-612) where
+    BosonsBulk adds D/(N-1): same walkers, same bins, ratio (N-1)/D."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "pb_eval_d3_n64_p10.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    R = soa(z["cfgs"])
+    nw = len(R)
+    pb = gpu_pb(z, nw, "fp64")
+    bulk = T.BosonsBulk(dim, n, p, L, nw, system_params=z["sysp"], user_knots=z["knots"], precision="fp64")
+    out = []
+    for s in (pb, bulk):
+        s.SetParameters(z["uR"], z["uI"])
+        s.SetWalkers(R)
+        out.append(s.CalculateAdditionalSystemProperties(100)["gr"])
+    assert out[0].size == out[1].size == 100
+    assert np.abs(out[0] - out[1] * (n - 1) / dim).max() <= 1e-12 * np.abs(out[0]).max()

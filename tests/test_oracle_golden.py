@@ -227,3 +227,22 @@ def test_pb_move_matches_reference(path):
     for R, part, new, ref in zip(z["move_cfg"], z["move_part"], z["move_new"], z["ref_move"]):
         d = s.move_delta(z["uR"], R, int(part), new)
         assert abs(d - (ref[1] - ref[0])) < RTOL_REF * max(abs(ref[0]), 1.0)
+
+
+@pytest.mark.parametrize("path", PB_FILES, ids=[os.path.basename(p)[8:-4] for p in PB_FILES])
+def test_pb_adjoint_is_the_derivative_of_the_local_energy(path):
+    """dE_loc/d uR_k of the mirrored-distance system (the reference has no
+    adjoint for it): E_loc is quadratic in uR, so central differences with step
+    h are exact up to rounding; relative 1e-7 of the largest component."""
+    z = np.load(path)
+    s = load_pb(z)
+    uR, uI = np.asarray(z["uR"], dtype=np.float64), np.asarray(z["uI"], dtype=np.float64)
+    R = z["cfgs"][0]
+    dE = s.eval(uR, uI, R, adjoint=True)["dE"].reshape(-1, 2)
+    h = 1e-3
+    fd = np.zeros_like(dE)
+    for k in range(len(uR)):
+        e = np.zeros_like(uR)
+        e[k] = h
+        fd[k] = (s.eval(uR + e, uI, R)["eloc"] - s.eval(uR - e, uI, R)["eloc"]) / (2 * h)
+    assert np.abs(dE - fd).max() < 1e-7 * np.abs(fd).max()
