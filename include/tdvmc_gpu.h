@@ -63,6 +63,12 @@ extern "C" {
  * mirrored distance is non-negative (below that the reference indexes its
  * spline tables out of range). */
 #define TDVMC_SYS_NU_BOSONS_BULK_PB 1
+/* NUBosonsBulkPB with the exact derivatives of the mirrored pair term
+ * u(2 r_max - r): at a pair beyond r_max the gradient term is -u'(r') d / r and
+ * the Laplacian's -(D-1)/r u'(r') (d r'/d r = -1, the sign flip the reference
+ * has commented out at NUBosonsBulkPB.cpp:387); ln psi, O_k, the moves and the
+ * potential as TDVMC_SYS_NU_BOSONS_BULK_PB. */
+#define TDVMC_SYS_NU_BOSONS_BULK_PB_EXACT 2
 
 typedef struct tdvmc_ctx tdvmc_ctx;
 

@@ -24,7 +24,8 @@ LIB_PATH = os.path.join(BUILD_DIR, "libtdvmc_oracle.so")
 SRC = os.path.join(HERE, "tdvmc_oracle.c")
 
 POT_NONE, POT_SQUARE, POT_GAUSS, POT_LJ = 0, 1, 2, 3
-SYS_BOSONS_BULK, SYS_NU_PB = 0, 1  # BosonsBulk, NUBosonsBulkPB (tdvmc_oracle.h)
+# BosonsBulk, NUBosonsBulkPB, NUBosonsBulkPB with exact derivatives (tdvmc_oracle.h)
+SYS_BOSONS_BULK, SYS_NU_PB, SYS_NU_PB_EXACT = 0, 1, 2
 
 _lib = None
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")

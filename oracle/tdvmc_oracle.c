@@ -183,7 +183,7 @@ orc_sys* orc_create(int dim, int n, int p, double L, const double* user_knots, i
 void orc_set_variant(orc_sys* s, int variant)
 {
 	s->variant = variant;
-	if (variant != ORC_SYS_NU_PB) return;
+	if (variant != ORC_SYS_NU_PB && variant != ORC_SYS_NU_PB_EXACT) return;
 	int P = s->p, ns = s->ns;
 	memset(s->fold, 0, (size_t)P * ns * sizeof(double));
 	for (int k = 0; k < P; k++) s->fold[k * ns + k + 1] = 1.0;
@@ -194,15 +194,21 @@ void orc_set_variant(orc_sys* s, int variant)
 /* The distance a pair enters the spline sums with, and whether it does.
  * BosonsBulk: r, inside r <= r_max (r < r_max for a moved particle's new
  * position, strict).  NUBosonsBulkPB: r' = 2 r_max - r beyond r_max, inside
- * r' < r_max (NUBosonsBulkPB.cpp:240-247, 321-326, 629-660). */
-static int pair_inside(const orc_sys* s, double r, int strict, double* reff)
+ * r' < r_max (NUBosonsBulkPB.cpp:249-253, 333-336, 690-693).  rdiv (may be
+ * NULL): what the derivative terms divide by, d / rdiv in the gradient and
+ * (D-1) / rdiv in the Laplacian -- r' for NUBosonsBulkPB (:381-398), and for
+ * its exact form -r at a mirrored pair (d r'/d r = -1 and grad r = d / r). */
+static int pair_inside(const orc_sys* s, double r, int strict, double* reff, double* rdiv)
 {
-	if (s->variant == ORC_SYS_NU_PB)
+	if (s->variant == ORC_SYS_NU_PB || s->variant == ORC_SYS_NU_PB_EXACT)
 	{
-		double rr = (r < s->rmax) ? r : 2.0 * s->rmax - r;
+		int mirrored = !(r < s->rmax);
+		double rr = mirrored ? 2.0 * s->rmax - r : r;
+		if (rdiv) *rdiv = (mirrored && s->variant == ORC_SYS_NU_PB_EXACT) ? -r : rr;
 		*reff = rr;
 		return rr < s->rmax;
 	}
+	if (rdiv) *rdiv = r;
 	*reff = r;
 	return strict ? (r < s->rmax) : (r <= s->rmax);
 }
@@ -311,7 +317,7 @@ static void spline_sums(const orc_sys* s, const double* R, double* S, double* no
 		for (int i = 0; i < a; i++)
 		{
 			double re, r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
-			if (pair_inside(s, r, 0, &re))
+			if (pair_inside(s, r, 0, &re, NULL))
 			{
 				int b = find_bin(s, re);
 				spline_eval(s, b, re, v, NULL, NULL);
@@ -368,8 +374,8 @@ void orc_eval(const orc_sys* s, const double* uR, const double* uI, const double
 		for (int i = 0; i < n; i++)
 		{
 			if (i == a) continue;
-			double r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
-			if (!pair_inside(s, r, 0, &r)) continue; /* r: the distance the pair enters with */
+			double rq, r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
+			if (!pair_inside(s, r, 0, &r, &rq)) continue; /* r: the distance the pair enters with */
 			if (i < a) vint += pair_potential(s, r);
 			int b = find_bin(s, r);
 			spline_eval(s, b, r, NULL, d1, d2);
@@ -381,16 +387,16 @@ void orc_eval(const orc_sys* s, const double* uR, const double* uI, const double
 				u1I += wI[sp] * d1[q];
 				u2R += wR[sp] * d2[q];
 				u2I += wI[sp] * d2[q];
-				Lsp[sp] += d2[q] + (D - 1.0) / r * d1[q];
+				Lsp[sp] += d2[q] + (D - 1.0) / rq * d1[q];
 			}
 			for (int c = 0; c < D; c++)
 			{
-				double e_c = d[c] / r;
+				double e_c = d[c] / rq;
 				G[a * 6 + c] += u1R * e_c;
 				G[a * 6 + 3 + c] += u1I * e_c;
 			}
-			lapR += u2R + (D - 1.0) / r * u1R;
-			lapI += u2I + (D - 1.0) / r * u1I;
+			lapR += u2R + (D - 1.0) / rq * u1R;
+			lapI += u2I + (D - 1.0) / rq * u1I;
 		}
 	}
 	double sR1 = 0, sI1 = 0, sR1I1 = 0;
@@ -427,15 +433,15 @@ void orc_eval(const orc_sys* s, const double* uR, const double* uI, const double
 			for (int i = 0; i < n; i++)
 			{
 				if (i == a) continue;
-				double r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
-				if (!pair_inside(s, r, 0, &r)) continue;
+				double rq, r = orc_nic_disp(R + a * D, R + i * D, D, s->L, d);
+				if (!pair_inside(s, r, 0, &r, &rq)) continue;
 				int b = find_bin(s, r);
 				spline_eval(s, b, r, NULL, d1, NULL);
 				double gR = 0, gI = 0;
 				for (int cc = 0; cc < D; cc++)
 				{
-					gR += G[a * 6 + cc] * d[cc] / r;
-					gI += G[a * 6 + 3 + cc] * d[cc] / r;
+					gR += G[a * 6 + cc] * d[cc] / rq;
+					gI += G[a * 6 + 3 + cc] * d[cc] / rq;
 				}
 				for (int q = 0; q < 4; q++)
 				{
@@ -488,7 +494,7 @@ static void move_sums(const orc_sys* s, const double* R, int p, const double* x,
 	{
 		if (i == p) continue;
 		double r = orc_nic_disp(R + i * D, x, D, s->L, d);
-		int inside = pair_inside(s, r, strict, &r);
+		int inside = pair_inside(s, r, strict, &r, NULL);
 		if (inside)
 		{
 			int b = find_bin(s, r);

@@ -42,7 +42,11 @@ typedef struct orc_sys orc_sys;
  * displacement over r', and the sign flip of the mirrored pairs' derivative is
  * commented out), and r < r_max (strict) for the old and the new position of a
  * move (:622-660). */
-enum { ORC_SYS_BOSONS_BULK = 0, ORC_SYS_NU_PB = 1 };
+/* ORC_SYS_NU_PB_EXACT: NUBosonsBulkPB with the exact derivatives of the
+ * mirrored pair term u(2 r_max - r) -- gradient -u'(r') d / r and Laplacian
+ * term -(D-1)/r u'(r') at a mirrored pair -- the form the reference's
+ * commented-out sign flip (NUBosonsBulkPB.cpp:333-336, 387) points to. */
+enum { ORC_SYS_BOSONS_BULK = 0, ORC_SYS_NU_PB = 1, ORC_SYS_NU_PB_EXACT = 2 };
 
 /* Build a system.  user_knots == NULL (nuser = 0) gives the uniform grid of
  * BosonsBulk.cpp:61-67; otherwise the grid is mirrored as in

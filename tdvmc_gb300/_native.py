@@ -14,7 +14,7 @@ from . import build as _build
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_NOT_PD, ERR_NONFINITE = range(7)
 PREC_FP64, PREC_MIXED = 0, 1
 POT_NONE, POT_SQUARE, POT_GAUSS, POT_LJ = 0, 1, 2, 3
-SYS_BOSONS_BULK, SYS_NU_BOSONS_BULK_PB = 0, 1
+SYS_BOSONS_BULK, SYS_NU_BOSONS_BULK_PB, SYS_NU_BOSONS_BULK_PB_EXACT = 0, 1, 2
 
 # every entry point of include/tdvmc_gpu.h
 EXPORTS = ("tdvmc_status_string", "tdvmc_create", "tdvmc_destroy", "tdvmc_get_stream", "tdvmc_set_time",

@@ -41,7 +41,8 @@ struct SysConst {
 	// -2 (L - Lf), Lf the FP32 box length: the first-order share of the FP32 box
 	// length's remainder in the r^2 of a wrapped pair (see pair_r2_f32)
 	float lc;
-	// 1: NUBosonsBulkPB, a pair at r >= r_max enters at r' = 2 r_max - r (mirror_r)
+	// NUBosonsBulkPB, a pair at r >= r_max enters at r' = 2 r_max - r (mirror_r):
+	// 1 the reference's derivative terms, 2 the exact ones; 0 BosonsBulk
 	int mirror;
 };
 
@@ -136,22 +137,24 @@ __device__ __forceinline__ float pair_r(float r2) {
 }
 __device__ __forceinline__ double pair_r(double r2) { return r2 * rsqrt_(r2); }
 
-// NUBosonsBulkPB (NUBosonsBulkPB.cpp:249-253, 333-336, 690-693): a pair at r >= r_max enters at
-// the mirrored distance r' = 2 r_max - r (m2 = 2 r_max), and q ~ 1/r becomes
-// 1/r' (correctly rounded).  The pair's direction keeps the sign of d: the
-// reference's first-derivative factor stays 1 (outsideL2 is never set).
-__device__ __forceinline__ void mirror_r(float m2, float& r, float& q) {
+// NUBosonsBulkPB (NUBosonsBulkPB.cpp:249-253, 333-336, 690-693): a pair at
+// r >= r_max enters at the mirrored distance r' = 2 r_max - r (m2 = 2 r_max).
+// q ~ 1/r is what the derivative terms scale the displacement d and (D-1) by.
+// The reference's form: q = 1/r' (correctly rounded), the direction keeping the
+// sign of d (its first-derivative factor stays 1, outsideL2 is never set, :387).
+// exact: the derivatives of u(2 r_max - r) itself, q = -1/r (d r'/d r = -1).
+__device__ __forceinline__ void mirror_r(float m2, float& r, float& q, bool exact) {
 	const float rm = __fsub_rn(m2, r);
 	if (rm < r) {
 		r = rm;
-		q = __frcp_rn(rm);
+		q = exact ? -q : __frcp_rn(rm);
 	}
 }
-__device__ __forceinline__ void mirror_r(double m2, double& r, double& q) {
+__device__ __forceinline__ void mirror_r(double m2, double& r, double& q, bool exact) {
 	const double rm = __dsub_rn(m2, r);
 	if (rm < r) {
 		r = rm;
-		q = __drcp_rn(rm);
+		q = exact ? -q : __drcp_rn(rm);
 	}
 }
 

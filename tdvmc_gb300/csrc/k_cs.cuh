@@ -97,7 +97,7 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
 	bool cut;
 	if (sc.mirror) {
 		// NUBosonsBulkPB: the mirrored distance, counted iff r' < r_max (no second look)
-		mirror_r((T)(2.0 * sc.rmax), g.r, g.rinv);
+		mirror_r((T)(2.0 * sc.rmax), g.r, g.rinv, sc.mirror == 2);
 		cut = g.r < (T)sc.rmax;
 	} else {
 		cut = force || g.r <= (T)sc.rmax;

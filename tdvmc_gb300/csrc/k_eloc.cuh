@@ -330,7 +330,7 @@ __device__ __forceinline__ FwdPair<T> fwd_pair(const SysConst& sc, const Q4<T>& 
 	q.rinv = rsqrt_(r2);
 	q.r = r2 * q.rinv;
 	if constexpr (MIR) {
-		mirror_r((T)(2.0 * sc.rmax), q.r, q.rinv);
+		mirror_r((T)(2.0 * sc.rmax), q.r, q.rinv, sc.mirror == 2);
 		q.cut = q.r < (T)sc.rmax;
 	} else {
 		q.cut = within_rmax<T>(sc, q.r, xr, xi);
@@ -684,8 +684,8 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			bool inA, inB;
 			if constexpr (MIR) {
 				// mirrored distances: r' = r_max is a set of measure zero, no second look
-				mirror_r(m2, rA, qa);
-				mirror_r(m2, rB, qb);
+				mirror_r(m2, rA, qa, sc.mirror == 2);
+				mirror_r(m2, rB, qb, sc.mirror == 2);
 				r = f2_make(rA, rB);
 				inA = okA && (rA < rmax);
 				inB = okB && (rB < rmax);
@@ -1008,7 +1008,7 @@ __device__ __forceinline__ void rev_region(const SysConst& sc, int i0, int i1, i
 			T r = r2 * rinv;
 			bool cut;
 			if constexpr (MIR) {
-				mirror_r((T)(2.0 * sc.rmax), r, rinv);
+				mirror_r((T)(2.0 * sc.rmax), r, rinv, sc.mirror == 2);
 				cut = r < rmax;
 			} else {
 				cut = within_rmax<T>(sc, r, xr, xi);
@@ -1095,8 +1095,8 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			bool cA, cB;
 			if constexpr (MIR) {
 				// mirrored distances, formed as the forward sweep forms them (no second look)
-				mirror_r(m2, rA, qa);
-				mirror_r(m2, rB, qb);
+				mirror_r(m2, rA, qa, sc.mirror == 2);
+				mirror_r(m2, rB, qb, sc.mirror == 2);
 				r = f2_make(rA, rB);
 				cA = rA < rmax;
 				cB = rB < rmax;

@@ -768,8 +768,10 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 		return TDVMC_ERR_ARG;
 	if (d->n_user_knots > 0 && (d->user_knots == nullptr || d->n_user_knots != d->p)) return TDVMC_ERR_ARG;
 	if (d->n_pot < 0 || d->n_pot > 5) return TDVMC_ERR_ARG;
-	if (d->system_type != TDVMC_SYS_BOSONS_BULK && d->system_type != TDVMC_SYS_NU_BOSONS_BULK_PB) return TDVMC_ERR_ARG;
-	const bool pb = d->system_type == TDVMC_SYS_NU_BOSONS_BULK_PB;
+	if (d->system_type != TDVMC_SYS_BOSONS_BULK && d->system_type != TDVMC_SYS_NU_BOSONS_BULK_PB &&
+	    d->system_type != TDVMC_SYS_NU_BOSONS_BULK_PB_EXACT)
+		return TDVMC_ERR_ARG;
+	const bool pb = d->system_type != TDVMC_SYS_BOSONS_BULK;
 	// NUBosonsBulkPB reads r_max from its knot vector before it builds default knots
 	// (NUBosonsBulkPB.cpp:76, 91-97), and its potential is the square well (347-350)
 	if (pb && (d->n_user_knots == 0 || d->pot_kind != TDVMC_POT_SQUARE)) return TDVMC_ERR_ARG;
@@ -807,7 +809,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	s.Lr = 1.0 / d->box_length;
 	s.hbar2_2m = d->hbar2_2m;
 	s.pot_kind = d->pot_kind;
-	s.mirror = pb ? 1 : 0;
+	s.mirror = d->system_type == TDVMC_SYS_NU_BOSONS_BULK_PB ? 1 : pb ? 2 : 0;
 	// r_max below 1.5 L: the samplers' phantom slots (kPhantomBoxes) lie beyond it.
 	// Mirrored distances 2 r_max - r stay non-negative for every pair (the largest
 	// minimum-image distance is sqrt(dim) L / 2; a margin of 1e-5 covers rounding).

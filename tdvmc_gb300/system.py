@@ -209,12 +209,19 @@ class NUBosonsBulkPB(BosonsBulk):
     r_max), gradient terms d / r' with the sign of d, the square-well potential
     and the fold O_k = S_{k+1}, O_1 += S_0, O_{p-1} += S_{p+1}.  ``user_knots``
     (NURBS_GRID) is required: the reference reads r_max from them before it
-    would build default knots (NUBosonsBulkPB.cpp:76, 91-97)."""
+    would build default knots (NUBosonsBulkPB.cpp:76, 91-97).
+
+    ``exact_derivatives=True`` switches the derivative terms of the mirrored
+    pairs from the reference's form (d / r', the sign flip of
+    NUBosonsBulkPB.cpp:387 commented out) to the exact derivatives of
+    u(2 r_max - r): -u'(r') d / r in the gradient, -(D-1)/r u'(r') in the
+    Laplacian."""
 
     SYSTEM_TYPE = N.SYS_NU_BOSONS_BULK_PB
 
     def __init__(self, dim, n, n_param, box_length, n_walkers, user_knots, system_params=(0.5, 2.0),
-                 hbar2_2m=1.0, precision="fp64"):
+                 hbar2_2m=1.0, precision="fp64", exact_derivatives=False):
+        self.SYSTEM_TYPE = N.SYS_NU_BOSONS_BULK_PB_EXACT if exact_derivatives else N.SYS_NU_BOSONS_BULK_PB
         super().__init__(dim, n, n_param, box_length, n_walkers, system_params=system_params, potential="square",
                          user_knots=user_knots, hbar2_2m=hbar2_2m, precision=precision)
 

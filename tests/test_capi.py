@@ -103,3 +103,4 @@ def test_mirrored_system_descriptor_checks():
     assert create(system_type=7) == N.ERR_ARG
     # 1D: r_max = L / 4 + 0.4 is enough
     assert create(knots=(0.0, 0.35, 0.7, 1.05, 1.4), dim=1) != N.ERR_ARG
+    assert create(knots=(0.0, 0.35, 0.7, 1.05, 1.4), dim=1, system_type=N.SYS_NU_BOSONS_BULK_PB_EXACT) != N.ERR_ARG

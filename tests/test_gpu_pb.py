@@ -37,33 +37,37 @@ def soa(cfgs):
     return np.ascontiguousarray(np.transpose(np.asarray(cfgs), (0, 2, 1)))
 
 
-def gpu_pb(z, nw, precision, hbar2_2m=1.0):
+def gpu_pb(z, nw, precision, hbar2_2m=1.0, exact=False):
     import tdvmc_gb300 as T
     s = T.NUBosonsBulkPB(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), nw, user_knots=z["knots"],
-                         system_params=z["sysp"], hbar2_2m=hbar2_2m, precision=precision)
+                         system_params=z["sysp"], hbar2_2m=hbar2_2m, precision=precision, exact_derivatives=exact)
     s.SetTime(float(z["time"]))
     return s
 
 
-def oracle_pb(z, hbar2_2m=1.0):
+def oracle_pb(z, hbar2_2m=1.0, exact=False):
     return orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"]), user_knots=z["knots"],
                             pot_kind=orc.POT_SQUARE, pot=z["sysp"], time=float(z["time"]), hbar2_2m=hbar2_2m,
-                            variant=orc.SYS_NU_PB)
+                            variant=orc.SYS_NU_PB_EXACT if exact else orc.SYS_NU_PB)
 
 
-CASES = [(f, prec) for f in PB_FILES for prec in ("fp64", "mixed")]
+CASES = [(f, prec, form) for f in PB_FILES for prec in ("fp64", "mixed") for form in ("reference", "exact")]
 
 
-@pytest.mark.parametrize("path,precision", CASES,
-                         ids=["%s-%s" % (os.path.basename(c[0])[8:-4], c[1]) for c in CASES])
-def test_pb_eval_and_adjoint_match_oracle(path, precision):
+@pytest.mark.parametrize("path,precision,form", CASES,
+                         ids=["%s-%s-%s" % (os.path.basename(c[0])[8:-4], c[1], c[2]) for c in CASES])
+def test_pb_eval_and_adjoint_match_oracle(path, precision, form):
+    """Both forms of the mirrored pairs' derivative terms (the reference's and
+    the exact one) against the oracle; the reference's form also against the
+    reference's own numbers."""
     z = np.load(path)
     cfgs = z["cfgs"]
     if precision == "mixed":
         cfgs = cfgs.astype(np.float32).astype(np.float64)
     nw = len(cfgs)
-    s = gpu_pb(z, nw, precision)
-    o = oracle_pb(z)
+    exact = form == "exact"
+    s = gpu_pb(z, nw, precision, exact=exact)
+    o = oracle_pb(z, exact=exact)
     s.SetParameters(z["uR"], z["uI"], float(z["phiR"]), float(z["phiI"]))
     s.SetWalkers(soa(cfgs))
     fwd = s.CalculateExpectationValues()
@@ -79,7 +83,7 @@ def test_pb_eval_and_adjoint_match_oracle(path, precision):
         assert np.abs(fwd["other"][c] - r["other"]).max() < tol * scaleE
         scaled = max(np.abs(r["dE"]).max(), 1.0)
         assert np.abs(dE[c] - r["dE"]).max() < tol * scaled
-        if precision == "fp64":
+        if precision == "fp64" and not exact:
             # the reference's own evaluation of the same configuration
             assert relmax(fwd["lnpsi"][c], z["ref_lnpsi"][c]) < RTOL_REF
             assert relmax(fwd["O"][c], z["ref_O"][c]) < RTOL_REF
@@ -125,10 +129,11 @@ def test_pb_sampler_follows_oracle_chain(name, precision):
         assert abs(acc - acc_o) <= 0.01 * acc_o, (acc, acc_o)
 
 
-@pytest.mark.parametrize("ode", [2, 3])
-def test_pb_tdvp_step_matches_oracle_fp64(ode):
+@pytest.mark.parametrize("ode,exact", [(2, False), (3, False), (2, True), (3, True)])
+def test_pb_tdvp_step_matches_oracle_fp64(ode, exact):
     """One RK4 step of the mirrored-distance system, direct (ODE_SOLVER_TYPE 2)
-    and on stored samples (3): sampling, evaluation, reduction, solve, update."""
+    and on stored samples (3), in both forms of the derivative terms: sampling,
+    evaluation, reduction, solve, update."""
     import tdvmc_gb300 as T
     z = np.load(os.path.join(GOLD, "pb_eval_d3_n64_p10.npz"))
     dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
@@ -137,7 +142,7 @@ def test_pb_tdvp_step_matches_oracle_fp64(ode):
     R0 = np.concatenate([soa(z["cfgs"])] * 4)[:nw] + rng.normal(0, 0.02, size=(nw, dim, n))
     R0 = np.vectorize(lambda v: orc.lib().orc_nic_coord(v, L))(R0)
     uR, uI = 0.5 * np.asarray(z["uR"]), np.asarray(z["uI"])
-    s = gpu_pb(z, nw, "fp64", hbar2_2m=0.09)
+    s = gpu_pb(z, nw, "fp64", hbar2_2m=0.09, exact=exact)
     s.SetParameters(uR, uI, 0.0, 0.0)
     s.SetWalkers(R0)
     s.DoMetropolisSteps(0, step, seed, pass0)  # sets the Philox pass counter
@@ -146,7 +151,7 @@ def test_pb_tdvp_step_matches_oracle_fp64(ode):
     td.step()
     gR, gI, gpR, gpI = s.GetParameters()
 
-    o = oracle_pb(z, hbar2_2m=0.09)
+    o = oracle_pb(z, hbar2_2m=0.09, exact=exact)
     base = np.concatenate([uR, uI, [0.0, 0.0]])
     cur = base.copy()
     Ro = R0.copy()
@@ -169,8 +174,9 @@ def test_pb_tdvp_step_matches_oracle_fp64(ode):
     assert relmax(np.concatenate([gR, gI, [gpR, gpI]]), new) < 1e-9
 
 
+@pytest.mark.parametrize("exact", [False, True])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
-def test_pb_stored_eval_matches_direct_eval(precision, tol):
+def test_pb_stored_eval_matches_direct_eval(precision, tol, exact):
     """The stored-sample columns (k_cs_store) of the mirrored distances give the
     direct evaluation at the stored parameters and at others."""
     z = np.load(os.path.join(GOLD, "pb_eval_d2_n64_k20.npz"))
@@ -178,7 +184,7 @@ def test_pb_stored_eval_matches_direct_eval(precision, tol):
     nw = 2 * len(cfgs)
     rng = np.random.default_rng(12)
     R = np.concatenate([cfgs] * 2) + rng.normal(0, 0.01, size=(nw,) + cfgs.shape[1:])
-    s = gpu_pb(z, nw, precision, hbar2_2m=0.09)
+    s = gpu_pb(z, nw, precision, hbar2_2m=0.09, exact=exact)
     uR, uI = np.asarray(z["uR"]), np.asarray(z["uI"])
     s.SetParameters(uR, uI)
     s.SetWalkers(R)

@@ -246,3 +246,48 @@ def test_pb_adjoint_is_the_derivative_of_the_local_energy(path):
         e[k] = h
         fd[k] = (s.eval(uR + e, uI, R)["eloc"] - s.eval(uR - e, uI, R)["eloc"]) / (2 * h)
     assert np.abs(dE - fd).max() < 1e-7 * np.abs(fd).max()
+
+
+def test_pb_exact_derivatives_are_those_of_ln_psi():
+    """The exact form of the mirrored-distance system (ORC_SYS_NU_PB_EXACT): the
+    kinetic sums sum_a |grad_a ln psi|^2 and sum_a lap_a ln psi (real part from
+    uR, imaginary part from uI) agree with central differences of ln psi, on
+    configurations with no pair within 2e-4 of r_max or of the minimum-image
+    wrap |d_a| = L/2, where ln psi has kinks.  The reference's form (d / r', no
+    sign flip) does not: its sums differ from the derivatives of its own ln psi."""
+    z = np.load(os.path.join(GOLD, "pb_eval_d3_n64_p10.npz"))
+    L, rmax = float(z["L"]), float(z["knots"][-1])
+    uR, uI = np.asarray(z["uR"]), np.asarray(z["uI"])
+    systems = {v: orc.OracleSystem(int(z["dim"]), int(z["n"]), int(z["p"]), L, user_knots=z["knots"],
+                                   pot_kind=orc.POT_SQUARE, pot=z["sysp"], variant=v)
+               for v in (orc.SYS_NU_PB, orc.SYS_NU_PB_EXACT)}
+    h1, h2 = 1e-6, 1e-4
+    checked = 0
+    for R in z["cfgs"]:
+        d = R[:, None, :] - R[None, :, :]
+        d -= L * np.round(d / L)
+        iu = np.triu_indices(len(R), 1)
+        r = np.sqrt((d * d).sum(-1))[iu]
+        if np.abs(r - rmax).min() < 2 * h2 or np.abs(np.abs(d[iu]) - L / 2).min() < 2 * h2:
+            continue
+        checked += 1
+        for v, s in systems.items():
+            res = s.eval(uR, uI, R)
+            for u, kg, kl in ((uR, 2, 4), (uI, 3, 5)):
+                f = lambda X: s.eval(u, uI, X)["lnpsi"]  # noqa: E731
+                f0, g2, lap = f(R), 0.0, 0.0
+                for a in range(len(R)):
+                    for k in range(R.shape[1]):
+                        e = np.zeros_like(R)
+                        e[a, k] = h1
+                        g2 += ((f(R + e) - f(R - e)) / (2 * h1)) ** 2
+                        e[a, k] = h2
+                        lap += (f(R + e) - 2 * f0 + f(R - e)) / h2 ** 2
+                if v == orc.SYS_NU_PB_EXACT:
+                    assert abs(res["other"][kg] - g2) < 1e-7 * abs(g2)
+                    assert abs(res["other"][kl] - lap) < 1e-5 * max(abs(lap), abs(g2))
+                else:
+                    assert abs(res["other"][kg] - g2) > 1e-3 * abs(g2)
+        if checked == 2:
+            break
+    assert checked >= 1
