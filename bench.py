@@ -147,12 +147,17 @@ def ncu_traffic(kernel):
     return None
 
 
-def cpu_port_rate(threads, walkers_per_thread=1, seed=11):
+def cpu_port_rate(threads, walkers_per_thread=1, seed=11, mirrored=False):
     """The reference algorithm (FP64 CPU port) on a bounded sample: one stage
     (sampling pass + evaluation + adjoint) of threads*walkers_per_thread walkers.
+    mirrored: the NUBosonsBulkPB workload (pb_system).
     Returns (steps/s extrapolated to the full workload, seconds, walkers)."""
     from oracle import oracle as orc
-    s = orc.OracleSystem(DIM, N, P, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0), hbar2_2m=HBAR2_2M)
+    if mirrored:
+        s = orc.OracleSystem(DIM, N, P, L, user_knots=PB_KNOTS, pot_kind=orc.POT_SQUARE, pot=PB_SYSP,
+                             hbar2_2m=HBAR2_2M, variant=orc.SYS_NU_PB)
+    else:
+        s = orc.OracleSystem(DIM, N, P, L, pot_kind=orc.POT_LJ, pot=(1.0, 1.0), hbar2_2m=HBAR2_2M)
     nws = threads * walkers_per_thread
     R = initial_walkers(nws, seed=seed)
     uR, uI = initial_params()
@@ -241,6 +246,64 @@ def run_drops(sync, steps, warmup, walkers=DROP_WALKERS):
             "kernels_ms_per_stage": {k: v for k, v in prof}, "tiles": tiles,
             "gpu_launches_per_step": launches // steps, "status_ok": bool((out["status"] == 0).all()),
             "energy_per_particle_mean": float(np.mean(e / ns))}
+
+
+# mirrored-distance system (NUBosonsBulkPB): the headline's bosons, walkers, moves and
+# time step with every pair beyond r_max = L/2 entering at 2 r_max - r, the system's
+# square well (a = sigma, b = 1) and its boundary fold; knots given (as the system
+# requires) on the headline's uniform grid
+PB_KNOTS = np.linspace(0.0, L / 2, P)
+PB_SYSP = (1.0, 1.0)
+PB_GATE_WALKERS = 8192
+
+
+def run_pb(sync, steps, warmup, nw=NW, cpu=True):
+    """RK4 steps/s of the mirrored-distance system in mixed precision, its kernels
+    per stage, the |dE/N| gate against an FP64 evaluation of the same walkers, and
+    the FP64 CPU port of the same system on the host cores."""
+    import tdvmc_gb300 as T
+    uR, uI = initial_params()
+    s = T.NUBosonsBulkPB(DIM, N, P, L, nw, user_knots=PB_KNOTS, system_params=PB_SYSP, hbar2_2m=HBAR2_2M,
+                         precision="mixed")
+    s.SetParameters(uR, uI)
+    s.SetWalkers(initial_walkers(nw))
+    td = T.TDVP(s, DT, MOVES, MC_STEP, seed=1, use_adjoint=1)
+    td.time_steps(warmup)
+    sync()
+    l0 = s.LaunchCount()
+    ms = td.time_steps(steps)
+    launches = s.LaunchCount() - l0
+    prof = td.profile_stage()
+    out = td.step(1)
+    nsub = min(nw, PB_GATE_WALKERS)
+    Rm = s.GetWalkers()[:nsub]
+    fm = s.CalculateExpectationValues()
+    gp = s.GetParameters()
+    tiles = s.Tiles()
+    s.close()
+    s64 = T.NUBosonsBulkPB(DIM, N, P, L, nsub, user_knots=PB_KNOTS, system_params=PB_SYSP, hbar2_2m=HBAR2_2M,
+                           precision="fp64")
+    s64.SetParameters(*gp)
+    s64.SetWalkers(Rm)
+    f64 = s64.CalculateExpectationValues()
+    s64.close()
+    dE = abs(fm["eloc"][:nsub, 0].mean() - f64["eloc"][:, 0].mean()) / N
+    res = {"value": steps / (ms / 1000.0), "unit": "steps/s", "walkers": nw, "ms_per_step": ms / steps,
+           "kernels_ms_per_stage": {k: v for k, v in prof}, "gpu_launches_per_step": launches // steps,
+           "tiles": tiles, "status": int(out["status"]), "accept_rate": out["accept_rate"],
+           "gate": {"dE_per_N": dE, "pass": bool(dE < 1e-5), "walkers": nsub,
+                    "against": "FP64 GPU evaluation of the same FP32-held walkers"},
+           "workload": "NUBosonsBulkPB: 3D N=343 rho=0.365, P=30 knots on [0, L/2], square well a=1 b=1, "
+                       "65536 walkers, RK4 dt=5e-4, 2 sweeps/stage, adjoint"}
+    if cpu:
+        threads = os.cpu_count() or 1
+        _, t_probe, _ = cpu_port_rate(threads, 2, mirrored=True)
+        wpt = int(min(1024, max(2, np.ceil(2 * 6.0 / max(t_probe, 1e-3)))))  # about 6 s of CPU work
+        v, t, w = cpu_port_rate(threads, wpt, mirrored=True)
+        res["cpu_port"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                           "sample": "one RK stage of %d walkers on %d threads (%.1f s), extrapolated x4 stages "
+                                     "x65536 walkers" % (w, threads, t)}
+    return res
 
 
 # large bulk: N = 1,000 on a 10x10x10 start, LJ at density 0.365, 64 knots,
@@ -504,6 +567,8 @@ def run_ours(args):
     # large bulk (N = 1,000, 262,144 walkers): one imaginary-time step driven by the
     # adjoint, the density quench, one real-time step, then two timed real-time steps
     c5 = run_c5(sync, 1, 3, 2, check_every=0) if args.extras_c5 else None
+    # the mirrored-distance system (NUBosonsBulkPB) on the headline's shape
+    pb = run_pb(sync, args.steps, args.warmup, cpu=(world == 1)) if args.extras_pb else None
     if c5:
         c5["workload"] = ("3D N=1000 LJ bosons rho=0.365 -> 0.40 quench, P=64, 262144 walkers, "
                           "RK4 dt=2.5e-4, 2 sweeps/stage")
@@ -559,6 +624,7 @@ def run_ours(args):
                  "against": "FP64 GPU evaluation of the same FP32-held walkers"},
         "batched_drops": drops,
         "large_bulk": c5,
+        "mirrored_distance": pb,
         "stored_sample_rk4": {"value": args.steps / (ms3 / 1000.0), "unit": "steps/s", "update_every": 1,
                               "update_percent": 25.0, "kernels_ms_refresh_stage": prof3},
         "stored_sample_pc": {"value": args.steps / (ms5 / 1000.0), "unit": "steps/s", "update_every": 1,
@@ -580,7 +646,9 @@ def run_workload(args):
     import torch
     torch.cuda.set_device(0)
     sync = torch.cuda.synchronize
-    if args.workload == "drops":
+    if args.workload == "pb":
+        out = run_pb(sync, args.steps, args.warmup, nw=args.walkers)
+    elif args.workload == "drops":
         out = run_drops(sync, args.steps, args.warmup, walkers=args.drop_walkers)
         out["workload"] = ("512 trapped 3D drops, N in {3,6,10,20}, 12-knot spline + one-body width, "
                            "4096 walkers/drop, RK4 dt=1e-3, 2 sweeps/stage, adjoint, autotuned tiles")
@@ -615,9 +683,11 @@ def main():
                     help="with --no-extras: time steps on stored samples (RK4 or the predictor-corrector)")
     ap.add_argument("--extras-drops", type=int, default=1, help="time the batched-drops workload as an extra")
     ap.add_argument("--extras-c5", type=int, default=1, help="time the large-bulk workload as an extra")
+    ap.add_argument("--extras-pb", type=int, default=1,
+                    help="time the mirrored-distance system (NUBosonsBulkPB) on the headline shape as an extra")
     ap.add_argument("--drop-walkers", type=int, default=DROP_WALKERS,
                     help="with --workload drops: walkers per drop (smaller for profiler runs)")
-    ap.add_argument("--workload", choices=["bulk", "drops", "c5"], default="bulk",
+    ap.add_argument("--workload", choices=["bulk", "drops", "c5", "pb"], default="bulk",
                     help="drops: the batched-drops workload alone; c5: the full large-bulk run (50 imaginary-"
                          "time steps, quench, 200 real-time steps, FP64 check every 10 steps)")
     args = ap.parse_args()

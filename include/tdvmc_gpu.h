@@ -247,7 +247,10 @@ int tdvmc_time_steps(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, int32_t nsteps
 /* Run ONE stage of a step eagerly (no graph) with a CUDA event pair around
  * every kernel; ms[i] receives the duration of kernel i and names[i] (may be
  * NULL) a static name.  *count receives the number of kernels (<= 16).
- * The stage advances the state like a graph launch would. */
+ * The stage moves the walkers and the Philox pass counter like a graph launch
+ * would; the parameters and the stage index are then put back to the step
+ * boundary the call started from (base parameters, stage 0), so that the next
+ * step is a whole step. */
 int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* opts, float* ms, const char** names, int32_t* count);
 
 /* Choose the group width (lanes per walker) and walkers per block of the

@@ -143,19 +143,27 @@ __device__ __forceinline__ double pair_r(double r2) { return r2 * rsqrt_(r2); }
 // The reference's form: q = 1/r' (correctly rounded), the direction keeping the
 // sign of d (its first-derivative factor stays 1, outsideL2 is never set, :387).
 // exact: the derivatives of u(2 r_max - r) itself, q = -1/r (d r'/d r = -1).
+// Branch-free (about half of the pairs of a bulk system are mirrored); FP32 takes
+// the hardware reciprocal (PTX rcp.approx.ftz.f32, as q ~ 1/r is the hardware
+// rsqrt), FP64 the correctly rounded one.
+__device__ __forceinline__ float rcp_approx(float x) {
+	float r;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return r;
+}
 __device__ __forceinline__ void mirror_r(float m2, float& r, float& q, bool exact) {
 	const float rm = __fsub_rn(m2, r);
-	if (rm < r) {
-		r = rm;
-		q = exact ? -q : __frcp_rn(rm);
-	}
+	const bool mir = rm < r;
+	const float qm = exact ? -q : rcp_approx(rm);
+	r = mir ? rm : r;
+	q = mir ? qm : q;
 }
 __device__ __forceinline__ void mirror_r(double m2, double& r, double& q, bool exact) {
 	const double rm = __dsub_rn(m2, r);
-	if (rm < r) {
-		r = rm;
-		q = exact ? -q : __drcp_rn(rm);
-	}
+	const bool mir = rm < r;
+	const double qm = exact ? -q : __drcp_rn(rm);
+	r = mir ? rm : r;
+	q = mir ? qm : q;
 }
 
 // Interval lookup over [0, r_max]: returns j (interval index; knot k_{j+3})

@@ -34,6 +34,7 @@ RevFn<double> pick_eloc_rev_f64(int lanes, int hist);
 // NUBosonsBulkPB (mirrored distances): 32 lanes, histogram mode 0, the scalar
 // sampler; null for any other tile
 template <typename T> SampleFn<T> pick_sample_pb(int lanes, int slots);
+SampleFn<float> pick_sample_f32_packed_pb(int lanes, int slots);  // FP32, uniform knots
 template <typename T> ElocFn<T> pick_eloc_pb(int lanes, bool adj, int hist);
 template <typename T> RevFn<T> pick_eloc_rev_pb(int lanes, int hist);
 template <> SampleFn<float> pick_sample_pb<float>(int lanes, int slots);

@@ -752,6 +752,24 @@ int tdvmc_drops_profile_stage(tdvmc_drops* ctx, const tdvmc_step_opts* o, float*
 	ctx->prof = nullptr;
 	ctx->prof_names = nullptr;
 	cudaStreamSynchronize(ctx->st);
+	if (!rc) {
+		// back to the step boundary: every drop's next step starts at stage 0 from its
+		// unchanged base parameters
+		std::vector<DynState> d(ctx->S);
+		if (cudaMemcpyAsync(ctx->stage, ctx->base, (size_t)ctx->S * ctx->np * sizeof(double), cudaMemcpyDeviceToDevice,
+		                    ctx->st) != cudaSuccess ||
+		    cudaMemcpyAsync(d.data(), ctx->dyn, d.size() * sizeof(DynState), cudaMemcpyDeviceToHost, ctx->st) !=
+		        cudaSuccess ||
+		    cudaStreamSynchronize(ctx->st) != cudaSuccess) {
+			rc = TDVMC_ERR_CUDA;
+		} else {
+			for (auto& x : d) x.stage = 0;
+			if (cudaMemcpyAsync(ctx->dyn, d.data(), d.size() * sizeof(DynState), cudaMemcpyHostToDevice, ctx->st) !=
+			        cudaSuccess ||
+			    cudaStreamSynchronize(ctx->st) != cudaSuccess)
+				rc = TDVMC_ERR_CUDA;
+		}
+	}
 	const int k = (int)std::min<size_t>(ev.size(), 16);
 	cudaEvent_t prev = e0;
 	for (int i = 0; i < k; i++) {

@@ -21,6 +21,19 @@ static SampleFn<T> pick_sample_pb_t(int lanes, int slots) {
 	return nullptr;
 }
 template <> SampleFn<float> pick_sample_pb<float>(int lanes, int slots) { return pick_sample_pb_t<float>(lanes, slots); }
+SampleFn<float> pick_sample_f32_packed_pb(int lanes, int slots) {
+	if (lanes != 32) return nullptr;
+	switch (slots) {
+	case 1: return k_sample_f2<32, 1, false, true>;
+	case 2: return k_sample_f2<32, 2, false, true>;
+	case 4: return k_sample_f2<32, 4, false, true>;
+	case 8: return k_sample_f2<32, 8, false, true>;
+	case 11: return k_sample_f2<32, 11, false, true>;
+	case 16: return k_sample_f2<32, 16, false, true>;
+	case 32: return k_sample_f2<32, 32, true, true>;
+	}
+	return nullptr;
+}
 template <> SampleFn<double> pick_sample_pb<double>(int lanes, int slots) { return pick_sample_pb_t<double>(lanes, slots); }
 
 template <> ElocFn<float> pick_eloc_pb<float>(int lanes, bool adj, int hist) {

@@ -96,9 +96,10 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
 	}
 	bool cut;
 	if (sc.mirror) {
-		// NUBosonsBulkPB: the mirrored distance, counted iff r' < r_max (no second look)
+		// NUBosonsBulkPB: the mirrored distance, counted iff r' < r_max (no second look;
+		// FP32: an r' rounded onto r_max counted inside, as in the evaluation kernels)
 		mirror_r((T)(2.0 * sc.rmax), g.r, g.rinv, sc.mirror == 2);
-		cut = g.r < (T)sc.rmax;
+		cut = sizeof(T) == 4 ? g.r <= (T)sc.rmax : g.r < (T)sc.rmax;
 	} else {
 		cut = force || g.r <= (T)sc.rmax;
 		if constexpr (sizeof(T) == 4) nearmin = fminf(nearmin, fabsf(g.r - (T)sc.rmax));

@@ -683,12 +683,14 @@ __device__ __forceinline__ void half_block_f32(const SysConst& sc, int sp, int n
 			f2_split(r, rA, rB);
 			bool inA, inB;
 			if constexpr (MIR) {
-				// mirrored distances: r' = r_max is a set of measure zero, no second look
+				// mirrored distances: no second look.  r' = r_max, where the reference counts
+				// the pair outside, has measure zero in FP64; an FP32 r' rounded onto r_max
+				// is counted inside, as FP64 counts the pair with probability one
 				mirror_r(m2, rA, qa, sc.mirror == 2);
 				mirror_r(m2, rB, qb, sc.mirror == 2);
 				r = f2_make(rA, rB);
-				inA = okA && (rA < rmax);
-				inB = okB && (rB < rmax);
+				inA = okA && (rA <= rmax);
+				inB = okB && (rB <= rmax);
 			} else {
 				inA = okA && (rA <= rmax);
 				inB = okB && (rB <= rmax);
@@ -1089,17 +1091,18 @@ __device__ __forceinline__ void rev_region_f2(const SysConst& sc, int i0, int i1
 			f2_t dy = f2_sub(Y2, f2_make(pA.y, pB.y));
 			f2_t dz = f2_sub(Z2, f2_make(pA.z, pB.z));
 			float qa, qb;
-			f2_t r = MIR ? pair_r_f2<true>(box, dx, dy, dz, qa, qb) : pair_r_f2<false>(box, dx, dy, dz, qa, qb);
+			f2_t r = pair_r_f2<false>(box, dx, dy, dz, qa, qb);
 			float rA, rB;
 			f2_split(r, rA, rB);
 			bool cA, cB;
 			if constexpr (MIR) {
-				// mirrored distances, formed as the forward sweep forms them (no second look)
+				// mirrored distances (no second look; r' rounded onto r_max counted inside,
+				// as in the forward sweep)
 				mirror_r(m2, rA, qa, sc.mirror == 2);
 				mirror_r(m2, rB, qb, sc.mirror == 2);
 				r = f2_make(rA, rB);
-				cA = rA < rmax;
-				cB = rB < rmax;
+				cA = rA <= rmax;
+				cB = rB <= rmax;
 			} else {
 				cA = rA <= rmax;
 				cB = rB <= rmax;

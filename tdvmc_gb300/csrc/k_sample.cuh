@@ -288,7 +288,9 @@ constexpr int kCoefCopies = 8;
 // the shared mirror at each move (two 16-byte loads per slot pair) instead of
 // being held in registers, for slot counts whose coordinates would not fit in
 // registers (32 slots: 96 registers); same arithmetic, same chain.
-template <int G, int SLOTS, bool CS = false>
+// MIR (NUBosonsBulkPB): both distances enter as r' = min(r, 2 r_max - r), held
+// at 0 and above (pair_u).
+template <int G, int SLOTS, bool CS = false, bool MIR = false>
 __global__ void __launch_bounds__(128, CS ? (SLOTS > 16 ? 3 : 4) : (SLOTS <= 11 ? 5 : 3)) k_sample_f2(SysConst sc, const Q4<float>* __restrict__ coef_g,
                                                    const float* __restrict__ uout_g, const float* __restrict__ kb_g,
                                                    const float* __restrict__ hv_g, const int* __restrict__ lut_g,
@@ -328,6 +330,7 @@ __global__ void __launch_bounds__(128, CS ? (SLOTS > 16 ? 3 : 4) : (SLOTS <= 11 
 	const uint32_t pass = *pass_ptr;
 	const bool last_ok = (SLOTS - 1) * G + lane < n;
 	const float half = 0.5f * L * (1.f + 1e-5f);
+	const float m2 = (float)(2.0 * sc.rmax);
 	const int64_t w0 = wstart ? (int64_t)*wstart : 0;
 
 	for (int64_t wi = (int64_t)blockIdx.x * gpb + gib; wi < nw; wi += (int64_t)gridDim.x * gpb) {
@@ -432,7 +435,12 @@ __global__ void __launch_bounds__(128, CS ? (SLOTS > 16 ? 3 : 4) : (SLOTS <= 11 
 					const f2_t r2 = f2_fma(mz, mz, f2_fma(my, my, f2_fma(mx, mx, tiny2)));
 					float ra, rb;
 					f2_split(r2, ra, rb);
-					const f2_t r = f2_make(pair_r(ra), pair_r(rb));
+					float sa = pair_r(ra), sb = pair_r(rb);
+					if constexpr (MIR) {
+						sa = fmaxf(fminf(sa, m2 - sa), 0.f);
+						sb = fmaxf(fminf(sb, m2 - sb), 0.f);
+					}
+					const f2_t r = f2_make(sa, sb);
 					// floor(x) = round(x - 1/2), x = r / h (see nic)
 					const f2_t xm = f2_fma(r, H2, mhalf2);
 					const f2_t yv = f2_add(xm, R2);

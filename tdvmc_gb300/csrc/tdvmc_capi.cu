@@ -229,9 +229,13 @@ int launch_sample(tdvmc_ctx* ctx, int moves, double step, uint64_t seed, int64_t
 	const int slots = slots_for(ctx->sc.n, G);
 	SampleFn<T> fn = nullptr;
 	if constexpr (std::is_same<T, float>::value)
-		if (ctx->packed_sampler && ctx->sc.uniform && !ctx->sc.mirror) {
-			if (ctx->shared_coords) fn = pick_sample_f32_packed_shared(G, slots);
-			if (!fn) fn = pick_sample_f32_packed(G, slots);
+		if (ctx->packed_sampler && ctx->sc.uniform) {
+			if (ctx->sc.mirror) {
+				fn = pick_sample_f32_packed_pb(G, slots);
+			} else {
+				if (ctx->shared_coords) fn = pick_sample_f32_packed_shared(G, slots);
+				if (!fn) fn = pick_sample_f32_packed(G, slots);
+			}
 		}
 	const bool packed = fn != nullptr;
 	if (!fn) fn = ctx->sc.mirror ? pick_sample_pb<T>(G, slots) : pick_sample<T>(G, slots);
@@ -1542,6 +1546,16 @@ int tdvmc_profile_stage(tdvmc_ctx* ctx, const tdvmc_step_opts* o, float* ms, con
 	}
 	ctx->prof = nullptr;
 	ctx->prof_names = nullptr;
+	if (!rc) {
+		// the stage's solve left the context inside a step (the next stage's parameters
+		// and stage index): back to the step boundary, so that the next step starts at
+		// stage 0 from the unchanged base parameters
+		const uint32_t zero = 0;
+		const size_t pb = (size_t)(2 * ctx->sc.p + 2) * sizeof(double);
+		if (cudaMemcpyAsync(ctx->stage, ctx->base, pb, cudaMemcpyDeviceToDevice, ctx->st) != cudaSuccess ||
+		    cudaMemcpyAsync(&ctx->dyn->stage, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st) != cudaSuccess)
+			rc = TDVMC_ERR_CUDA;
+	}
 	cudaError_t se = cudaStreamSynchronize(ctx->st);
 	int nk = 0;
 	cudaEvent_t prev = e0;

@@ -536,3 +536,33 @@ def test_evaluation_variants_match_oracle(precision, env):
         assert np.abs(fwd["other"][c] - r["other"]).max() < tol * scaleE
         scaled = max(np.abs(r["dE"]).max(), 1.0)
         assert np.abs(dE[c] - r["dE"]).max() < tol * scaled
+
+
+def test_profile_stage_leaves_the_step_boundary():
+    """tdvmc_profile_stage runs one stage eagerly and then puts the parameters and
+    the stage index back to the step boundary: the parameters are unchanged, and
+    after one more step the evaluation uses that step's final parameters (a fresh
+    context given the same walkers and parameters evaluates identically)."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "sample_d3_n27.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    nw = 64
+    rng = np.random.default_rng(5)
+    R0 = np.repeat(z["R0"].T[None], nw, axis=0) + rng.normal(0, 0.05, size=(nw, dim, n))
+    mk = lambda: T.BosonsBulk(dim, n, p, L, nw, system_params=(1.0, 1.0), potential="lj", hbar2_2m=0.09,  # noqa
+                              precision="fp64")
+    s = mk()
+    s.SetParameters(z["uR"], z["uI"], 0.0, 0.0)
+    s.SetWalkers(R0)
+    td = T.TDVP(s, 1e-3, n, 0.35, seed=3)
+    before = np.concatenate(s.GetParameters()[:2])
+    td.profile_stage()
+    assert np.array_equal(np.concatenate(s.GetParameters()[:2]), before)
+    td.step()
+    got = s.CalculateExpectationValues()
+    f = mk()
+    f.SetParameters(*s.GetParameters())
+    f.SetWalkers(s.GetWalkers())
+    ref = f.CalculateExpectationValues()
+    for key in ("lnpsi", "O", "eloc", "other"):
+        assert np.array_equal(got[key], ref[key]), key

@@ -215,3 +215,46 @@ def test_pb_pair_distribution_weight():
         out.append(s.CalculateAdditionalSystemProperties(100)["gr"])
     assert out[0].size == out[1].size == 100
     assert np.abs(out[0] - out[1] * (n - 1) / dim).max() <= 1e-12 * np.abs(out[0]).max()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed-scalar"])
+@pytest.mark.parametrize("n", [150, 343, 600])
+def test_pb_sampler_padded_slots_follow_oracle_chain(n, mode):
+    """Mirrored-distance moves with register slots past N (150 particles on 32
+    lanes in 8 slots, 343 in 11, 600 in 32 read from shared memory), uniform
+    knots: FP64 the oracle's chain; FP32 packed (f32x2) and scalar samplers the
+    same moves on at least 90 % of the walkers, acceptance within 1 %."""
+    import tdvmc_gb300 as T
+    dim, p, nw = 3, 10, 32
+    L = (n / 0.5) ** (1.0 / dim)
+    knots = np.linspace(0.0, L / 2, p)
+    moves, step = 2 * n, 0.5
+    rng = np.random.default_rng(n)
+    uR, uI = 0.3 * rng.normal(size=p), 0.1 * rng.normal(size=p)
+    R0 = rng.uniform(-L / 2, L / 2, size=(nw, dim, n))
+    precision = "fp64" if mode == "fp64" else "mixed"
+    if precision == "mixed":
+        R0 = R0.astype(np.float32).astype(np.float64)
+    if mode == "mixed-scalar":
+        os.environ["TDVMC_SAMPLER"] = "scalar"
+    try:
+        s = T.NUBosonsBulkPB(dim, n, p, L, nw, user_knots=knots, system_params=(0.8, 1.0), precision=precision)
+    finally:
+        os.environ.pop("TDVMC_SAMPLER", None)
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R0)
+    acc = s.DoMetropolisSteps(moves, step, seed=31, pass_id=2)
+    Rg = s.GetWalkers()
+    s.close()
+    o = orc.OracleSystem(dim, n, p, L, user_knots=knots, pot_kind=orc.POT_SQUARE, pot=(0.8, 1.0),
+                         variant=orc.SYS_NU_PB)
+    Ro = np.ascontiguousarray(R0.copy())
+    acc_o = o.sample(uR, Ro, moves, step, seed=31, pass_id=2)
+    assert 0.1 < acc_o / (moves * nw) < 0.95
+    if precision == "fp64":
+        assert acc == acc_o
+        assert np.abs(Rg - Ro).max() < 1e-9
+    else:
+        d = np.abs(Rg - Ro).reshape(nw, -1).max(1)
+        assert (d < 1e-4).mean() >= 0.9, d
+        assert abs(acc - acc_o) <= 0.01 * acc_o, (acc, acc_o)
