@@ -365,10 +365,13 @@ int main(int argc, char** argv) {
 		             required_version.c_str(), cfg.str("CONFIG_VERSION", "").c_str());
 		return 1;
 	}
-	if (cfg.str("SYSTEM_TYPE", "BosonsBulk") != "BosonsBulk") {
-		std::fprintf(stderr, "only SYSTEM_TYPE BosonsBulk is implemented on the GPU\n");
+	// BosonsBulk (TDVMC.cpp:2843-2850) or NUBosonsBulkPB (2953-2960)
+	const std::string system = cfg.str("SYSTEM_TYPE", "BosonsBulk");
+	if (system != "BosonsBulk" && system != "NUBosonsBulkPB") {
+		std::fprintf(stderr, "only SYSTEM_TYPE BosonsBulk and NUBosonsBulkPB are implemented on the GPU\n");
 		return 2;
 	}
+	const bool pb = system == "NUBosonsBulkPB";
 	g_out = argc > 2 ? std::string(argv[2]) : cfg.str("OUTPUT_DIRECTORY", "./");
 	if (!g_out.empty() && g_out.back() != '/') g_out += "/";
 	mkdir(g_out.c_str(), 0755);
@@ -402,6 +405,16 @@ int main(int argc, char** argv) {
 	}
 	d.box_length = LBOX;
 	d.pot_kind = pot == "lj" ? TDVMC_POT_LJ : (pot == "gauss" ? TDVMC_POT_GAUSS : TDVMC_POT_SQUARE);
+	if (pb) {
+		// its square well (NUBosonsBulkPB.cpp:347-350); GPU_PB_EXACT_DERIVATIVES = 1 selects the
+		// exact derivatives of the mirrored pair term instead of the reference's form
+		d.pot_kind = TDVMC_POT_SQUARE;
+		d.system_type = (int)cfg.num("GPU_PB_EXACT_DERIVATIVES", 0) == 1 ? TDVMC_SYS_NU_BOSONS_BULK_PB_EXACT
+		                                                                  : TDVMC_SYS_NU_BOSONS_BULK_PB;
+	}
+	// NUBosonsBulkPB reports 9 + GR_BIN_COUNT other expectation values (400 bins when the
+	// count is 0), the g(r) entries never filled (NUBosonsBulkPB.cpp:55-61, 578-582)
+	const int pb_gr = pb ? ((int)cfg.num("GR_BIN_COUNT", 0) > 0 ? (int)cfg.num("GR_BIN_COUNT", 0) : 400) : 0;
 	std::vector<double> sp = cfg.vec("SYSTEM_PARAMS");
 	d.n_pot = (int)std::min<size_t>(5, sp.size());
 	for (int i = 0; i < d.n_pot; i++) d.pot[i] = sp[i];
@@ -602,6 +615,7 @@ int main(int argc, char** argv) {
 		const bool set_back = acceptance_check && trial == 2;
 		tdvmc_get_step_operators(ctx, O.data());
 		std::vector<double> other(st.other, st.other + 9);
+		other.resize(9 + pb_gr, 0.0);
 		std::vector<double> parR = pR, parI = pI;
 		parR.push_back(p0R);
 		parI.push_back(p0I);

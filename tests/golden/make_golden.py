@@ -141,25 +141,29 @@ DRIVER_CONFIG = {
     "PARAMS_REAL": [-2.0, -2.0, -1.0, -0.5, -0.2, -0.1, -0.05, 0.0, 0.0, 0.0], "PARAMS_IMAGINARY": [0.0] * 10,
     "PARAM_PHIR": 0.0, "PARAM_PHII": 0.0,
 }
+# the same run with the mirrored-distance system (knots to r_max = L/2; its square well)
+DRIVER_PB_CONFIG = dict(DRIVER_CONFIG, SYSTEM_TYPE="NUBosonsBulkPB", USE_NURBS=1,
+                        NURBS_GRID=[round(0.2 * k, 10) for k in range(10)])
 DRIVER_FILES = ("LocalEnergyR", "LocalEnergyI", "ParametersR", "ParametersI", "OtherExpectationValues",
                 "LocalOperators", "timesSystem")
 
 
-def driver_run(ref_root):
-    """Runs the reference program (``ref_harness --run``) on DRIVER_CONFIG in a
-    scratch directory that also holds the k-vector tables it reads from the
-    config's directory, and keeps the config and the output files above."""
+def driver_run(ref_root, config=DRIVER_CONFIG, name="driver_d3_n27"):
+    """Runs the reference program (``ref_harness --run``) on a config (DRIVER_CONFIG,
+    DRIVER_PB_CONFIG) in a scratch directory that also holds the k-vector tables it
+    reads from the config's directory, and keeps the config and the output files
+    above under tests/golden/<name>."""
     import json
     import shutil
     import tempfile
-    dst = os.path.join(HERE, "driver_d3_n27")
+    dst = os.path.join(HERE, name)
     os.makedirs(dst, exist_ok=True)
     with open(os.path.join(dst, "run.config"), "w") as f:
-        json.dump(DRIVER_CONFIG, f, indent=1)
+        json.dump(config, f, indent=1)
     with tempfile.TemporaryDirectory() as tmp:
         for name in ("kVectors3D.json", "kNorm3D.csv"):
             os.symlink(os.path.join(ref_root, "config", name), os.path.join(tmp, name))
-        cfg = dict(DRIVER_CONFIG, OUTPUT_DIRECTORY=tmp + "/out/")
+        cfg = dict(config, OUTPUT_DIRECTORY=tmp + "/out/")
         os.makedirs(cfg["OUTPUT_DIRECTORY"])
         with open(os.path.join(tmp, "run.config"), "w") as f:
             json.dump(cfg, f, indent=1)
@@ -228,7 +232,8 @@ def pb_systems(ref_root):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] not in ("obs", "driver", "pb") else "/root/reference"
+    ref_root = (sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] not in ("obs", "driver", "pb", "driver-pb")
+                else "/root/reference")
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root])
     if "obs" in sys.argv[1:]:
@@ -237,10 +242,14 @@ def main():
     if "driver" in sys.argv[1:]:
         driver_run(ref_root)
         return
+    if "driver-pb" in sys.argv[1:]:
+        driver_run(ref_root, DRIVER_PB_CONFIG, "driver_pb_d3_n27")
+        return
     if "pb" in sys.argv[1:]:
         pb_systems(ref_root)
         return
     driver_run(ref_root)
+    driver_run(ref_root, DRIVER_PB_CONFIG, "driver_pb_d3_n27")
     pb_systems(ref_root)
     observables(ref_root)
 

@@ -57,7 +57,7 @@ int tdvmc_create(const tdvmc_system_desc* d, tdvmc_ctx** out) {
 	c->uR.assign(c->p, 0.0);
 	c->uI.assign(c->p, 0.0);
 	*out = c;
-	logf("create");
+	logf("create system %.0f pot %.0f", d->system_type, d->pot_kind);
 	return 0;
 }
 

@@ -228,18 +228,23 @@ def test_hundred_step_real_time_run_is_stable():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_native_driver_tracks_the_reference_program(tmp_path, precision):
-    """The driver and the reference's own program (tests/golden/driver_d3_n27,
-    made by tests/golden/make_golden.py with the reference built from its
-    sources) on the same config: 3D N=27 square well, 8,192 samples per stage,
-    two imaginary-time RK4 steps.  The chains differ (Philox walkers here, the
-    reference's mt19937 chain there), so the values agree statistically: the
-    start row exactly, E^R per step within 1 %, the steps' increments of uR_k
-    within 3 % of the largest increment (measured 0.4 %).  phi^R is -ln psi of
-    one sampled configuration (USE_NORMALIZE_WF), so it is only checked finite."""
+@pytest.mark.parametrize("fixture", ["driver_d3_n27", "driver_pb_d3_n27"])
+def test_native_driver_tracks_the_reference_program(tmp_path, precision, fixture):
+    """The driver and the reference's own program (tests/golden/driver_d3_n27 for
+    BosonsBulk, driver_pb_d3_n27 for NUBosonsBulkPB with knots to L/2, made by
+    tests/golden/make_golden.py with the reference built from its sources) on the
+    same config: 3D N=27 square well, 8,192 samples per stage, two imaginary-time
+    RK4 steps.  The chains differ (Philox walkers here, the reference's mt19937
+    chain there), so the values agree statistically: the start row exactly;
+    BosonsBulk E^R per step within 1 % and the steps' increments of uR_k within 3 %
+    of the largest increment (measured 0.4 %); NUBosonsBulkPB, whose local energy is
+    heavy-tailed, the first E^R within its statistical band.  phi^R is -ln psi of
+    one sampled configuration (USE_NORMALIZE_WF), so it is only checked finite.
+    The other expectation values have the reference's column count (9, or
+    9 + GR_BIN_COUNT for NUBosonsBulkPB)."""
     from tdvmc_gb300 import build as B
     B.build()
-    gold = os.path.join(ROOT, "tests", "golden", "driver_d3_n27")
+    gold = os.path.join(ROOT, "tests", "golden", fixture)
     cfg = json.load(open(os.path.join(gold, "run.config")))
     cfg["GPU_PRECISION"] = precision
     path = tmp_path / "run.config"
@@ -252,10 +257,21 @@ def test_native_driver_tracks_the_reference_program(tmp_path, precision):
     er, er_ref = load(out, "LocalEnergyR")[:, 0], load(gold, "LocalEnergyR")[:, 0]
     assert pr.shape == pr_ref.shape and er.shape == er_ref.shape
     np.testing.assert_array_equal(pr[0], pr_ref[0])
+    np.testing.assert_array_equal(load(out, "ParametersI")[0], load(gold, "ParametersI")[0])
+    assert load(out, "OtherExpectationValues").shape == load(gold, "OtherExpectationValues").shape
+    if fixture == "driver_pb_d3_n27":
+        # NUBosonsBulkPB's local energy is heavy-tailed: at the start parameters the FP64
+        # oracle's walkers give a per-sample standard deviation of about 100 at E^R = 13,
+        # so 8,192 samples carry a standard error of 1.1 (the reference's chain samples,
+        # two sweeps apart, up to about twice that); the first row, sampled at the same
+        # parameters by both, must agree within 4 combined standard errors (10), and the
+        # steps after it, whose parameters carry that noise, stay finite
+        assert abs(er[0] - er_ref[0]) < 10.0, (er, er_ref)
+        assert np.all(np.isfinite(pr)) and np.all(np.isfinite(er))
+        return
     P = int(cfg["N_PARAM"])
     for k in range(1, len(pr)):
         d, d_ref = pr[k, :P] - pr[0, :P], pr_ref[k, :P] - pr_ref[0, :P]
         assert np.abs(d - d_ref).max() < 0.03 * np.abs(d_ref).max(), (k, d, d_ref)
         assert np.isfinite(pr[k, P])
     assert np.all(np.abs(er - er_ref) < 0.01 * np.abs(er_ref)), (er, er_ref)
-    np.testing.assert_array_equal(load(out, "ParametersI")[0], load(gold, "ParametersI")[0])

@@ -124,14 +124,16 @@ def test_unimplemented_check_type_is_refused(driver, tmp_path):
     assert r.returncode == 2 and "PARAMETER_ACCEPTANCE_CHECK_TYPE 3" in r.stderr
 
 
-def test_output_files_have_the_reference_layout(driver, tmp_path):
-    """The driver on the config of tests/golden/driver_d3_n27 (the reference's
-    own program run on it, tests/golden/make_golden.py): every file the fixture
-    holds comes out with the same header line, the same number of rows and
-    columns, and every number in the reference's 24-wide %.15e layout
-    (Utils.cpp:809-858); the start-parameter files equal the reference's."""
+@pytest.mark.parametrize("fixture", ["driver_d3_n27", "driver_pb_d3_n27"])
+def test_output_files_have_the_reference_layout(driver, tmp_path, fixture):
+    """The driver on the configs of tests/golden/driver_d3_n27 (BosonsBulk) and
+    driver_pb_d3_n27 (NUBosonsBulkPB), the reference's own program run on them
+    (tests/golden/make_golden.py): every file the fixture holds comes out with
+    the same header line, the same number of rows and columns, and every number
+    in the reference's 24-wide %.15e layout (Utils.cpp:809-858); the
+    start-parameter files equal the reference's."""
     import re
-    gold = os.path.join(ROOT, "tests", "golden", "driver_d3_n27")
+    gold = os.path.join(ROOT, "tests", "golden", fixture)
     cfg = json.load(open(os.path.join(gold, "run.config")))
     r, out, _ = run(driver, tmp_path, cfg)
     assert r.returncode == 0, r.stderr
@@ -154,3 +156,24 @@ def test_output_files_have_the_reference_layout(driver, tmp_path):
     assert np.array_equal(p0, np.asarray(cfg["PARAMS_REAL"]))
     assert open(out / "AllParametersR.dat").read().splitlines()[0] == "%24s%24s" % ("uR_k", "...")
     assert open(out / "AllLocalEnergyR.dat").read().splitlines()[0] == "ER"
+
+
+def test_mirrored_distance_system(driver, tmp_path):
+    """SYSTEM_TYPE NUBosonsBulkPB (TDVMC.cpp:2953-2960): the descriptor carries the
+    system type and its square well whatever POTENTIAL says; GPU_PB_EXACT_DERIVATIVES
+    switches to the exact form; OtherExpectationValues rows carry 9 + GR_BIN_COUNT
+    values, the g(r) entries zero as the reference leaves them."""
+    cfg = base_cfg(SYSTEM_TYPE="NUBosonsBulkPB", USE_NURBS=1, NURBS_GRID=[0.0, 0.4, 0.7, 1.0],
+                   POTENTIAL="lj", GR_BIN_COUNT=12)
+    r, out, log = run(driver, tmp_path, cfg)
+    assert r.returncode == 0, r.stderr
+    assert "create system 1 pot 1" in log
+    other = table(out / "OtherExpectationValues.dat")
+    assert other.shape == (10, 9 + 12)
+    assert np.all(other[:, 9:] == 0.0)
+    r, out, log = run(driver, tmp_path, dict(cfg, GPU_PB_EXACT_DERIVATIVES=1, GR_BIN_COUNT=0))
+    assert r.returncode == 0, r.stderr
+    assert "create system 2 pot 1" in log
+    assert table(out / "OtherExpectationValues.dat").shape[1] == 9 + 400
+    r, _, _ = run(driver, tmp_path, base_cfg(SYSTEM_TYPE="NUBosonsBulkPBBox"))
+    assert r.returncode == 2
