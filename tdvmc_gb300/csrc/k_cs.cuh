@@ -70,8 +70,8 @@ template <typename T> struct CsGeom {
 // FP32: r <= r_max from the FP32 distance; nearmin collects |r - r_max|, and the
 // pairs within rounding of r_max are decided again in FP64 after the slot
 // (cs_fix_slot).  force: the pair as within r_max whatever r is (the fix-up).
-// sc.mirror: the distances of NUBosonsBulkPB (mirror_r).
-template <typename T>
+// MIR: the distances of NUBosonsBulkPB (mirror_r).
+template <typename T, bool MIR = false>
 __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
                                              const T* __restrict__ kb, const T* __restrict__ hv,
                                              const int* __restrict__ lut, T& nearmin, bool force = false) {
@@ -95,7 +95,7 @@ __device__ __forceinline__ CsGeom<T> cs_geom(const SysConst& sc, const Q4<T>& xr
 		g.r = r2 * g.rinv;
 	}
 	bool cut;
-	if (sc.mirror) {
+	if constexpr (MIR) {
 		// NUBosonsBulkPB: the mirrored distance, counted iff r' < r_max (no second look;
 		// FP32: an r' rounded onto r_max counted inside, as in the evaluation kernels)
 		mirror_r((T)(2.0 * sc.rmax), g.r, g.rinv, sc.mirror == 2);
@@ -179,20 +179,20 @@ __device__ __forceinline__ void cs_accum(const SysConst& sc, const CsGeom<T>& g,
 	}
 }
 
-template <typename T, int G, bool STATS, bool UNI>
+template <typename T, int G, bool STATS, bool UNI, bool MIR = false>
 __device__ __forceinline__ void cs_pair(const SysConst& sc, const Q4<T>& xr, const Q4<T>& xi, bool ok,
                                         const CsPieceRow<T>& pu, const T* __restrict__ piece, const T* __restrict__ kb,
                                         const T* __restrict__ hv, const int* __restrict__ lut, T* __restrict__ drow,
                                         T* __restrict__ oacc, T* __restrict__ d2acc, int lane, T pa, T pb, KSum<T>& vs,
                                         int& nout, T& nearmin) {
-	cs_accum<T, G, STATS, UNI>(sc, cs_geom<T>(sc, xr, xi, ok, kb, hv, lut, nearmin), pu, piece, drow, oacc, d2acc, lane, pa, pb,
+	cs_accum<T, G, STATS, UNI>(sc, cs_geom<T, MIR>(sc, xr, xi, ok, kb, hv, lut, nearmin), pu, piece, drow, oacc, d2acc, lane, pa, pb,
 	                           vs, nout);
 }
 
 // kCsBatch partners [i, i + kCsBatch): all geometries first, then the accumulations
 // in partner order.
 constexpr int kCsBatch = 4;
-template <typename T, int G, bool STATS, bool UNI>
+template <typename T, int G, bool STATS, bool UNI, bool MIR = false>
 __device__ __forceinline__ void cs_batch(const SysConst& sc, const Q4<T>& xr, const Q4<T>* __restrict__ xs, int i,
                                          bool ok, const CsPieceRow<T>& pu, const T* __restrict__ piece,
                                          const T* __restrict__ kb, const T* __restrict__ hv,
@@ -201,7 +201,7 @@ __device__ __forceinline__ void cs_batch(const SysConst& sc, const Q4<T>& xr, co
                                          T& nearmin) {
 	CsGeom<T> g[kCsBatch];
 #pragma unroll
-	for (int u = 0; u < kCsBatch; u++) g[u] = cs_geom<T>(sc, xr, xs[i + u], ok, kb, hv, lut, nearmin);
+	for (int u = 0; u < kCsBatch; u++) g[u] = cs_geom<T, MIR>(sc, xr, xs[i + u], ok, kb, hv, lut, nearmin);
 #pragma unroll
 	for (int u = 0; u < kCsBatch; u++)
 		cs_accum<T, G, STATS, UNI>(sc, g[u], pu, piece, drow, oacc, d2acc, lane, pa, pb, vs, nout);
@@ -265,7 +265,8 @@ __device__ __noinline__ CsFix cs_fix_slot(SysConst sc, CsPieceRow<float> pu, con
 
 // Stores the correlated-sampling data of walkers (start + w) mod nw_total,
 // w < count (start from *wstart when given, else 0).
-template <typename T, int G, bool UNI>
+// MIR: NUBosonsBulkPB (mirrored distances; no cutoff fix-up).
+template <typename T, int G, bool UNI, bool MIR = false>
 __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const CsPieceRow<T> pu, const DynState* __restrict__ dyn,
                                                   const T* __restrict__ piece_g, const T* __restrict__ kb_g,
                                                   const T* __restrict__ hv_g, const int* __restrict__ lut_g,
@@ -336,26 +337,26 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const CsPieceR
 			// partners below the slot: every lane's pair is counted once (i < nrow);
 			// base is a multiple of G, so of kCsBatch
 			for (int i = 0; i < base; i += kCsBatch)
-				cs_batch<T, G, true, UNI>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
+				cs_batch<T, G, true, UNI, MIR>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
 				                          vs, nout, nearmin);
 			// the slot's own block: counted iff i < nrow
 			for (int i = base; i < dend; i++) {
 				if (i < nrow)
-					cs_pair<T, G, true, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs,
+					cs_pair<T, G, true, UNI, MIR>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb, vs,
 					                    nout, nearmin);
 				else
-					cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok && i != nrow, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane,
+					cs_pair<T, G, false, UNI, MIR>(sc, xr, xs[i], rowok && i != nrow, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane,
 					                     pa, pb, vs, nout, nearmin);
 			}
 			// partners above the slot: D only
 			int i = dend;
 			for (; i + kCsBatch <= n; i += kCsBatch)
-				cs_batch<T, G, false, UNI>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
+				cs_batch<T, G, false, UNI, MIR>(sc, xr, xs, i, rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
 				                           vs, nout, nearmin);
 			for (; i < n; i++)
-				cs_pair<T, G, false, UNI>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
+				cs_pair<T, G, false, UNI, MIR>(sc, xr, xs[i], rowok, pu, piece, kb, hv, lut, drow, oacc, d2acc, lane, pa, pb,
 				                          vs, nout, nearmin);
-			if constexpr (sizeof(T) == 4) {
+			if constexpr (sizeof(T) == 4 && !MIR) {
 				if (rowok && nearmin < sc.rcut_band) {
 					const CsFix f = cs_fix_slot<G, UNI>(sc, pu, piece, kb, hv, lut, xs, drow, oacc, d2acc, n, nrow, lane,
 					                                    pa, pb);

@@ -462,7 +462,8 @@ int launch_cs_store(tdvmc_ctx* ctx, int64_t count, const int32_t* wstart) {
 	int gpb = 4;
 	while (gpb > 1 && cta + gpb * grp > 200 * 1024) gpb--;
 	const size_t smem = cta + gpb * grp;
-	auto fn = ctx->cs_uni ? k_cs_store<T, G, true> : k_cs_store<T, G, false>;
+	auto fn = s.mirror ? (ctx->cs_uni ? k_cs_store<T, G, true, true> : k_cs_store<T, G, false, true>)
+	                   : (ctx->cs_uni ? k_cs_store<T, G, true> : k_cs_store<T, G, false>);
 	CsPieceRow<T> pu;
 	for (int k = 0; k < kCsPiece; k++) pu.c[k] = (T)ctx->cs_pu[k];
 	CK(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
