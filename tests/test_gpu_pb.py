@@ -258,3 +258,27 @@ def test_pb_sampler_padded_slots_follow_oracle_chain(n, mode):
         d = np.abs(Rg - Ro).reshape(nw, -1).max(1)
         assert (d < 1e-4).mean() >= 0.9, d
         assert abs(acc - acc_o) <= 0.01 * acc_o, (acc, acc_o)
+
+
+def test_pb_autotune_stays_on_its_kernels():
+    """The autotuner on the mirrored-distance system: its kernels exist for 32
+    lanes and histogram mode 0 only, so every other candidate is skipped; the
+    walkers are restored and the results equal those of the default tiles."""
+    import tdvmc_gb300 as T
+    z = np.load(os.path.join(GOLD, "pb_eval_d3_n64_p10.npz"))
+    nw = 1024
+    R = np.concatenate([soa(z["cfgs"])] * (nw // len(z["cfgs"])))
+    s = gpu_pb(z, nw, "mixed")
+    s.SetParameters(z["uR"], z["uI"])
+    s.SetWalkers(R.astype(np.float32).astype(np.float64))
+    s.DoMetropolisSteps(64, 0.3, seed=1, pass_id=0)
+    before = s.GetWalkers()
+    ref = s.CalculateExpectationValues()
+    dref = s.CalculateLocalEnergyAdjoint()
+    tiles = s.Autotune(64, 0.3)
+    assert tiles["sample_lanes"] == 32 and tiles["eval_lanes"] == 32
+    assert np.array_equal(s.GetWalkers(), before)
+    got = s.CalculateExpectationValues()
+    for key in ("lnpsi", "O", "eloc", "other"):
+        assert np.array_equal(got[key], ref[key]), key
+    assert np.array_equal(s.CalculateLocalEnergyAdjoint(), dref)
