@@ -29,6 +29,15 @@
 // (WriteConfig, TDVMC.cpp:387-407, 4027-4034; numbers with 17 significant
 // digits where the reference prints 6).
 //
+// Random-number state for a successive run, as the reference keeps its
+// generators' states (random/state_*_<rank>.dat read from the config directory
+// at the start when present and written to the output directory at the end,
+// Utils.cpp:48-78, TDVMC.cpp:515-525, 3958-3964): the Philox streams are keyed
+// by (GPU_SEED, epoch) with the epoch in the key's upper 32 bits;
+// random/state_philox.dat holds "seed epoch", a run that finds it in the config
+// directory continues with that seed at the next epoch (fresh streams, none of
+// the previous run's repeated), and every run writes its own pair at the end.
+//
 // Parameter acceptance (USE_PARAMETER_ACCEPTANCE_CHECK = 1, TDVMC.cpp:3648-
 // 3800, AcceptNewParams 2585-2630): a step is tried at most twice, the second
 // time with twice the sampling effort; PARAMETER_ACCEPTANCE_CHECK_TYPE 0
@@ -43,7 +52,7 @@
 // Extra keys (all optional): GPU_WALKERS (default MC_NSTEPS), GPU_PRECISION
 // ("mixed" or "fp64"), POTENTIAL ("square" as BosonsBulk, "gauss", "lj"),
 // HBAR2_2M (default 1.0, the reference's constant), GPU_ADJOINT (0/1),
-// GPU_SEED, GPU_COORDS_FILES.
+// GPU_SEED (its low 32 bits key the Philox streams), GPU_COORDS_FILES.
 //
 // usage: tdvmc_run <config file> [output directory]
 #include "tdvmc_gpu.h"
@@ -387,12 +396,26 @@ int main(int argc, char** argv) {
 	const int64_t walkers = (int64_t)cfg.num("GPU_WALKERS", MC_NSTEPS);
 	const std::string prec = cfg.str("GPU_PRECISION", "mixed");
 	const std::string pot = cfg.str("POTENTIAL", "square");
-	const uint64_t seed = (uint64_t)cfg.num("GPU_SEED", 1);
+	uint64_t seed_base = (uint64_t)cfg.num("GPU_SEED", 1) & 0xFFFFFFFFull;
+	uint64_t epoch = 0;
 	const int ADD_NTH = (int)cfg.num("CALCULATE_ADDITIONAL_DATA_EVERY_NTH_STEP", 0);
 	const int ADD_THERM = (int)cfg.num("MC_NADDITIONALTHERMSTEPS", 0);
 	const int GR_BINS = (int)cfg.num("GR_BIN_COUNT", 50);
 	std::string cfg_dir = argv[1];
 	cfg_dir = cfg_dir.find_last_of("\\/") == std::string::npos ? "./" : cfg_dir.substr(0, cfg_dir.find_last_of("\\/")) + "/";
+
+	{
+		// the previous run's random-number state, when the config directory holds it
+		std::ifstream fs(cfg_dir + "random/state_philox.dat");
+		uint64_t sb = 0, ep = 0;
+		if (fs >> sb >> ep) {
+			seed_base = sb & 0xFFFFFFFFull;
+			epoch = (ep + 1) & 0xFFFFFFFFull;
+			std::printf("random state from %srandom/state_philox.dat: seed %llu, epoch %llu\n", cfg_dir.c_str(),
+			            (unsigned long long)seed_base, (unsigned long long)epoch);
+		}
+	}
+	const uint64_t seed = (epoch << 32) | seed_base;
 
 	tdvmc_system_desc d{};
 	d.dim = DIM;
@@ -694,6 +717,11 @@ int main(int argc, char** argv) {
 		                xf, k, N, DIM);
 	write_positions(g_out + "AAFinish_particleconfiguration_" + std::to_string(N) + "_" + std::to_string(DIM) + "D.dat",
 	                xf, 0, N, DIM);
+	{
+		mkdir((g_out + "random").c_str(), 0755);
+		std::ofstream fs(g_out + "random/state_philox.dat");
+		fs << seed_base << " " << epoch << "\n";
+	}
 	{
 		std::vector<double> fR(P), fI(P);
 		double fPR, fPI;

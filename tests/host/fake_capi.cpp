@@ -99,9 +99,9 @@ int tdvmc_get_walkers(tdvmc_ctx* c, double* x, int64_t nw) {
 	return 0;
 }
 
-int tdvmc_sample(tdvmc_ctx*, int32_t moves, double, uint64_t, uint32_t, int64_t* accepted) {
+int tdvmc_sample(tdvmc_ctx*, int32_t moves, double, uint64_t seed, uint32_t, int64_t* accepted) {
 	if (accepted) *accepted = 0;
-	logf("sample %.0f", moves);
+	logf("sample %.0f seed %.0f", moves, (double)seed);
 	return 0;
 }
 

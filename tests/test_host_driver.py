@@ -103,7 +103,7 @@ def test_rejected_step_retries_then_sets_back_five_steps(driver, tmp_path):
     assert len(E) == 10
     # the walkers restarted from their initial configuration with the thermalisation moves
     assert sum(1 for l in log if l.startswith("set_walkers")) == 2
-    assert sum(1 for l in log if l == "sample 5") == 2
+    assert sum(1 for l in log if l.startswith("sample 5 ")) == 2
     # parameters restored to the start of the third step: 1 + 0.01 * (1 + 2)
     sets = [float(l.split()[1]) for l in log if l.startswith("set_params")]
     assert any(abs(v - (1.0 + 0.01 * 3)) < 1e-12 for v in sets)
@@ -177,3 +177,24 @@ def test_mirrored_distance_system(driver, tmp_path):
     assert table(out / "OtherExpectationValues.dat").shape[1] == 9 + 400
     r, _, _ = run(driver, tmp_path, base_cfg(SYSTEM_TYPE="NUBosonsBulkPBBox"))
     assert r.returncode == 2
+
+
+def test_random_state_for_a_successive_run(driver, tmp_path):
+    """random/state_philox.dat (the counterpart of the reference's random/state_*
+    files, Utils.cpp:48-78, TDVMC.cpp:515-525, 3958-3964): a run writes its seed
+    and epoch; a run that finds the file in its config directory keeps the seed
+    and takes the next epoch, so its Philox streams (key = epoch << 32 | seed)
+    are new ones."""
+    import shutil
+    cfg = base_cfg(GPU_SEED=7)
+    r, out, log = run(driver, tmp_path, cfg)
+    assert r.returncode == 0, r.stderr
+    assert (out / "random" / "state_philox.dat").read_text().split() == ["7", "0"]
+    assert any(l.startswith("sample 5 seed 7") for l in log)
+    (tmp_path / "cfg" / "random").mkdir()
+    shutil.copy(out / "random" / "state_philox.dat", tmp_path / "cfg" / "random" / "state_philox.dat")
+    (tmp_path / "fake.log").unlink()
+    r, out, log = run(driver, tmp_path, cfg)
+    assert r.returncode == 0, r.stderr
+    assert any(l.startswith("sample 5 seed %d" % ((1 << 32) | 7)) for l in log), log[:5]
+    assert (out / "random" / "state_philox.dat").read_text().split() == ["7", "1"]
