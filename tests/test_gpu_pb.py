@@ -282,3 +282,38 @@ def test_pb_autotune_stays_on_its_kernels():
     for key in ("lnpsi", "O", "eloc", "other"):
         assert np.array_equal(got[key], ref[key]), key
     assert np.array_equal(s.CalculateLocalEnergyAdjoint(), dref)
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_pb_mixed_tracks_fp64_at_the_benchmark_shape(exact):
+    """3D N=343, rho=0.365, P=30 knots on [0, L/2] (the benchmark's shape), 16
+    jittered-lattice walkers held in FP32: the mixed evaluation against the FP64
+    evaluation of the same walkers within 1e-5 (ln psi, O_k, E_loc, the kinetic
+    sums, dE/d alpha), in both forms of the derivative terms.  Every pair with
+    r > L/2 is mirrored here (about half of them), including the pairs across
+    the minimum-image wrap where the mirrored form's gradient changes sign."""
+    import tdvmc_gb300 as T
+    import bench as B
+    nw = 16
+    R = B.initial_walkers(nw, seed=77).astype(np.float32).astype(np.float64)
+    knots = np.linspace(0.0, B.L / 2, B.P)
+    uR, uI = B.initial_params()
+    uI = 0.01 * np.random.default_rng(3).normal(size=B.P)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = T.NUBosonsBulkPB(B.DIM, B.N, B.P, B.L, nw, user_knots=knots, system_params=(1.0, 1.0),
+                             hbar2_2m=B.HBAR2_2M, precision=prec, exact_derivatives=exact)
+        s.SetParameters(uR, uI)
+        s.SetWalkers(R)
+        f = s.CalculateExpectationValues()
+        f["dE"] = s.CalculateLocalEnergyAdjoint()
+        out[prec] = f
+        s.close()
+    a, b = out["mixed"], out["fp64"]
+    for c in range(nw):
+        assert abs(a["lnpsi"][c] - b["lnpsi"][c]) < 1e-5 * max(abs(b["lnpsi"][c]), 1.0)
+        assert relmax(a["O"][c], b["O"][c]) < 1e-5
+        sc = max(np.abs(b["other"][c]).max(), 1.0)
+        assert np.abs(a["eloc"][c] - b["eloc"][c]).max() < 1e-5 * sc
+        assert np.abs(a["other"][c] - b["other"][c]).max() < 1e-5 * sc
+        assert np.abs(a["dE"][c] - b["dE"][c]).max() < 1e-5 * max(np.abs(b["dE"][c]).max(), 1.0)
