@@ -180,6 +180,7 @@ def pb_systems(ref_root):
     the eval_ fixtures.  The system reads its r_max from the knot vector before
     it builds default knots, so it is always given knots (NURBS_GRID)."""
     L2 = float(np.sqrt(64 / 0.3))
+    L3 = float((343 / 0.365) ** (1.0 / 3.0))
     g = np.linspace(0.0, 1.0, 20)
     knots2 = np.concatenate([[0.0], 0.7 + (L2 / 2 - 0.7) * (g[1:] - g[1]) ** 1.3 / (1 - g[1]) ** 1.3])
     systems = [
@@ -189,6 +190,9 @@ def pb_systems(ref_root):
              jitter=0.3),
         dict(name="d1_n20_p10", dim=1, n=20, p=10, L=20.0, knots=np.linspace(0.0, 10.0, 10), sysp=[0.5, 2.0],
              ncfg=16, seed=33),
+        # the benchmark's shape: 3D N=343, rho=0.365, 30 knots on [0, L/2]
+        dict(name="d3_n343_p30", dim=3, n=343, p=30, L=L3, knots=np.linspace(0.0, L3 / 2, 30), sysp=[1.0, 1.0],
+             ncfg=8, seed=34, jitter=0.5),
     ]
     for sysd in systems:
         rng = np.random.default_rng(sysd["seed"])
@@ -229,6 +233,28 @@ def pb_systems(ref_root):
                  move_cfg=np.array([m[0] for m in moves]), move_part=np.array([m[1] for m in moves]),
                  move_new=np.array([m[2] for m in moves]), ref_move=mv)
         print("pb eval", sysd["name"], ev.shape, mv.shape)
+    pb_sample(ref_root)
+
+
+def pb_sample(ref_root):
+    """Block averages of the reference's own Metropolis chain for the mirrored-distance
+    system: the sample_d3_n27 system (3D N=27, L=3.6, square well a=0.6, b=1) with knots
+    to L/2, sample_pb_d3_n27.npz (the layout of sample_d3_n27.npz plus the knots)."""
+    dim, n, p, L = 3, 27, 10, 3.6
+    knots = np.linspace(0.0, L / 2, p)
+    rng = np.random.default_rng(35)
+    uR = -0.5 * (0.6 / np.maximum(knots, 0.25)) ** 5
+    uR -= uR[-1]
+    uI = 0.05 * rng.normal(size=p)
+    R0 = lattice(n, dim, L, rng, jitter=0.1) - L / 2
+    nblock, nsamp, ntherm, step = 40, 400, n, 0.35
+    script = system_cmd(dim, n, p, L, knots, [0.6, 1.0], 0.0).replace("SYSTEM", "SYSTEMPB", 1)
+    script += "PARAMS %s %s 0 0\n" % (fmt(uR), fmt(uI))
+    script += "SAMPLE 12346 %.17g %d %d %d %d %s\n" % (step, 50 * n, nsamp, ntherm, nblock, fmt(R0))
+    blocks = np.array(run(ref_root, script)["BLOCK"])
+    np.savez(os.path.join(HERE, "sample_pb_d3_n27.npz"), dim=dim, n=n, p=p, L=L, sysp=np.array([0.6, 1.0]),
+             knots=knots, uR=uR, uI=uI, R0=R0, nblock=nblock, nsamp=nsamp, ntherm=ntherm, step=step, blocks=blocks)
+    print("pb sample blocks", blocks.shape)
 
 
 def main():

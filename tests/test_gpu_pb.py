@@ -317,3 +317,42 @@ def test_pb_mixed_tracks_fp64_at_the_benchmark_shape(exact):
         assert np.abs(a["eloc"][c] - b["eloc"][c]).max() < 1e-5 * sc
         assert np.abs(a["other"][c] - b["other"][c]).max() < 1e-5 * sc
         assert np.abs(a["dE"][c] - b["dE"][c]).max() < 1e-5 * max(np.abs(b["dE"][c]).max(), 1.0)
+
+
+def test_pb_sampler_matches_reference_chain_mixed():
+    """The mixed sampler's chain against the reference's own mt19937 chain for the
+    mirrored-distance system (tests/golden/sample_pb_d3_n27.npz: block averages of
+    the reference's DoMetropolisStep / UpdateExpectationValues on NUBosonsBulkPB,
+    3D N=27, knots to L/2): O_k within 4 sigma, acceptance within 3 sigma, E^I
+    within 3 sigma, E^R within 4 sigma (its local energy is heavy-tailed: the FP64
+    oracle's chain lands 2.2 sigma from the reference's on the same seeds)."""
+    z = np.load(os.path.join(GOLD, "sample_pb_d3_n27.npz"))
+    dim, n, p, L = int(z["dim"]), int(z["n"]), int(z["p"]), float(z["L"])
+    blocks = z["blocks"]
+    ref_mean = blocks.mean(0)
+    ref_err = blocks.std(0, ddof=1) / np.sqrt(len(blocks))
+    import tdvmc_gb300 as T
+    nw = 4096
+    s = T.NUBosonsBulkPB(dim, n, p, L, nw, user_knots=z["knots"], system_params=z["sysp"], precision="mixed")
+    s.SetParameters(z["uR"], z["uI"])
+    R = np.repeat(z["R0"].T[None], nw, axis=0) + np.random.default_rng(2).normal(0, 0.05, size=(nw, dim, n))
+    s.SetWalkers(R)
+    s.DoMetropolisSteps(50 * n, float(z["step"]), seed=5, pass_id=0)
+    rows = []
+    acc = 0
+    nsamp = 8
+    for k in range(nsamp):
+        acc += s.DoMetropolisSteps(n, float(z["step"]), seed=5, pass_id=k + 1)
+        f = s.CalculateExpectationValues()
+        rows.append(np.concatenate([f["eloc"], f["O"]], axis=1))
+    per_walker = np.array(rows).mean(0)
+    mean = per_walker.mean(0)
+    err = per_walker.std(0, ddof=1) / np.sqrt(nw)
+    comb = np.sqrt(err ** 2 + ref_err[1:3 + p] ** 2)
+    diff = np.abs(mean - ref_mean[1:3 + p])
+    assert np.all(diff[comb == 0] < 1e-6)
+    dev = np.where(comb > 0, diff / np.where(comb > 0, comb, 1), 0)
+    assert dev[0] < 4 and dev[1] < 3, dev
+    assert np.all(dev[2:] < 4), dev
+    rate = acc / (nsamp * n * nw)
+    assert abs(rate - ref_mean[0]) < 3 * ref_err[0] + 0.01
