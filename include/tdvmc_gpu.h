@@ -73,8 +73,10 @@ extern "C" {
 typedef struct tdvmc_ctx tdvmc_ctx;
 
 /* System description: the reference's globals N, DIM, N_PARAM, LBOX
- * (src/TDVMC.cpp:84-89), SYSTEM_PARAMS, NURBS_GRID (TDVMC.cpp:128-131) and
- * the compile-time HBAR2_2M (src/Constants.h:12), plus the walker count. */
+ * (src/TDVMC.cpp:84-89), SYSTEM_PARAMS, NURBS_GRID (TDVMC.cpp:128-131),
+ * SYSTEM_TYPE and the compile-time HBAR2_2M (src/Constants.h:12), plus the
+ * walker count.  Zero-initialise it (`tdvmc_system_desc d = {};`): a field
+ * left 0 takes its default (system_type 0 is BosonsBulk). */
 typedef struct tdvmc_system_desc {
 	int32_t dim;               /* 1, 2 or 3 */
 	int32_t n;                 /* particles per walker, 2..1024 */
