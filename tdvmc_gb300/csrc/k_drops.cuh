@@ -250,9 +250,10 @@ __device__ __forceinline__ int drop_locate(const DropSys& sy, T r, T& t) {
 	}
 }
 
-// Per-thread shared-memory rows of the evaluation kernel (nmax particles, ns splines)
+// Per-thread shared-memory rows of the evaluation kernel (nmax particles, ns splines,
+// ns - 3 knot intervals)
 __host__ __device__ inline int drop_eval_rows(int nmax, int ns, bool adj) {
-	return 9 * nmax + ns * (adj ? 4 : 1);
+	return 9 * nmax + ns * (adj ? 4 : 1) + 4 * (ns - 3);
 }
 
 // Local quantities of every walker of every drop: ln psi, O_k (the folded
@@ -261,7 +262,10 @@ __host__ __device__ inline int drop_eval_rows(int nmax, int ns, bool adj) {
 // one-body and trap terms).  Shared memory: the item's table coefC[nbin_max]
 // (three 4-vectors per interval) | rows [drop_eval_rows][blockDim]:
 //   X[3 nmax] | G[6 nmax] (gRx gRy gRz gIx gIy gIz per particle) | S[ns] |
-//   (ADJ) Lsp[ns] | AR[ns] | AI[ns]
+//   (ADJ) Lsp[ns] | AR[ns] | AI[ns] | M[4 (ns - 3)]
+// M: the forward sweep's moments sum t^c (c = 0..3) of the pairs in each interval,
+// turned into the spline sums S and the B'' part of Lsp after the sweep (one
+// record update per pair instead of one per spline and sum).
 // loc: the uniform piece polynomials [q][c] (also constant for all drops).
 template <typename T, bool ADJ>
 __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* __restrict__ sys,
@@ -278,6 +282,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 	const int ns = dc.ns, P = dc.p, p1 = dc.p1;
 	auto R = [&](int row) -> T& { return rows[(size_t)row * B + tid]; };
 	const int oG = 3 * nmax, oS = 9 * nmax, oL = oS + ns, oA = oL + ns, oB = oA + ns;
+	const int oM = oS + (ADJ ? 4 : 1) * ns, nbm = ns - 3;
 	// uniform pieces: value, first and second derivative in t
 	T lv[4][4];
 #pragma unroll
@@ -348,6 +353,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 		for (int e = 0; e < 3 * n; e++) R(e) = pw[e];
 		for (int e = 0; e < 6 * n; e++) R(oG + e) = T(0);
 		for (int k = 0; k < (ADJ ? 4 : 1) * ns; k++) R(oS + k) = T(0);
+		for (int k = 0; k < 4 * nbm; k++) R(oM + k) = T(0);
 		const T rmaxT = (T)sy.rmax;
 		const T hj = (T)sy.hinv;
 		KSum<T> vsum, lapR, lapI;
@@ -382,24 +388,33 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 				}
 				lr += d2R + dm1 * gR;
 				li += d2I + dm1 * gI;
-				const T t2 = t * t, t3 = t2 * t;
-#pragma unroll
-				for (int qq = 0; qq < 4; qq++) {
-					const int sp = j + 3 - qq;
-					R(oS + sp) += lv[qq][0] + lv[qq][1] * t + lv[qq][2] * t2 + lv[qq][3] * t3;
-					if (ADJ) {
-						// B'' of both orderings; the (D-1)/r B' part of the Laplacian of O_k
-						// enters through the reverse sweep's (D-1)/r term
-						const T b2 = hj * hj * (T(2) * lv[qq][2] + T(6) * lv[qq][3] * t);
-						R(oL + sp) += T(2) * b2;
-					}
-				}
+				const T t2 = t * t;
+				R(oM + 4 * j) += T(1);
+				R(oM + 4 * j + 1) += t;
+				R(oM + 4 * j + 2) += t2;
+				R(oM + 4 * j + 3) += t2 * t;
 			}
 #pragma unroll
 			for (int c = 0; c < 6; c++) R(oG + c * n + a) += ga[c];
 			lapR.add(T(2) * lr);
 			lapI.add(T(2) * li);
 			vsum.add(vb);
+		}
+		// moments -> spline sums S_s and (ADJ) the B'' part of Lsp: spline s = j + 3 - q on
+		// interval j; B'' of both orderings (the (D-1)/r B' part of the Laplacian of O_k enters
+		// through the reverse sweep's (D-1)/r term)
+		for (int sp = 0; sp < ns; sp++) {
+			T sv = T(0), lv2 = T(0);
+#pragma unroll
+			for (int qq = 0; qq < 4; qq++) {
+				const int j = sp - 3 + qq;
+				if (j < 0 || j >= nbm) continue;
+				const T m0 = R(oM + 4 * j), m1 = R(oM + 4 * j + 1), m2 = R(oM + 4 * j + 2), m3 = R(oM + 4 * j + 3);
+				sv += lv[qq][0] * m0 + lv[qq][1] * m1 + lv[qq][2] * m2 + lv[qq][3] * m3;
+				if (ADJ) lv2 += T(2) * lv[qq][2] * m0 + T(6) * lv[qq][3] * m1;
+			}
+			R(oS + sp) = sv;
+			if (ADJ) R(oL + sp) = T(2) * hj * hj * lv2;
 		}
 		// one-body term and trap: gradient 2 alpha_p r, Laplacian 2 D alpha_p per particle
 		const T aR = (T)prm[P], aI = (T)prm[p1 + P];
