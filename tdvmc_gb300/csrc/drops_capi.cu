@@ -208,7 +208,10 @@ int dl_eval(tdvmc_drops* ctx, bool adj) {
 
 template <typename T>
 int dl_reduce(tdvmc_drops* ctx, bool adj) {
-	k_drop_reduce<T><<<ctx->S, kDropReduceThreads, 0, ctx->st>>>(ctx->dc, (const T*)ctx->O, (const T*)ctx->eloc,
+	// the staged chunk: kDropRedStage walkers x the column count
+	const size_t smem = (size_t)kDropRedStage * DropCols{ctx->p1}.count() * sizeof(T);
+	DK(cudaFuncSetAttribute((const void*)k_drop_reduce<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	k_drop_reduce<T><<<ctx->S, kDropReduceThreads, smem, ctx->st>>>(ctx->dc, (const T*)ctx->O, (const T*)ctx->eloc,
 	                                                              (const T*)ctx->other7, ctx->acc, (const T*)ctx->dE,
 	                                                              adj ? 1 : 0, ctx->means, ctx->Sm, ctx->cov);
 	ctx->launches++;

@@ -506,62 +506,138 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 }
 
 // Per-drop walker means and centred second moments (one block per drop):
-// pass 1 the means of the DropCols columns (FP64 sums in a fixed order), pass 2
+// pass 1 the means of the DropCols columns (FP64 sums in a fixed order; FP32
+// inputs summed per chunk with carried rounding errors), pass 2
 // S_kl = <(O_k - <O_k>)(O_l - <O_l>)> and cov(O_k, E^R), cov(O_k, E^I).  The
 // centred products are formed in T and summed in T over runs of 32 walkers,
 // each run added in FP64 (FP64 issue is scarce on this GPU).  Both passes stage
-// the drop's walkers in chunks of 32 through shared memory with coalesced loads
-// (the walker rows are contiguous), so the sums read shared memory instead of
-// waiting on a strided global load per walker; the order of every sum is that
-// of a walker-by-walker loop.
+// the drop's walkers in chunks of kDropRedStage through shared memory: each
+// per-walker array (O, E, the other values, the acceptance count, dE) is one
+// contiguous range of global memory for a chunk, copied as such (coalesced,
+// several loads in flight per thread, no per-element column arithmetic), and a
+// summing thread reads its column with a fixed base and stride.  The order of
+// every sum is that of a walker-by-walker loop.
 constexpr int kDropReduceThreads = 256;
-constexpr int kDropRedChunk = 32;                     // walkers per staged chunk = the pass-2 run
+constexpr int kDropRedChunk = 32;   // walkers per pass-2 run
+constexpr int kDropRedStage = 128;  // walkers per staged chunk (whole runs)
 constexpr int kDropCols = 3 * (kDropMaxP + 1) + 10;   // DropCols count at the largest p
 constexpr int kDropEntries = (kDropMaxP + 1) * (kDropMaxP + 2) / 2 + 2 * (kDropMaxP + 1);
 constexpr int kDropEntriesPerThread = (kDropEntries + kDropReduceThreads - 1) / kDropReduceThreads;
+// pass 1: the four interleaved partial sums of a column (walkers w = q mod 4) are
+// summed by four threads
+constexpr int kDropMeanSlots = (4 * kDropCols + kDropReduceThreads - 1) / kDropReduceThreads;
+static_assert(kDropRedStage % 4 == 0 && kDropRedStage % kDropRedChunk == 0, "chunks of whole runs and phases");
+
+// dst[0, count) <- src[0, count) by the block's threads
+template <typename D, typename S>
+__device__ __forceinline__ void red_copy(D* __restrict__ dst, const S* __restrict__ src, int count, int tid) {
+#pragma unroll 4
+	for (int e = tid; e < count; e += kDropReduceThreads) dst[e] = (D)src[e];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kDropReduceThreads) k_drop_reduce(
     DropConst dc, const T* __restrict__ O, const T* __restrict__ eloc, const T* __restrict__ other7,
     const int* __restrict__ acc, const T* __restrict__ dE, int use_dE, double* __restrict__ means,
     double* __restrict__ S, double* __restrict__ cov) {
 	__shared__ double m_s[kDropCols];
-	__shared__ T ch[kDropRedChunk * kDropCols];
+	__shared__ double part_s[4 * kDropCols];
+	// staged chunk: sO[cw p1] | sE[2 cw] | sX[7 cw] | sA[cw] | sD[2 p1 cw]
+	extern __shared__ __align__(16) unsigned char red_raw[];
 	const int s = blockIdx.x, tid = threadIdx.x;
 	const int p1 = dc.p1;
 	const DropCols cl{p1};
 	const int K = cl.count();
+	T* sO = reinterpret_cast<T*>(red_raw);
+	T* sE = sO + (size_t)kDropRedStage * p1;
+	T* sX = sE + 2 * kDropRedStage;
+	T* sA = sX + 7 * kDropRedStage;
+	T* sD = sA + kDropRedStage;
 	const int64_t g0 = (int64_t)s * dc.nws, nw = dc.nws;
-	// pass 1: thread per column (K <= kDropCols < blockDim), four interleaved FP64 sums
-	double a[4] = {0, 0, 0, 0};
-	for (int64_t w0 = 0; w0 < nw; w0 += kDropRedChunk) {
-		const int cw = (int)(nw - w0 < kDropRedChunk ? nw - w0 : kDropRedChunk);
-		__syncthreads();
-		for (int e = tid; e < cw * K; e += blockDim.x) {
-			const int w = e / K, col = e - w * K;
-			const int64_t g = g0 + w0 + w;
-			T v;
-			if (col < p1) v = O[(size_t)g * p1 + col];
-			else if (col == cl.ER()) v = eloc[2 * g];
-			else if (col == cl.EI()) v = eloc[2 * g + 1];
-			else if (col < cl.acc()) v = other7[(size_t)g * 7 + (col - cl.other())];
-			else if (col == cl.acc()) v = (T)acc[g];
-			else v = use_dE ? dE[(size_t)g * 2 * p1 + (col - cl.dE())] : T(0);
-			ch[w * K + col] = v;
+	// pass 1: slot (column c, phase q) sums walkers w = q mod 4 of column c in FP64,
+	// the four interleaved sums of a walker-by-walker loop; a thread owns
+	// kDropMeanSlots slots (tid + k blockDim)
+	const T* cb[kDropMeanSlots];  // the slot's column: cb[w * cs]
+	int cs[kDropMeanSlots], cq[kDropMeanSlots];
+	bool live[kDropMeanSlots];
+	double a[kDropMeanSlots];
+#pragma unroll
+	for (int k = 0; k < kDropMeanSlots; k++) {
+		const int slot = tid + k * kDropReduceThreads, c = slot >> 2;
+		cq[k] = slot & 3;
+		a[k] = 0.0;
+		cb[k] = sO;
+		cs[k] = 0;
+		live[k] = c < K;
+		if (c < p1) {
+			cb[k] = sO + c;
+			cs[k] = p1;
+		} else if (c < cl.other()) {
+			cb[k] = sE + (c - cl.ER());
+			cs[k] = 2;
+		} else if (c < cl.acc()) {
+			cb[k] = sX + (c - cl.other());
+			cs[k] = 7;
+		} else if (c == cl.acc()) {
+			cb[k] = sA;
+			cs[k] = 1;
+		} else if (c < K) {
+			cb[k] = sD + (c - cl.dE());
+			cs[k] = 2 * p1;
+			live[k] = use_dE != 0;
 		}
-		__syncthreads();
-		if (tid < K)
-			for (int w = 0; w < cw; w++) a[(w0 + w) & 3] += (double)ch[w * K + tid];
 	}
+	for (int64_t w0 = 0; w0 < nw; w0 += kDropRedStage) {
+		const int cw = (int)(nw - w0 < kDropRedStage ? nw - w0 : kDropRedStage);
+		const int64_t g = g0 + w0;
+		__syncthreads();
+		red_copy(sO, O + (size_t)g * p1, cw * p1, tid);
+		red_copy(sE, eloc + 2 * (size_t)g, 2 * cw, tid);
+		red_copy(sX, other7 + 7 * (size_t)g, 7 * cw, tid);
+		red_copy(sA, acc + g, cw, tid);
+		if (use_dE) red_copy(sD, dE + (size_t)g * 2 * p1, 2 * p1 * cw, tid);
+		__syncthreads();
+		// w0 is a multiple of 4, so walker w of the chunk has phase w mod 4.  FP32: the
+		// slot's walkers of the chunk are summed in FP32 with the error of every addition
+		// carried (two-sum), and the chunk's sum and error are added in FP64 (with one FP64
+		// addition per walker, FP64 issue bounded the pass: 0.71 -> 0.37 ms per stage)
+#pragma unroll
+		for (int k = 0; k < kDropMeanSlots; k++) {
+			if (!live[k]) continue;
+			if constexpr (sizeof(T) == 4) {
+				float sum = 0.f, err = 0.f;
+				for (int w = cq[k]; w < cw; w += 4) {
+					const float x = cb[k][(size_t)w * cs[k]];
+					const float t = sum + x, bp = t - sum;
+					err += (sum - (t - bp)) + (x - bp);
+					sum = t;
+				}
+				a[k] += (double)sum + (double)err;
+			} else {
+				for (int w = cq[k]; w < cw; w += 4) a[k] += (double)cb[k][(size_t)w * cs[k]];
+			}
+		}
+	}
+#pragma unroll
+	for (int k = 0; k < kDropMeanSlots; k++) {
+		const int slot = tid + k * kDropReduceThreads;
+		if (slot < 4 * K) part_s[slot] = a[k];
+	}
+	__syncthreads();
 	if (tid < K) {
-		const double mval = ((a[0] + a[1]) + (a[2] + a[3])) / (double)nw;
+		const double* pq = part_s + 4 * tid;
+		const double mval = ((pq[0] + pq[1]) + (pq[2] + pq[3])) / (double)nw;
 		m_s[tid] = mval;
 		means[(size_t)s * K + tid] = mval;
 	}
 	__syncthreads();
 	// pass 2: thread per entry of the upper triangle of S and the two covariance
-	// columns; the chunk holds the centred O_k and E^R, E^I of its walkers
-	const int nS = p1 * (p1 + 1) / 2, nE = nS + 2 * p1, R = p1 + 2;
-	int ei[kDropEntriesPerThread], ej[kDropEntriesPerThread];
+	// columns (column p1: E^R, p1 + 1: E^I), each factor centred in T as it is read
+	const int nS = p1 * (p1 + 1) / 2, nE = nS + 2 * p1;
+	const T* bi[kDropEntriesPerThread];
+	const T* bj[kDropEntriesPerThread];
+	int si[kDropEntriesPerThread], sj[kDropEntriesPerThread], ei[kDropEntriesPerThread], ej[kDropEntriesPerThread];
+	T mi[kDropEntriesPerThread], mj[kDropEntriesPerThread];
 	double acc64[kDropEntriesPerThread];
 #pragma unroll
 	for (int q = 0; q < kDropEntriesPerThread; q++) {
@@ -577,30 +653,42 @@ __global__ void __launch_bounds__(kDropReduceThreads) k_drop_reduce(
 			j = i + rem;
 		} else if (e < nE) {
 			i = (e - nS) >> 1;
-			j = p1 + ((e - nS) & 1);  // column p1: E^R, p1 + 1: E^I
+			j = p1 + ((e - nS) & 1);
 		}
 		ei[q] = i;
 		ej[q] = j;
+		bi[q] = sO + i;
+		si[q] = p1;
+		mi[q] = (T)m_s[i];
+		if (j < p1) {
+			bj[q] = sO + j;
+			sj[q] = p1;
+			mj[q] = (T)m_s[j];
+		} else {
+			bj[q] = sE + (j - p1);
+			sj[q] = 2;
+			mj[q] = (T)m_s[j == p1 ? cl.ER() : cl.EI()];
+		}
 		acc64[q] = 0.0;
 	}
-	for (int64_t w0 = 0; w0 < nw; w0 += kDropRedChunk) {
-		const int cw = (int)(nw - w0 < kDropRedChunk ? nw - w0 : kDropRedChunk);
+	for (int64_t w0 = 0; w0 < nw; w0 += kDropRedStage) {
+		const int cw = (int)(nw - w0 < kDropRedStage ? nw - w0 : kDropRedStage);
+		const int64_t g = g0 + w0;
 		__syncthreads();
-		for (int e = tid; e < cw * R; e += blockDim.x) {
-			const int w = e / R, col = e - w * R;
-			const int64_t g = g0 + w0 + w;
-			T v;
-			if (col < p1) v = O[(size_t)g * p1 + col] - (T)m_s[col];
-			else v = eloc[2 * g + (col - p1)] - (T)m_s[col == p1 ? cl.ER() : cl.EI()];
-			ch[w * R + col] = v;
-		}
+		red_copy(sO, O + (size_t)g * p1, cw * p1, tid);
+		red_copy(sE, eloc + 2 * (size_t)g, 2 * cw, tid);
 		__syncthreads();
+		// runs of kDropRedChunk walkers in order, each summed in T and added in FP64
+		for (int r0 = 0; r0 < cw; r0 += kDropRedChunk) {
+			const int r1 = r0 + kDropRedChunk < cw ? r0 + kDropRedChunk : cw;
 #pragma unroll
-		for (int q = 0; q < kDropEntriesPerThread; q++) {
-			if (tid + q * kDropReduceThreads >= nE) break;
-			T run = T(0);
-			for (int w = 0; w < cw; w++) run = fma(ch[w * R + ei[q]], ch[w * R + ej[q]], run);
-			acc64[q] += (double)run;
+			for (int q = 0; q < kDropEntriesPerThread; q++) {
+				if (tid + q * kDropReduceThreads >= nE) break;
+				T run = T(0);
+				for (int w = r0; w < r1; w++)
+					run = fma(bi[q][(size_t)w * si[q]] - mi[q], bj[q][(size_t)w * sj[q]] - mj[q], run);
+				acc64[q] += (double)run;
+			}
 		}
 	}
 #pragma unroll
