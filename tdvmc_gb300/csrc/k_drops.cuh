@@ -296,6 +296,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 	constexpr int kNnzMax = 4 * (kDropMaxP + 2);
 	__shared__ int fk_start[kDropMaxP + 1], fk_sp[kNnzMax];
 	__shared__ double fk_f[kNnzMax];
+	__shared__ float fk_f32[kNnzMax];
 	__shared__ int fk_dense;
 	if (tid == 0) {
 		int e = 0;
@@ -308,6 +309,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 				if (e < kNnzMax) {
 					fk_sp[e] = sp;
 					fk_f[e] = f;
+					fk_f32[e] = (float)f;
 				}
 				e++;
 			}
@@ -317,7 +319,20 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 	}
 	__syncthreads();
 	auto fold_row = [&](int k, int oRow, double scale, int oAdd) -> double {
-		// sum over sp of fold[k][sp] * (scale * R(oRow + sp) + R(oAdd + sp)) (oAdd < 0: none)
+		// sum over sp of fold[k][sp] * (scale * R(oRow + sp) + R(oAdd + sp)) (oAdd < 0: none).
+		// FP32: in FP32, the outputs' precision (the FP64 pipe issues a small fraction of
+		// the FP32 rate, and a few dozen FP64 operations per walker showed in the kernel)
+		if constexpr (sizeof(T) == 4) {
+			if (!fk_dense) {
+				float v = 0.f;
+				const float sc = (float)scale;
+				for (int e = fk_start[k]; e < fk_start[k + 1]; e++) {
+					const int sp = fk_sp[e];
+					v += fk_f32[e] * (sc * R(oRow + sp) + (oAdd >= 0 ? R(oAdd + sp) : 0.f));
+				}
+				return (double)v;
+			}
+		}
 		double v = 0.0;
 		if (!fk_dense) {
 			for (int e = fk_start[k]; e < fk_start[k + 1]; e++) {
@@ -446,7 +461,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 		const double kinR = -(sR1 - sI1 + sR2) * c;
 		const double kinI = -(sR1I1 + sI2) * c;
 		const double vtot = (double)vsum.value() + dc.kappa * r2sum;
-		// O_k: fold of the spline sums (FP64), O_p; ln psi in FP64
+		// O_k: fold of the spline sums (in T, see fold_row), O_p; ln psi in FP64
 		double lnp = prm[P - 1] * (double)nout + prm[P] * r2sum;
 		for (int k = 0; k < P; k++) {
 			const double ok = fold_row(k, oS, 1.0, -1);
