@@ -166,6 +166,11 @@ __device__ __forceinline__ void mirror_r(double m2, double& r, double& q, bool e
 	q = mir ? qm : q;
 }
 
+// A fold entry that is exactly +0.0, tested on its bit pattern: the ALU's integer
+// compare instead of an FP64 compare (the FP64 pipe issues a small fraction of the
+// FP32 rate on this GPU); the fold tables hold +0.0, never -0.0, for absent entries.
+__device__ __forceinline__ bool fold_zero(double f) { return __double_as_longlong(f) == 0; }
+
 // Interval lookup over [0, r_max]: returns j (interval index; knot k_{j+3})
 // and the local coordinate t in [0, 1].  kb[j] = left knot, hv[j] = 1/width,
 // lut[c] = first candidate interval of lookup cell c (non-uniform grids).

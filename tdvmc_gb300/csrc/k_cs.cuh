@@ -382,7 +382,10 @@ __global__ void __launch_bounds__(128, 2) k_cs_store(SysConst sc, const CsPieceR
 		__syncwarp(gmask);
 		for (int k = lane; k < P; k += G) {
 			double o = 0.0;
-			for (int sp = 0; sp < ns; sp++) o += fold_g[(size_t)k * ns + sp] * (double)drow[sp];
+			for (int sp = 0; sp < ns; sp++) {
+				const double f = fold_g[(size_t)k * ns + sp];
+				if (!fold_zero(f)) o += f * (double)drow[sp];
+			}
 			O_o[(size_t)w * P + k] = (T)o;
 		}
 		const T v = group_sum<T, G>(vs.value(), gmask);
@@ -493,7 +496,7 @@ __device__ __forceinline__ void cs_finish_walker(const SysConst& sc, const doubl
 			double dR = 0.0, dI = 0.0;
 			for (int s = 0; s < ns; s++) {
 				const double f = fold_g[(size_t)k * ns + s];
-				if (f == 0.0) continue;
+				if (fold_zero(f)) continue;
 				dR += f * (2.0 * (double)asum[2 * s] + (double)D2[(size_t)w * ns + s]);
 				dI += f * (2.0 * (double)asum[2 * s + 1]);
 			}

@@ -1405,7 +1405,7 @@ __global__ void __launch_bounds__((G == 32 && sizeof(T) == 4) ? 64 : 128, (G == 
 			double Ok = 0.0, dR = 0.0;
 			for (int sp = 0; sp < ns; sp++) {
 				const double f = fold_g[(size_t)k * ns + sp];
-				if (f == 0.0) continue;
+				if (fold_zero(f)) continue;
 				Ok += f * (double)spl[sp * 4 + 0];
 				if (ADJ) dR += f * (double)spl[sp * 4 + 1];
 			}
@@ -1557,7 +1557,7 @@ __global__ void __launch_bounds__(128, 1) k_eloc_rev(SysConst sc, const T* __res
 			double dR = 0.0, dI = 0.0;
 			for (int sp = 0; sp < ns; sp++) {
 				const double f = fold_g[(size_t)k * ns + sp];
-				if (f == 0.0) continue;
+				if (fold_zero(f)) continue;
 				dR += f * (2.0 * (double)spl[sp * 4 + 2]);
 				dI += f * (2.0 * (double)spl[sp * 4 + 3]);
 			}
