@@ -318,10 +318,10 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 		fk_dense = e > kNnzMax;
 	}
 	__syncthreads();
-	auto fold_row = [&](int k, int oRow, double scale, int oAdd) -> double {
-		// sum over sp of fold[k][sp] * (scale * R(oRow + sp) + R(oAdd + sp)) (oAdd < 0: none).
-		// FP32: in FP32, the outputs' precision (the FP64 pipe issues a small fraction of
-		// the FP32 rate, and a few dozen FP64 operations per walker showed in the kernel)
+	auto fold_row = [&](int k, int oRow, double scale, int oAdd) -> T {
+		// sum over sp of fold[k][sp] * (scale * R(oRow + sp) + R(oAdd + sp)) (oAdd < 0: none),
+		// in T: FP32 in the mixed path, the outputs' precision (the FP64 pipe issues a small
+		// fraction of the FP32 rate, and the FP64 terms per walker showed in the kernel)
 		if constexpr (sizeof(T) == 4) {
 			if (!fk_dense) {
 				float v = 0.f;
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 					const int sp = fk_sp[e];
 					v += fk_f32[e] * (sc * R(oRow + sp) + (oAdd >= 0 ? R(oAdd + sp) : 0.f));
 				}
-				return (double)v;
+				return v;
 			}
 		}
 		double v = 0.0;
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 				v += f * (scale * (double)R(oRow + sp) + (oAdd >= 0 ? (double)R(oAdd + sp) : 0.0));
 			}
 		}
-		return v;
+		return (T)v;
 	};
 	for (;;) {
 		const int it = next_item(counter);
@@ -464,9 +464,9 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 		// O_k: fold of the spline sums (in T, see fold_row), O_p; ln psi in FP64
 		double lnp = prm[P - 1] * (double)nout + prm[P] * r2sum;
 		for (int k = 0; k < P; k++) {
-			const double ok = fold_row(k, oS, 1.0, -1);
-			O_o[(size_t)g * p1 + k] = (T)ok;
-			lnp += prm[k] * ok;
+			const T ok = fold_row(k, oS, 1.0, -1);
+			O_o[(size_t)g * p1 + k] = ok;
+			lnp += prm[k] * (double)ok;
 		}
 		O_o[(size_t)g * p1 + P] = (T)r2sum;
 		lnpsi_o[g] = (T)lnp;
@@ -510,9 +510,9 @@ __global__ void __launch_bounds__(128) k_drop_eval(DropConst dc, const DropSys* 
 				}
 			}
 			for (int k = 0; k < P; k++) {
-				const double re = fold_row(k, oA, 2.0, oL), im = fold_row(k, oB, 2.0, -1);
-				dE_o[((size_t)g * p1 + k) * 2 + 0] = (T)(-c * re);
-				dE_o[((size_t)g * p1 + k) * 2 + 1] = (T)(-c * im);
+				const T re = fold_row(k, oA, 2.0, oL), im = fold_row(k, oB, 2.0, -1);
+				dE_o[((size_t)g * p1 + k) * 2 + 0] = (T)(-c) * re;
+				dE_o[((size_t)g * p1 + k) * 2 + 1] = (T)(-c) * im;
 			}
 			dE_o[((size_t)g * p1 + P) * 2 + 0] = (T)(-c * (6.0 * n + 4.0 * (double)gxr.value()));
 			dE_o[((size_t)g * p1 + P) * 2 + 1] = (T)(-c * 4.0 * (double)gxi.value());
