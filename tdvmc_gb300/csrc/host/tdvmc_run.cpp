@@ -381,6 +381,12 @@ int main(int argc, char** argv) {
 		return 2;
 	}
 	const bool pb = system == "NUBosonsBulkPB";
+	if (pb && (int)cfg.num("USE_NURBS", 0) != 1) {
+		// NUBosonsBulkPB reads r_max from the knot vector before it would build default
+		// knots (NUBosonsBulkPB.cpp:76, 91-97): the reference program crashes without them
+		std::fprintf(stderr, "SYSTEM_TYPE NUBosonsBulkPB needs USE_NURBS = 1 and its NURBS_GRID\n");
+		return 2;
+	}
 	g_out = argc > 2 ? std::string(argv[2]) : cfg.str("OUTPUT_DIRECTORY", "./");
 	if (!g_out.empty() && g_out.back() != '/') g_out += "/";
 	mkdir(g_out.c_str(), 0755);

@@ -177,6 +177,8 @@ def test_mirrored_distance_system(driver, tmp_path):
     assert table(out / "OtherExpectationValues.dat").shape[1] == 9 + 400
     r, _, _ = run(driver, tmp_path, base_cfg(SYSTEM_TYPE="NUBosonsBulkPBBox"))
     assert r.returncode == 2
+    r, _, _ = run(driver, tmp_path, base_cfg(SYSTEM_TYPE="NUBosonsBulkPB"))  # no knots
+    assert r.returncode == 2 and "USE_NURBS" in r.stderr
 
 
 def test_random_state_for_a_successive_run(driver, tmp_path):
