@@ -356,3 +356,43 @@ def test_pb_sampler_matches_reference_chain_mixed():
     assert np.all(dev[2:] < 4), dev
     rate = acc / (nsamp * n * nw)
     assert abs(rate - ref_mean[0]) < 3 * ref_err[0] + 0.01
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("dim,n", [(1, 2), (3, 3), (2, 5), (3, 33), (3, 65)])
+def test_pb_ragged_sizes_match_oracle(dim, n, precision):
+    """Particle counts that leave the 32-lane groups of the mirrored-distance kernels
+    partly empty (N = 2, 3, 5), one slot and one particle more (33), two slots and one
+    more (65): evaluation, adjoint and a sampling pass against the oracle (FP64 1e-12
+    and the same chain; mixed 1e-5 on FP32-held walkers)."""
+    import tdvmc_gb300 as T
+    p, nw = 8, 5
+    L = (n / 0.4) ** (1.0 / dim)
+    knots = np.linspace(0.0, L / 2, p)
+    rng = np.random.default_rng(10 * n + dim)
+    uR, uI = 0.3 * rng.normal(size=p), 0.1 * rng.normal(size=p)
+    R = rng.uniform(-L / 2, L / 2, size=(nw, dim, n))
+    if precision == "mixed":
+        R = R.astype(np.float32).astype(np.float64)
+    s = T.NUBosonsBulkPB(dim, n, p, L, nw, user_knots=knots, system_params=(0.5, 1.0), precision=precision)
+    s.SetParameters(uR, uI)
+    s.SetWalkers(R)
+    f = s.CalculateExpectationValues()
+    dE = s.CalculateLocalEnergyAdjoint()
+    o = orc.OracleSystem(dim, n, p, L, user_knots=knots, pot_kind=orc.POT_SQUARE, pot=(0.5, 1.0),
+                         variant=orc.SYS_NU_PB)
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    for w in range(nw):
+        r = o.eval(uR, uI, R[w].T, adjoint=True)
+        assert abs(f["lnpsi"][w] - r["lnpsi"]) < tol * max(abs(r["lnpsi"]), np.abs(uR).max() * n)
+        assert relmax(f["O"][w], r["O"]) < tol
+        sc = max(np.abs(r["other"]).max(), 1.0)
+        assert np.abs(f["eloc"][w] - r["eloc"]).max() < tol * sc
+        assert np.abs(f["other"][w] - r["other"]).max() < tol * sc
+        assert np.abs(dE[w] - r["dE"]).max() < tol * max(np.abs(r["dE"]).max(), 1.0)
+    if precision == "fp64":
+        acc = s.DoMetropolisSteps(4 * n, 0.5, seed=8, pass_id=3)
+        Ro = np.ascontiguousarray(R.copy())
+        acc_o = o.sample(uR, Ro, 4 * n, 0.5, seed=8, pass_id=3)
+        assert acc == acc_o
+        assert np.abs(s.GetWalkers() - Ro).max() < 1e-9
