@@ -104,3 +104,36 @@ def test_mirrored_system_descriptor_checks():
     # 1D: r_max = L / 4 + 0.4 is enough
     assert create(knots=(0.0, 0.35, 0.7, 1.05, 1.4), dim=1) != N.ERR_ARG
     assert create(knots=(0.0, 0.35, 0.7, 1.05, 1.4), dim=1, system_type=N.SYS_NU_BOSONS_BULK_PB_EXACT) != N.ERR_ARG
+
+
+def test_header_compiles_as_c_and_matches_the_ctypes_layout(tmp_path):
+    """The header is plain C99 (no C++ types cross the boundary), and the struct
+    layouts the Python binding declares match the compiler's: size and the offset
+    of every field of tdvmc_system_desc, tdvmc_stats, tdvmc_step_opts and
+    tdvmc_drops_desc."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from tdvmc_gb300 import _native as N
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"tdvmc_system_desc": N.SystemDesc, "tdvmc_stats": N.Stats, "tdvmc_step_opts": N.StepOpts,
+               "tdvmc_drops_desc": N.DropsDesc}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "tdvmc_gpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%%s size %%zu\\n", "%s", sizeof(%s));' % (cname, cname))
+        for f in py._fields_:
+            lines.append('printf("%%s %%s %%zu\\n", "%s", "%s", offsetof(%s, %s));' % (cname, f[0], cname, f[0]))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-I" + os.path.join(ROOT, "include"),
+                           str(src), "-o", str(exe)])
+    out = subprocess.check_output([str(exe)], text=True).split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
